@@ -1,0 +1,415 @@
+#!/usr/bin/env python
+"""Benchmark of the KillingFusion registration loop on GB300.
+
+Workload: the 256^3 / 5 mm sequence -- a union of 5 ellipsoids bending about
+a seeded hinge, 640x480 float32 depth with 1.5 mm noise -- with the paper
+weights and 200 psi iterations per frame.  One step is one frame of the
+per-frame pipeline of KillingFusion::processNextFrame
+(KillingFusion.cpp:123-170): integrate the live frame, zero psi, 200 fused
+Jacobi iterations, mesh the live SDF, warp it by psi and fuse it into the
+canonical SDF, mesh the registered and the canonical SDF.
+
+value: voxel-updates/s = 256^3 * 200 * steps / time, every frame's inputs
+resident in HBM.  e2e: the same through the C ABI with the depth frame copied
+from pinned host memory and the three meshes copied back each step.
+
+`--impl reference` times the FP64 CPU restatement of the reference (the
+oracle) on the host cores on a bounded sample of the same frame.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "voxel-updates/s at 256³ fused vs plain GPU (ψ err≤1e-4 vox); ms/frame; HBM %"
+ALGO_BYTES_PER_VOXEL = 32  # psi read 12 + write 12, phi_live 4, phi_can 4 per voxel-update
+MESH_CAP = 4_000_000       # triangles per mesh buffer
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--iters", type=int, default=200)
+    ap.add_argument("--solver", default="fused", choices=["fused", "plain"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-iters", type=int, default=2, help="Jacobi iterations in the CPU sample")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per voxel of one fused iteration from the committed ncu
+    summary (profiles/fused_iteration_traffic.json), if present."""
+    p = os.path.join(ROOT, "profiles", "fused_iteration_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.out.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def mesh_once(capi, L, g, P, buf, cap):
+    n = C.c_int64(0)
+    capi.check(L.kf_marching_cubes(g.h, C.byref(P.c()), buf, cap, C.byref(n), None))
+    return n.value
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    from killingfusion_gb300 import capi, synth
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = capi.load()
+    seq = synth.EllipsoidSequence(seed=2, frames=30, n=args.size)
+    grid = seq.grid
+    P = capi.Params.paper(grid.voxel)
+    nframes = 1 + args.warmup + args.steps
+    host_frames = [seq.frame(f % 30) for f in range(nframes)]
+    dev_frames = [torch.from_numpy(f).to(dev) for f in host_frames]
+    pinned = [torch.from_numpy(f).pin_memory() for f in host_frames]
+
+    can = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
+    live = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
+    psi = capi.Field(grid.dims, capi.KF_F32)
+    can.integrate(dev_frames[0], min_depth=0.05, max_depth=1.6)
+    meshes = [torch.empty((MESH_CAP, 9), dtype=torch.float32, device=dev) for _ in range(3)]
+    host_mesh = [torch.empty((MESH_CAP, 9), dtype=torch.float32).pin_memory() for _ in range(3)]
+    N3 = int(np.prod(grid.dims))
+    solver = capi.SOLVERS[args.solver]
+    stats = capi.SolveStats()
+    stream = torch.cuda.current_stream(dev)
+    launches_per_frame = 1 + 1 + 2 * args.iters + 1 + 3 * 3 if args.solver == "fused" else \
+        1 + 1 + 7 * args.iters + 1 + 3 * 3
+
+    def frame(depth, e2e=False):
+        """One processNextFrame: returns (solve event pair, mesh triangle counts, d2h bytes)."""
+        live.reset(P)
+        if e2e:
+            d = depth  # pinned host tensor: the ABI copies it in
+            capi.check(L.kf_integrate_depth(live.h, d.data_ptr(), d.shape[1], d.shape[0],
+                                            capi._d(np.eye(4).ravel()), capi._d(synth.K.ravel()),
+                                            0.05, 1.6, None))
+        else:
+            live.integrate(depth, min_depth=0.05, max_depth=1.6)
+        psi.zero()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = L.kf_psi_solve(live.h, can.h, psi.h, C.byref(P.c()), args.iters, solver,
+                            C.byref(stats), None)
+        e1.record(stream)
+        capi.check(st)
+        n0 = mesh_once(capi, L, live, P, meshes[0].data_ptr(), MESH_CAP)
+        capi.check(L.kf_warp_fuse(can.h, live.h, psi.h, C.byref(P.c()), None))
+        n1 = mesh_once(capi, L, live, P, meshes[1].data_ptr(), MESH_CAP)
+        n2 = mesh_once(capi, L, can, P, meshes[2].data_ptr(), MESH_CAP)
+        d2h = 0
+        if e2e:
+            for k, n in enumerate((n0, n1, n2)):
+                host_mesh[k][:n].copy_(meshes[k][:n], non_blocking=True)
+                d2h += n * 36
+        return (e0, e1), (n0, n1, n2), d2h
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up (also captures the solve graph)
+    for f in range(1, 1 + args.warmup):
+        frame(dev_frames[f])
+    barrier()
+
+    clocks = Clocks(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    ev_start, ev_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev_start.record(stream)
+    solve_events, tri_counts = [], []
+    for f in range(1 + args.warmup, nframes):
+        se, tc, _ = frame(dev_frames[f])
+        solve_events.append(se)
+        tri_counts.append(tc)
+    ev_end.record(stream)
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    elapsed_ms = ev_start.elapsed_time(ev_end)
+    solve_ms = [a.elapsed_time(b) for a, b in solve_events]
+    active = stats.active_first
+
+    # end to end through the C ABI with host buffers
+    can_e2e = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
+    capi.check(L.kf_integrate_depth(can_e2e.h, pinned[0].data_ptr(), 640, 480,
+                                    capi._d(np.eye(4).ravel()), capi._d(synth.K.ravel()), 0.05, 1.6,
+                                    None))
+    can, can_e2e = can_e2e, can
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    d2h_total = 0
+    for f in range(1 + args.warmup, nframes):
+        _, _, d2h = frame(pinned[f], e2e=True)
+        d2h_total += d2h
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+
+    # plain per-term solver on the same frame (fewer iterations), for the ratio
+    plain_it = 10
+    live.reset(P)
+    live.integrate(dev_frames[-1], min_depth=0.05, max_depth=1.6)
+    psi.zero()
+    st_plain = capi.psi_solve(live, can_e2e, psi, P, plain_it, "plain" if args.solver == "fused" else "fused")
+    other_vups = N3 * plain_it / (st_plain["device_ms"] / 1e3)
+
+    res = {
+        "elapsed_ms": elapsed_ms, "wall_s": wall, "solve_ms": solve_ms, "e2e_ms": e2e_ms,
+        "d2h_bytes_per_step": d2h_total / args.steps, "tris": tri_counts, "active": active,
+        "clocks": clk, "N3": N3, "other_vups": other_vups, "launches": launches_per_frame * args.steps,
+    }
+    return res, seq, P
+
+
+def cpu_sample(seq, P, iters, nthreads=0):
+    """Bounded FP64 sample of one frame on the host cores: integrate, `iters`
+    Jacobi iterations, update + fuse, three meshes; extrapolated to the
+    frame's full iteration count by the caller."""
+    import numpy as np
+
+    from oracle.oracle import Oracle, Params as OParams
+    from killingfusion_gb300 import synth
+
+    O = Oracle()
+    OP = OParams(**{k: getattr(P, k) for k in OParams.__dataclass_fields__})
+    g = seq.grid
+    n = g.dims[::-1]
+    f0 = seq.frame(0).astype(np.float64)
+    f1 = seq.frame(1).astype(np.float64)
+    base = np.full(n, OP.max_surface + OP.epsilon)
+    w0 = np.zeros(n, np.int64)
+    can, wc = O.integrate(base, w0, g.voxel, g.origin, OP.unknown_clip, f0, np.eye(4), synth.K, 0.05, 1.6)
+    t = {}
+    a = time.perf_counter()
+    live, wl = O.integrate(base, w0, g.voxel, g.origin, OP.unknown_clip, f1, np.eye(4), synth.K, 0.05, 1.6)
+    t["integrate"] = time.perf_counter() - a
+    a = time.perf_counter()
+    st, psi = O.solve(live, can, np.zeros(n + (3,)), iters, OP, nthreads=nthreads)
+    t["solve"] = time.perf_counter() - a
+    a = time.perf_counter()
+    m0 = O.mesh(live, OP)
+    uphi, uw = O.update(live, wl, psi, OP)
+    fphi, fw = O.fuse(can, wc, uphi, uw)
+    m1 = O.mesh(uphi, OP)
+    m2 = O.mesh(fphi, OP)
+    t["fuse_mesh"] = time.perf_counter() - a
+    return t
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
+
+    if args.impl == "reference" and rank != 0:
+        return
+    run_main(args, rank, world, local)
+
+
+def run_main(args, rank, world, local):
+    import numpy as np
+
+    if args.impl == "reference":
+        from killingfusion_gb300 import synth
+        seq = synth.EllipsoidSequence(seed=2, frames=30, n=args.size)
+        from killingfusion_gb300.capi import Params
+        P = Params.paper(seq.grid.voxel)
+        N3 = int(np.prod(seq.grid.dims))
+        cores = cpu_threads()
+        per = []
+        for s in range(args.warmup + args.steps):
+            t = cpu_sample(seq, P, args.cpu_iters)
+            frame_s = t["integrate"] + t["solve"] / args.cpu_iters * args.iters + t["fuse_mesh"]
+            if s >= args.warmup:
+                per.append(frame_s)
+        frame_s = statistics.mean(per)
+        value = N3 * args.iters / frame_s
+        sample = ("one frame of the %d^3 sequence: integrate, %d of %d Jacobi iterations, update+fuse, "
+                  "3 meshes; FP64 oracle port on %d threads; frame time extrapolated to %d iterations"
+                  % (args.size, args.cpu_iters, args.iters, cores, args.iters))
+        line = {
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "voxel-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": frame_s * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "ellipsoid-sequence-%d" % args.size, "grid": [args.size] * 3,
+                       "voxel_mm": 5.0 * 256 / args.size, "iterations_per_frame": args.iters,
+                       "weights": "paper"},
+            "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
+
+    res, seq, P = run_ours(args, rank, world, local)
+    import torch
+    el = res["elapsed_ms"]
+    e2e_ms = res["e2e_ms"]
+    if world > 1:
+        t = torch.tensor([el, e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        el, e2e_ms = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    N3 = res["N3"]
+    updates = N3 * args.iters * args.steps * world
+    value = updates / (el / 1e3)
+    e2e_value = updates / (e2e_ms / 1e3)
+    solve_ms = statistics.mean(res["solve_ms"])
+    iter_ms = solve_ms / args.iters
+    peak, peak_kind = peaks()
+    achieved = ALGO_BYTES_PER_VOXEL * N3 / (iter_ms / 1e3) / 1e9
+    prof = profile_traffic()
+    traffic = None
+    if prof and prof.get("dram_bytes_per_voxel"):
+        traffic = prof["dram_bytes_per_voxel"] * N3
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "voxel-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": el / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": "ellipsoid-sequence-%d" % args.size, "grid": [args.size] * 3,
+            "voxel_mm": 5.0 * 256 / args.size, "iterations_per_frame": args.iters,
+            "weights": "paper", "solver": args.solver, "frames": "1 canonical + warmup + steps",
+            "step": "one processNextFrame: integrate, zero psi, %d psi iterations, 3 meshes, warp+fuse"
+                    % args.iters,
+            "l2": "inputs larger than L2 (psi 2x201 MB, phi 2x67 MB per grid)",
+            "parallelism": "replicas" if world > 1 else "1 GPU",
+        },
+        "e2e": {"value": e2e_value, "unit": "voxel-updates/s",
+                "h2d_bytes_per_step": 640 * 480 * 4, "d2h_bytes_per_step": res["d2h_bytes_per_step"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "fused psi iteration (k_fused_stream + k_fused_band)",
+                     "algorithmic_bytes_per_voxel": ALGO_BYTES_PER_VOXEL, "peak_source": peak_kind},
+        "clocks": res["clocks"],
+        "gpu_launches": res["launches"],
+        "solve_ms_per_frame": solve_ms,
+        "solve_voxel_updates_per_s": N3 * args.iters / (solve_ms / 1e3),
+        "plain_voxel_updates_per_s" if args.solver == "fused" else "fused_voxel_updates_per_s": res["other_vups"],
+        "band_voxels": res["active"],
+        "triangles_last_frame": res["tris"][-1],
+    }
+    if args.solver == "fused":
+        line["fused_over_plain"] = line["solve_voxel_updates_per_s"] / res["other_vups"]
+    if world == 1 and not args.no_cpu_baseline:
+        t = cpu_sample(seq, P, args.cpu_iters)
+        frame_s = t["integrate"] + t["solve"] / args.cpu_iters * args.iters + t["fuse_mesh"]
+        line["cpu_baseline"] = {
+            "value": N3 * args.iters / frame_s, "unit": "voxel-updates/s", "cores": cpu_threads(),
+            "kind": "port",
+            "sample": "one frame, %d of %d Jacobi iterations timed, frame time extrapolated"
+                      % (args.cpu_iters, args.iters),
+        }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,191 @@
+/*
+ * killingfusion.h -- C ABI of the GB300 KillingFusion registration loop.
+ *
+ * A drop-in for the hot path of saurabheights/KillingFusion: the TSDF grid
+ * (class SDF), the displacement field psi (class DisplacementField), the
+ * gradient-descent psi update (KillingFusion::computeDisplacementField) and
+ * the mesher (SDF::getMesh / Polygonise).  The reference has no FFI; its
+ * boundary is the C++ class API, and each entry point below names the method
+ * it stands in for (file:line in the reference).  The C++ classes with the
+ * reference's names and call shapes (killingfusion_gb300/csrc/host/) are
+ * written on top of these functions.
+ *
+ * Conventions
+ *  - Every function returns a kf_status; kf_last_error() describes the last
+ *    failure of the calling thread.
+ *  - Grids are dense, x fastest: idx = z*nx*ny + y*nx + x (SDF.cpp:27).
+ *    phi is float32 metres (value of voxel i at its centre i+0.5), weights
+ *    int32; psi is three float32 (or float64, see kf_precision) planes in
+ *    voxel units, stored at integer positions (DisplacementField.cpp:40-58).
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  All work is
+ *    stream-ordered; functions that return host values synchronise `stream`.
+ *  - Buffers documented as "host or device" may be either (the copy uses
+ *    cudaMemcpyDefault); all others are device pointers.
+ */
+#ifndef KILLINGFUSION_GB300_H
+#define KILLINGFUSION_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KF_ABI_VERSION 1
+
+typedef enum kf_status {
+  KF_OK = 0,
+  KF_ERR_INVALID = 1,  /* bad argument: null handle, size mismatch, range   */
+  KF_ERR_OOM = 2,      /* device or pinned allocation failed                */
+  KF_ERR_CUDA = 3,     /* CUDA runtime error                                */
+  KF_ERR_DIVERGED = 4, /* psi non-finite at a voxel in the band; the
+                          reference throws -1 (KillingFusion.cpp:328-332)   */
+  KF_ERR_TIMEOUT = 5,  /* a bounded device-side wait gave up                */
+  KF_ERR_CAPACITY = 6  /* caller buffer too small (count is still returned) */
+} kf_status;
+
+/* Arithmetic of the psi solve. */
+typedef enum kf_precision {
+  KF_F32 = 0, /* float32 fields and arithmetic (production)                */
+  KF_F64 = 1  /* float64 psi and arithmetic, no fused multiply-add, in the
+                 reference's operation order: reproduces the reference's
+                 FP64 result bit for bit given the same float32 SDFs        */
+} kf_precision;
+
+/* Form of the psi update kernel(s). */
+typedef enum kf_solver {
+  KF_SOLVER_FUSED = 0, /* one stencil pass per iteration, CUDA-graph loop  */
+  KF_SOLVER_PLAIN = 1, /* one kernel per energy term, fields through HBM   */
+  KF_SOLVER_EXACT = 2  /* float64 replay of the reference (needs KF_F64 psi) */
+} kf_solver;
+
+/* The reference's config.h globals that the hot path reads. */
+typedef struct kf_params {
+  double voxel_size;    /* VoxelSize (config.cpp:4)                        */
+  double unknown_clip;  /* UnknownClipDistance (config.cpp:5)              */
+  double max_surface;   /* MaxSurfaceVoxelDistance (config.cpp:6)          */
+  double epsilon;       /* epsilon (config.cpp:57)                         */
+  double delta_size;    /* deltaSize h, voxel units (config.cpp:29)        */
+  double alpha;         /* gradient step (config.cpp:45)                   */
+  double omega_k;       /* Killing weight (config.cpp:48)                  */
+  double gamma_k;       /* Killing rigidity gamma (config.cpp:51)          */
+  double omega_s;       /* level-set weight (config.cpp:54)                */
+  double threshold;     /* convergence threshold on max |dpsi| (config.cpp:43),
+                           used only when early_exit is set                */
+  double killing_clamp; /* |g| clamp, DisplacementField.cpp:342 (0.1)     */
+  int use_data;         /* EnergyTypeUsed[0..2] (config.cpp:23)            */
+  int use_levelset;
+  int use_killing;
+  int early_exit;       /* 0: run every requested iteration, as the
+                           reference's Jacobi schedule does; 1: stop once
+                           max |dpsi| <= threshold, the criterion of its
+                           per-voxel schedule (KillingFusion.cpp:381)      */
+} kf_params;
+
+typedef struct kf_solve_stats {
+  int32_t iterations_run; /* iterations executed                           */
+  int32_t converged;      /* 1 if max |dpsi| fell to params.threshold      */
+  int32_t diverged;       /* 1 if psi turned non-finite inside the band    */
+  int32_t reserved;
+  int64_t active_first;   /* voxels inside the band, first iteration       */
+  int64_t active_last;    /* ... last executed iteration                   */
+  double energy_first;    /* monitored energy (FP64 reduction)             */
+  double energy_last;
+  double max_delta_last;  /* max |dpsi| of the last executed iteration     */
+  double device_ms;       /* device time of the solve                      */
+} kf_solve_stats;
+
+typedef struct kf_grid_s *kf_grid;   /* an SDF: phi + weights on a grid     */
+typedef struct kf_field_s *kf_field; /* a displacement field psi           */
+typedef struct kf_fusion_s *kf_fusion; /* the per-frame pipeline           */
+
+/* ---- library -------------------------------------------------------- */
+int kf_version(void);
+const char *kf_last_error(void);
+/* The reference's compiled-in values (config.cpp:4-57). */
+void kf_params_reference(kf_params *p);
+/* Paper weights (alpha 0.1, omega_k 0.5, gamma 0.1, omega_s 0.2) with the
+ * truncation band set to trunc_voxels voxels (config.cpp:32-41 comment). */
+void kf_params_paper(kf_params *p, double voxel_size, double trunc_voxels);
+/* Introspection of the marching-cubes table (MarchingCubes.h:26-318): edge
+ * mask of a cube configuration and its triangle list (edge ids, -1 padded). */
+int kf_mc_case(int cubeindex, int *edge_mask, int tri_edges[16]);
+
+/* ---- SDF grid (SDF.h:16-200) ------------------------------------------ */
+/* SDF::SDF(voxelSize, min, max, unknownClip) with the grid size given
+ * directly (SDF.cpp:14-30, 117-135); phi = max_surface+epsilon, w = 0. */
+int kf_grid_create(const int dims[3], double voxel_size, const double min3d[3],
+                   double unknown_clip, const kf_params *p, kf_grid *out);
+int kf_grid_destroy(kf_grid g);
+int kf_grid_info(kf_grid g, int dims[3], double *voxel_size, double min3d[3],
+                 double *unknown_clip);
+/* Refill with phi = max_surface+epsilon, w = 0 (SDF.cpp:126-135). */
+int kf_grid_reset(kf_grid g, const kf_params *p, void *stream);
+/* Copy N phi values / weights in or out (host or device; NULL skips). */
+int kf_grid_upload(kf_grid g, const float *phi, const int32_t *weight, void *stream);
+int kf_grid_download(kf_grid g, float *phi, int32_t *weight, void *stream);
+/* Raw device pointers (owned by the grid). */
+int kf_grid_device(kf_grid g, float **phi, int32_t **weight);
+
+/* ---- displacement field (DisplacementField.h:9-66) -------------------- */
+/* DisplacementField(gridSize, voxelSize): zero-initialised
+ * (DisplacementField.cpp:8-16). */
+int kf_field_create(const int dims[3], kf_precision prec, kf_field *out);
+int kf_field_destroy(kf_field f);
+int kf_field_zero(kf_field f, void *stream);
+/* Copy psi in or out as [N][3] (array of structs, the reference's layout),
+ * float for KF_F32 fields and double for KF_F64 (host or device). */
+int kf_field_upload(kf_field f, const void *xyz, void *stream);
+int kf_field_download(kf_field f, void *xyz, void *stream);
+int kf_field_device(kf_field f, void **px, void **py, void **pz);
+
+/* ---- hot path --------------------------------------------------------- */
+/* SDF::integrateDepthFrame (SDF.cpp:137-197).  depth: float32 metres,
+ * row-major [height][width] (host or device); c2w: row-major camera->world
+ * pose; K: row-major intrinsics. */
+int kf_integrate_depth(kf_grid g, const float *depth, int width, int height,
+                       const double c2w[16], const double K[9], double min_depth,
+                       double max_depth, void *stream);
+
+/* KillingFusion::computeDisplacementField, Jacobi schedule
+ * (KillingFusion.cpp:240-352): `iterations` gradient-descent steps of psi
+ * registering `live` onto `canonical`.  Returns KF_ERR_DIVERGED when psi
+ * turned non-finite inside the band.  stats may be NULL. */
+int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
+                 int iterations, kf_solver solver, kf_solve_stats *stats, void *stream);
+
+/* KillingFusion::computeEnergyGradient (KillingFusion.cpp:399-442) at
+ * `count` voxels (device int32 xyz triples), in the field's precision;
+ * out: device double[count][3].  Also the band test (KillingFusion.cpp:272)
+ * into active (device uint8[count], may be NULL). */
+int kf_psi_gradient_ref(kf_grid live, kf_grid canonical, kf_field psi,
+                        const kf_params *p, const int32_t *voxels, int count,
+                        double *out, uint8_t *active, void *stream);
+
+/* SDF::update(psi) (SDF.cpp:300-328): resample g at i+0.5+psi(i), weights
+ * truncated to integers. */
+int kf_warp(kf_grid g, kf_field psi, const kf_params *p, void *stream);
+/* SDF::fuse(other) with FUSE_BY_MERGE (SDF.cpp:199-241). */
+int kf_fuse(kf_grid canonical, kf_grid other, void *stream);
+/* SDF::update(psi) on `live` followed by canonical->fuse(live)
+ * (KillingFusion.cpp:158-159) in one pass; live is left warped. */
+int kf_warp_fuse(kf_grid canonical, kf_grid live, kf_field psi, const kf_params *p,
+                 void *stream);
+/* SDF::fuse(other, psi) (SDF.cpp:244-297). */
+int kf_fuse_warped(kf_grid dst, kf_grid other, kf_field psi, const kf_params *p,
+                   void *stream);
+
+/* SDF::getMesh (SDF.cpp:396-414) + Polygonise (MarchingCubes.h:366-422):
+ * triangle soup in the reference's order (cells z, y, x; triangles in table
+ * order), 9 floats per triangle (3 vertices, y negated as
+ * SimpleMesh::AddVertex does).  *ntri receives the count; verts (device, may
+ * be NULL) receives min(count, capacity) triangles; KF_ERR_CAPACITY when
+ * capacity < count. */
+int kf_marching_cubes(kf_grid g, const kf_params *p, float *verts, int64_t capacity,
+                      int64_t *ntri, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,319 @@
+"""ctypes binding of the C ABI (include/killingfusion.h).
+
+The library is ``killingfusion_gb300/_lib/libkillingfusion.so``, built in-tree
+by ``killingfusion_gb300._build`` (``__graft_entry__.build()``).  There is no
+fallback: if the library is missing, importing this module raises.
+
+Device buffers that the ABI writes into (mesh vertices, gradient queries) are
+torch CUDA tensors; torch is used only as device-memory plumbing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, asdict, replace
+
+import numpy as np
+
+from . import _build
+
+LIB_PATH = _build.LIB
+
+KF_OK, KF_ERR_INVALID, KF_ERR_OOM, KF_ERR_CUDA, KF_ERR_DIVERGED, KF_ERR_TIMEOUT, KF_ERR_CAPACITY = range(7)
+KF_F32, KF_F64 = 0, 1
+KF_SOLVER_FUSED, KF_SOLVER_PLAIN, KF_SOLVER_EXACT = 0, 1, 2
+SOLVERS = {"fused": KF_SOLVER_FUSED, "plain": KF_SOLVER_PLAIN, "exact": KF_SOLVER_EXACT}
+
+
+class KFError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("kf status %d: %s" % (status, msg))
+        self.status = status
+
+
+class DivergedError(KFError):
+    """psi turned non-finite inside the band (the reference throws -1)."""
+
+
+class _Params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "voxel_size", "unknown_clip", "max_surface", "epsilon", "delta_size", "alpha",
+        "omega_k", "gamma_k", "omega_s", "threshold", "killing_clamp")] + [
+        ("use_data", C.c_int), ("use_levelset", C.c_int), ("use_killing", C.c_int),
+        ("early_exit", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations_run", C.c_int32), ("converged", C.c_int32), ("diverged", C.c_int32),
+                ("reserved", C.c_int32), ("active_first", C.c_int64), ("active_last", C.c_int64),
+                ("energy_first", C.c_double), ("energy_last", C.c_double),
+                ("max_delta_last", C.c_double), ("device_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+@dataclass(frozen=True)
+class Params:
+    """kf_params: the reference's config.h globals (config.cpp:4-57)."""
+
+    voxel_size: float = 0.012
+    unknown_clip: float = 0.048
+    max_surface: float = 0.048
+    epsilon: float = 1e-5
+    delta_size: float = 0.05
+    alpha: float = 0.025
+    omega_k: float = 0.04
+    gamma_k: float = 0.0
+    omega_s: float = 0.1
+    threshold: float = 1e-6
+    killing_clamp: float = 0.1
+    use_data: bool = True
+    use_levelset: bool = True
+    use_killing: bool = True
+    early_exit: bool = False
+
+    @staticmethod
+    def reference(voxel_size: float = 0.012, trunc_voxels: float = 4.0) -> "Params":
+        """The reference's compiled-in weights, with a chosen voxel/band."""
+        t = voxel_size * trunc_voxels
+        return Params(voxel_size=voxel_size, unknown_clip=t, max_surface=t)
+
+    @staticmethod
+    def paper(voxel_size: float, trunc_voxels: float = 5.0) -> "Params":
+        t = voxel_size * trunc_voxels
+        return Params(voxel_size=voxel_size, unknown_clip=t, max_surface=t, alpha=0.1,
+                      omega_k=0.5, gamma_k=0.1, omega_s=0.2)
+
+    def with_(self, **kw) -> "Params":
+        return replace(self, **kw)
+
+    def c(self) -> _Params:
+        d = asdict(self)
+        return _Params(**{k: (int(v) if isinstance(v, bool) else v) for k, v in d.items()})
+
+
+_vp = C.c_void_p
+_ip3 = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+_PP = C.POINTER(_Params)
+
+# name -> (restype, argtypes); the full ABI of include/killingfusion.h
+SIGNATURES = {
+    "kf_version": (C.c_int, []),
+    "kf_last_error": (C.c_char_p, []),
+    "kf_params_reference": (None, [_PP]),
+    "kf_params_paper": (None, [_PP, C.c_double, C.c_double]),
+    "kf_mc_case": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "kf_grid_create": (C.c_int, [_ip3, C.c_double, _dp, C.c_double, _PP, C.POINTER(_vp)]),
+    "kf_grid_destroy": (C.c_int, [_vp]),
+    "kf_grid_info": (C.c_int, [_vp, _ip3, _dp, _dp, _dp]),
+    "kf_grid_reset": (C.c_int, [_vp, _PP, _vp]),
+    "kf_grid_upload": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "kf_grid_download": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "kf_grid_device": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp)]),
+    "kf_field_create": (C.c_int, [_ip3, C.c_int, C.POINTER(_vp)]),
+    "kf_field_destroy": (C.c_int, [_vp]),
+    "kf_field_zero": (C.c_int, [_vp, _vp]),
+    "kf_field_upload": (C.c_int, [_vp, _vp, _vp]),
+    "kf_field_download": (C.c_int, [_vp, _vp, _vp]),
+    "kf_field_device": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
+    "kf_integrate_depth": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _dp, _dp, C.c_double,
+                                     C.c_double, _vp]),
+    "kf_psi_solve": (C.c_int, [_vp, _vp, _vp, _PP, C.c_int, C.c_int, C.POINTER(SolveStats), _vp]),
+    "kf_psi_gradient_ref": (C.c_int, [_vp, _vp, _vp, _PP, _vp, C.c_int, _vp, _vp, _vp]),
+    "kf_warp": (C.c_int, [_vp, _vp, _PP, _vp]),
+    "kf_fuse": (C.c_int, [_vp, _vp, _vp]),
+    "kf_warp_fuse": (C.c_int, [_vp, _vp, _vp, _PP, _vp]),
+    "kf_fuse_warped": (C.c_int, [_vp, _vp, _vp, _PP, _vp]),
+    "kf_marching_cubes": (C.c_int, [_vp, _PP, _vp, C.c_int64, C.POINTER(C.c_int64), _vp]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the in-tree library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("%s is missing: run __graft_entry__.build() (or python -m "
+                              "killingfusion_gb300._build) first" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int):
+    if status != KF_OK:
+        msg = load().kf_last_error().decode()
+        if status == KF_ERR_DIVERGED:
+            raise DivergedError(status, msg)
+        raise KFError(status, msg)
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        return None
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+def _i3(v):
+    return (C.c_int * 3)(*[int(x) for x in v])
+
+
+def _d(v):
+    v = list(v)
+    return (C.c_double * len(v))(*[float(x) for x in v])
+
+
+class Grid:
+    """An SDF grid (class SDF): float32 phi + int32 weights on the device."""
+
+    def __init__(self, dims, voxel_size: float, origin, unknown_clip: float, params: Params):
+        L = load()
+        self.dims = tuple(int(d) for d in dims)  # (nx, ny, nz)
+        self.shape = self.dims[::-1]
+        self.voxel_size = float(voxel_size)
+        self.origin = np.asarray(origin, dtype=np.float64)
+        h = _vp()
+        check(L.kf_grid_create(_i3(self.dims), voxel_size, _d(self.origin), unknown_clip,
+                               C.byref(params.c()), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().kf_grid_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def upload(self, phi=None, weight=None, stream=None):
+        p = np.ascontiguousarray(phi, dtype=np.float32) if phi is not None else None
+        w = np.ascontiguousarray(weight, dtype=np.int32) if weight is not None else None
+        if p is not None:
+            assert p.size == np.prod(self.dims)
+        check(load().kf_grid_upload(self.h, p.ctypes.data if p is not None else None,
+                                    w.ctypes.data if w is not None else None, _stream(stream)))
+
+    def download(self, stream=None):
+        phi = np.empty(self.shape, dtype=np.float32)
+        w = np.empty(self.shape, dtype=np.int32)
+        check(load().kf_grid_download(self.h, phi.ctypes.data, w.ctypes.data, _stream(stream)))
+        return phi, w
+
+    def reset(self, params: Params, stream=None):
+        check(load().kf_grid_reset(self.h, C.byref(params.c()), _stream(stream)))
+
+    def device_ptrs(self):
+        p, w = _vp(), _vp()
+        check(load().kf_grid_device(self.h, C.byref(p), C.byref(w)))
+        return p.value, w.value
+
+    def integrate(self, depth, c2w=None, K=None, min_depth=0.05, max_depth=1.2, stream=None):
+        """SDF::integrateDepthFrame; depth: numpy float32 [h, w] or a CUDA tensor."""
+        from . import synth
+        c2w = np.eye(4) if c2w is None else np.asarray(c2w, dtype=np.float64)
+        K = synth.K if K is None else np.asarray(K, dtype=np.float64)
+        if isinstance(depth, np.ndarray):
+            d = np.ascontiguousarray(depth, dtype=np.float32)
+            ptr, (hh, ww) = d.ctypes.data, d.shape
+        else:
+            ptr, (hh, ww) = depth.data_ptr(), tuple(depth.shape)
+        check(load().kf_integrate_depth(self.h, ptr, ww, hh, _d(c2w.ravel()), _d(K.ravel()),
+                                        min_depth, max_depth, _stream(stream)))
+
+
+class Field:
+    """A displacement field psi (class DisplacementField)."""
+
+    def __init__(self, dims, precision: int = KF_F32):
+        L = load()
+        self.dims = tuple(int(d) for d in dims)
+        self.shape = self.dims[::-1]
+        self.precision = precision
+        self.dtype = np.float32 if precision == KF_F32 else np.float64
+        h = _vp()
+        check(L.kf_field_create(_i3(self.dims), precision, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().kf_field_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def zero(self, stream=None):
+        check(load().kf_field_zero(self.h, _stream(stream)))
+
+    def upload(self, psi, stream=None):
+        a = np.ascontiguousarray(psi, dtype=self.dtype)
+        assert a.shape == self.shape + (3,)
+        check(load().kf_field_upload(self.h, a.ctypes.data, _stream(stream)))
+
+    def download(self, stream=None):
+        a = np.empty(self.shape + (3,), dtype=self.dtype)
+        check(load().kf_field_download(self.h, a.ctypes.data, _stream(stream)))
+        return a
+
+
+def psi_solve(live: Grid, can: Grid, psi: Field, params: Params, iterations: int,
+              solver: str = "fused", stream=None) -> dict:
+    st = SolveStats()
+    check(load().kf_psi_solve(live.h, can.h, psi.h, C.byref(params.c()), int(iterations),
+                              SOLVERS[solver], C.byref(st), _stream(stream)))
+    return st.as_dict()
+
+
+def psi_gradient_ref(live: Grid, can: Grid, psi: Field, params: Params, voxels_xyz):
+    """Reference gradient (KillingFusion::computeEnergyGradient) and band flag
+    at voxels (int [n, 3] of x, y, z)."""
+    import torch
+    v = torch.as_tensor(np.ascontiguousarray(voxels_xyz, dtype=np.int32)).cuda()
+    n = v.shape[0]
+    out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    act = torch.empty((n,), dtype=torch.uint8, device="cuda")
+    check(load().kf_psi_gradient_ref(live.h, can.h, psi.h, C.byref(params.c()), v.data_ptr(),
+                                     n, out.data_ptr(), act.data_ptr(), None))
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), act.cpu().numpy()
+
+
+def warp(g: Grid, psi: Field, params: Params, stream=None):
+    check(load().kf_warp(g.h, psi.h, C.byref(params.c()), _stream(stream)))
+
+
+def fuse(can: Grid, other: Grid, stream=None):
+    check(load().kf_fuse(can.h, other.h, _stream(stream)))
+
+
+def warp_fuse(can: Grid, live: Grid, psi: Field, params: Params, stream=None):
+    check(load().kf_warp_fuse(can.h, live.h, psi.h, C.byref(params.c()), _stream(stream)))
+
+
+def fuse_warped(dst: Grid, other: Grid, psi: Field, params: Params, stream=None):
+    check(load().kf_fuse_warped(dst.h, other.h, psi.h, C.byref(params.c()), _stream(stream)))
+
+
+def marching_cubes(g: Grid, params: Params):
+    """SDF::getMesh as float32 [T, 3, 3] (numpy)."""
+    import torch
+    L = load()
+    n = C.c_int64(0)
+    check(L.kf_marching_cubes(g.h, C.byref(params.c()), None, 0, C.byref(n), None))
+    t = torch.empty((max(n.value, 1), 9), dtype=torch.float32, device="cuda")
+    check(L.kf_marching_cubes(g.h, C.byref(params.c()), t.data_ptr(), n.value, C.byref(n), None))
+    torch.cuda.synchronize()
+    return t[: n.value].cpu().numpy().reshape(-1, 3, 3)
+
+
+def mc_case(cube: int):
+    em = C.c_int(0)
+    row = (C.c_int * 16)()
+    check(load().kf_mc_case(cube, C.byref(em), row))
+    return em.value, list(row)

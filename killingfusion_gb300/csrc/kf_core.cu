@@ -1,0 +1,632 @@
+// Library core: error state, parameters, grid and field handles, and the
+// host side of the hot-path entry points declared in include/killingfusion.h.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+
+#include "kf_internal.h"
+#include "kf_mc_tables.h"
+
+// ---------------------------------------------------------------------------
+// error state
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+int kf_fail(int status, const std::string &msg) {
+  g_last_error = msg;
+  return status;
+}
+
+int kf_cuda_fail(cudaError_t e, const char *what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return e == cudaErrorMemoryAllocation ? KF_ERR_OOM : KF_ERR_CUDA;
+}
+
+extern "C" int kf_version(void) { return KF_ABI_VERSION; }
+
+extern "C" const char *kf_last_error(void) { return g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------
+// parameters
+// ---------------------------------------------------------------------------
+extern "C" void kf_params_reference(kf_params *p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->voxel_size = 0.012;
+  p->unknown_clip = 0.012 * 4;
+  p->max_surface = 0.012 * 4;
+  p->epsilon = 0.00001;
+  p->delta_size = 0.05;
+  p->alpha = 0.025;
+  p->omega_k = 0.04;
+  p->gamma_k = 0.0;
+  p->omega_s = 0.1;
+  p->threshold = 0.000001;
+  p->killing_clamp = 0.1;
+  p->use_data = p->use_levelset = p->use_killing = 1;
+  p->early_exit = 0;
+}
+
+extern "C" void kf_params_paper(kf_params *p, double voxel_size, double trunc_voxels) {
+  kf_params_reference(p);
+  if (!p) return;
+  p->voxel_size = voxel_size;
+  p->unknown_clip = voxel_size * trunc_voxels;
+  p->max_surface = voxel_size * trunc_voxels;
+  p->alpha = 0.1;
+  p->omega_k = 0.5;
+  p->gamma_k = 0.1;
+  p->omega_s = 0.2;
+}
+
+int kf_check_params(const kf_params *p) {
+  KF_REQUIRE(p, "params is NULL");
+  KF_REQUIRE(p->voxel_size > 0 && isfinite(p->voxel_size), "voxel_size must be > 0");
+  KF_REQUIRE(p->delta_size > 0 && p->delta_size < 0.25, "delta_size must lie in (0, 0.25)");
+  KF_REQUIRE(isfinite(p->unknown_clip) && isfinite(p->max_surface) && isfinite(p->epsilon),
+             "non-finite band parameters");
+  KF_REQUIRE(p->killing_clamp > 0, "killing_clamp must be > 0");
+  return KF_OK;
+}
+
+// Largest float <= v and smallest float >= v.
+static float float_down(double v) {
+  float f = (float)v;
+  if ((double)f > v) f = nextafterf(f, -INFINITY);
+  return f;
+}
+static float float_up(double v) {
+  float f = (float)v;
+  if ((double)f < v) f = nextafterf(f, INFINITY);
+  return f;
+}
+
+DevParams kf_make_dev_params(const int n[3], const kf_params *p) {
+  DevParams d;
+  memset(&d, 0, sizeof(d));
+  d.nx = n[0];
+  d.ny = n[1];
+  d.nz = n[2];
+  d.count = (int64_t)n[0] * n[1] * n[2];
+  d.voxel_size = p->voxel_size;
+  d.unknown_clip = p->unknown_clip;
+  d.max_surface = p->max_surface;
+  d.epsilon = p->epsilon;
+  d.delta_size = p->delta_size;
+  d.alpha = p->alpha;
+  d.omega_k = p->omega_k;
+  d.gamma_k = p->gamma_k;
+  d.omega_s = p->omega_s;
+  d.killing_clamp = p->killing_clamp;
+  d.oob_phi = p->max_surface + p->epsilon;
+  d.band_hi = p->max_surface - p->epsilon;
+  d.band_hi_f = float_down(d.band_hi);
+  d.band_lo_f = float_up(-p->unknown_clip);
+  d.mc_hi_f = float_down(p->max_surface);
+  d.oob_phi_f = (float)d.oob_phi;
+  d.use_data = p->use_data;
+  d.use_levelset = p->use_levelset;
+  d.use_killing = p->use_killing;
+  d.early_exit = p->early_exit;
+  d.threshold = p->threshold;
+  return d;
+}
+
+int kf_num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+extern "C" int kf_mc_case(int cube, int *edge_mask, int tri_edges[16]) {
+  KF_REQUIRE(cube >= 0 && cube < 256, "cube index out of range");
+  if (edge_mask) *edge_mask = kf_mc_edge_mask_host(cube);
+  if (tri_edges) kf_mc_tri_row_host(cube, tri_edges);
+  return KF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// grids
+// ---------------------------------------------------------------------------
+static bool dims_ok(const int n[3]) {
+  if (!n) return false;
+  for (int k = 0; k < 3; ++k)
+    if (n[k] <= 0) return false;
+  // the reference indexes with int (DisplacementField.cpp:24-34)
+  return (int64_t)n[0] * n[1] * n[2] < (int64_t)INT32_MAX;
+}
+
+__global__ void k_fill(float *phi, int32_t *w, int64_t n, float v) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    phi[i] = v;
+    w[i] = 0;
+  }
+}
+
+extern "C" int kf_grid_reset(kf_grid g, const kf_params *p, void *stream) {
+  KF_REQUIRE(g, "grid is NULL");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  float v = (float)(p->max_surface + p->epsilon);
+  k_fill<<<(unsigned)((g->count + 255) / 256), 256, 0, kf_stream(stream)>>>(g->phi, g->w, g->count, v);
+  KF_CHECK_LAUNCH("k_fill");
+  return KF_OK;
+}
+
+extern "C" int kf_grid_create(const int dims[3], double voxel_size, const double min3d[3],
+                              double unknown_clip, const kf_params *p, kf_grid *out) {
+  KF_REQUIRE(out, "out is NULL");
+  *out = nullptr;
+  KF_REQUIRE(dims_ok(dims), "grid dims must be positive with fewer than 2^31 voxels");
+  KF_REQUIRE(voxel_size > 0, "voxel_size must be > 0");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  kf_grid g = new kf_grid_s();
+  memset(g, 0, sizeof(*g));
+  for (int k = 0; k < 3; ++k) {
+    g->n[k] = dims[k];
+    g->min3d[k] = min3d ? min3d[k] : 0.0;
+  }
+  g->count = (int64_t)dims[0] * dims[1] * dims[2];
+  g->voxel = voxel_size;
+  g->unknown_clip = unknown_clip;
+  if (cudaMalloc(&g->phi, g->count * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&g->w, g->count * sizeof(int32_t)) != cudaSuccess) {
+    cudaGetLastError();
+    kf_grid_destroy(g);
+    return kf_fail(KF_ERR_OOM, "cudaMalloc of the SDF grid failed");
+  }
+  rc = kf_grid_reset(g, p, nullptr);
+  if (rc) {
+    kf_grid_destroy(g);
+    return rc;
+  }
+  *out = g;
+  return KF_OK;
+}
+
+extern "C" int kf_grid_destroy(kf_grid g) {
+  if (!g) return KF_OK;
+  cudaFree(g->phi);
+  cudaFree(g->w);
+  cudaFree(g->phi_alt);
+  cudaFree(g->w_alt);
+  cudaFree(g->depth);
+  delete g;
+  return KF_OK;
+}
+
+extern "C" int kf_grid_info(kf_grid g, int dims[3], double *voxel_size, double min3d[3],
+                            double *unknown_clip) {
+  KF_REQUIRE(g, "grid is NULL");
+  for (int k = 0; k < 3; ++k) {
+    if (dims) dims[k] = g->n[k];
+    if (min3d) min3d[k] = g->min3d[k];
+  }
+  if (voxel_size) *voxel_size = g->voxel;
+  if (unknown_clip) *unknown_clip = g->unknown_clip;
+  return KF_OK;
+}
+
+extern "C" int kf_grid_upload(kf_grid g, const float *phi, const int32_t *weight, void *stream) {
+  KF_REQUIRE(g, "grid is NULL");
+  cudaStream_t s = kf_stream(stream);
+  if (phi) KF_CHECK_CUDA(cudaMemcpyAsync(g->phi, phi, g->count * sizeof(float), cudaMemcpyDefault, s));
+  if (weight)
+    KF_CHECK_CUDA(cudaMemcpyAsync(g->w, weight, g->count * sizeof(int32_t), cudaMemcpyDefault, s));
+  KF_CHECK_CUDA(cudaStreamSynchronize(s));
+  return KF_OK;
+}
+
+extern "C" int kf_grid_download(kf_grid g, float *phi, int32_t *weight, void *stream) {
+  KF_REQUIRE(g, "grid is NULL");
+  cudaStream_t s = kf_stream(stream);
+  if (phi) KF_CHECK_CUDA(cudaMemcpyAsync(phi, g->phi, g->count * sizeof(float), cudaMemcpyDefault, s));
+  if (weight)
+    KF_CHECK_CUDA(cudaMemcpyAsync(weight, g->w, g->count * sizeof(int32_t), cudaMemcpyDefault, s));
+  KF_CHECK_CUDA(cudaStreamSynchronize(s));
+  return KF_OK;
+}
+
+extern "C" int kf_grid_device(kf_grid g, float **phi, int32_t **weight) {
+  KF_REQUIRE(g, "grid is NULL");
+  if (phi) *phi = g->phi;
+  if (weight) *weight = g->w;
+  return KF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// displacement fields
+// ---------------------------------------------------------------------------
+size_t kf_prec_size(kf_precision p) { return p == KF_F64 ? sizeof(double) : sizeof(float); }
+
+extern "C" int kf_field_destroy(kf_field f) {
+  if (!f) return KF_OK;
+  for (int k = 0; k < 3; ++k) {
+    cudaFree(f->p[k]);
+    cudaFree(f->q[k]);
+  }
+  kf_field_release_solver(f);
+  delete f;
+  return KF_OK;
+}
+
+extern "C" int kf_field_create(const int dims[3], kf_precision prec, kf_field *out) {
+  KF_REQUIRE(out, "out is NULL");
+  *out = nullptr;
+  KF_REQUIRE(dims_ok(dims), "field dims must be positive with fewer than 2^31 voxels");
+  KF_REQUIRE(prec == KF_F32 || prec == KF_F64, "unknown precision");
+  kf_field f = new kf_field_s();
+  memset(f, 0, sizeof(*f));
+  for (int k = 0; k < 3; ++k) f->n[k] = dims[k];
+  f->count = (int64_t)dims[0] * dims[1] * dims[2];
+  f->prec = prec;
+  for (int k = 0; k < 3; ++k) {
+    if (cudaMalloc(&f->p[k], f->count * kf_prec_size(prec)) != cudaSuccess) {
+      cudaGetLastError();
+      kf_field_destroy(f);
+      return kf_fail(KF_ERR_OOM, "cudaMalloc of the displacement field failed");
+    }
+  }
+  int rc = kf_field_zero(f, nullptr);
+  if (rc) {
+    kf_field_destroy(f);
+    return rc;
+  }
+  KF_CHECK_CUDA(cudaDeviceSynchronize());
+  *out = f;
+  return KF_OK;
+}
+
+int kf_field_stats(kf_field f, int iterations, IterStats **dev) {
+  if (f->stats_cap < iterations) {
+    cudaFree(f->stats);
+    cudaFreeHost(f->stats_host);
+    f->stats = nullptr;
+    f->stats_host = nullptr;
+    f->stats_cap = 0;
+    int cap = iterations < 64 ? 64 : iterations;
+    if (cudaMalloc(&f->stats, sizeof(IterStats) * cap) != cudaSuccess ||
+        cudaMallocHost(&f->stats_host, sizeof(IterStats) * cap) != cudaSuccess) {
+      cudaGetLastError();
+      return kf_fail(KF_ERR_OOM, "allocation of the solver statistics failed");
+    }
+    f->stats_cap = cap;
+  }
+  *dev = f->stats;
+  return KF_OK;
+}
+
+int kf_field_band_list(kf_field f, int **out) {
+  if (!f->band && cudaMalloc(&f->band, f->count * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    f->band = nullptr;
+    return kf_fail(KF_ERR_OOM, "cudaMalloc of the band voxel list failed");
+  }
+  *out = f->band;
+  return KF_OK;
+}
+
+void kf_field_release_solver(kf_field f) {
+  cudaFree(f->band);
+  f->band = nullptr;
+  cudaFree(f->stats);
+  cudaFreeHost(f->stats_host);
+  cudaFree(f->plain_scratch);
+  kf_fused_graph_destroy(f->graph);
+  f->stats = nullptr;
+  f->stats_host = nullptr;
+  f->plain_scratch = nullptr;
+  f->graph = nullptr;
+  f->stats_cap = 0;
+  f->plain_bytes = 0;
+}
+
+int kf_field_ensure_pair(kf_field f) {
+  if (f->q[0]) return KF_OK;
+  for (int k = 0; k < 3; ++k)
+    if (cudaMalloc(&f->q[k], f->count * kf_prec_size(f->prec)) != cudaSuccess) {
+      cudaGetLastError();
+      for (int j = 0; j < 3; ++j) {
+        cudaFree(f->q[j]);
+        f->q[j] = nullptr;
+      }
+      return kf_fail(KF_ERR_OOM, "cudaMalloc of the displacement ping-pong buffer failed");
+    }
+  return KF_OK;
+}
+
+extern "C" int kf_field_zero(kf_field f, void *stream) {
+  KF_REQUIRE(f, "field is NULL");
+  for (int k = 0; k < 3; ++k)
+    KF_CHECK_CUDA(cudaMemsetAsync(f->p[k], 0, f->count * kf_prec_size(f->prec), kf_stream(stream)));
+  return KF_OK;
+}
+
+template <typename T>
+__global__ void k_aos_to_soa(const T *__restrict__ aos, T *x, T *y, T *z, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    x[i] = aos[3 * i];
+    y[i] = aos[3 * i + 1];
+    z[i] = aos[3 * i + 2];
+  }
+}
+template <typename T>
+__global__ void k_soa_to_aos(T *__restrict__ aos, const T *x, const T *y, const T *z, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    aos[3 * i] = x[i];
+    aos[3 * i + 1] = y[i];
+    aos[3 * i + 2] = z[i];
+  }
+}
+
+static int field_copy(kf_field f, void *xyz, bool upload, cudaStream_t s) {
+  size_t bytes = 3 * f->count * kf_prec_size(f->prec);
+  void *tmp = nullptr;
+  KF_CHECK_CUDA(cudaMallocAsync(&tmp, bytes, s));
+  unsigned nb = (unsigned)((f->count + 255) / 256);
+  if (upload) {
+    KF_CHECK_CUDA(cudaMemcpyAsync(tmp, xyz, bytes, cudaMemcpyDefault, s));
+    if (f->prec == KF_F32)
+      k_aos_to_soa<float><<<nb, 256, 0, s>>>((const float *)tmp, (float *)f->p[0], (float *)f->p[1],
+                                              (float *)f->p[2], f->count);
+    else
+      k_aos_to_soa<double><<<nb, 256, 0, s>>>((const double *)tmp, (double *)f->p[0],
+                                               (double *)f->p[1], (double *)f->p[2], f->count);
+  } else {
+    if (f->prec == KF_F32)
+      k_soa_to_aos<float><<<nb, 256, 0, s>>>((float *)tmp, (const float *)f->p[0],
+                                              (const float *)f->p[1], (const float *)f->p[2], f->count);
+    else
+      k_soa_to_aos<double><<<nb, 256, 0, s>>>((double *)tmp, (const double *)f->p[0],
+                                               (const double *)f->p[1], (const double *)f->p[2],
+                                               f->count);
+    KF_CHECK_CUDA(cudaMemcpyAsync(xyz, tmp, bytes, cudaMemcpyDefault, s));
+  }
+  KF_CHECK_LAUNCH("field layout conversion");
+  KF_CHECK_CUDA(cudaFreeAsync(tmp, s));
+  KF_CHECK_CUDA(cudaStreamSynchronize(s));
+  return KF_OK;
+}
+
+extern "C" int kf_field_upload(kf_field f, const void *xyz, void *stream) {
+  KF_REQUIRE(f && xyz, "field or buffer is NULL");
+  return field_copy(f, const_cast<void *>(xyz), true, kf_stream(stream));
+}
+
+extern "C" int kf_field_download(kf_field f, void *xyz, void *stream) {
+  KF_REQUIRE(f && xyz, "field or buffer is NULL");
+  return field_copy(f, xyz, false, kf_stream(stream));
+}
+
+extern "C" int kf_field_device(kf_field f, void **px, void **py, void **pz) {
+  KF_REQUIRE(f, "field is NULL");
+  if (px) *px = f->p[0];
+  if (py) *py = f->p[1];
+  if (pz) *pz = f->p[2];
+  return KF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// hot path
+// ---------------------------------------------------------------------------
+static bool same_dims(const int a[3], const int b[3]) {
+  return a[0] == b[0] && a[1] == b[1] && a[2] == b[2];
+}
+
+// Gauss-Jordan inverse with partial pivoting of a row-major 4x4 matrix.
+static bool invert4(const double m[16], double out[16]) {
+  double a[4][8];
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 8; ++c) a[r][c] = c < 4 ? m[4 * r + c] : (c - 4 == r ? 1.0 : 0.0);
+  for (int c = 0; c < 4; ++c) {
+    int p = c;
+    for (int r = c + 1; r < 4; ++r)
+      if (fabs(a[r][c]) > fabs(a[p][c])) p = r;
+    if (a[p][c] == 0.0) return false;
+    if (p != c)
+      for (int k = 0; k < 8; ++k) {
+        double t = a[c][k];
+        a[c][k] = a[p][k];
+        a[p][k] = t;
+      }
+    double piv = a[c][c];
+    for (int k = 0; k < 8; ++k) a[c][k] = a[c][k] / piv;
+    for (int r = 0; r < 4; ++r) {
+      if (r == c) continue;
+      double f = a[r][c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < 8; ++k) a[r][k] = a[r][k] - f * a[c][k];
+    }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) out[4 * r + c] = a[r][c + 4];
+  return true;
+}
+
+extern "C" int kf_integrate_depth(kf_grid g, const float *depth, int width, int height,
+                                  const double c2w[16], const double K[9], double min_depth,
+                                  double max_depth, void *stream) {
+  KF_REQUIRE(g && depth && c2w && K, "NULL argument");
+  KF_REQUIRE(width > 0 && height > 0, "depth frame size must be positive");
+  cudaStream_t s = kf_stream(stream);
+  double w2c[16];
+  KF_REQUIRE(invert4(c2w, w2c), "camera pose is singular");
+  cudaPointerAttributes attr;
+  const float *dev = depth;
+  if (cudaPointerGetAttributes(&attr, depth) != cudaSuccess || attr.type == cudaMemoryTypeUnregistered ||
+      attr.type == cudaMemoryTypeHost) {
+    cudaGetLastError();
+    size_t bytes = (size_t)width * height * sizeof(float);
+    if (g->depth_cap < bytes) {
+      cudaFree(g->depth);
+      g->depth = nullptr;
+      g->depth_cap = 0;
+      if (cudaMalloc(&g->depth, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return kf_fail(KF_ERR_OOM, "cudaMalloc of the depth staging buffer failed");
+      }
+      g->depth_cap = bytes;
+    }
+    KF_CHECK_CUDA(cudaMemcpyAsync(g->depth, depth, bytes, cudaMemcpyHostToDevice, s));
+    dev = g->depth;
+  }
+  return kf_launch_integrate(g, dev, width, height, w2c, K, min_depth, max_depth, s);
+}
+
+extern "C" int kf_warp(kf_grid g, kf_field psi, const kf_params *p, void *stream) {
+  KF_REQUIRE(g && psi, "NULL argument");
+  KF_REQUIRE(same_dims(g->n, psi->n), "grid and field sizes differ");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  DevParams dp = kf_make_dev_params(g->n, p);
+  return kf_launch_warp(g, psi, dp, kf_stream(stream));
+}
+
+extern "C" int kf_fuse(kf_grid canonical, kf_grid other, void *stream) {
+  KF_REQUIRE(canonical && other, "NULL argument");
+  KF_REQUIRE(same_dims(canonical->n, other->n), "grid sizes differ");
+  return kf_launch_fuse(canonical, other, kf_stream(stream));
+}
+
+extern "C" int kf_warp_fuse(kf_grid canonical, kf_grid live, kf_field psi, const kf_params *p,
+                            void *stream) {
+  KF_REQUIRE(canonical && live && psi, "NULL argument");
+  KF_REQUIRE(canonical != live, "canonical and live must differ");
+  KF_REQUIRE(same_dims(canonical->n, live->n) && same_dims(live->n, psi->n), "sizes differ");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  DevParams dp = kf_make_dev_params(live->n, p);
+  return kf_launch_warp_fuse(canonical, live, psi, dp, kf_stream(stream));
+}
+
+extern "C" int kf_fuse_warped(kf_grid dst, kf_grid other, kf_field psi, const kf_params *p,
+                              void *stream) {
+  KF_REQUIRE(dst && other && psi, "NULL argument");
+  KF_REQUIRE(dst != other, "dst and other must differ");
+  KF_REQUIRE(same_dims(dst->n, other->n) && same_dims(dst->n, psi->n), "sizes differ");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  DevParams dp = kf_make_dev_params(dst->n, p);
+  return kf_launch_fuse_warped(dst, other, psi, dp, kf_stream(stream));
+}
+
+extern "C" int kf_psi_gradient_ref(kf_grid live, kf_grid canonical, kf_field psi,
+                                   const kf_params *p, const int32_t *voxels, int count,
+                                   double *out, uint8_t *active, void *stream) {
+  KF_REQUIRE(live && canonical && psi && out && (voxels || count == 0), "NULL argument");
+  KF_REQUIRE(count >= 0, "count must be >= 0");
+  KF_REQUIRE(same_dims(live->n, canonical->n) && same_dims(live->n, psi->n), "sizes differ");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  DevParams dp = kf_make_dev_params(live->n, p);
+  return kf_gradient_ref_launch(live, canonical, psi, dp, voxels, count, out, active,
+                                kf_stream(stream));
+}
+
+extern "C" int kf_marching_cubes(kf_grid g, const kf_params *p, float *verts, int64_t capacity,
+                                 int64_t *ntri, void *stream) {
+  KF_REQUIRE(g && ntri, "NULL argument");
+  KF_REQUIRE(capacity >= 0, "capacity must be >= 0");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  DevParams dp = kf_make_dev_params(g->n, p);
+  return kf_mc_run(g, dp, verts, capacity, ntri, kf_stream(stream));
+}
+
+// ---------------------------------------------------------------------------
+// psi solve
+// ---------------------------------------------------------------------------
+extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
+                            int iterations, kf_solver solver, kf_solve_stats *stats,
+                            void *stream) {
+  KF_REQUIRE(live && canonical && psi, "NULL argument");
+  KF_REQUIRE(live != canonical, "live and canonical must differ");
+  KF_REQUIRE(same_dims(live->n, canonical->n) && same_dims(live->n, psi->n), "sizes differ");
+  KF_REQUIRE(iterations >= 0, "iterations must be >= 0");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  KF_REQUIRE(solver == KF_SOLVER_FUSED || solver == KF_SOLVER_PLAIN || solver == KF_SOLVER_EXACT,
+             "unknown solver");
+  KF_REQUIRE((solver == KF_SOLVER_EXACT) == (psi->prec == KF_F64),
+             "KF_SOLVER_EXACT runs on KF_F64 fields and the other solvers on KF_F32 fields");
+  if (stats) memset(stats, 0, sizeof(*stats));
+  if (iterations == 0) return KF_OK;
+  cudaStream_t s = kf_stream(stream);
+  DevParams dp = kf_make_dev_params(live->n, p);
+  IterStats *st = nullptr;
+  rc = kf_field_stats(psi, iterations, &st);
+  if (rc) return rc;
+  KF_CHECK_CUDA(cudaMemsetAsync(st, 0, sizeof(IterStats) * iterations, s));
+  cudaEvent_t e0, e1;
+  KF_CHECK_CUDA(cudaEventCreate(&e0));
+  KF_CHECK_CUDA(cudaEventCreate(&e1));
+  KF_CHECK_CUDA(cudaEventRecord(e0, s));
+  if (solver == KF_SOLVER_FUSED)
+    rc = kf_solve_fused(live, canonical, psi, dp, iterations, st, s);
+  else if (solver == KF_SOLVER_PLAIN)
+    rc = kf_solve_plain(live, canonical, psi, dp, iterations, st, s);
+  else
+    rc = kf_solve_exact(live, canonical, psi, dp, iterations, st, s);
+  if (rc) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
+  KF_CHECK_CUDA(cudaEventRecord(e1, s));
+  IterStats *host = psi->stats_host;
+  KF_CHECK_CUDA(cudaMemcpyAsync(host, st, sizeof(IterStats) * iterations, cudaMemcpyDeviceToHost, s));
+  KF_CHECK_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  int executed = 0;
+  int diverged = 0;
+  for (int k = 0; k < iterations; ++k) {
+    if (host[k].skipped) break;
+    ++executed;
+    if (host[k].diverged) {
+      diverged = 1;
+      break;
+    }
+  }
+  // Iteration k reads buffer k%2 and writes (k+1)%2; a diverged iteration
+  // still wrote its output.  Put the result into the primary planes.
+  if (executed & 1)
+    for (int k = 0; k < 3; ++k) {
+      void *t = psi->p[k];
+      psi->p[k] = psi->q[k];
+      psi->q[k] = t;
+    }
+  if (stats) {
+    stats->iterations_run = executed;
+    stats->converged = (!diverged && executed < iterations) ? 1 : 0;
+    stats->diverged = diverged;
+    if (executed > 0) {
+      stats->active_first = host[0].active;
+      stats->active_last = host[executed - 1].active;
+      stats->energy_first = host[0].energy;
+      stats->energy_last = host[executed - 1].energy;
+      float md;
+      unsigned bits = host[executed - 1].max_delta;
+      memcpy(&md, &bits, sizeof(md));
+      stats->max_delta_last = md;
+    }
+    stats->device_ms = ms;
+  }
+  if (diverged)
+    return kf_fail(KF_ERR_DIVERGED, "deformation field diverged (non-finite psi inside the band)");
+  return KF_OK;
+}

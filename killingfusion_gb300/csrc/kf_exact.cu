@@ -1,0 +1,419 @@
+// Kernels whose outcome hinges on the reference's double-precision rounding.
+//
+// This translation unit is compiled with -fmad=false: no multiply-add is
+// fused, so every float64 expression rounds exactly as the reference's
+// (compiled with -ffp-contract=off) does.  It holds
+//   - projective integration (the pixel a voxel projects to is decided by a
+//     rounding of a double, SDF.cpp:162-172),
+//   - the warp / fuse family (the warped weight is a truncation of an
+//     interpolated double, SDF.cpp:316-320),
+//   - the float64 psi solver that replays the reference bit for bit, and the
+//     per-voxel reference-gradient query.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "kf_internal.h"
+#include "kf_ref_math.cuh"
+
+using namespace kfref;
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline unsigned blocks_for(int64_t n, int per = kBlock) {
+  return (unsigned)((n + per - 1) / per);
+}
+
+__device__ __forceinline__ void voxel_xyz(int64_t i, int nx, int ny, int &x, int &y, int &z) {
+  int64_t plane = (int64_t)nx * ny;
+  z = (int)(i / plane);
+  int64_t r = i - (int64_t)z * plane;
+  y = (int)(r / nx);
+  x = (int)(r - (int64_t)y * nx);
+}
+
+// ---------------------------------------------------------------------------
+// SDF::integrateDepthFrame (SDF.cpp:137-197)
+// ---------------------------------------------------------------------------
+struct IntegrateArgs {
+  double W[16];  // world -> camera, row-major
+  double K[9];   // intrinsics, row-major
+  double voxel, min0, min1, min2, unknown_clip, min_depth, max_depth;
+  int width, height;
+};
+
+__global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, int32_t *__restrict__ w,
+                                                      int nx, int ny, int nz,
+                                                      const float *__restrict__ depth,
+                                                      IntegrateArgs a) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nx * ny * nz) return;
+  int x, y, z;
+  voxel_xyz(i, nx, ny, x, y, z);
+  double Z = a.voxel * ((double)z + 0.5) + a.min2;
+  double Y = a.voxel * ((double)y + 0.5) + a.min1;
+  double X = a.voxel * ((double)x + 0.5) + a.min0;
+  double c[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    c[r] = a.W[4 * r + 0] * X + a.W[4 * r + 1] * Y + a.W[4 * r + 2] * Z + a.W[4 * r + 3] * 1.0;
+  double pa = c[0] / c[2], pb = c[1] / c[2];
+  double u = a.K[0] * pa + a.K[1] * pb + a.K[2] * 1.0;
+  double v = a.K[3] * pa + a.K[4] * pb + a.K[5] * 1.0;
+  // roundf of the double converted to float (SDF.cpp:167,171); a non-finite
+  // value never lands inside the image (x86-64 converts it to INT_MIN).
+  float fu = (float)(u + 0.5);
+  if (!isfinite(fu)) return;
+  int col = (int)roundf(fu);
+  if (col < 0 || col >= a.width) return;
+  float fv = (float)(v + 0.5);
+  if (!isfinite(fv)) return;
+  int row = (int)roundf(fv);
+  if (row < 0 || row >= a.height) return;
+  double d = (double)depth[(int64_t)row * a.width + col];
+  if (d < a.min_depth || d > a.max_depth) return;
+  double dist = d - c[2];
+  if (dist < -a.unknown_clip) return;
+  int32_t wi = w[i];
+  phi[i] = (float)(((double)phi[i] * (double)wi + dist) / (double)(wi + 1));
+  w[i] = wi + 1;
+}
+
+// ---------------------------------------------------------------------------
+// warp / fuse
+// ---------------------------------------------------------------------------
+template <typename P>
+struct PsiPlanes {
+  const P *x, *y, *z;
+};
+
+// Resample (phi, w) of `src` at i+0.5+psi(i) in float64 (SDF::update,
+// SDF.cpp:309-321; SDF::getWeight SDF.cpp:584-604).  A voxel with psi == 0
+// samples exactly its own cell (zero interpolation weights), so it keeps its
+// values without arithmetic.
+template <typename P>
+__device__ __forceinline__ void warp_sample(const float *__restrict__ phi, const int32_t *__restrict__ w,
+                                            int nx, int ny, int nz, double oob, PsiPlanes<P> f,
+                                            int64_t i, int x, int y, int z, double &out_phi,
+                                            double &out_w, bool &moved) {
+  double d0 = (double)f.x[i], d1 = (double)f.y[i], d2 = (double)f.z[i];
+  if (d0 == 0.0 && d1 == 0.0 && d2 == 0.0) {
+    out_phi = (double)phi[i];
+    out_w = (double)w[i];
+    moved = false;
+    return;
+  }
+  moved = true;
+  double l0 = ((double)x + 0.5) + d0, l1 = ((double)y + 0.5) + d1, l2 = ((double)z + 0.5) + d2;
+  double t0 = l0 - 0.5, t1 = l1 - 0.5, t2 = l2 - 0.5;
+  int b0 = (int)t0, b1 = (int)t1, b2 = (int)t2;
+  double vp[8], vw[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    int cx = b0 + (c & 1), cy = b1 + ((c >> 1) & 1), cz = b2 + (c >> 2);
+    bool in = cx >= 0 && cx < nx && cy >= 0 && cy < ny && cz >= 0 && cz < nz;
+    int64_t j = ((int64_t)cz * ny + cy) * nx + cx;
+    vp[c] = in ? (double)phi[j] : oob;
+    vw[c] = in ? (double)w[j] : 0.0;
+  }
+  double f0 = t0 - (double)b0, f1 = t1 - (double)b1, f2 = t2 - (double)b2;
+  out_w = lerp3(vw, f0, f1, f2);
+  out_phi = lerp3(vp, f0, f1, f2);
+}
+
+// SDF::update followed by canonical->fuse(live) (KillingFusion.cpp:158-159,
+// SDF.cpp:199-241, 300-328).  When `can` is null only the warp is done.
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ lphi,
+                                                      const int32_t *__restrict__ lw,
+                                                      float *__restrict__ lphi_out,
+                                                      int32_t *__restrict__ lw_out,
+                                                      float *__restrict__ cphi, int32_t *__restrict__ cw,
+                                                      PsiPlanes<P> f, int nx, int ny, int nz,
+                                                      double oob) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nx * ny * nz) return;
+  int x, y, z;
+  voxel_xyz(i, nx, ny, x, y, z);
+  double dphi, dw;
+  bool moved;
+  warp_sample(lphi, lw, nx, ny, nz, oob, f, i, x, y, z, dphi, dw, moved);
+  float nphi = moved ? (float)dphi : lphi[i];
+  int32_t nw = moved ? (int32_t)(int64_t)dw : lw[i];
+  lphi_out[i] = nphi;
+  lw_out[i] = nw;
+  if (!cphi) return;
+  if (nw == 0) return;
+  int32_t w1 = cw[i];
+  if (w1 == 0) {
+    cphi[i] = nphi;
+    cw[i] = nw;
+  } else {
+    double d1 = (double)cphi[i];
+    cphi[i] = (float)(((double)w1 * d1 + (double)nw * (double)nphi) / (double)(w1 + nw));
+    cw[i] = w1 + nw;
+  }
+}
+
+// SDF::fuse(other) with FUSE_BY_MERGE (SDF.cpp:199-241).
+__global__ void __launch_bounds__(kBlock) k_fuse(float *__restrict__ phi1, int32_t *__restrict__ w1,
+                                                 const float *__restrict__ phi2,
+                                                 const int32_t *__restrict__ w2, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int32_t b = w2[i];
+  if (b == 0) return;
+  int32_t a = w1[i];
+  float d2 = phi2[i];
+  if (a == 0) {
+    phi1[i] = d2;
+    w1[i] = b;
+  } else {
+    double d1 = (double)phi1[i];
+    phi1[i] = (float)(((double)a * d1 + (double)b * (double)d2) / (double)(a + b));
+    w1[i] = a + b;
+  }
+}
+
+// SDF::fuse(other, psi) (SDF.cpp:244-297): the other SDF's weight stays an
+// interpolated double until it is stored.
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_fuse_warped(float *__restrict__ phi1, int32_t *__restrict__ w1,
+                                                        const float *__restrict__ phi2,
+                                                        const int32_t *__restrict__ w2,
+                                                        PsiPlanes<P> f, int nx, int ny, int nz,
+                                                        double oob) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nx * ny * nz) return;
+  int x, y, z;
+  voxel_xyz(i, nx, ny, x, y, z);
+  double d2, b;
+  bool moved;
+  warp_sample(phi2, w2, nx, ny, nz, oob, f, i, x, y, z, d2, b, moved);
+  if (fabs(b) < (double)1e-5f) return;
+  int32_t a = w1[i];
+  if (a == 0) {
+    phi1[i] = (float)d2;
+    w1[i] = (int32_t)(int64_t)b;
+  } else {
+    double d1 = (double)phi1[i];
+    phi1[i] = (float)(((double)a * d1 + b * d2) / ((double)a + b));
+    w1[i] = (int32_t)(int64_t)((double)a + b);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// float64 replay of the Jacobi psi update (KillingFusion.cpp:248-352)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_exact_step(PhiView<double> live, PhiView<double> can,
+                                                       PsiView<double, double> fin,
+                                                       double *__restrict__ ox,
+                                                       double *__restrict__ oy,
+                                                       double *__restrict__ oz, DevParams dp,
+                                                       IterStats *st, int iter) {
+  if (iteration_gated(st, iter, dp)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st[iter].skipped = 1;
+    return;
+  }
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool active = false;
+  double dn = 0.0;
+  if (i < dp.count) {
+    int x, y, z;
+    voxel_xyz(i, dp.nx, dp.ny, x, y, z);
+    double p0 = fin.px[i], p1 = fin.py[i], p2 = fin.pz[i];
+    double s = warped_distance(live, fin, x, y, z);
+    double d[3] = {0.0, 0.0, 0.0};
+    if (in_band(s, dp.band_hi, -dp.unknown_clip)) {
+      active = true;
+      TParams<double> tp(dp);
+      double g[3];
+      energy_gradient(live, can, fin, tp, x, y, z, g);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) d[k] = d[k] + -tp.alpha * g[k];
+      if (!isfinite(p0) || !isfinite(p1) || !isfinite(p2)) st[iter].diverged = 1;
+      dn = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    }
+    ox[i] = p0 + d[0];
+    oy[i] = p1 + d[1];
+    oz[i] = p2 + d[2];
+  }
+  unsigned ballot = __ballot_sync(0xffffffffu, active);
+  float m = (float)dn;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && ballot) {
+    atomicAdd(&st[iter].active, (unsigned)__popc(ballot));
+    atomicMax(&st[iter].max_delta, __float_as_uint(m));
+  }
+}
+
+// Reference gradient at a list of voxels (KillingFusion.cpp:399-442).
+template <typename T, typename P>
+__global__ void k_gradient_ref(PhiView<T> live, PhiView<T> can, PsiView<T, P> f, DevParams dp,
+                               const int32_t *__restrict__ vox, int count, double *__restrict__ out,
+                               uint8_t *__restrict__ active) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  int x = vox[3 * i], y = vox[3 * i + 1], z = vox[3 * i + 2];
+  TParams<T> tp(dp);
+  T g[3];
+  energy_gradient(live, can, f, tp, x, y, z, g);
+  out[3 * i + 0] = (double)g[0];
+  out[3 * i + 1] = (double)g[1];
+  out[3 * i + 2] = (double)g[2];
+  if (active) {
+    T s = warped_distance(live, f, x, y, z);
+    active[i] = in_band(s, band_hi<T>(dp), band_lo<T>(dp)) ? 1 : 0;
+  }
+}
+
+template <typename T>
+PhiView<T> phi_view(const kf_grid g, const float *phi, double oob) {
+  PhiView<T> v;
+  v.phi = phi;
+  v.nx = g->n[0];
+  v.ny = g->n[1];
+  v.nz = g->n[2];
+  v.oob = (T)oob;
+  return v;
+}
+
+}  // namespace
+
+int kf_grid_ensure_alt(kf_grid g) {
+  if (g->phi_alt) return KF_OK;
+  if (cudaMalloc(&g->phi_alt, g->count * sizeof(float)) != cudaSuccess)
+    return kf_fail(KF_ERR_OOM, "cudaMalloc of the resampling buffer failed");
+  if (cudaMalloc(&g->w_alt, g->count * sizeof(int32_t)) != cudaSuccess) {
+    cudaFree(g->phi_alt);
+    g->phi_alt = nullptr;
+    return kf_fail(KF_ERR_OOM, "cudaMalloc of the resampling buffer failed");
+  }
+  return KF_OK;
+}
+
+int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height,
+                        const double w2c[16], const double K[9], double min_depth,
+                        double max_depth, cudaStream_t s) {
+  IntegrateArgs a;
+  for (int k = 0; k < 16; ++k) a.W[k] = w2c[k];
+  for (int k = 0; k < 9; ++k) a.K[k] = K[k];
+  a.voxel = g->voxel;
+  a.min0 = g->min3d[0];
+  a.min1 = g->min3d[1];
+  a.min2 = g->min3d[2];
+  a.unknown_clip = g->unknown_clip;
+  a.min_depth = min_depth;
+  a.max_depth = max_depth;
+  a.width = width;
+  a.height = height;
+  k_integrate<<<blocks_for(g->count), kBlock, 0, s>>>(g->phi, g->w, g->n[0], g->n[1], g->n[2],
+                                                      depth_dev, a);
+  KF_CHECK_LAUNCH("k_integrate");
+  return KF_OK;
+}
+
+template <typename P>
+static PsiPlanes<P> planes(kf_field f) {
+  return PsiPlanes<P>{(const P *)f->p[0], (const P *)f->p[1], (const P *)f->p[2]};
+}
+
+static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevParams &dp,
+                          cudaStream_t s) {
+  int st = kf_grid_ensure_alt(live);
+  if (st) return st;
+  float *cphi = can ? can->phi : nullptr;
+  int32_t *cw = can ? can->w : nullptr;
+  if (psi->prec == KF_F32)
+    k_warp_fuse<float><<<blocks_for(live->count), kBlock, 0, s>>>(
+        live->phi, live->w, live->phi_alt, live->w_alt, cphi, cw, planes<float>(psi),
+        live->n[0], live->n[1], live->n[2], dp.oob_phi);
+  else
+    k_warp_fuse<double><<<blocks_for(live->count), kBlock, 0, s>>>(
+        live->phi, live->w, live->phi_alt, live->w_alt, cphi, cw, planes<double>(psi),
+        live->n[0], live->n[1], live->n[2], dp.oob_phi);
+  KF_CHECK_LAUNCH("k_warp_fuse");
+  float *tp = live->phi;
+  live->phi = live->phi_alt;
+  live->phi_alt = tp;
+  int32_t *tw = live->w;
+  live->w = live->w_alt;
+  live->w_alt = tw;
+  return KF_OK;
+}
+
+int kf_launch_warp(kf_grid g, kf_field psi, const DevParams &dp, cudaStream_t s) {
+  return warp_fuse_impl(nullptr, g, psi, dp, s);
+}
+
+int kf_launch_warp_fuse(kf_grid can, kf_grid live, kf_field psi, const DevParams &dp,
+                        cudaStream_t s) {
+  return warp_fuse_impl(can, live, psi, dp, s);
+}
+
+int kf_launch_fuse(kf_grid can, kf_grid other, cudaStream_t s) {
+  k_fuse<<<blocks_for(can->count), kBlock, 0, s>>>(can->phi, can->w, other->phi, other->w,
+                                                   can->count);
+  KF_CHECK_LAUNCH("k_fuse");
+  return KF_OK;
+}
+
+int kf_launch_fuse_warped(kf_grid dst, kf_grid other, kf_field psi, const DevParams &dp,
+                          cudaStream_t s) {
+  if (psi->prec == KF_F32)
+    k_fuse_warped<float><<<blocks_for(dst->count), kBlock, 0, s>>>(
+        dst->phi, dst->w, other->phi, other->w, planes<float>(psi), dst->n[0], dst->n[1],
+        dst->n[2], dp.oob_phi);
+  else
+    k_fuse_warped<double><<<blocks_for(dst->count), kBlock, 0, s>>>(
+        dst->phi, dst->w, other->phi, other->w, planes<double>(psi), dst->n[0], dst->n[1],
+        dst->n[2], dp.oob_phi);
+  KF_CHECK_LAUNCH("k_fuse_warped");
+  return KF_OK;
+}
+
+int kf_solve_exact(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp, int iterations,
+                   IterStats *st, cudaStream_t s) {
+  if (psi->prec != KF_F64)
+    return kf_fail(KF_ERR_INVALID, "KF_SOLVER_EXACT needs a KF_F64 displacement field");
+  int rc = kf_field_ensure_pair(psi);
+  if (rc) return rc;
+  PhiView<double> lv = phi_view<double>(live, live->phi, dp.oob_phi);
+  PhiView<double> cv = phi_view<double>(can, can->phi, dp.oob_phi);
+  void *buf[2][3] = {{psi->p[0], psi->p[1], psi->p[2]}, {psi->q[0], psi->q[1], psi->q[2]}};
+  for (int it = 0; it < iterations; ++it) {
+    void **in = buf[it & 1], **out = buf[(it + 1) & 1];
+    PsiView<double, double> fin{(const double *)in[0], (const double *)in[1],
+                                (const double *)in[2], dp.nx, dp.ny, dp.nz};
+    k_exact_step<<<blocks_for(dp.count), kBlock, 0, s>>>(lv, cv, fin, (double *)out[0],
+                                                         (double *)out[1], (double *)out[2], dp,
+                                                         st, it);
+    KF_CHECK_LAUNCH("k_exact_step");
+  }
+  return KF_OK;
+}
+
+int kf_gradient_ref_launch(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
+                           const int32_t *voxels, int count, double *out, uint8_t *active,
+                           cudaStream_t s) {
+  if (count <= 0) return KF_OK;
+  unsigned nb = (unsigned)((count + 127) / 128);
+  if (psi->prec == KF_F32) {
+    PsiView<float, float> f{(const float *)psi->p[0], (const float *)psi->p[1],
+                            (const float *)psi->p[2], dp.nx, dp.ny, dp.nz};
+    k_gradient_ref<float, float><<<nb, 128, 0, s>>>(phi_view<float>(live, live->phi, dp.oob_phi),
+                                                    phi_view<float>(can, can->phi, dp.oob_phi), f,
+                                                    dp, voxels, count, out, active);
+  } else {
+    PsiView<double, double> f{(const double *)psi->p[0], (const double *)psi->p[1],
+                              (const double *)psi->p[2], dp.nx, dp.ny, dp.nz};
+    k_gradient_ref<double, double><<<nb, 128, 0, s>>>(
+        phi_view<double>(live, live->phi, dp.oob_phi), phi_view<double>(can, can->phi, dp.oob_phi),
+        f, dp, voxels, count, out, active);
+  }
+  KF_CHECK_LAUNCH("k_gradient_ref");
+  return KF_OK;
+}

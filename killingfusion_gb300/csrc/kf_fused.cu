@@ -1,0 +1,406 @@
+// Fused float32 psi update: one stencil pass per Jacobi iteration
+// (KillingFusion::computeDisplacementField, KillingFusion.cpp:248-352, with
+// the gradient of KillingFusion::computeEnergyGradient, :399-476), and the
+// CUDA-graph capture of the fixed-iteration loop.
+//
+// A CTA owns a 32 x 8 column tile and a slab of kZSlab planes.
+//   Phase A streams the slab: psi (three coalesced planes) and phi_live at the
+//   voxel; the band test needs the warped value phi_live(i + psi(i)), which is
+//   phi_live(i) itself when psi(i) == 0 (zero interpolation weights), so only
+//   voxels that have moved gather their 8 corners.  Voxels outside the band
+//   pass psi through; voxels inside are queued in shared memory.
+//   Phase B spreads the queue over all threads of the CTA and evaluates the
+//   full gradient there, so warps stay converged on the heavy stencil.
+// In the interior the stencil is evaluated in closed form: the psi samples
+// the reference takes at sub-voxel offsets of the integer point (Killing) and
+// of the cell centre (gradient / Hessian of the warped SDF) are fixed linear
+// combinations of the 3x3x3 neighbourhood, so they come from per-cell moments
+// instead of 44 trilinear interpolations.  Voxels on the grid's outer shell
+// take the generic path with the reference's exact sampling rules
+// (truncating casts, linear-index wrap, outside values).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstring>
+
+#include "kf_internal.h"
+#include "kf_ref_math.cuh"
+
+using namespace kfref;
+
+namespace {
+
+constexpr int kTX = 32, kTY = 8, kThreads = kTX * kTY;
+constexpr int kZSlab = 8;
+constexpr int kTile = kThreads * kZSlab;
+
+struct FusedArgs {
+  const float *__restrict__ live;
+  const float *__restrict__ can;
+  const float *__restrict__ ix;
+  const float *__restrict__ iy;
+  const float *__restrict__ iz;
+  float *__restrict__ ox;
+  float *__restrict__ oy;
+  float *__restrict__ oz;
+  IterStats *st;
+  int iter;
+  DevParams dp;
+  // float copies of the parameters
+  float h, alpha, omega_k, gamma_k, omega_s, clamp, eps, voxel, oob, band_hi, band_lo;
+};
+
+__device__ __forceinline__ float phi_at(const FusedArgs &a, int x, int y, int z) {
+  const DevParams &d = a.dp;
+  if (x < 0 || x >= d.nx || y < 0 || y >= d.ny || z < 0 || z >= d.nz) return a.oob;
+  return __ldg(a.live + ((int64_t)z * d.ny + y) * d.nx + x);
+}
+
+// phi_live at grid coordinate t (already shifted by -0.5), truncating base.
+__device__ __forceinline__ float phi_tri(const FusedArgs &a, float t0, float t1, float t2) {
+  int b0 = (int)t0, b1 = (int)t1, b2 = (int)t2;
+  float f0 = t0 - (float)b0, f1 = t1 - (float)b1, f2 = t2 - (float)b2;
+  float v[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) v[c] = phi_at(a, b0 + (c & 1), b1 + ((c >> 1) & 1), b2 + (c >> 2));
+  return lerp3(v, f0, f1, f2);
+}
+
+// The 25 sub-voxel offsets (units of h) the warped-SDF derivatives sample at
+// the cell centre: 0, +-e_k (gradient), +-2e_k and +-e_j+-e_k (Hessian).
+__device__ __constant__ const signed char kOff25[25][3] = {
+    {0, 0, 0},   {1, 0, 0},   {-1, 0, 0},  {0, 1, 0},  {0, -1, 0},  {0, 0, 1},  {0, 0, -1},
+    {2, 0, 0},   {-2, 0, 0},  {0, 2, 0},   {0, -2, 0}, {0, 0, 2},   {0, 0, -2}, {1, 0, 1},
+    {-1, 0, 1},  {0, 1, 1},   {0, -1, 1},  {1, 1, 0},  {-1, 1, 0},  {-1, 0, -1}, {1, 0, -1},
+    {0, -1, -1}, {0, 1, -1},  {-1, -1, 0}, {1, -1, 0}};
+enum { S0 = 0, SXP, SXM, SYP, SYM, SZP, SZM, SXP2, SXM2, SYP2, SYM2, SZP2, SZM2, SXPZP, SXMZP,
+       SYPZP, SYMZP, SXPYP, SXMYP, SXMZM, SXPZM, SYMZM, SYPZM, SXMYM, SXPYM };
+
+// Gradient of an interior voxel (1 <= x,y,z <= n-2).  Returns the step
+// -alpha * g in d[] and the warped value, gradient for the energy monitor.
+__device__ void gradient_interior(const FusedArgs &a, int x, int y, int z, int64_t idx,
+                                  float d[3], float &s_out, float g_out[3]) {
+  const DevParams &dp = a.dp;
+  const int64_t sy = dp.nx, sz = (int64_t)dp.nx * dp.ny;
+  const float h = a.h;
+  const float *P[3] = {a.ix, a.iy, a.iz};
+
+  // --- Killing term (DisplacementField.cpp:301-347) from the 19-point
+  // neighbourhood: second differences of the trilinear samples at
+  // i + h*o equal 2h*(psi(+1)-2psi(0)+psi(-1)) on the axes and
+  // h^2*(psi(++)-psi(+-)-psi(-+)+psi(--)) on the diagonals.
+  float kg[3] = {0.f, 0.f, 0.f};
+  float div[3] = {0.f, 0.f, 0.f};
+  float m[3][8];  // per-component cell moments for the cell-centre samples
+  float c0[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float *p = P[c] + idx;
+    float v000 = __ldg(p);
+    float vxp = __ldg(p + 1), vxm = __ldg(p - 1);
+    float vyp = __ldg(p + sy), vym = __ldg(p - sy);
+    float vzp = __ldg(p + sz), vzm = __ldg(p - sz);
+    float vxpyp = __ldg(p + 1 + sy), vxpym = __ldg(p + 1 - sy);
+    float vxmyp = __ldg(p - 1 + sy), vxmym = __ldg(p - 1 - sy);
+    float vxpzp = __ldg(p + 1 + sz), vxpzm = __ldg(p + 1 - sz);
+    float vxmzp = __ldg(p - 1 + sz), vxmzm = __ldg(p - 1 - sz);
+    float vypzp = __ldg(p + sy + sz), vypzm = __ldg(p + sy - sz);
+    float vymzp = __ldg(p - sy + sz), vymzm = __ldg(p - sy - sz);
+    float v111 = __ldg(p + 1 + sy + sz);
+    c0[c] = v000;
+    float two_h = 2.f * h, hh = h * h;
+    float xx = two_h * ((vxp - v000) + (vxm - v000));
+    float yy = two_h * ((vyp - v000) + (vym - v000));
+    float zz = two_h * ((vzp - v000) + (vzm - v000));
+    float xy = hh * ((vxpyp - vxpym) - (vxmyp - vxmym));
+    float xz = hh * ((vxpzp - vxpzm) - (vxmzp - vxmzm));
+    float yz = hh * ((vypzp - vypzm) - (vymzp - vymzm));
+    kg[c] = -2.f * (xx + yy + zz);
+    if (c == 0) { div[0] += xx; div[1] += xy; div[2] += xz; }
+    if (c == 1) { div[0] += xy; div[1] += yy; div[2] += yz; }
+    if (c == 2) { div[0] += xz; div[1] += yz; div[2] += zz; }
+    // corners of the cell [i, i+1]^3 for the cell-centre samples
+    float k000 = v000, k100 = vxp, k010 = vyp, k110 = vxpyp;
+    float k001 = vzp, k101 = vxpzp, k011 = vypzp, k111 = v111;
+    // moments: psi~(0.5 + h*o) = m0 + h*(ox*mx + oy*my + oz*mz)
+    //          + h^2*(ox*oy*mxy + ox*oz*mxz + oy*oz*myz)   (|o| has <= 2 nonzeros)
+    float sx0 = (k000 + k010) + (k001 + k011), sx1 = (k100 + k110) + (k101 + k111);
+    float sy0 = (k000 + k100) + (k001 + k101), sy1 = (k010 + k110) + (k011 + k111);
+    float sz0 = (k000 + k100) + (k010 + k110), sz1 = (k001 + k101) + (k011 + k111);
+    m[c][0] = 0.125f * (sx0 + sx1);
+    m[c][1] = 0.25f * (sx1 - sx0);
+    m[c][2] = 0.25f * (sy1 - sy0);
+    m[c][3] = 0.25f * (sz1 - sz0);
+    m[c][4] = 0.5f * ((k110 - k010) - (k100 - k000) + (k111 - k011) - (k101 - k001));
+    m[c][5] = 0.5f * ((k101 - k001) - (k100 - k000) + (k111 - k011) - (k110 - k010));
+    m[c][6] = 0.5f * ((k011 - k001) - (k010 - k000) + (k111 - k101) - (k110 - k100));
+    m[c][7] = 0.f;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) kg[c] += (-2.f * a.gamma_k) * div[c];
+  {
+    float nrm = sqrtf(kg[0] * kg[0] + kg[1] * kg[1] + kg[2] * kg[2]);
+    float sc = nrm > a.clamp ? a.clamp / nrm : 1.f;
+    float den = 4.f * h * h;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) kg[c] = kg[c] * sc / den;
+  }
+
+  // --- warped-SDF samples at the cell centre (SDF.cpp:726-886)
+  float f[25];
+  const float bx = (float)x + 0.5f, by = (float)y + 0.5f, bz = (float)z + 0.5f;
+#pragma unroll
+  for (int j = 0; j < 25; ++j) {
+    float ox = (float)kOff25[j][0], oy = (float)kOff25[j][1], oz = (float)kOff25[j][2];
+    float t[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float lin = ox * m[c][1] + oy * m[c][2] + oz * m[c][3];
+      float quad = ox * oy * m[c][4] + ox * oz * m[c][5] + oy * oz * m[c][6];
+      t[c] = m[c][0] + h * (lin + h * quad);
+    }
+    // grid coordinate of the sample: (centre + h*o) + psi~ (the reference adds
+    // and removes the half-voxel shift around getDistance)
+    f[j] = phi_tri(a, (bx + h * ox) + t[0] - 0.5f, (by + h * oy) + t[1] - 0.5f,
+                   (bz + h * oz) + t[2] - 0.5f);
+  }
+  const float inv2h = 1.f / (2.f * h), inv4hh = 1.f / (4.f * h * h);
+  float g[3] = {(f[SXP] - f[SXM]) * inv2h, (f[SYP] - f[SYM]) * inv2h, (f[SZP] - f[SZM]) * inv2h};
+  float H[6];
+  H[0] = ((f[SXP2] - f[S0]) + (f[SXM2] - f[S0])) * inv4hh;  // xx
+  H[1] = ((f[SYP2] - f[S0]) + (f[SYM2] - f[S0])) * inv4hh;  // yy
+  H[2] = ((f[SZP2] - f[S0]) + (f[SZM2] - f[S0])) * inv4hh;  // zz
+  H[3] = ((f[SXPYP] - f[SXPYM]) - (f[SXMYP] - f[SXMYM])) * inv4hh;  // xy
+  H[4] = ((f[SXPZP] - f[SXPZM]) - (f[SXMZP] - f[SXMZM])) * inv4hh;  // xz
+  H[5] = ((f[SYPZP] - f[SYPZM]) - (f[SYMZP] - f[SYMZM])) * inv4hh;  // yz
+
+  // --- warped value at the integer point (SDF.cpp:570-575)
+  float s = phi_tri(a, (float)x + c0[0], (float)y + c0[1], (float)z + c0[2]);
+  float grad[3] = {0.f, 0.f, 0.f};
+  if (dp.use_data) {
+    float cc = (s - __ldg(a.can + idx)) / a.voxel;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) grad[k] += cc * g[k];
+  }
+  if (dp.use_killing) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) grad[k] += kg[k] * a.omega_k;
+  }
+  if (dp.use_levelset) {
+    float hg0 = H[0] * g[0] + H[3] * g[1] + H[4] * g[2];
+    float hg1 = H[3] * g[0] + H[1] * g[1] + H[5] * g[2];
+    float hg2 = H[4] * g[0] + H[5] * g[1] + H[2] * g[2];
+    float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    float sc = (gn - 1.f) / (gn + a.eps) * a.omega_s;
+    grad[0] += hg0 * sc;
+    grad[1] += hg1 * sc;
+    grad[2] += hg2 * sc;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    d[k] = -a.alpha * grad[k];
+    g_out[k] = g[k];
+  }
+  s_out = s;
+}
+
+// Generic gradient with the reference's sampling rules (outer shell).
+__device__ void gradient_generic(const FusedArgs &a, int x, int y, int z, float d[3],
+                                 float &s_out, float g_out[3]) {
+  const DevParams &dp = a.dp;
+  PhiView<float> lv{a.live, dp.nx, dp.ny, dp.nz, a.oob};
+  PhiView<float> cv{a.can, dp.nx, dp.ny, dp.nz, a.oob};
+  PsiView<float, float> f{a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz};
+  TParams<float> tp(dp);
+  float g[3];
+  energy_gradient(lv, cv, f, tp, x, y, z, g);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = -tp.alpha * g[k];
+  s_out = warped_distance(lv, f, x, y, z);
+  distance_gradient(lv, f, tp.delta_size, x, y, z, g_out);
+}
+
+// Phase A: stream the slab, pass psi through outside the band and append the
+// band voxels to the iteration's list (st[iter].active counts them).
+__global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__restrict__ band) {
+  if (iteration_gated(a.st, a.iter, a.dp)) {
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+      a.st[a.iter].skipped = 1;
+    return;
+  }
+  __shared__ int queue[kTile];
+  __shared__ int qn, qbase;
+  const DevParams &dp = a.dp;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  const int x = blockIdx.x * kTX + threadIdx.x;
+  const int y = blockIdx.y * kTY + threadIdx.y;
+  const int z0 = blockIdx.z * kZSlab;
+  if (tid == 0) qn = 0;
+  __syncthreads();
+  const bool col = x < dp.nx && y < dp.ny;
+  const int64_t sz = (int64_t)dp.nx * dp.ny;
+  const int64_t base = ((int64_t)z0 * dp.ny + y) * dp.nx + x;
+  float px[kZSlab], py[kZSlab], pz[kZSlab], ph[kZSlab];
+#pragma unroll
+  for (int j = 0; j < kZSlab; ++j) {
+    bool ok = col && (z0 + j) < dp.nz;
+    int64_t i = base + j * sz;
+    px[j] = ok ? __ldcs(a.ix + i) : 0.f;
+    py[j] = ok ? __ldcs(a.iy + i) : 0.f;
+    pz[j] = ok ? __ldcs(a.iz + i) : 0.f;
+    ph[j] = ok ? __ldg(a.live + i) : 0.f;
+  }
+#pragma unroll
+  for (int j = 0; j < kZSlab; ++j) {
+    int z = z0 + j;
+    if (!col || z >= dp.nz) continue;
+    int64_t i = base + j * sz;
+    float s = ph[j];
+    // psi == 0 samples its own cell with zero weights: phi_live(i) exactly
+    if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f)
+      s = phi_tri(a, (((float)x + px[j]) + 0.5f) - 0.5f, (((float)y + py[j]) + 0.5f) - 0.5f,
+                  (((float)z + pz[j]) + 0.5f) - 0.5f);
+    if (in_band(s, a.band_hi, a.band_lo)) {
+      queue[atomicAdd(&qn, 1)] = (int)i;
+    } else {
+      __stcs(a.ox + i, px[j]);
+      __stcs(a.oy + i, py[j]);
+      __stcs(a.oz + i, pz[j]);
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && qn) qbase = (int)atomicAdd(&a.st[a.iter].active, (unsigned)qn);
+  __syncthreads();
+  for (int k = tid; k < qn; k += kThreads) band[qbase + k] = queue[k];
+}
+
+// Phase B: the full gradient at every band voxel of the iteration.
+constexpr int kBandThreads = 128;
+
+__global__ void __launch_bounds__(kBandThreads) k_fused_band(FusedArgs a, const int *__restrict__ band) {
+  if (iteration_gated(a.st, a.iter, a.dp)) return;
+  const DevParams &dp = a.dp;
+  const int64_t sz = (int64_t)dp.nx * dp.ny;
+  const int nq = (int)a.st[a.iter].active;
+  float maxd = 0.f;
+  double energy = 0.0;
+  bool diverged = false;
+  for (int k = blockIdx.x * kBandThreads + threadIdx.x; k < nq; k += gridDim.x * kBandThreads) {
+    int64_t i = band[k];
+    int z = (int)(i / sz);
+    int64_t r = i - (int64_t)z * sz;
+    int yy = (int)(r / dp.nx);
+    int xx = (int)(r - (int64_t)yy * dp.nx);
+    float d[3], s, g[3];
+    bool interior = xx >= 1 && yy >= 1 && z >= 1 && xx <= dp.nx - 2 && yy <= dp.ny - 2 &&
+                    z <= dp.nz - 2;
+    if (interior)
+      gradient_interior(a, xx, yy, z, i, d, s, g);
+    else
+      gradient_generic(a, xx, yy, z, d, s, g);
+    float p0 = a.ix[i], p1 = a.iy[i], p2 = a.iz[i];
+    if (!isfinite(p0) || !isfinite(p1) || !isfinite(p2)) diverged = true;
+    a.ox[i] = p0 + d[0];
+    a.oy[i] = p1 + d[1];
+    a.oz[i] = p2 + d[2];
+    maxd = fmaxf(maxd, sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+    energy += (double)monitor_energy(a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz, xx, yy, z, s,
+                                     __ldg(a.can + i), g, dp);
+  }
+  reduce_iter_stats<kBandThreads>(a.st + a.iter, 0u, maxd, energy, diverged);
+}
+
+FusedArgs make_args(kf_grid live, kf_grid can, const DevParams &dp, IterStats *st) {
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.live = live->phi;
+  a.can = can->phi;
+  a.st = st;
+  a.dp = dp;
+  a.h = (float)dp.delta_size;
+  a.alpha = (float)dp.alpha;
+  a.omega_k = (float)dp.omega_k;
+  a.gamma_k = (float)dp.gamma_k;
+  a.omega_s = (float)dp.omega_s;
+  a.clamp = (float)dp.killing_clamp;
+  a.eps = (float)dp.epsilon;
+  a.voxel = (float)dp.voxel_size;
+  a.oob = dp.oob_phi_f;
+  a.band_hi = dp.band_hi_f;
+  a.band_lo = dp.band_lo_f;
+  return a;
+}
+
+}  // namespace
+
+// A captured iteration loop, valid for one set of buffers and parameters.
+struct FusedGraph {
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t capture = nullptr;
+  const void *key_ptr[10] = {};
+  int iterations = 0;
+  DevParams dp;
+};
+
+void kf_fused_graph_destroy(FusedGraph *g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->capture) cudaStreamDestroy(g->capture);
+  delete g;
+}
+
+static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
+                              int iterations, IterStats *st, int *band, cudaStream_t s) {
+  dim3 block(kTX, kTY);
+  const unsigned band_blocks = (unsigned)kf_num_sms() * 4;
+  dim3 grid((dp.nx + kTX - 1) / kTX, (dp.ny + kTY - 1) / kTY, (dp.nz + kZSlab - 1) / kZSlab);
+  FusedArgs a = make_args(live, can, dp, st);
+  void *buf[2][3] = {{psi->p[0], psi->p[1], psi->p[2]}, {psi->q[0], psi->q[1], psi->q[2]}};
+  for (int it = 0; it < iterations; ++it) {
+    void **in = buf[it & 1], **out = buf[(it + 1) & 1];
+    a.ix = (const float *)in[0];
+    a.iy = (const float *)in[1];
+    a.iz = (const float *)in[2];
+    a.ox = (float *)out[0];
+    a.oy = (float *)out[1];
+    a.oz = (float *)out[2];
+    a.iter = it;
+    k_fused_stream<<<grid, block, 0, s>>>(a, band);
+    k_fused_band<<<band_blocks, kBandThreads, 0, s>>>(a, band);
+  }
+}
+
+int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp, int iterations,
+                   IterStats *st, cudaStream_t s) {
+  int rc = kf_field_ensure_pair(psi);
+  if (rc) return rc;
+  rc = kf_field_band_list(psi, &psi->band);
+  if (rc) return rc;
+  const void *key[10] = {live->phi, can->phi, psi->p[0], psi->p[1], psi->p[2],
+                         psi->q[0], psi->q[1], psi->q[2], st, psi->band};
+  FusedGraph *g = psi->graph;
+  bool hit = g && g->iterations == iterations && memcmp(g->key_ptr, key, sizeof(key)) == 0 &&
+             memcmp(&g->dp, &dp, sizeof(dp)) == 0;
+  if (!hit) {
+    kf_fused_graph_destroy(psi->graph);
+    psi->graph = g = new FusedGraph();
+    KF_CHECK_CUDA(cudaStreamCreateWithFlags(&g->capture, cudaStreamNonBlocking));
+    cudaGraph_t graph;
+    KF_CHECK_CUDA(cudaStreamBeginCapture(g->capture, cudaStreamCaptureModeThreadLocal));
+    launch_iterations(live, can, psi, dp, iterations, st, psi->band, g->capture);
+    cudaError_t le = cudaGetLastError();
+    KF_CHECK_CUDA(cudaStreamEndCapture(g->capture, &graph));
+    if (le != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return kf_cuda_fail(le, "fused kernel launch during capture");
+    }
+    cudaError_t ie = cudaGraphInstantiate(&g->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return kf_cuda_fail(ie, "cudaGraphInstantiate");
+    g->iterations = iterations;
+    memcpy(g->key_ptr, key, sizeof(key));
+    g->dp = dp;
+  }
+  KF_CHECK_CUDA(cudaGraphLaunch(g->exec, s));
+  return KF_OK;
+}

@@ -1,0 +1,143 @@
+// Internal declarations shared by the CUDA translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "killingfusion.h"
+
+// ---------------------------------------------------------------------------
+// handles
+// ---------------------------------------------------------------------------
+struct kf_grid_s {
+  int n[3];
+  int64_t count;
+  double voxel;
+  double min3d[3];
+  double unknown_clip;
+  float *phi;      // device, count
+  int32_t *w;      // device, count
+  float *phi_alt;  // second buffers for out-of-place resampling (lazy)
+  int32_t *w_alt;
+  float *depth;    // device staging for host depth frames (lazily sized)
+  size_t depth_cap;
+};
+
+struct IterStats;
+struct FusedGraph;
+
+struct kf_field_s {
+  int n[3];
+  int64_t count;
+  kf_precision prec;
+  void *p[3];      // device planes x, y, z (float or double)
+  void *q[3];      // second buffer of the Jacobi ping-pong (lazily allocated)
+  // solver workspace (lazily allocated, kept until the field is destroyed)
+  IterStats *stats;       // device, per iteration
+  IterStats *stats_host;  // pinned mirror
+  int stats_cap;
+  void *plain_scratch;    // intermediate fields of the per-term solver
+  size_t plain_bytes;
+  FusedGraph *graph;      // captured fused iteration loop
+  int *band;              // voxels inside the band of the current iteration
+};
+
+// ---------------------------------------------------------------------------
+// error state
+// ---------------------------------------------------------------------------
+int kf_fail(int status, const std::string &msg);
+int kf_cuda_fail(cudaError_t e, const char *what);
+
+#define KF_CHECK_CUDA(expr)                                    \
+  do {                                                         \
+    cudaError_t e_ = (expr);                                   \
+    if (e_ != cudaSuccess) return kf_cuda_fail(e_, #expr);     \
+  } while (0)
+
+#define KF_REQUIRE(cond, msg)                                  \
+  do {                                                         \
+    if (!(cond)) return kf_fail(KF_ERR_INVALID, (msg));        \
+  } while (0)
+
+inline cudaStream_t kf_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Launch-error check right after a kernel launch.
+#define KF_CHECK_LAUNCH(what)                                  \
+  do {                                                         \
+    cudaError_t e_ = cudaGetLastError();                       \
+    if (e_ != cudaSuccess) return kf_cuda_fail(e_, what);      \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// device-side parameter block (all thresholds precomputed on the host)
+// ---------------------------------------------------------------------------
+struct DevParams {
+  int nx, ny, nz;
+  int64_t count;
+  double voxel_size, unknown_clip, max_surface, epsilon, delta_size, alpha, omega_k,
+      gamma_k, omega_s, killing_clamp;
+  double oob_phi;        // max_surface + epsilon (value outside the grid)
+  double band_hi;        // max_surface - epsilon (upper band edge, exclusive)
+  float band_hi_f;       // largest float <= band_hi  (s > band_hi <=> s > band_hi_f)
+  float band_lo_f;       // smallest float >= -unknown_clip (s < lo <=> s < band_lo_f)
+  float mc_hi_f;         // largest float <= max_surface
+  float oob_phi_f;       // (float)(max_surface + epsilon)
+  int use_data, use_levelset, use_killing;
+  int early_exit;
+  double threshold;
+};
+
+DevParams kf_make_dev_params(const int n[3], const kf_params *p);
+int kf_check_params(const kf_params *p);
+
+// Per-iteration device statistics of a psi solve.
+struct IterStats {
+  double energy;          // FP64 reduction of the monitored energy
+  unsigned int active;    // voxels inside the band
+  unsigned int max_delta; // bits of max |dpsi| (non-negative float)
+  int diverged;           // psi non-finite inside the band
+  int skipped;            // iteration skipped after convergence
+};
+
+// solver entry points implemented in the solver translation units
+int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
+                   int iterations, IterStats *stats_dev, cudaStream_t s);
+int kf_solve_plain(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
+                   int iterations, IterStats *stats_dev, cudaStream_t s);
+int kf_solve_exact(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
+                   int iterations, IterStats *stats_dev, cudaStream_t s);
+int kf_gradient_ref_launch(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
+                           const int32_t *voxels, int count, double *out, uint8_t *active,
+                           cudaStream_t s);
+
+// ensure the ping-pong buffer of a field exists
+int kf_field_ensure_pair(kf_field f);
+// per-iteration statistics buffers of a field (device + pinned host)
+int kf_field_stats(kf_field f, int iterations, IterStats **dev);
+// list of band voxels (one int per voxel of the grid)
+int kf_field_band_list(kf_field f, int **out);
+// free the solver workspace of a field (graph, scratch, statistics)
+void kf_field_release_solver(kf_field f);
+void kf_fused_graph_destroy(FusedGraph *g);
+size_t kf_prec_size(kf_precision p);
+
+// Number of SMs of the current device (cached).
+int kf_num_sms();
+
+// launches implemented in kf_exact.cu (float64 arithmetic without fused
+// multiply-add where the reference's rounding decides a discrete outcome)
+int kf_grid_ensure_alt(kf_grid g);
+int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height,
+                        const double w2c[16], const double K[9], double min_depth,
+                        double max_depth, cudaStream_t s);
+int kf_launch_warp(kf_grid g, kf_field psi, const DevParams &dp, cudaStream_t s);
+int kf_launch_fuse(kf_grid can, kf_grid other, cudaStream_t s);
+int kf_launch_warp_fuse(kf_grid can, kf_grid live, kf_field psi, const DevParams &dp,
+                        cudaStream_t s);
+int kf_launch_fuse_warped(kf_grid dst, kf_grid other, kf_field psi, const DevParams &dp,
+                          cudaStream_t s);
+// marching cubes (kf_mc.cu)
+int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, int64_t *ntri,
+              cudaStream_t s);

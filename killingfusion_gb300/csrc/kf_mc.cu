@@ -1,0 +1,243 @@
+// Marching cubes in the reference's order (SDF::getMesh, SDF.cpp:396-414;
+// ProcessVolumeCell, SDF.cpp:330-378; Polygonise, MarchingCubes.h:366-422).
+//
+// Three passes keep the triangle soup in the reference's order (cells in
+// z, y, x order; triangles of a cell in table order):
+//   1. k_mc_count: each CTA classifies a contiguous run of cells and writes
+//      its triangle total;
+//   2. k_mc_scan:  one CTA turns the totals into exclusive offsets;
+//   3. k_mc_emit:  each CTA re-classifies its run, scans the per-thread
+//      totals and writes every triangle at its final position.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kf_internal.h"
+#include "kf_mc_tables.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kCellsPerThread = 4;
+constexpr int kCellsPerBlock = kThreads * kCellsPerThread;
+
+struct McTables {
+  signed char tri[256][16];
+  unsigned short edge[256];
+  unsigned char ntri[256];
+  signed char corner[8][3];
+  signed char ends[12][2];
+};
+
+constexpr int hexv(char c) { return c <= '9' ? c - '0' : c - 'a' + 10; }
+
+constexpr McTables build_tables() {
+  McTables t{};
+  for (int c = 0; c < 256; ++c) {
+    const char *s = kfmc::kTriRows[c];
+    int k = 0;
+    for (; s[k]; ++k) t.tri[c][k] = (signed char)hexv(s[k]);
+    t.ntri[c] = (unsigned char)(k / 3);
+    for (; k < 16; ++k) t.tri[c][k] = -1;
+    int m = 0;
+    for (int e = 0; e < 12; ++e) {
+      int a = (c >> kfmc::kEdge[e][0]) & 1, b = (c >> kfmc::kEdge[e][1]) & 1;
+      if (a != b) m |= 1 << e;
+    }
+    t.edge[c] = (unsigned short)m;
+  }
+  for (int k = 0; k < 8; ++k)
+    for (int j = 0; j < 3; ++j) t.corner[k][j] = (signed char)kfmc::kCellCorner[k][j];
+  for (int e = 0; e < 12; ++e)
+    for (int j = 0; j < 2; ++j) t.ends[e][j] = (signed char)kfmc::kEdge[e][j];
+  return t;
+}
+
+__constant__ McTables c_mc = build_tables();
+
+struct McGrid {
+  const float *phi;
+  int nx, ny, nz;
+  int64_t count;
+  float hi, lo, oob;  // skip if phi > hi or phi < lo; value outside the grid
+  float hx, hy, hz;   // half grid size
+};
+
+__device__ __forceinline__ float at(const McGrid &g, int x, int y, int z) {
+  if (x < 0 || x >= g.nx || y < 0 || y >= g.ny || z < 0 || z >= g.nz) return g.oob;
+  return __ldg(g.phi + ((int64_t)z * g.ny + y) * g.nx + x);
+}
+
+// Cube configuration of cell i, or -1 when the cell is skipped.
+__device__ __forceinline__ int classify(const McGrid &g, int64_t i, int &x, int &y, int &z,
+                                        float val[8]) {
+  int64_t plane = (int64_t)g.nx * g.ny;
+  z = (int)(i / plane);
+  int64_t r = i - (int64_t)z * plane;
+  y = (int)(r / g.nx);
+  x = (int)(r - (int64_t)y * g.nx);
+  float d = __ldg(g.phi + i);
+  if (d > g.hi || d < g.lo) return -1;
+  int cube = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    val[k] = at(g, x + c_mc.corner[k][0], y + c_mc.corner[k][1], z + c_mc.corner[k][2]);
+    if (val[k] < 0.0f) cube |= 1 << k;
+  }
+  return cube;
+}
+
+__device__ __forceinline__ int cell_tris(const McGrid &g, int64_t i) {
+  if (i >= g.count) return 0;
+  int x, y, z;
+  float val[8];
+  int cube = classify(g, i, x, y, z, val);
+  if (cube < 0 || c_mc.edge[cube] == 0) return 0;
+  return c_mc.ntri[cube];
+}
+
+template <typename T>
+__device__ T block_exclusive_scan(T v, T *total) {
+  __shared__ T warp_sums[kThreads / 32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  T inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T n = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += n;
+  }
+  if (lane == 31) warp_sums[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    T w = lane < kThreads / 32 ? warp_sums[lane] : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T n = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += n;
+    }
+    if (lane < kThreads / 32) warp_sums[lane] = w;
+  }
+  __syncthreads();
+  T prefix = (wid > 0 ? warp_sums[wid - 1] : T(0)) + inc - v;
+  if (total) *total = warp_sums[kThreads / 32 - 1];
+  __syncthreads();
+  return prefix;
+}
+
+__global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block_tris) {
+  int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + (int64_t)threadIdx.x * kCellsPerThread;
+  uint32_t n = 0;
+#pragma unroll
+  for (int j = 0; j < kCellsPerThread; ++j) n += cell_tris(g, base + j);
+  uint32_t total;
+  block_exclusive_scan<uint32_t>(n, &total);
+  if (threadIdx.x == 0) block_tris[blockIdx.x] = total;
+}
+
+// Exclusive scan of the per-block totals into 64-bit offsets (one CTA).
+__global__ void __launch_bounds__(kThreads) k_mc_scan(const uint32_t *block_tris, int64_t nblocks,
+                                                      int64_t *block_off, int64_t *grand_total) {
+  int64_t per = (nblocks + kThreads - 1) / kThreads;
+  int64_t b0 = (int64_t)threadIdx.x * per;
+  int64_t s = 0;
+  for (int64_t b = b0; b < b0 + per && b < nblocks; ++b) s += block_tris[b];
+  int64_t total;
+  int64_t off = block_exclusive_scan<int64_t>(s, &total);
+  for (int64_t b = b0; b < b0 + per && b < nblocks; ++b) {
+    block_off[b] = off;
+    off += block_tris[b];
+  }
+  if (threadIdx.x == 0) *grand_total = total;
+}
+
+__device__ __forceinline__ void vinterp(const float p1[3], const float p2[3], float v1, float v2,
+                                        float out[3]) {
+  float t = (0.0f - v1) / (v1 - v2);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) out[k] = p1[k] + t * (p1[k] - p2[k]);
+}
+
+__global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *block_off,
+                                                      float *__restrict__ verts, int64_t capacity) {
+  int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + (int64_t)threadIdx.x * kCellsPerThread;
+  uint32_t n = 0;
+#pragma unroll
+  for (int j = 0; j < kCellsPerThread; ++j) n += cell_tris(g, base + j);
+  int64_t out = block_off[blockIdx.x] + (int64_t)block_exclusive_scan<uint32_t>(n, nullptr);
+  if (n == 0) return;
+  for (int j = 0; j < kCellsPerThread; ++j) {
+    int64_t i = base + j;
+    if (i >= g.count) break;
+    int x, y, z;
+    float val[8];
+    int cube = classify(g, i, x, y, z, val);
+    if (cube < 0) continue;
+    int em = c_mc.edge[cube];
+    if (em == 0) continue;
+    float p[8][3];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      p[k][0] = (float)(x + c_mc.corner[k][0]) / g.hx - 1.0f;
+      p[k][1] = (float)(y + c_mc.corner[k][1]) / g.hy - 1.0f;
+      p[k][2] = (float)(z + c_mc.corner[k][2]) / g.hz - 1.0f;
+    }
+    float vl[12][3];
+#pragma unroll
+    for (int e = 0; e < 12; ++e)
+      if (em & (1 << e))
+        vinterp(p[c_mc.ends[e][0]], p[c_mc.ends[e][1]], val[c_mc.ends[e][0]],
+                val[c_mc.ends[e][1]], vl[e]);
+    int nt = c_mc.ntri[cube];
+    for (int t = 0; t < nt; ++t, ++out) {
+      if (out >= capacity) return;
+      float *o = verts + 9 * out;
+#pragma unroll
+      for (int j2 = 0; j2 < 3; ++j2) {
+        const float *v = vl[c_mc.tri[cube][3 * t + j2]];
+        o[3 * j2 + 0] = v[0];
+        o[3 * j2 + 1] = -v[1];
+        o[3 * j2 + 2] = v[2];
+      }
+    }
+  }
+}
+
+}  // namespace
+
+int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, int64_t *ntri,
+              cudaStream_t s) {
+  McGrid mg;
+  mg.phi = g->phi;
+  mg.nx = g->n[0];
+  mg.ny = g->n[1];
+  mg.nz = g->n[2];
+  mg.count = g->count;
+  mg.hi = dp.mc_hi_f;
+  mg.lo = dp.band_lo_f;
+  mg.oob = dp.oob_phi_f;
+  mg.hx = (float)g->n[0] / 2.0f;
+  mg.hy = (float)g->n[1] / 2.0f;
+  mg.hz = (float)g->n[2] / 2.0f;
+  int64_t nblocks = (g->count + kCellsPerBlock - 1) / kCellsPerBlock;
+  // scratch: per-block totals (u32), offsets (i64), grand total (i64)
+  size_t bytes = nblocks * sizeof(uint32_t) + (nblocks + 1) * sizeof(int64_t) + 16;
+  char *scratch = nullptr;
+  KF_CHECK_CUDA(cudaMallocAsync((void **)&scratch, bytes, s));
+  int64_t *off = (int64_t *)(((uintptr_t)scratch + 15) & ~(uintptr_t)15);
+  int64_t *total_dev = off + nblocks;
+  uint32_t *tris = (uint32_t *)(total_dev + 1);
+  k_mc_count<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris);
+  k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev);
+  KF_CHECK_LAUNCH("k_mc_count/k_mc_scan");
+  int64_t total = 0;
+  KF_CHECK_CUDA(cudaMemcpyAsync(&total, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  KF_CHECK_CUDA(cudaStreamSynchronize(s));
+  *ntri = total;
+  if (verts && total > 0 && capacity > 0) {
+    k_mc_emit<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, off, verts, capacity);
+    KF_CHECK_LAUNCH("k_mc_emit");
+  }
+  KF_CHECK_CUDA(cudaFreeAsync(scratch, s));
+  if (verts && capacity < total)
+    return kf_fail(KF_ERR_CAPACITY, "vertex buffer holds fewer triangles than the mesh has");
+  return KF_OK;
+}

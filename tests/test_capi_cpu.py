@@ -1,0 +1,74 @@
+"""Host-side checks of the C ABI library that need no GPU: it loads, it
+exports every function include/killingfusion.h declares, and its host-side
+tables and parameter presets are the reference's."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for f in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if f.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(kf_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def capi():
+    from killingfusion_gb300 import _build, capi
+    if not os.path.exists(_build.LIB):
+        _build.build()
+    return capi
+
+
+def test_library_exports_every_declared_symbol(capi):
+    L = C.CDLL(capi.LIB_PATH)
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    # the ctypes signature table covers the whole header
+    assert set(names) <= set(capi.SIGNATURES), sorted(set(names) - set(capi.SIGNATURES))
+
+
+def test_version_and_params_presets(capi):
+    L = capi.load()
+    assert L.kf_version() == 1
+    p = capi._Params()
+    L.kf_params_reference(C.byref(p))
+    assert (p.voxel_size, p.alpha, p.omega_k, p.gamma_k, p.omega_s) == (0.012, 0.025, 0.04, 0.0, 0.1)
+    assert (p.unknown_clip, p.max_surface, p.delta_size, p.epsilon) == (0.048, 0.048, 0.05, 1e-5)
+    assert p.killing_clamp == 0.1 and p.early_exit == 0
+    L.kf_params_paper(C.byref(p), 0.004, 5.0)
+    assert (p.alpha, p.omega_k, p.gamma_k, p.omega_s) == (0.1, 0.5, 0.1, 0.2)
+    assert abs(p.unknown_clip - 0.02) < 1e-15
+
+
+def test_mc_table_matches_oracle(capi, oracle):
+    edges, tris = oracle.mc_tables()
+    for c in range(256):
+        em, row = capi.mc_case(c)
+        assert em == edges[c]
+        assert row == list(tris[c])
+
+
+def test_invalid_arguments_fail_cleanly(capi):
+    """Argument checks run on the host before any device call."""
+    L = capi.load()
+    h = C.c_void_p()
+    p = capi.Params().c()
+    assert L.kf_grid_create((C.c_int * 3)(0, 4, 4), 0.01, None, 0.05, C.byref(p), C.byref(h)) == capi.KF_ERR_INVALID
+    assert "dims" in L.kf_last_error().decode()
+    assert L.kf_field_create((C.c_int * 3)(4, 4, 4), 7, C.byref(h)) == capi.KF_ERR_INVALID
+    assert L.kf_mc_case(256, None, None) == capi.KF_ERR_INVALID
+    bad = capi.Params(delta_size=0.5).c()
+    assert L.kf_grid_create((C.c_int * 3)(4, 4, 4), 0.01, None, 0.05, C.byref(bad), C.byref(h)) == capi.KF_ERR_INVALID
+    assert L.kf_psi_solve(None, None, None, C.byref(p), 1, 0, None, None) == capi.KF_ERR_INVALID

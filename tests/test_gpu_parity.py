@@ -1,0 +1,331 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the FP64
+oracle (which tests/test_oracle_golden.py pins to the reference).
+
+Tolerances
+* integer/index results (weights, band flags, triangle counts, topology):
+  exact;
+* float64 "exact" solver: bit-identical to the oracle given the same float32
+  SDFs;
+* float32 solvers: |psi - psi_oracle| <= 1e-4 voxel where the reference's
+  iteration is stable (its own default weights), see test_fp32_* below;
+* float32 SDF values written by float64 arithmetic: equal to the oracle's
+  double rounded to float32.
+"""
+import numpy as np
+import pytest
+
+from killingfusion_gb300 import synth
+from oracle.oracle import Params as OParams
+from helpers import small_pair, integrate_oracle
+
+pytestmark = pytest.mark.gpu
+
+PSI_TOL = 1e-4  # voxel
+
+
+def oparams(p):
+    """capi.Params -> oracle.Params (same fields, minus early_exit)."""
+    d = {k: getattr(p, k) for k in OParams.__dataclass_fields__}
+    return OParams(**d)
+
+
+def make_grid(capi, phi, voxel, params, origin=(0.0, 0.0, 0.0), weight=None):
+    nz, ny, nx = phi.shape
+    g = capi.Grid((nx, ny, nz), voxel, origin, params.unknown_clip, params)
+    w = weight if weight is not None else (phi <= params.max_surface).astype(np.int32)
+    g.upload(phi.astype(np.float32), w.astype(np.int32))
+    return g
+
+
+# ---------------------------------------------------------------------------
+# integration
+# ---------------------------------------------------------------------------
+
+def test_integrate_sphere_frames(gpu, oracle):
+    grid, frames = synth.sphere_pair()
+    P = gpu.Params.paper(grid.voxel)
+    for f in frames:
+        g = gpu.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
+        g.integrate(f, min_depth=0.05, max_depth=1.2)
+        phi, w = g.download()
+        ophi, ow = integrate_oracle(oracle, grid, f, oparams(P))
+        np.testing.assert_array_equal(w, ow)
+        np.testing.assert_array_equal(phi, ophi.astype(np.float32))
+        assert (w > 0).sum() > 1000
+
+
+def test_integrate_pose_and_running_mean(gpu, oracle):
+    """A rotated camera and a second frame into the same grid (weights 2)."""
+    import os
+    gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "integrate_small.npz"))
+    P = gpu.Params.paper(0.01)
+    g = gpu.Grid((20, 20, 20), 0.01, gold["origin"], P.unknown_clip, P)
+    g.integrate(gold["depth"].astype(np.float32), gold["c2w"], gold["K"], 0.05, 1.2)
+    phi, w = g.download()
+    np.testing.assert_array_equal(w, gold["w_pose"])
+    np.testing.assert_array_equal(phi, gold["phi_pose"].astype(np.float32))
+    # second frame: the running mean starts from the float32 value on the GPU
+    g.integrate((gold["depth"] * 1.01).astype(np.float32), gold["c2w"], gold["K"], 0.05, 1.2)
+    phi2, w2 = g.download()
+    np.testing.assert_array_equal(w2, gold["w2_pose"])
+    ref = gold["phi2_pose"]
+    m = w2 > 0
+    assert np.abs(phi2[m] - ref[m]).max() <= 2e-7 * np.abs(ref[m]).max() + 1e-9
+
+
+# ---------------------------------------------------------------------------
+# reference gradient at single voxels
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("weights", ["reference", "paper"])
+def test_gradient_ref_f64_bitexact(gpu, oracle, weights):
+    """KillingFusion::computeEnergyGradient at every voxel of a 20^3 pair,
+    including the outer shell and displacements that leave the grid."""
+    voxel = 0.004
+    P = gpu.Params.reference(voxel, 5.0) if weights == "reference" else gpu.Params.paper(voxel)
+    can, live = small_pair(20, voxel, 5.0, seed=3)
+    rng = np.random.default_rng(4)
+    psi = rng.normal(0.0, 0.6, live.shape + (3,))
+    psi.reshape(-1, 3)[rng.integers(0, psi.size // 3, 50)] *= 20
+    gl, gc = make_grid(gpu, live, voxel, P), make_grid(gpu, can, voxel, P)
+    f = gpu.Field(gl.dims, gpu.KF_F64)
+    f.upload(psi)
+    z, y, x = np.meshgrid(*[np.arange(20)] * 3, indexing="ij")
+    xyz = np.stack([x, y, z], -1).reshape(-1, 3)
+    g, act = gpu.psi_gradient_ref(gl, gc, f, P, xyz)
+    OP = oparams(P)
+    og = oracle.voxel_query("grad", live, can, psi, xyz, OP)
+    oa = oracle.voxel_query("active", live, can, psi, xyz, OP)[:, 0]
+    np.testing.assert_array_equal(g, og)
+    np.testing.assert_array_equal(act, oa.astype(np.uint8))
+
+
+def test_gradient_ref_f32_close(gpu, oracle):
+    voxel = 0.004
+    P = gpu.Params.paper(voxel)
+    can, live = small_pair(20, voxel, 5.0, seed=5)
+    rng = np.random.default_rng(6)
+    psi = rng.normal(0.0, 0.3, live.shape + (3,)).astype(np.float32)
+    gl, gc = make_grid(gpu, live, voxel, P), make_grid(gpu, can, voxel, P)
+    f = gpu.Field(gl.dims, gpu.KF_F32)
+    f.upload(psi)
+    xyz = np.argwhere(np.ones(live.shape, bool))[:, ::-1]
+    g, _ = gpu.psi_gradient_ref(gl, gc, f, P, xyz)
+    og = oracle.voxel_query("grad", live, can, psi.astype(np.float64), xyz, oparams(P))
+    scale = np.abs(og).max()
+    assert np.abs(g - og).max() <= 1e-3 * scale
+
+
+# ---------------------------------------------------------------------------
+# psi solve
+# ---------------------------------------------------------------------------
+
+def sphere_sdfs(gpu, P):
+    """GPU-integrated canonical and live SDFs of the 64^3 sphere pair, and
+    their float32 values as float64 for the oracle."""
+    grid, frames = synth.sphere_pair()
+    grids = []
+    for f in frames:
+        g = gpu.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
+        g.integrate(f, min_depth=0.05, max_depth=1.2)
+        grids.append(g)
+    can, live = grids
+    return can, live, can.download()[0].astype(np.float64), live.download()[0].astype(np.float64)
+
+
+@pytest.mark.parametrize("weights", ["paper", "reference"])
+def test_exact_solver_bitexact_64cubed(gpu, oracle, weights):
+    """100 float64 iterations at 64^3 replay the reference bit for bit, with
+    the paper weights as well (where any other rounding diverges)."""
+    voxel = 0.004
+    P = gpu.Params.paper(voxel) if weights == "paper" else gpu.Params.reference(voxel, 5.0)
+    can, live, ocan, olive = sphere_sdfs(gpu, P)
+    f = gpu.Field(live.dims, gpu.KF_F64)
+    st = gpu.psi_solve(live, can, f, P, 100, "exact")
+    psi = f.download()
+    ost, opsi, counts = oracle.solve(olive, ocan, np.zeros(olive.shape + (3,)), 100, oparams(P),
+                                     active_counts=True)
+    assert ost == 0 and st["iterations_run"] == 100
+    assert st["active_first"] == counts[0] and st["active_last"] == counts[-1]
+    np.testing.assert_array_equal(psi, opsi)
+
+
+@pytest.mark.parametrize("solver", ["fused", "plain"])
+def test_fp32_solvers_match_oracle_stable_weights(gpu, oracle, solver):
+    """Float32 solvers within 1e-4 voxel of the FP64 oracle after 100
+    iterations with the reference's own weights (config.cpp:45-54)."""
+    voxel = 0.004
+    P = gpu.Params.reference(voxel, 5.0)
+    can, live, ocan, olive = sphere_sdfs(gpu, P)
+    f = gpu.Field(live.dims, gpu.KF_F32)
+    st = gpu.psi_solve(live, can, f, P, 100, solver)
+    psi = f.download().astype(np.float64)
+    _, opsi, counts = oracle.solve(olive, ocan, np.zeros(olive.shape + (3,)), 100, oparams(P),
+                                   active_counts=True)
+    err = np.abs(psi - opsi).max()
+    assert err <= PSI_TOL, err
+    assert np.abs(opsi).max() > 0.05  # the field did move
+    assert st["active_first"] == counts[0]
+
+
+def test_fused_and_plain_agree(gpu):
+    voxel = 0.004
+    P = gpu.Params.reference(voxel, 5.0)
+    can, live, _, _ = sphere_sdfs(gpu, P)
+    out = {}
+    for solver in ("fused", "plain"):
+        f = gpu.Field(live.dims, gpu.KF_F32)
+        gpu.psi_solve(live, can, f, P, 50, solver)
+        out[solver] = f.download()
+    assert np.abs(out["fused"] - out["plain"]).max() <= 1e-5
+
+
+def test_fp32_paper_weights_short_horizon(gpu, oracle):
+    """With the paper weights the reference's iteration amplifies rounding
+    (about 10x per iteration once the Killing term is active), so float32
+    tracks the FP64 oracle only over the first iterations."""
+    voxel = 0.004
+    P = gpu.Params.paper(voxel)
+    can, live, ocan, olive = sphere_sdfs(gpu, P)
+    for solver in ("fused", "plain"):
+        f = gpu.Field(live.dims, gpu.KF_F32)
+        gpu.psi_solve(live, can, f, P, 3, solver)
+        _, opsi = oracle.solve(olive, ocan, np.zeros(olive.shape + (3,)), 3, oparams(P))
+        assert np.abs(f.download() - opsi).max() <= PSI_TOL
+
+
+def test_solve_is_repeatable_and_graph_reuse(gpu):
+    """A second solve reuses the captured graph and gives the same field."""
+    voxel = 0.004
+    P = gpu.Params.reference(voxel, 5.0)
+    can, live, _, _ = sphere_sdfs(gpu, P)
+    f = gpu.Field(live.dims, gpu.KF_F32)
+    gpu.psi_solve(live, can, f, P, 20, "fused")
+    a = f.download()
+    f.zero()
+    gpu.psi_solve(live, can, f, P, 20, "fused")
+    np.testing.assert_array_equal(a, f.download())
+    f.zero()
+    gpu.psi_solve(live, can, f, P, 21, "fused")  # odd count: result in the other buffer
+    b = f.download()
+    assert np.abs(b - a).max() > 0
+
+
+def test_divergence_is_reported(gpu):
+    """A non-finite psi inside the band stops the solve with KF_ERR_DIVERGED
+    (the reference throws -1, KillingFusion.cpp:328-332)."""
+    voxel = 0.004
+    P = gpu.Params.reference(voxel, 5.0)
+    can, live = small_pair(24, voxel, 5.0, seed=1)
+    gl, gc = make_grid(gpu, live, voxel, P), make_grid(gpu, can, voxel, P)
+    for prec, solver in ((gpu.KF_F32, "fused"), (gpu.KF_F32, "plain"), (gpu.KF_F64, "exact")):
+        f = gpu.Field(gl.dims, prec)
+        psi = np.zeros(live.shape + (3,))
+        z, y, x = np.argwhere((live > -0.01) & (live < 0.01))[0]
+        psi[z, y, x, 0] = np.nan
+        f.upload(psi)
+        with pytest.raises(gpu.DivergedError):
+            gpu.psi_solve(gl, gc, f, P, 5, solver)
+
+
+def test_early_exit_convergence_flag(gpu):
+    """With early_exit the loop stops once max |dpsi| <= threshold."""
+    voxel = 0.004
+    P = gpu.Params.reference(voxel, 5.0).with_(early_exit=True, threshold=1e-4)
+    can, live, _, _ = sphere_sdfs(gpu, P)
+    f = gpu.Field(live.dims, gpu.KF_F32)
+    st = gpu.psi_solve(live, can, f, P, 400, "fused")
+    assert st["converged"] == 1 and st["iterations_run"] < 400
+    assert st["max_delta_last"] <= 1e-4
+
+
+# ---------------------------------------------------------------------------
+# warp / fuse / marching cubes
+# ---------------------------------------------------------------------------
+
+def test_warp_fuse_exact(gpu, oracle):
+    """SDF::update + SDF::fuse on the same psi: integer weights exact (the
+    truncation of an interpolated double), SDF values the oracle's doubles
+    rounded to float32."""
+    voxel = 0.004
+    P = gpu.Params.paper(voxel)
+    can, live = small_pair(24, voxel, 5.0, seed=21)
+    rng = np.random.default_rng(3)
+    psi = rng.normal(0, 0.4, live.shape + (3,)).astype(np.float32)
+    psi[rng.random(live.shape) < 0.5] = 0.0
+    wl = rng.integers(0, 3, live.shape).astype(np.int32)
+    wc = rng.integers(0, 3, live.shape).astype(np.int32)
+    gl, gc = make_grid(gpu, live, voxel, P, weight=wl), make_grid(gpu, can, voxel, P, weight=wc)
+    f = gpu.Field(gl.dims, gpu.KF_F32)
+    f.upload(psi)
+    gpu.warp_fuse(gc, gl, f, P)
+    lphi, lw = gl.download()
+    cphi, cw = gc.download()
+    OP = oparams(P)
+    uphi, uw = oracle.update(live.astype(np.float64), wl.astype(np.int64), psi.astype(np.float64), OP)
+    np.testing.assert_array_equal(lw, uw)
+    np.testing.assert_array_equal(lphi, uphi.astype(np.float32))
+    fphi, fw = oracle.fuse(can.astype(np.float64), wc.astype(np.int64), uphi.astype(np.float32).astype(np.float64), uw)
+    np.testing.assert_array_equal(cw, fw)
+    np.testing.assert_array_equal(cphi, fphi.astype(np.float32))
+
+
+def test_fuse_and_fuse_warped(gpu, oracle):
+    voxel = 0.004
+    P = gpu.Params.paper(voxel)
+    can, live = small_pair(24, voxel, 5.0, seed=22)
+    rng = np.random.default_rng(8)
+    psi = rng.normal(0, 0.5, live.shape + (3,)).astype(np.float32)
+    wl = rng.integers(0, 3, live.shape).astype(np.int32)
+    wc = rng.integers(0, 3, live.shape).astype(np.int32)
+    OP = oparams(P)
+    gl, gc = make_grid(gpu, live, voxel, P, weight=wl), make_grid(gpu, can, voxel, P, weight=wc)
+    gpu.fuse(gc, gl)
+    cphi, cw = gc.download()
+    ophi, ow = oracle.fuse(can.astype(np.float64), wc.astype(np.int64), live.astype(np.float64), wl.astype(np.int64))
+    np.testing.assert_array_equal(cw, ow)
+    np.testing.assert_array_equal(cphi, ophi.astype(np.float32))
+    gl, gc = make_grid(gpu, live, voxel, P, weight=wl), make_grid(gpu, can, voxel, P, weight=wc)
+    f = gpu.Field(gl.dims, gpu.KF_F32)
+    f.upload(psi)
+    gpu.fuse_warped(gc, gl, f, P)
+    cphi, cw = gc.download()
+    ophi, ow = oracle.fuse_psi(can.astype(np.float64), wc.astype(np.int64), live.astype(np.float64),
+                               wl.astype(np.int64), psi.astype(np.float64), OP)
+    np.testing.assert_array_equal(cw, ow)
+    np.testing.assert_array_equal(cphi, ophi.astype(np.float32))
+
+
+@pytest.mark.parametrize("which", ["sphere64", "pair24"])
+def test_marching_cubes_counts_exact(gpu, oracle, which):
+    """Triangle counts and order bit-exact, vertices within 1e-4 voxel."""
+    if which == "sphere64":
+        P = gpu.Params.paper(0.004)
+        can, live, ocan, olive = sphere_sdfs(gpu, P)
+        grids = [(can, ocan), (live, olive)]
+    else:
+        P = gpu.Params.paper(0.004)
+        c, l = small_pair(24, 0.004, 5.0, seed=30)
+        grids = [(make_grid(gpu, c, 0.004, P), c.astype(np.float64)),
+                 (make_grid(gpu, l, 0.004, P), l.astype(np.float64))]
+    for g, ophi in grids:
+        tris = gpu.marching_cubes(g, P)
+        otris = oracle.mesh(ophi, oparams(P))
+        assert tris.shape == otris.shape and len(tris) > 100
+        # vertices lie in [-1, 1]; one voxel is 2/n of that range
+        n = max(g.dims)
+        err_vox = np.abs(tris - otris).max() / (2.0 / n)
+        assert err_vox <= 1e-4, err_vox
+
+
+def test_mesh_capacity_error(gpu):
+    import ctypes as C
+    import torch
+    P = gpu.Params.paper(0.004)
+    c, _ = small_pair(24, 0.004, 5.0, seed=31)
+    g = make_grid(gpu, c, 0.004, P)
+    L = gpu.load()
+    n = C.c_int64(0)
+    buf = torch.empty((4, 9), dtype=torch.float32, device="cuda")
+    st = L.kf_marching_cubes(g.h, C.byref(P.c()), buf.data_ptr(), 4, C.byref(n), None)
+    assert st == gpu.KF_ERR_CAPACITY and n.value > 4
