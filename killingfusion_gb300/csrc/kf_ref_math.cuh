@@ -354,8 +354,8 @@ __device__ void reduce_iter_stats(IterStats *st, unsigned active, float max_delt
       max_delta = fmaxf(max_delta, __shfl_xor_sync(0xffffffffu, max_delta, o));
       active += __shfl_xor_sync(0xffffffffu, active, o);
     }
-    if (lane == 0 && active) {
-      atomicAdd(&st->active, active);
+    if (lane == 0 && (active || max_delta > 0.f || energy != 0.0)) {
+      if (active) atomicAdd(&st->active, active);
       atomicMax(&st->max_delta, __float_as_uint(max_delta));
       atomicAdd(&st->energy, energy);
     }
