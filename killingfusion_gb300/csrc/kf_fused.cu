@@ -159,10 +159,10 @@ __device__ void gradient_interior(const FusedArgs &a, int x, int y, int z, int64
       float quad = ox * oy * m[c][4] + ox * oz * m[c][5] + oy * oz * m[c][6];
       t[c] = m[c][0] + h * (lin + h * quad);
     }
-    // grid coordinate of the sample: (centre + h*o) + psi~ (the reference adds
-    // and removes the half-voxel shift around getDistance)
-    f[j] = phi_tri(a, (bx + h * ox) + t[0] - 0.5f, (by + h * oy) + t[1] - 0.5f,
-                   (bz + h * oz) + t[2] - 0.5f);
+    // sample coordinate (centre + h*o) + psi~: getDistancef adds half a voxel
+    // that getDistance takes away again (SDF.cpp:506, 580), so the cell-centre
+    // samples sit half a voxel off the value sample at i + psi(i)
+    f[j] = phi_tri(a, (bx + h * ox) + t[0], (by + h * oy) + t[1], (bz + h * oz) + t[2]);
   }
   const float inv2h = 1.f / (2.f * h), inv4hh = 1.f / (4.f * h * h);
   float g[3] = {(f[SXP] - f[SXM]) * inv2h, (f[SYP] - f[SYM]) * inv2h, (f[SZP] - f[SZM]) * inv2h};
