@@ -185,6 +185,25 @@ int kf_fuse_warped(kf_grid dst, kf_grid other, kf_field psi, const kf_params *p,
 int kf_marching_cubes(kf_grid g, const kf_params *p, float *verts, int64_t capacity,
                       int64_t *ntri, void *stream);
 
+/* Marching cubes that allocates nothing.  No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory on their own --
+ * a frame loop where a cudaMalloc/cudaFree would block on the device and
+ * break the frame budget, or a host whose device memory is handed out by
+ * another allocator (a framework's caching pool, a fixed arena reserved at
+ * start-up).  Same output as kf_marching_cubes, but it takes the SDF as a
+ * plain device array (phi, float32, dims[0]*dims[1]*dims[2] values, x
+ * fastest) and keeps its scratch in a fixed device array inside the library
+ * (about 1.5 MB, held on every GPU that loads the library until the process
+ * exits); it calls no cudaMalloc, cudaFree or allocating library routine.
+ * Grids above KF_MC_NOALLOC_MAX_CELLS cells are rejected with
+ * KF_ERR_INVALID.  The first call on a device looks up the array's address
+ * on that device (make that first call outside any CUDA stream capture).
+ * All calls share the one array: calls that overlap on the GPU (from two
+ * streams or two host threads at once) race and must be serialised. */
+#define KF_MC_NOALLOC_MAX_CELLS (512LL * 512LL * 512LL)
+int kf_marching_cubes_noalloc(const float *phi, const int dims[3], const kf_params *p,
+                              float *verts, int64_t capacity, int64_t *ntri, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

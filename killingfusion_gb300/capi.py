@@ -127,6 +127,8 @@ SIGNATURES = {
     "kf_warp_fuse": (C.c_int, [_vp, _vp, _vp, _PP, _vp]),
     "kf_fuse_warped": (C.c_int, [_vp, _vp, _vp, _PP, _vp]),
     "kf_marching_cubes": (C.c_int, [_vp, _PP, _vp, C.c_int64, C.POINTER(C.c_int64), _vp]),
+    "kf_marching_cubes_noalloc": (C.c_int, [_vp, _ip3, _PP, _vp, C.c_int64, C.POINTER(C.c_int64),
+                                            _vp]),
 }
 
 _lib = None

@@ -11,6 +11,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+#include <string>
+
 #include "kf_internal.h"
 #include "kf_mc_tables.h"
 
@@ -237,6 +240,97 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
     KF_CHECK_LAUNCH("k_mc_emit");
   }
   KF_CHECK_CUDA(cudaFreeAsync(scratch, s));
+  if (verts && capacity < total)
+    return kf_fail(KF_ERR_CAPACITY, "vertex buffer holds fewer triangles than the mesh has");
+  return KF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Marching cubes without any allocation (kf_marching_cubes_noalloc).
+//
+// The scratch of the three passes -- per-block triangle totals (u32), their
+// exclusive offsets (i64) and the grand total (i64) -- lives in one
+// file-scope device array sized for the largest grid this entry point
+// accepts, KF_MC_NOALLOC_MAX_CELLS cells.  Each GPU that loads the library
+// holds it until the process exits.  Host code cannot use the array's name as
+// a device address, so the address is looked up with cudaGetSymbolAddress
+// once per device, with that device current, on the first call there.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kNoAllocMaxBlocks = (KF_MC_NOALLOC_MAX_CELLS + kCellsPerBlock - 1) / kCellsPerBlock;
+constexpr size_t kNoAllocOffBytes = (size_t)(kNoAllocMaxBlocks + 1) * sizeof(int64_t);
+constexpr size_t kNoAllocBytes = kNoAllocOffBytes + (size_t)kNoAllocMaxBlocks * sizeof(uint32_t);
+
+static __device__ __align__(256) unsigned char g_mc_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[kMaxDevices] = {};
+
+int noalloc_scratch(void **out) {
+  int dev = 0;
+  KF_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return kf_fail(KF_ERR_INVALID, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_mc_noalloc_scratch);
+    if (e != cudaSuccess) return kf_cuda_fail(e, "cudaGetSymbolAddress(marching-cubes scratch)");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return KF_OK;
+}
+
+}  // namespace
+
+extern "C" int kf_marching_cubes_noalloc(const float *phi, const int dims[3], const kf_params *p,
+                                         float *verts, int64_t capacity, int64_t *ntri,
+                                         void *stream) {
+  KF_REQUIRE(phi && dims && ntri, "NULL argument");
+  KF_REQUIRE(capacity >= 0, "capacity must be >= 0");
+  KF_REQUIRE(dims[0] > 0 && dims[1] > 0 && dims[2] > 0, "grid dims must be positive");
+  const int64_t cells = (int64_t)dims[0] * dims[1] * dims[2];
+  if (cells > KF_MC_NOALLOC_MAX_CELLS)
+    return kf_fail(KF_ERR_INVALID,
+                   "grid has " + std::to_string(cells) + " cells; kf_marching_cubes_noalloc handles "
+                   "at most " + std::to_string((long long)KF_MC_NOALLOC_MAX_CELLS) +
+                   " (512^3); use kf_marching_cubes");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  void *base = nullptr;
+  rc = noalloc_scratch(&base);
+  if (rc) return rc;
+  cudaStream_t s = kf_stream(stream);
+  DevParams dp = kf_make_dev_params(dims, p);
+  McGrid mg;
+  mg.phi = phi;
+  mg.nx = dims[0];
+  mg.ny = dims[1];
+  mg.nz = dims[2];
+  mg.count = cells;
+  mg.hi = dp.mc_hi_f;
+  mg.lo = dp.band_lo_f;
+  mg.oob = dp.oob_phi_f;
+  mg.hx = (float)dims[0] / 2.0f;
+  mg.hy = (float)dims[1] / 2.0f;
+  mg.hz = (float)dims[2] / 2.0f;
+  const int64_t nblocks = (cells + kCellsPerBlock - 1) / kCellsPerBlock;
+  int64_t *off = (int64_t *)base;               // nblocks offsets, then the grand total
+  int64_t *total_dev = off + kNoAllocMaxBlocks;
+  uint32_t *tris = (uint32_t *)((char *)base + kNoAllocOffBytes);
+  // Every word read below is written earlier in this call; the grand total is
+  // cleared anyway so a failed launch cannot report a previous call's count.
+  KF_CHECK_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(int64_t), s));
+  k_mc_count<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris);
+  k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev);
+  if (verts && capacity > 0) k_mc_emit<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, off, verts, capacity);
+  KF_CHECK_LAUNCH("kf_marching_cubes_noalloc kernels");
+  int64_t total = 0;
+  KF_CHECK_CUDA(cudaMemcpyAsync(&total, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  KF_CHECK_CUDA(cudaStreamSynchronize(s));
+  *ntri = total;
   if (verts && capacity < total)
     return kf_fail(KF_ERR_CAPACITY, "vertex buffer holds fewer triangles than the mesh has");
   return KF_OK;
