@@ -240,10 +240,18 @@ def run_ours(args, rank, world, local):
     st_plain = capi.psi_solve(live, can_e2e, psi, P, plain_it, "plain" if args.solver == "fused" else "fused")
     other_vups = N3 * plain_it / (st_plain["device_ms"] / 1e3)
 
+    # band-only solver on the same frame: same psi, visits only the band
+    band_ms = []
+    for _ in range(3):
+        psi.zero()
+        stb = capi.psi_solve(live, can_e2e, psi, P, args.iters, "band")
+        band_ms.append(stb["device_ms"])
+
     res = {
         "elapsed_ms": elapsed_ms, "wall_s": wall, "solve_ms": solve_ms, "e2e_ms": e2e_ms,
         "d2h_bytes_per_step": d2h_total / args.steps, "tris": tri_counts, "active": active,
         "clocks": clk, "N3": N3, "other_vups": other_vups, "launches": launches_per_frame * args.steps,
+        "band_ms": statistics.median(band_ms[1:]), "band_active_last": stb["active_last"],
     }
     return res, seq, P
 
@@ -399,6 +407,15 @@ def run_main(args, rank, world, local):
     }
     if args.solver == "fused":
         line["fused_over_plain"] = line["solve_voxel_updates_per_s"] / res["other_vups"]
+    frame_other_ms = el / args.steps - solve_ms
+    line["band_solver"] = {
+        "solve_ms_per_frame": res["band_ms"],
+        "ms_per_frame_est": frame_other_ms + res["band_ms"],
+        "dense_equivalent_voxel_updates_per_s": N3 * args.iters / (res["band_ms"] / 1e3),
+        "band_voxels_last_iteration": res["band_active_last"],
+        "note": "KF_SOLVER_BAND: identical psi; after the first dense pass it visits only the band, "
+                "which can only shrink (a voxel outside the band keeps psi)",
+    }
     if world == 1 and not args.no_cpu_baseline:
         t = cpu_sample(seq, P, args.cpu_iters)
         frame_s = t["integrate"] + t["solve"] / args.cpu_iters * args.iters + t["fuse_mesh"]

@@ -57,7 +57,12 @@ typedef enum kf_precision {
 typedef enum kf_solver {
   KF_SOLVER_FUSED = 0, /* one stencil pass per iteration, CUDA-graph loop  */
   KF_SOLVER_PLAIN = 1, /* one kernel per energy term, fields through HBM   */
-  KF_SOLVER_EXACT = 2  /* float64 replay of the reference (needs KF_F64 psi) */
+  KF_SOLVER_EXACT = 2, /* float64 replay of the reference (needs KF_F64 psi) */
+  KF_SOLVER_BAND = 3   /* the fused stencil on the band only: a voxel outside
+                          the band keeps psi, so its band test keeps failing
+                          and the band can only shrink; after the first dense
+                          pass each iteration visits the previous iteration's
+                          band.  Same psi as KF_SOLVER_FUSED.               */
 } kf_solver;
 
 /* The reference's config.h globals that the hot path reads. */

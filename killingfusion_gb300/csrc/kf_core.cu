@@ -307,7 +307,7 @@ int kf_field_stats(kf_field f, int iterations, IterStats **dev) {
 }
 
 int kf_field_band_list(kf_field f, int **out) {
-  if (!f->band && cudaMalloc(&f->band, f->count * sizeof(int)) != cudaSuccess) {
+  if (!f->band && cudaMalloc(&f->band, 2 * f->count * sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     f->band = nullptr;
     return kf_fail(KF_ERR_OOM, "cudaMalloc of the band voxel list failed");
@@ -557,7 +557,8 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
   KF_REQUIRE(iterations >= 0, "iterations must be >= 0");
   int rc = kf_check_params(p);
   if (rc) return rc;
-  KF_REQUIRE(solver == KF_SOLVER_FUSED || solver == KF_SOLVER_PLAIN || solver == KF_SOLVER_EXACT,
+  KF_REQUIRE(solver == KF_SOLVER_FUSED || solver == KF_SOLVER_PLAIN || solver == KF_SOLVER_EXACT ||
+                 solver == KF_SOLVER_BAND,
              "unknown solver");
   KF_REQUIRE((solver == KF_SOLVER_EXACT) == (psi->prec == KF_F64),
              "KF_SOLVER_EXACT runs on KF_F64 fields and the other solvers on KF_F32 fields");
@@ -566,15 +567,16 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
   cudaStream_t s = kf_stream(stream);
   DevParams dp = kf_make_dev_params(live->n, p);
   IterStats *st = nullptr;
-  rc = kf_field_stats(psi, iterations, &st);
+  // one extra record: the band solver counts the next iteration's list there
+  rc = kf_field_stats(psi, iterations + 1, &st);
   if (rc) return rc;
-  KF_CHECK_CUDA(cudaMemsetAsync(st, 0, sizeof(IterStats) * iterations, s));
+  KF_CHECK_CUDA(cudaMemsetAsync(st, 0, sizeof(IterStats) * (iterations + 1), s));
   cudaEvent_t e0, e1;
   KF_CHECK_CUDA(cudaEventCreate(&e0));
   KF_CHECK_CUDA(cudaEventCreate(&e1));
   KF_CHECK_CUDA(cudaEventRecord(e0, s));
-  if (solver == KF_SOLVER_FUSED)
-    rc = kf_solve_fused(live, canonical, psi, dp, iterations, st, s);
+  if (solver == KF_SOLVER_FUSED || solver == KF_SOLVER_BAND)
+    rc = kf_solve_fused(live, canonical, psi, dp, iterations, st, solver == KF_SOLVER_BAND, s);
   else if (solver == KF_SOLVER_PLAIN)
     rc = kf_solve_plain(live, canonical, psi, dp, iterations, st, s);
   else

@@ -40,10 +40,43 @@ __device__ __forceinline__ void voxel_xyz(int64_t i, int nx, int ny, int &x, int
 struct IntegrateArgs {
   double W[16];  // world -> camera, row-major
   double K[9];   // intrinsics, row-major
+  float Wf[12], Kf[6];
   double voxel, min0, min1, min2, unknown_clip, min_depth, max_depth;
+  float min_depth_up, max_depth_down;  // float neighbours of the depth range
   int width, height;
 };
 
+// Pixel coordinates exactly as SDF::integrateDepthFrame computes them, in
+// float64 (SDF.cpp:151-164).
+__device__ __forceinline__ void project_exact(const IntegrateArgs &a, int x, int y, int z, double &u,
+                                              double &v, double &zc) {
+  double Z = a.voxel * ((double)z + 0.5) + a.min2;
+  double Y = a.voxel * ((double)y + 0.5) + a.min1;
+  double X = a.voxel * ((double)x + 0.5) + a.min0;
+  double c[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    c[r] = a.W[4 * r + 0] * X + a.W[4 * r + 1] * Y + a.W[4 * r + 2] * Z + a.W[4 * r + 3] * 1.0;
+  double pa = c[0] / c[2], pb = c[1] / c[2];
+  u = a.K[0] * pa + a.K[1] * pb + a.K[2] * 1.0;
+  v = a.K[3] * pa + a.K[4] * pb + a.K[5] * 1.0;
+  zc = c[2];
+}
+
+// The reference's pixel index: roundf of the double converted to float
+// (SDF.cpp:167,171).  A non-finite value never lands inside the image
+// (x86-64 converts it to INT_MIN); -1 stands for "outside".
+__device__ __forceinline__ int pixel_of(double u) {
+  float f = (float)(u + 0.5);
+  if (!isfinite(f)) return -1;
+  return (int)roundf(f);
+}
+
+// SDF::integrateDepthFrame for one voxel per thread.  The pixel a voxel reads
+// flips only where u or v crosses an integer, so the projection runs in float
+// and is redone in float64 when either coordinate lies within 1/128 pixel of
+// an integer (the float error is below 1e-3 pixel) or is not finite.  The
+// distance and the running mean are float64 as in the reference.
 __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, int32_t *__restrict__ w,
                                                       int nx, int ny, int nz,
                                                       const float *__restrict__ depth,
@@ -52,29 +85,44 @@ __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, i
   if (i >= (int64_t)nx * ny * nz) return;
   int x, y, z;
   voxel_xyz(i, nx, ny, x, y, z);
-  double Z = a.voxel * ((double)z + 0.5) + a.min2;
-  double Y = a.voxel * ((double)y + 0.5) + a.min1;
-  double X = a.voxel * ((double)x + 0.5) + a.min0;
-  double c[4];
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-    c[r] = a.W[4 * r + 0] * X + a.W[4 * r + 1] * Y + a.W[4 * r + 2] * Z + a.W[4 * r + 3] * 1.0;
-  double pa = c[0] / c[2], pb = c[1] / c[2];
-  double u = a.K[0] * pa + a.K[1] * pb + a.K[2] * 1.0;
-  double v = a.K[3] * pa + a.K[4] * pb + a.K[5] * 1.0;
-  // roundf of the double converted to float (SDF.cpp:167,171); a non-finite
-  // value never lands inside the image (x86-64 converts it to INT_MIN).
-  float fu = (float)(u + 0.5);
-  if (!isfinite(fu)) return;
-  int col = (int)roundf(fu);
+  const float Xf = (float)(a.voxel * ((double)x + 0.5) + a.min0);
+  const float Yf = (float)(a.voxel * ((double)y + 0.5) + a.min1);
+  const float Zf = (float)(a.voxel * ((double)z + 0.5) + a.min2);
+  const float c0 = a.Wf[0] * Xf + a.Wf[1] * Yf + a.Wf[2] * Zf + a.Wf[3];
+  const float c1 = a.Wf[4] * Xf + a.Wf[5] * Yf + a.Wf[6] * Zf + a.Wf[7];
+  const float c2 = a.Wf[8] * Xf + a.Wf[9] * Yf + a.Wf[10] * Zf + a.Wf[11];
+  const float pa = c0 / c2, pb = c1 / c2;
+  const float uf = a.Kf[0] * pa + a.Kf[1] * pb + a.Kf[2];
+  const float vf = a.Kf[3] * pa + a.Kf[4] * pb + a.Kf[5];
+  constexpr float kMargin = 1.0f / 128.0f;
+  int col, row;
+  bool exact_zc = false;
+  double zc = 0.0;
+  if (isfinite(uf) && isfinite(vf) && fabsf(uf - rintf(uf)) > kMargin &&
+      fabsf(vf - rintf(vf)) > kMargin && fabsf(uf) < 1e7f && fabsf(vf) < 1e7f) {
+    col = (int)floorf(uf + 1.0f);  // == roundf(u + 0.5) away from the flips
+    row = (int)floorf(vf + 1.0f);
+    if (uf < -1.0f) col = -1;      // roundf(u + 0.5) < 0: outside
+    if (vf < -1.0f) row = -1;
+  } else {
+    double u, v;
+    project_exact(a, x, y, z, u, v, zc);
+    exact_zc = true;
+    col = pixel_of(u);
+    row = pixel_of(v);
+  }
   if (col < 0 || col >= a.width) return;
-  float fv = (float)(v + 0.5);
-  if (!isfinite(fv)) return;
-  int row = (int)roundf(fv);
   if (row < 0 || row >= a.height) return;
-  double d = (double)depth[(int64_t)row * a.width + col];
-  if (d < a.min_depth || d > a.max_depth) return;
-  double dist = d - c[2];
+  const float df = depth[(int64_t)row * a.width + col];
+  // d < min_depth || d > max_depth on the float value compared as a double
+  if (df < a.min_depth_up || df > a.max_depth_down) return;
+  if (!exact_zc) {
+    const double Z = a.voxel * ((double)z + 0.5) + a.min2;
+    const double Y = a.voxel * ((double)y + 0.5) + a.min1;
+    const double X = a.voxel * ((double)x + 0.5) + a.min0;
+    zc = a.W[8] * X + a.W[9] * Y + a.W[10] * Z + a.W[11] * 1.0;
+  }
+  const double dist = (double)df - zc;
   if (dist < -a.unknown_clip) return;
   int32_t wi = w[i];
   phi[i] = (float)(((double)phi[i] * (double)wi + dist) / (double)(wi + 1));
@@ -301,6 +349,8 @@ int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height
   IntegrateArgs a;
   for (int k = 0; k < 16; ++k) a.W[k] = w2c[k];
   for (int k = 0; k < 9; ++k) a.K[k] = K[k];
+  for (int k = 0; k < 12; ++k) a.Wf[k] = (float)w2c[k];
+  for (int k = 0; k < 6; ++k) a.Kf[k] = (float)K[k];
   a.voxel = g->voxel;
   a.min0 = g->min3d[0];
   a.min1 = g->min3d[1];
@@ -308,6 +358,12 @@ int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height
   a.unknown_clip = g->unknown_clip;
   a.min_depth = min_depth;
   a.max_depth = max_depth;
+  // float x < min_depth  <=>  x < smallest float >= min_depth, and likewise
+  float lo = (float)min_depth, hi = (float)max_depth;
+  if ((double)lo < min_depth) lo = nextafterf(lo, INFINITY);
+  if ((double)hi > max_depth) hi = nextafterf(hi, -INFINITY);
+  a.min_depth_up = lo;
+  a.max_depth_down = hi;
   a.width = width;
   a.height = height;
   k_integrate<<<blocks_for(g->count), kBlock, 0, s>>>(g->phi, g->w, g->n[0], g->n[1], g->n[2],

@@ -1,22 +1,34 @@
-// Fused float32 psi update: one stencil pass per Jacobi iteration
-// (KillingFusion::computeDisplacementField, KillingFusion.cpp:248-352, with
-// the gradient of KillingFusion::computeEnergyGradient, :399-476), and the
-// CUDA-graph capture of the fixed-iteration loop.
+// Fused float32 psi update (KillingFusion::computeDisplacementField,
+// KillingFusion.cpp:248-352, with the gradient of
+// KillingFusion::computeEnergyGradient, :399-476) and the CUDA-graph capture
+// of the fixed-iteration loop.
 //
-// A CTA owns a 32 x 8 column tile and a slab of kZSlab planes.
-//   Phase A streams the slab: psi (three coalesced planes) and phi_live at the
-//   voxel; the band test needs the warped value phi_live(i + psi(i)), which is
-//   phi_live(i) itself when psi(i) == 0 (zero interpolation weights), so only
-//   voxels that have moved gather their 8 corners.  Voxels outside the band
-//   pass psi through; voxels inside are queued in shared memory.
-//   Phase B spreads the queue over all threads of the CTA and evaluates the
-//   full gradient there, so warps stay converged on the heavy stencil.
-// In the interior the stencil is evaluated in closed form: the psi samples
-// the reference takes at sub-voxel offsets of the integer point (Killing) and
-// of the cell centre (gradient / Hessian of the warped SDF) are fixed linear
-// combinations of the 3x3x3 neighbourhood, so they come from per-cell moments
-// instead of 44 trilinear interpolations.  Voxels on the grid's outer shell
-// take the generic path with the reference's exact sampling rules
+// An iteration is two passes:
+//   k_fused_stream (dense)  streams psi and phi_live and applies the band test
+//     of KillingFusion.cpp:272-274.  The warped value phi_live(i + psi(i)) is
+//     phi_live(i) itself when psi(i) == 0 (zero interpolation weights), so only
+//     voxels that have moved gather their 8 corners.  Voxels outside the band
+//     pass psi through; voxels inside are compacted into a list.
+//   k_fused_band  evaluates the full gradient for every listed voxel with one
+//     warp per voxel: lanes 0-19 load the psi neighbourhood (shared by
+//     shuffles), lanes 0-24 each take one of the 25 warped-SDF samples of the
+//     gradient and Hessian, lane 25 the warped value, lane 26 phi_can, and the
+//     nine derivative sums are warp reductions of +-1-weighted sample
+//     differences.
+// The band-only solver (KF_SOLVER_BAND) runs the dense pass once: a voxel
+// outside the band keeps psi, so its band test keeps failing and the band can
+// only shrink.  Each band pass then re-tests its voxels at the new psi and
+// hands the survivors to the next iteration; a voxel that leaves the band is
+// copied once into the other Jacobi buffer.  Both solvers produce the same psi.
+//
+// In the interior the psi samples that the reference takes at sub-voxel offsets
+// are closed-form linear combinations of the 3x3x3 neighbourhood:
+//   Killing (at i + h*o):  second differences 2h*(psi(+1) - 2psi(0) + psi(-1))
+//     on the axes and h^2*(psi(++) - psi(+-) - psi(-+) + psi(--)) on the
+//     diagonals;
+//   cell centre (at i + 0.5 + h*o):  m0 + h*(o.m1) + h^2*(pairwise o o.m2)
+//     from eight moments of the cell [i, i+1]^3.
+// Voxels on the grid's outer shell take the generic reference-order path
 // (truncating casts, linear-index wrap, outside values).
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -33,6 +45,9 @@ namespace {
 constexpr int kTX = 32, kTY = 8, kThreads = kTX * kTY;
 constexpr int kZSlab = 8;
 constexpr int kTile = kThreads * kZSlab;
+constexpr int kBandWarps = 8;
+constexpr int kBandThreads = 32 * kBandWarps;
+constexpr unsigned kFull = 0xffffffffu;
 
 struct FusedArgs {
   const float *__restrict__ live;
@@ -56,7 +71,8 @@ __device__ __forceinline__ float phi_at(const FusedArgs &a, int x, int y, int z)
   return __ldg(a.live + ((int64_t)z * d.ny + y) * d.nx + x);
 }
 
-// phi_live at grid coordinate t (already shifted by -0.5), truncating base.
+// phi_live at grid coordinate t (SDF::getDistance after its -0.5 shift,
+// SDF.cpp:503-524): truncating base, outside corners read MaxSurface+eps.
 __device__ __forceinline__ float phi_tri(const FusedArgs &a, float t0, float t1, float t2) {
   int b0 = (int)t0, b1 = (int)t1, b2 = (int)t2;
   float f0 = t0 - (float)b0, f1 = t1 - (float)b1, f2 = t2 - (float)b2;
@@ -66,64 +82,85 @@ __device__ __forceinline__ float phi_tri(const FusedArgs &a, float t0, float t1,
   return lerp3(v, f0, f1, f2);
 }
 
-// The 25 sub-voxel offsets (units of h) the warped-SDF derivatives sample at
-// the cell centre: 0, +-e_k (gradient), +-2e_k and +-e_j+-e_k (Hessian).
-__device__ __constant__ const signed char kOff25[25][3] = {
+// The warped value of the band test, SDF::getDistance(i, psi) (SDF.cpp:570-575).
+__device__ __noinline__ float warped_value(const FusedArgs &a, int x, int y, int z, float p0, float p1,
+                                           float p2) {
+  return phi_tri(a, (((float)x + p0) + 0.5f) - 0.5f, (((float)y + p1) + 0.5f) - 0.5f,
+                 (((float)z + p2) + 0.5f) - 0.5f);
+}
+
+// The 25 sub-voxel offsets (units of h) of the cell-centre samples: 0, +-e_k
+// (gradient), +-2e_k and +-e_j+-e_k (Hessian), one per lane.
+__device__ const signed char kOff25[32][3] = {
     {0, 0, 0},   {1, 0, 0},   {-1, 0, 0},  {0, 1, 0},  {0, -1, 0},  {0, 0, 1},  {0, 0, -1},
     {2, 0, 0},   {-2, 0, 0},  {0, 2, 0},   {0, -2, 0}, {0, 0, 2},   {0, 0, -2}, {1, 0, 1},
     {-1, 0, 1},  {0, 1, 1},   {0, -1, 1},  {1, 1, 0},  {-1, 1, 0},  {-1, 0, -1}, {1, 0, -1},
-    {0, -1, -1}, {0, 1, -1},  {-1, -1, 0}, {1, -1, 0}};
-enum { S0 = 0, SXP, SXM, SYP, SYM, SZP, SZM, SXP2, SXM2, SYP2, SYM2, SZP2, SZM2, SXPZP, SXMZP,
-       SYPZP, SYMZP, SXPYP, SXMYP, SXMZM, SXPZM, SYMZM, SYPZM, SXMYM, SXPYM };
+    {0, -1, -1}, {0, 1, -1},  {-1, -1, 0}, {1, -1, 0}, {0, 0, 0},   {0, 0, 0},  {0, 0, 0},
+    {0, 0, 0},   {0, 0, 0},   {0, 0, 0},   {0, 0, 0}};
 
-// Gradient of an interior voxel (1 <= x,y,z <= n-2).  Returns the step
-// -alpha * g in d[] and the warped value, gradient for the energy monitor.
-__device__ void gradient_interior(const FusedArgs &a, int x, int y, int z, int64_t idx,
-                                  float d[3], float &s_out, float g_out[3]) {
+// The 20 psi neighbours of the interior stencil, one per lane: the 19-point
+// Killing stencil and the far corner (1,1,1) of the cell-centre cell.
+__device__ const signed char kNb20[32][3] = {
+    {0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},   {0, -1, 0}, {0, 0, 1},  {0, 0, -1},
+    {1, 1, 0},  {1, -1, 0}, {-1, 1, 0}, {-1, -1, 0}, {1, 0, 1},  {1, 0, -1}, {-1, 0, 1},
+    {-1, 0, -1}, {0, 1, 1}, {0, 1, -1}, {0, -1, 1},  {0, -1, -1}, {1, 1, 1},  {0, 0, 0},
+    {0, 0, 0},  {0, 0, 0},  {0, 0, 0},  {0, 0, 0},   {0, 0, 0},  {0, 0, 0},  {0, 0, 0},
+    {0, 0, 0},  {0, 0, 0},  {0, 0, 0},  {0, 0, 0}};
+enum { N000 = 0, NXP, NXM, NYP, NYM, NZP, NZM, NXPYP, NXPYM, NXMYP, NXMYM, NXPZP, NXPZM, NXMZP,
+       NXMZM, NYPZP, NYPZM, NYMZP, NYMZM, N111 };
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// Step d = -alpha * g of an interior voxel (1 <= x,y,z <= n-2), by one warp.
+// All lanes return the same d, warped value s, distance gradient g and
+// monitored energy e.
+__device__ void gradient_warp(const FusedArgs &a, int x, int y, int z, int64_t idx, int lane,
+                              float d[3], float &s_out, float g_out[3], float &e_out) {
   const DevParams &dp = a.dp;
   const int64_t sy = dp.nx, sz = (int64_t)dp.nx * dp.ny;
   const float h = a.h;
-  const float *P[3] = {a.ix, a.iy, a.iz};
 
-  // --- Killing term (DisplacementField.cpp:301-347) from the 19-point
-  // neighbourhood: second differences of the trilinear samples at
-  // i + h*o equal 2h*(psi(+1)-2psi(0)+psi(-1)) on the axes and
-  // h^2*(psi(++)-psi(+-)-psi(-+)+psi(--)) on the diagonals.
-  float kg[3] = {0.f, 0.f, 0.f};
-  float div[3] = {0.f, 0.f, 0.f};
-  float m[3][8];  // per-component cell moments for the cell-centre samples
-  float c0[3];
+  // loads: psi at lane's neighbour (lanes 0-19), phi_can (lane 26)
+  float q[3] = {0.f, 0.f, 0.f};
+  if (lane < 20) {
+    int64_t j = idx + __ldg(&kNb20[lane][0]) + __ldg(&kNb20[lane][1]) * sy + __ldg(&kNb20[lane][2]) * sz;
+    q[0] = __ldg(a.ix + j);
+    q[1] = __ldg(a.iy + j);
+    q[2] = __ldg(a.iz + j);
+  }
+  const float canv = lane == 26 ? __ldg(a.can + idx) : 0.f;
+
+  float kg[3], div[3] = {0.f, 0.f, 0.f}, m[3][7], c0[3], J[3][3];
+  const float two_h = 2.f * h, hh = h * h;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const float *p = P[c] + idx;
-    float v000 = __ldg(p);
-    float vxp = __ldg(p + 1), vxm = __ldg(p - 1);
-    float vyp = __ldg(p + sy), vym = __ldg(p - sy);
-    float vzp = __ldg(p + sz), vzm = __ldg(p - sz);
-    float vxpyp = __ldg(p + 1 + sy), vxpym = __ldg(p + 1 - sy);
-    float vxmyp = __ldg(p - 1 + sy), vxmym = __ldg(p - 1 - sy);
-    float vxpzp = __ldg(p + 1 + sz), vxpzm = __ldg(p + 1 - sz);
-    float vxmzp = __ldg(p - 1 + sz), vxmzm = __ldg(p - 1 - sz);
-    float vypzp = __ldg(p + sy + sz), vypzm = __ldg(p + sy - sz);
-    float vymzp = __ldg(p - sy + sz), vymzm = __ldg(p - sy - sz);
-    float v111 = __ldg(p + 1 + sy + sz);
+    float v[20];
+#pragma unroll
+    for (int n = 0; n < 20; ++n) v[n] = __shfl_sync(kFull, q[c], n);
+    const float v000 = v[N000];
     c0[c] = v000;
-    float two_h = 2.f * h, hh = h * h;
-    float xx = two_h * ((vxp - v000) + (vxm - v000));
-    float yy = two_h * ((vyp - v000) + (vym - v000));
-    float zz = two_h * ((vzp - v000) + (vzm - v000));
-    float xy = hh * ((vxpyp - vxpym) - (vxmyp - vxmym));
-    float xz = hh * ((vxpzp - vxpzm) - (vxmzp - vxmzm));
-    float yz = hh * ((vypzp - vypzm) - (vymzp - vymzm));
+    // Killing second differences (DisplacementField.cpp:326-331)
+    float xx = two_h * ((v[NXP] - v000) + (v[NXM] - v000));
+    float yy = two_h * ((v[NYP] - v000) + (v[NYM] - v000));
+    float zz = two_h * ((v[NZP] - v000) + (v[NZM] - v000));
+    float xy = hh * ((v[NXPYP] - v[NXPYM]) - (v[NXMYP] - v[NXMYM]));
+    float xz = hh * ((v[NXPZP] - v[NXPZM]) - (v[NXMZP] - v[NXMZM]));
+    float yz = hh * ((v[NYPZP] - v[NYPZM]) - (v[NYMZP] - v[NYMZM]));
     kg[c] = -2.f * (xx + yy + zz);
     if (c == 0) { div[0] += xx; div[1] += xy; div[2] += xz; }
     if (c == 1) { div[0] += xy; div[1] += yy; div[2] += yz; }
     if (c == 2) { div[0] += xz; div[1] += yz; div[2] += zz; }
-    // corners of the cell [i, i+1]^3 for the cell-centre samples
-    float k000 = v000, k100 = vxp, k010 = vyp, k110 = vxpyp;
-    float k001 = vzp, k101 = vxpzp, k011 = vypzp, k111 = v111;
-    // moments: psi~(0.5 + h*o) = m0 + h*(ox*mx + oy*my + oz*mz)
-    //          + h^2*(ox*oy*mxy + ox*oz*mxz + oy*oz*myz)   (|o| has <= 2 nonzeros)
+    // central differences for the monitored Killing energy
+    J[c][0] = 0.5f * (v[NXP] - v[NXM]);
+    J[c][1] = 0.5f * (v[NYP] - v[NYM]);
+    J[c][2] = 0.5f * (v[NZP] - v[NZM]);
+    // moments of the cell [i, i+1]^3 (corner k_abc = psi(i + (a,b,c)))
+    float k000 = v000, k100 = v[NXP], k010 = v[NYP], k110 = v[NXPYP];
+    float k001 = v[NZP], k101 = v[NXPZP], k011 = v[NYPZP], k111 = v[N111];
     float sx0 = (k000 + k010) + (k001 + k011), sx1 = (k100 + k110) + (k101 + k111);
     float sy0 = (k000 + k100) + (k001 + k101), sy1 = (k010 + k110) + (k011 + k111);
     float sz0 = (k000 + k100) + (k010 + k110), sz1 = (k001 + k101) + (k011 + k111);
@@ -134,8 +171,8 @@ __device__ void gradient_interior(const FusedArgs &a, int x, int y, int z, int64
     m[c][4] = 0.5f * ((k110 - k010) - (k100 - k000) + (k111 - k011) - (k101 - k001));
     m[c][5] = 0.5f * ((k101 - k001) - (k100 - k000) + (k111 - k011) - (k110 - k010));
     m[c][6] = 0.5f * ((k011 - k001) - (k010 - k000) + (k111 - k101) - (k110 - k100));
-    m[c][7] = 0.f;
   }
+  // Killing gradient: damped divergence term, clamp |g| to killing_clamp, /4h^2
 #pragma unroll
   for (int c = 0; c < 3; ++c) kg[c] += (-2.f * a.gamma_k) * div[c];
   {
@@ -146,55 +183,80 @@ __device__ void gradient_interior(const FusedArgs &a, int x, int y, int z, int64
     for (int c = 0; c < 3; ++c) kg[c] = kg[c] * sc / den;
   }
 
-  // --- warped-SDF samples at the cell centre (SDF.cpp:726-886)
-  float f[25];
-  const float bx = (float)x + 0.5f, by = (float)y + 0.5f, bz = (float)z + 0.5f;
-#pragma unroll
-  for (int j = 0; j < 25; ++j) {
-    float ox = (float)kOff25[j][0], oy = (float)kOff25[j][1], oz = (float)kOff25[j][2];
-    float t[3];
+  // one trilinear sample per lane: lanes 0-24 the cell-centre samples
+  // (SDF::getDistancef at i+0.5+h*o, SDF.cpp:577-582: the half voxel it adds is
+  // removed again by getDistance), lanes 25-31 the warped value at i + psi(i)
+  const int o0 = __ldg(&kOff25[lane][0]), o1 = __ldg(&kOff25[lane][1]), o2 = __ldg(&kOff25[lane][2]);
+  float t[3];
+  if (lane < 25) {
+    const float of[3] = {(float)o0, (float)o1, (float)o2};
+    const float base[3] = {(float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      float lin = ox * m[c][1] + oy * m[c][2] + oz * m[c][3];
-      float quad = ox * oy * m[c][4] + ox * oz * m[c][5] + oy * oz * m[c][6];
-      t[c] = m[c][0] + h * (lin + h * quad);
+      float lin = of[0] * m[c][1] + of[1] * m[c][2] + of[2] * m[c][3];
+      float quad = of[0] * of[1] * m[c][4] + of[0] * of[2] * m[c][5] + of[1] * of[2] * m[c][6];
+      t[c] = (base[c] + h * of[c]) + (m[c][0] + h * (lin + h * quad));
     }
-    // sample coordinate (centre + h*o) + psi~: getDistancef adds half a voxel
-    // that getDistance takes away again (SDF.cpp:506, 580), so the cell-centre
-    // samples sit half a voxel off the value sample at i + psi(i)
-    f[j] = phi_tri(a, (bx + h * ox) + t[0], (by + h * oy) + t[1], (bz + h * oz) + t[2]);
+  } else {
+    t[0] = (((float)x + c0[0]) + 0.5f) - 0.5f;
+    t[1] = (((float)y + c0[1]) + 0.5f) - 0.5f;
+    t[2] = (((float)z + c0[2]) + 0.5f) - 0.5f;
   }
+  const float f = phi_tri(a, t[0], t[1], t[2]);
+  const float f0 = __shfl_sync(kFull, f, 0);
+  const float s = __shfl_sync(kFull, f, 25);
+  const float cv = __shfl_sync(kFull, canv, 26);
+  // derivative stencils on sample differences (the constant f0 cancels):
+  // gradient +-1 on +-e_k, Hessian +1 on +-2e_k, o_j*o_k on the diagonals
+  const float df = lane < 25 ? f - f0 : 0.f;
+  const int nzc = (o0 != 0) + (o1 != 0) + (o2 != 0);
+  const int amax = max(abs(o0), max(abs(o1), abs(o2)));
+  const bool first = nzc == 1 && amax == 1, second = nzc == 1 && amax == 2;
+  float gx = warp_sum(first ? (float)o0 * df : 0.f);
+  float gy = warp_sum(first ? (float)o1 * df : 0.f);
+  float gz = warp_sum(first ? (float)o2 * df : 0.f);
+  float hxx = warp_sum(second && o0 ? df : 0.f);
+  float hyy = warp_sum(second && o1 ? df : 0.f);
+  float hzz = warp_sum(second && o2 ? df : 0.f);
+  float hxy = warp_sum(nzc == 2 && !o2 ? (float)(o0 * o1) * df : 0.f);
+  float hxz = warp_sum(nzc == 2 && !o1 ? (float)(o0 * o2) * df : 0.f);
+  float hyz = warp_sum(nzc == 2 && !o0 ? (float)(o1 * o2) * df : 0.f);
   const float inv2h = 1.f / (2.f * h), inv4hh = 1.f / (4.f * h * h);
-  float g[3] = {(f[SXP] - f[SXM]) * inv2h, (f[SYP] - f[SYM]) * inv2h, (f[SZP] - f[SZM]) * inv2h};
-  float H[6];
-  H[0] = ((f[SXP2] - f[S0]) + (f[SXM2] - f[S0])) * inv4hh;  // xx
-  H[1] = ((f[SYP2] - f[S0]) + (f[SYM2] - f[S0])) * inv4hh;  // yy
-  H[2] = ((f[SZP2] - f[S0]) + (f[SZM2] - f[S0])) * inv4hh;  // zz
-  H[3] = ((f[SXPYP] - f[SXPYM]) - (f[SXMYP] - f[SXMYM])) * inv4hh;  // xy
-  H[4] = ((f[SXPZP] - f[SXPZM]) - (f[SXMZP] - f[SXMZM])) * inv4hh;  // xz
-  H[5] = ((f[SYPZP] - f[SYPZM]) - (f[SYMZP] - f[SYMZM])) * inv4hh;  // yz
+  const float g[3] = {gx * inv2h, gy * inv2h, gz * inv2h};
+  hxx *= inv4hh; hyy *= inv4hh; hzz *= inv4hh; hxy *= inv4hh; hxz *= inv4hh; hyz *= inv4hh;
 
-  // --- warped value at the integer point (SDF.cpp:570-575)
-  float s = phi_tri(a, (float)x + c0[0], (float)y + c0[1], (float)z + c0[2]);
   float grad[3] = {0.f, 0.f, 0.f};
+  float e = 0.f;
   if (dp.use_data) {
-    float cc = (s - __ldg(a.can + idx)) / a.voxel;
+    float r = (s - cv) / a.voxel;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) grad[k] += cc * g[k];
+    for (int k = 0; k < 3; ++k) grad[k] += r * g[k];
+    e += 0.5f * r * r;
   }
   if (dp.use_killing) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) grad[k] += kg[k] * a.omega_k;
+    float fr = 0.f, tr = 0.f;
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        fr += J[p][k] * J[p][k];
+        tr += J[p][k] * J[k][p];
+      }
+    e += a.omega_k * (fr + a.gamma_k * tr);
   }
+  const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
   if (dp.use_levelset) {
-    float hg0 = H[0] * g[0] + H[3] * g[1] + H[4] * g[2];
-    float hg1 = H[3] * g[0] + H[1] * g[1] + H[5] * g[2];
-    float hg2 = H[4] * g[0] + H[5] * g[1] + H[2] * g[2];
-    float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    float hg0 = hxx * g[0] + hxy * g[1] + hxz * g[2];
+    float hg1 = hxy * g[0] + hyy * g[1] + hyz * g[2];
+    float hg2 = hxz * g[0] + hyz * g[1] + hzz * g[2];
     float sc = (gn - 1.f) / (gn + a.eps) * a.omega_s;
     grad[0] += hg0 * sc;
     grad[1] += hg1 * sc;
     grad[2] += hg2 * sc;
+    float r = gn / a.voxel - 1.f;
+    e += a.omega_s * 0.5f * r * r;
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -202,11 +264,12 @@ __device__ void gradient_interior(const FusedArgs &a, int x, int y, int z, int64
     g_out[k] = g[k];
   }
   s_out = s;
+  e_out = e;
 }
 
-// Generic gradient with the reference's sampling rules (outer shell).
-__device__ void gradient_generic(const FusedArgs &a, int x, int y, int z, float d[3],
-                                 float &s_out, float g_out[3]) {
+// Generic reference-order gradient for the outer shell (one thread).
+__device__ __noinline__ void gradient_generic(const FusedArgs &a, int x, int y, int z, float d[3],
+                                              float &s_out, float g_out[3], float &e_out) {
   const DevParams &dp = a.dp;
   PhiView<float> lv{a.live, dp.nx, dp.ny, dp.nz, a.oob};
   PhiView<float> cv{a.can, dp.nx, dp.ny, dp.nz, a.oob};
@@ -218,11 +281,21 @@ __device__ void gradient_generic(const FusedArgs &a, int x, int y, int z, float 
   for (int k = 0; k < 3; ++k) d[k] = -tp.alpha * g[k];
   s_out = warped_distance(lv, f, x, y, z);
   distance_gradient(lv, f, tp.delta_size, x, y, z, g_out);
+  e_out = monitor_energy(a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz, x, y, z, s_out, cv.at(x, y, z),
+                         g_out, dp);
 }
 
-// Phase A: stream the slab, pass psi through outside the band and append the
-// band voxels to the iteration's list (st[iter].active counts them).
-__global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__restrict__ band) {
+__device__ __forceinline__ void voxel_xyz(const DevParams &dp, int64_t i, int &x, int &y, int &z) {
+  const int64_t sz = (int64_t)dp.nx * dp.ny;
+  z = (int)(i / sz);
+  int64_t r = i - (int64_t)z * sz;
+  y = (int)(r / dp.nx);
+  x = (int)(r - (int64_t)y * dp.nx);
+}
+
+// Dense pass: stream the slab, pass psi through outside the band, list the
+// band voxels (st[iter].list counts them).
+__global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__restrict__ list) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
       a.st[a.iter].skipped = 1;
@@ -257,9 +330,7 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
     int64_t i = base + j * sz;
     float s = ph[j];
     // psi == 0 samples its own cell with zero weights: phi_live(i) exactly
-    if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f)
-      s = phi_tri(a, (((float)x + px[j]) + 0.5f) - 0.5f, (((float)y + py[j]) + 0.5f) - 0.5f,
-                  (((float)z + pz[j]) + 0.5f) - 0.5f);
+    if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f) s = warped_value(a, x, y, z, px[j], py[j], pz[j]);
     if (in_band(s, a.band_hi, a.band_lo)) {
       queue[atomicAdd(&qn, 1)] = (int)i;
     } else {
@@ -269,45 +340,91 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
     }
   }
   __syncthreads();
-  if (tid == 0 && qn) qbase = (int)atomicAdd(&a.st[a.iter].active, (unsigned)qn);
+  if (tid == 0 && qn) qbase = (int)atomicAdd(&a.st[a.iter].list, (unsigned)qn);
   __syncthreads();
-  for (int k = tid; k < qn; k += kThreads) band[qbase + k] = queue[k];
+  for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
 }
 
-// Phase B: the full gradient at every band voxel of the iteration.
-constexpr int kBandThreads = 128;
-
-__global__ void __launch_bounds__(kBandThreads) k_fused_band(FusedArgs a, const int *__restrict__ band) {
-  if (iteration_gated(a.st, a.iter, a.dp)) return;
+// Band pass: one warp per listed voxel.  kCarry: re-test the band at the new
+// psi and list the survivors for the next iteration (list_out, counted in
+// st[iter+1].list); a listed entry ~i marks a voxel that left the band, whose
+// value is copied into the output buffer.
+template <bool kCarry>
+__global__ void __launch_bounds__(kBandThreads) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
+                                                             int *__restrict__ list_out) {
+  if (iteration_gated(a.st, a.iter, a.dp)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.iter].skipped = 1;
+    return;
+  }
   const DevParams &dp = a.dp;
-  const int64_t sz = (int64_t)dp.nx * dp.ny;
-  const int nq = (int)a.st[a.iter].active;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nq = (int)a.st[a.iter].list;
+  const int total_warps = gridDim.x * kBandWarps;
+  const int rounds = (nq + total_warps - 1) / total_warps;
+  __shared__ int s_next[kBandWarps];
   float maxd = 0.f;
   double energy = 0.0;
+  unsigned active = 0;
   bool diverged = false;
-  for (int k = blockIdx.x * kBandThreads + threadIdx.x; k < nq; k += gridDim.x * kBandThreads) {
-    int64_t i = band[k];
-    int z = (int)(i / sz);
-    int64_t r = i - (int64_t)z * sz;
-    int yy = (int)(r / dp.nx);
-    int xx = (int)(r - (int64_t)yy * dp.nx);
-    float d[3], s, g[3];
-    bool interior = xx >= 1 && yy >= 1 && z >= 1 && xx <= dp.nx - 2 && yy <= dp.ny - 2 &&
-                    z <= dp.nz - 2;
-    if (interior)
-      gradient_interior(a, xx, yy, z, i, d, s, g);
-    else
-      gradient_generic(a, xx, yy, z, d, s, g);
-    float p0 = a.ix[i], p1 = a.iy[i], p2 = a.iz[i];
-    if (!isfinite(p0) || !isfinite(p1) || !isfinite(p2)) diverged = true;
-    a.ox[i] = p0 + d[0];
-    a.oy[i] = p1 + d[1];
-    a.oz[i] = p2 + d[2];
-    maxd = fmaxf(maxd, sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
-    energy += (double)monitor_energy(a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz, xx, yy, z, s,
-                                     __ldg(a.can + i), g, dp);
+  for (int r = 0; r < rounds; ++r) {
+    const int k = (r * gridDim.x + blockIdx.x) * kBandWarps + warp;
+    int next = INT32_MIN;  // entry this warp hands to the next iteration
+    if (k < nq) {
+      const int e = list_in[k];
+      if (e < 0) {
+        if (lane == 0) {  // left the band last iteration: settle both buffers
+          const int64_t i = ~e;
+          a.ox[i] = a.ix[i];
+          a.oy[i] = a.iy[i];
+          a.oz[i] = a.iz[i];
+        }
+      } else {
+        const int64_t i = e;
+        int x, y, z;
+        voxel_xyz(dp, i, x, y, z);
+        float d[3], s, g[3], en;
+        const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 &&
+                              z <= dp.nz - 2;
+        if (interior) {
+          gradient_warp(a, x, y, z, i, lane, d, s, g, en);
+        } else {
+          if (lane == 0) gradient_generic(a, x, y, z, d, s, g, en);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) d[c] = __shfl_sync(kFull, d[c], 0);
+        }
+        if (lane == 0) {
+          const float p0 = a.ix[i], p1 = a.iy[i], p2 = a.iz[i];
+          if (!isfinite(p0) || !isfinite(p1) || !isfinite(p2)) diverged = true;
+          const float n0 = p0 + d[0], n1 = p1 + d[1], n2 = p2 + d[2];
+          a.ox[i] = n0;
+          a.oy[i] = n1;
+          a.oz[i] = n2;
+          maxd = fmaxf(maxd, sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+          energy += (double)en;
+          ++active;
+          if (kCarry) {
+            const float s1 = warped_value(a, x, y, z, n0, n1, n2);
+            next = in_band(s1, a.band_hi, a.band_lo) ? e : ~e;
+          }
+        }
+      }
+    }
+    if (kCarry) {
+      if (lane == 0) s_next[warp] = next;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int cnt = 0;
+        for (int w = 0; w < kBandWarps; ++w) cnt += s_next[w] != INT32_MIN;
+        if (cnt) {
+          int b = (int)atomicAdd(&a.st[a.iter + 1].list, (unsigned)cnt);
+          for (int w = 0; w < kBandWarps; ++w)
+            if (s_next[w] != INT32_MIN) list_out[b++] = s_next[w];
+        }
+      }
+      __syncthreads();
+    }
   }
-  reduce_iter_stats<kBandThreads>(a.st + a.iter, 0u, maxd, energy, diverged);
+  reduce_iter_stats<kBandThreads>(a.st + a.iter, active, maxd, energy, diverged);
 }
 
 FusedArgs make_args(kf_grid live, kf_grid can, const DevParams &dp, IterStats *st) {
@@ -339,6 +456,7 @@ struct FusedGraph {
   cudaStream_t capture = nullptr;
   const void *key_ptr[10] = {};
   int iterations = 0;
+  bool band_only = false;
   DevParams dp;
 };
 
@@ -350,12 +468,14 @@ void kf_fused_graph_destroy(FusedGraph *g) {
 }
 
 static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
-                              int iterations, IterStats *st, int *band, cudaStream_t s) {
+                              int iterations, IterStats *st, int *lists, bool band_only,
+                              cudaStream_t s) {
   dim3 block(kTX, kTY);
-  const unsigned band_blocks = (unsigned)kf_num_sms() * 4;
+  const unsigned band_blocks = (unsigned)kf_num_sms() * 8;
   dim3 grid((dp.nx + kTX - 1) / kTX, (dp.ny + kTY - 1) / kTY, (dp.nz + kZSlab - 1) / kZSlab);
   FusedArgs a = make_args(live, can, dp, st);
   void *buf[2][3] = {{psi->p[0], psi->p[1], psi->p[2]}, {psi->q[0], psi->q[1], psi->q[2]}};
+  int *lst[2] = {lists, lists + dp.count};
   for (int it = 0; it < iterations; ++it) {
     void **in = buf[it & 1], **out = buf[(it + 1) & 1];
     a.ix = (const float *)in[0];
@@ -365,13 +485,18 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
     a.oy = (float *)out[1];
     a.oz = (float *)out[2];
     a.iter = it;
-    k_fused_stream<<<grid, block, 0, s>>>(a, band);
-    k_fused_band<<<band_blocks, kBandThreads, 0, s>>>(a, band);
+    if (!band_only) {
+      k_fused_stream<<<grid, block, 0, s>>>(a, lst[0]);
+      k_fused_band<false><<<band_blocks, kBandThreads, 0, s>>>(a, lst[0], nullptr);
+    } else {
+      if (it == 0) k_fused_stream<<<grid, block, 0, s>>>(a, lst[0]);
+      k_fused_band<true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
+    }
   }
 }
 
 int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp, int iterations,
-                   IterStats *st, cudaStream_t s) {
+                   IterStats *st, bool band_only, cudaStream_t s) {
   int rc = kf_field_ensure_pair(psi);
   if (rc) return rc;
   rc = kf_field_band_list(psi, &psi->band);
@@ -379,15 +504,15 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
   const void *key[10] = {live->phi, can->phi, psi->p[0], psi->p[1], psi->p[2],
                          psi->q[0], psi->q[1], psi->q[2], st, psi->band};
   FusedGraph *g = psi->graph;
-  bool hit = g && g->iterations == iterations && memcmp(g->key_ptr, key, sizeof(key)) == 0 &&
-             memcmp(&g->dp, &dp, sizeof(dp)) == 0;
+  bool hit = g && g->iterations == iterations && g->band_only == band_only &&
+             memcmp(g->key_ptr, key, sizeof(key)) == 0 && memcmp(&g->dp, &dp, sizeof(dp)) == 0;
   if (!hit) {
     kf_fused_graph_destroy(psi->graph);
     psi->graph = g = new FusedGraph();
     KF_CHECK_CUDA(cudaStreamCreateWithFlags(&g->capture, cudaStreamNonBlocking));
     cudaGraph_t graph;
     KF_CHECK_CUDA(cudaStreamBeginCapture(g->capture, cudaStreamCaptureModeThreadLocal));
-    launch_iterations(live, can, psi, dp, iterations, st, psi->band, g->capture);
+    launch_iterations(live, can, psi, dp, iterations, st, psi->band, band_only, g->capture);
     cudaError_t le = cudaGetLastError();
     KF_CHECK_CUDA(cudaStreamEndCapture(g->capture, &graph));
     if (le != cudaSuccess) {
@@ -398,6 +523,7 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) return kf_cuda_fail(ie, "cudaGraphInstantiate");
     g->iterations = iterations;
+    g->band_only = band_only;
     memcpy(g->key_ptr, key, sizeof(key));
     g->dp = dp;
   }

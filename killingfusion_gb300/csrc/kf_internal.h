@@ -41,7 +41,7 @@ struct kf_field_s {
   void *plain_scratch;    // intermediate fields of the per-term solver
   size_t plain_bytes;
   FusedGraph *graph;      // captured fused iteration loop
-  int *band;              // voxels inside the band of the current iteration
+  int *band;              // band-voxel lists (two, of one int per voxel each)
 };
 
 // ---------------------------------------------------------------------------
@@ -99,11 +99,13 @@ struct IterStats {
   unsigned int max_delta; // bits of max |dpsi| (non-negative float)
   int diverged;           // psi non-finite inside the band
   int skipped;            // iteration skipped after convergence
+  unsigned int list;      // entries of this iteration's band-voxel list
+  unsigned int pad;
 };
 
 // solver entry points implemented in the solver translation units
 int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
-                   int iterations, IterStats *stats_dev, cudaStream_t s);
+                   int iterations, IterStats *stats_dev, bool band_only, cudaStream_t s);
 int kf_solve_plain(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
                    int iterations, IterStats *stats_dev, cudaStream_t s);
 int kf_solve_exact(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
@@ -116,7 +118,7 @@ int kf_gradient_ref_launch(kf_grid live, kf_grid can, kf_field psi, const DevPar
 int kf_field_ensure_pair(kf_field f);
 // per-iteration statistics buffers of a field (device + pinned host)
 int kf_field_stats(kf_field f, int iterations, IterStats **dev);
-// list of band voxels (one int per voxel of the grid)
+// two band-voxel lists (one int per voxel of the grid each)
 int kf_field_band_list(kf_field f, int **out);
 // free the solver workspace of a field (graph, scratch, statistics)
 void kf_field_release_solver(kf_field f);

@@ -150,7 +150,7 @@ def test_exact_solver_bitexact_64cubed(gpu, oracle, weights):
     np.testing.assert_array_equal(psi, opsi)
 
 
-@pytest.mark.parametrize("solver", ["fused", "plain"])
+@pytest.mark.parametrize("solver", ["fused", "plain", "band"])
 def test_fp32_solvers_match_oracle_stable_weights(gpu, oracle, solver):
     """Float32 solvers within 1e-4 voxel of the FP64 oracle after 100
     iterations with the reference's own weights (config.cpp:45-54)."""
@@ -178,6 +178,26 @@ def test_fused_and_plain_agree(gpu):
         gpu.psi_solve(live, can, f, P, 50, solver)
         out[solver] = f.download()
     assert np.abs(out["fused"] - out["plain"]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("weights,iters", [("paper", 200), ("paper", 37), ("reference", 100)])
+def test_band_solver_equals_fused(gpu, weights, iters):
+    """The band-only solver visits only the shrinking band after the first
+    dense pass; psi, band counts and statistics equal the dense fused
+    solver's bit for bit -- at the paper weights too, over the full
+    iteration count, where any difference would be amplified."""
+    voxel = 0.004
+    P = gpu.Params.paper(voxel) if weights == "paper" else gpu.Params.reference(voxel, 5.0)
+    can, live, _, _ = sphere_sdfs(gpu, P)
+    out, st = {}, {}
+    for solver in ("fused", "band"):
+        f = gpu.Field(live.dims, gpu.KF_F32)
+        st[solver] = gpu.psi_solve(live, can, f, P, iters, solver)
+        out[solver] = f.download()
+    np.testing.assert_array_equal(out["band"], out["fused"])
+    for k in ("iterations_run", "active_first", "active_last", "max_delta_last"):
+        assert st["band"][k] == st["fused"][k], k
+    assert st["band"]["active_last"] <= st["band"]["active_first"]
 
 
 def test_fp32_paper_weights_short_horizon(gpu, oracle):
@@ -218,7 +238,8 @@ def test_divergence_is_reported(gpu):
     P = gpu.Params.reference(voxel, 5.0)
     can, live = small_pair(24, voxel, 5.0, seed=1)
     gl, gc = make_grid(gpu, live, voxel, P), make_grid(gpu, can, voxel, P)
-    for prec, solver in ((gpu.KF_F32, "fused"), (gpu.KF_F32, "plain"), (gpu.KF_F64, "exact")):
+    for prec, solver in ((gpu.KF_F32, "fused"), (gpu.KF_F32, "plain"), (gpu.KF_F32, "band"),
+                         (gpu.KF_F64, "exact")):
         f = gpu.Field(gl.dims, prec)
         psi = np.zeros(live.shape + (3,))
         z, y, x = np.argwhere((live > -0.01) & (live < 0.01))[0]
@@ -233,10 +254,15 @@ def test_early_exit_convergence_flag(gpu):
     voxel = 0.004
     P = gpu.Params.reference(voxel, 5.0).with_(early_exit=True, threshold=1e-4)
     can, live, _, _ = sphere_sdfs(gpu, P)
-    f = gpu.Field(live.dims, gpu.KF_F32)
-    st = gpu.psi_solve(live, can, f, P, 400, "fused")
-    assert st["converged"] == 1 and st["iterations_run"] < 400
-    assert st["max_delta_last"] <= 1e-4
+    res = {}
+    for solver in ("fused", "band"):
+        f = gpu.Field(live.dims, gpu.KF_F32)
+        st = gpu.psi_solve(live, can, f, P, 400, solver)
+        assert st["converged"] == 1 and st["iterations_run"] < 400
+        assert st["max_delta_last"] <= 1e-4
+        res[solver] = (st["iterations_run"], f.download())
+    assert res["fused"][0] == res["band"][0]
+    np.testing.assert_array_equal(res["fused"][1], res["band"][1])
 
 
 # ---------------------------------------------------------------------------
