@@ -41,6 +41,7 @@ struct IntegrateArgs {
   double W[16];  // world -> camera, row-major
   double K[9];   // intrinsics, row-major
   float Wf[12], Kf[6];
+  float vf, min0f, min1f, min2f;
   double voxel, min0, min1, min2, unknown_clip, min_depth, max_depth;
   float min_depth_up, max_depth_down;  // float neighbours of the depth range
   int width, height;
@@ -81,13 +82,15 @@ __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, i
                                                       int nx, int ny, int nz,
                                                       const float *__restrict__ depth,
                                                       IntegrateArgs a) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)nx * ny * nz) return;
-  int x, y, z;
-  voxel_xyz(i, nx, ny, x, y, z);
-  const float Xf = (float)(a.voxel * ((double)x + 0.5) + a.min0);
-  const float Yf = (float)(a.voxel * ((double)y + 0.5) + a.min1);
-  const float Zf = (float)(a.voxel * ((double)z + 0.5) + a.min2);
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= nx || y >= ny) return;
+  const int64_t i = ((int64_t)z * ny + y) * nx + x;
+  // voxel centre in float (its error, < 1e-6 m, is covered by the margin)
+  const float Xf = a.vf * ((float)x + 0.5f) + a.min0f;
+  const float Yf = a.vf * ((float)y + 0.5f) + a.min1f;
+  const float Zf = a.vf * ((float)z + 0.5f) + a.min2f;
   const float c0 = a.Wf[0] * Xf + a.Wf[1] * Yf + a.Wf[2] * Zf + a.Wf[3];
   const float c1 = a.Wf[4] * Xf + a.Wf[5] * Yf + a.Wf[6] * Zf + a.Wf[7];
   const float c2 = a.Wf[8] * Xf + a.Wf[9] * Yf + a.Wf[10] * Zf + a.Wf[11];
@@ -355,6 +358,10 @@ int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height
   a.min0 = g->min3d[0];
   a.min1 = g->min3d[1];
   a.min2 = g->min3d[2];
+  a.vf = (float)g->voxel;
+  a.min0f = (float)g->min3d[0];
+  a.min1f = (float)g->min3d[1];
+  a.min2f = (float)g->min3d[2];
   a.unknown_clip = g->unknown_clip;
   a.min_depth = min_depth;
   a.max_depth = max_depth;
@@ -366,8 +373,9 @@ int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height
   a.max_depth_down = hi;
   a.width = width;
   a.height = height;
-  k_integrate<<<blocks_for(g->count), kBlock, 0, s>>>(g->phi, g->w, g->n[0], g->n[1], g->n[2],
-                                                      depth_dev, a);
+  dim3 block(32, kBlock / 32);
+  dim3 grid((g->n[0] + 31) / 32, (g->n[1] + block.y - 1) / block.y, g->n[2]);
+  k_integrate<<<grid, block, 0, s>>>(g->phi, g->w, g->n[0], g->n[1], g->n[2], depth_dev, a);
   KF_CHECK_LAUNCH("k_integrate");
   return KF_OK;
 }

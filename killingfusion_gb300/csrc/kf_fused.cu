@@ -9,17 +9,18 @@
 //     phi_live(i) itself when psi(i) == 0 (zero interpolation weights), so only
 //     voxels that have moved gather their 8 corners.  Voxels outside the band
 //     pass psi through; voxels inside are compacted into a list.
-//   k_fused_band  evaluates the full gradient for every listed voxel with one
-//     warp per voxel: lanes 0-19 load the psi neighbourhood (shared by
-//     shuffles), lanes 0-24 each take one of the 25 warped-SDF samples of the
-//     gradient and Hessian, lane 25 the warped value, lane 26 phi_can, and the
-//     nine derivative sums are warp reductions of +-1-weighted sample
-//     differences.
-// The band-only solver (KF_SOLVER_BAND) runs the dense pass once: a voxel
+//   k_fused_band  evaluates the full gradient of every listed voxel with a
+//     group of 8 lanes per voxel (4 voxels per warp): the group loads the 20
+//     psi neighbours of the stencil and shares them by shuffles, takes the 25
+//     warped-SDF samples of the gradient and Hessian plus the warped value
+//     (3-4 independent trilinear gathers per lane), and reduces the nine
+//     derivative sums of +-1-weighted sample differences.
+// The band-only solver (KF_SOLVER_BAND) runs the dense pass once.  A voxel
 // outside the band keeps psi, so its band test keeps failing and the band can
-// only shrink.  Each band pass then re-tests its voxels at the new psi and
-// hands the survivors to the next iteration; a voxel that leaves the band is
-// copied once into the other Jacobi buffer.  Both solvers produce the same psi.
+// only shrink: each band pass hands the voxels it updated to the next
+// iteration, which re-tests them with the warped value it samples anyway and
+// copies the ones that left the band into its output buffer.  Both solvers
+// produce the same psi.
 //
 // In the interior the psi samples that the reference takes at sub-voxel offsets
 // are closed-form linear combinations of the 3x3x3 neighbourhood:
@@ -47,7 +48,8 @@ constexpr int kZSlab = 8;
 constexpr int kTile = kThreads * kZSlab;
 constexpr int kBandWarps = 8;
 constexpr int kBandThreads = 32 * kBandWarps;
-constexpr unsigned kFull = 0xffffffffu;
+constexpr int kGroup = 8;                       // lanes per band voxel
+constexpr int kGroupsPerBlock = kBandThreads / kGroup;
 
 struct FusedArgs {
   const float *__restrict__ live;
@@ -90,57 +92,62 @@ __device__ __noinline__ float warped_value(const FusedArgs &a, int x, int y, int
 }
 
 // The 25 sub-voxel offsets (units of h) of the cell-centre samples: 0, +-e_k
-// (gradient), +-2e_k and +-e_j+-e_k (Hessian), one per lane.
-__device__ const signed char kOff25[32][3] = {
+// (gradient), +-2e_k and +-e_j+-e_k (Hessian).
+__device__ const signed char kOff25[25][3] = {
     {0, 0, 0},   {1, 0, 0},   {-1, 0, 0},  {0, 1, 0},  {0, -1, 0},  {0, 0, 1},  {0, 0, -1},
     {2, 0, 0},   {-2, 0, 0},  {0, 2, 0},   {0, -2, 0}, {0, 0, 2},   {0, 0, -2}, {1, 0, 1},
     {-1, 0, 1},  {0, 1, 1},   {0, -1, 1},  {1, 1, 0},  {-1, 1, 0},  {-1, 0, -1}, {1, 0, -1},
-    {0, -1, -1}, {0, 1, -1},  {-1, -1, 0}, {1, -1, 0}, {0, 0, 0},   {0, 0, 0},  {0, 0, 0},
-    {0, 0, 0},   {0, 0, 0},   {0, 0, 0},   {0, 0, 0}};
+    {0, -1, -1}, {0, 1, -1},  {-1, -1, 0}, {1, -1, 0}};
 
-// The 20 psi neighbours of the interior stencil, one per lane: the 19-point
-// Killing stencil and the far corner (1,1,1) of the cell-centre cell.
-__device__ const signed char kNb20[32][3] = {
+// The 20 psi neighbours of the interior stencil: the 19-point Killing
+// stencil and the far corner (1,1,1) of the cell-centre cell.
+__device__ const signed char kNb20[24][3] = {
     {0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},   {0, -1, 0}, {0, 0, 1},  {0, 0, -1},
     {1, 1, 0},  {1, -1, 0}, {-1, 1, 0}, {-1, -1, 0}, {1, 0, 1},  {1, 0, -1}, {-1, 0, 1},
     {-1, 0, -1}, {0, 1, 1}, {0, 1, -1}, {0, -1, 1},  {0, -1, -1}, {1, 1, 1},  {0, 0, 0},
-    {0, 0, 0},  {0, 0, 0},  {0, 0, 0},  {0, 0, 0},   {0, 0, 0},  {0, 0, 0},  {0, 0, 0},
-    {0, 0, 0},  {0, 0, 0},  {0, 0, 0},  {0, 0, 0}};
+    {0, 0, 0},  {0, 0, 0},  {0, 0, 0}};
 enum { N000 = 0, NXP, NXM, NYP, NYM, NZP, NZM, NXPYP, NXPYM, NXMYP, NXMYM, NXPZP, NXPZM, NXMZP,
        NXMZM, NYPZP, NYPZM, NYMZP, NYMZM, N111 };
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+__device__ __forceinline__ float group_sum(float v, unsigned mask) {
+  v += __shfl_xor_sync(mask, v, 4, kGroup);
+  v += __shfl_xor_sync(mask, v, 2, kGroup);
+  v += __shfl_xor_sync(mask, v, 1, kGroup);
   return v;
 }
 
-// Step d = -alpha * g of an interior voxel (1 <= x,y,z <= n-2), by one warp.
-// All lanes return the same d, warped value s, distance gradient g and
-// monitored energy e.
-__device__ void gradient_warp(const FusedArgs &a, int x, int y, int z, int64_t idx, int lane,
-                              float d[3], float &s_out, float g_out[3], float &e_out) {
+// One interior voxel (1 <= x,y,z <= n-2) by a group of 8 lanes.  Every lane
+// of the group returns the step d = -alpha * g, the warped value s at
+// i + psi(i), and the monitored energy e.
+__device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t idx, int gl,
+                               unsigned gmask, float d[3], float &s_out, float &e_out, float c0[3]) {
   const DevParams &dp = a.dp;
   const int64_t sy = dp.nx, sz = (int64_t)dp.nx * dp.ny;
   const float h = a.h;
 
-  // loads: psi at lane's neighbour (lanes 0-19), phi_can (lane 26)
-  float q[3] = {0.f, 0.f, 0.f};
-  if (lane < 20) {
-    int64_t j = idx + __ldg(&kNb20[lane][0]) + __ldg(&kNb20[lane][1]) * sy + __ldg(&kNb20[lane][2]) * sz;
-    q[0] = __ldg(a.ix + j);
-    q[1] = __ldg(a.iy + j);
-    q[2] = __ldg(a.iz + j);
+  // psi neighbours gl, gl+8, gl+16 (those < 20); phi_can on lane 2
+  float q[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int n = gl + 8 * r;
+    if (n < 20) {
+      const int64_t j = idx + __ldg(&kNb20[n][0]) + __ldg(&kNb20[n][1]) * sy + __ldg(&kNb20[n][2]) * sz;
+      q[r][0] = __ldg(a.ix + j);
+      q[r][1] = __ldg(a.iy + j);
+      q[r][2] = __ldg(a.iz + j);
+    } else {
+      q[r][0] = q[r][1] = q[r][2] = 0.f;
+    }
   }
-  const float canv = lane == 26 ? __ldg(a.can + idx) : 0.f;
+  const float canv = gl == 2 ? __ldg(a.can + idx) : 0.f;
 
-  float kg[3], div[3] = {0.f, 0.f, 0.f}, m[3][7], c0[3], J[3][3];
+  float kg[3], div[3] = {0.f, 0.f, 0.f}, m[3][7], J[3][3];
   const float two_h = 2.f * h, hh = h * h;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     float v[20];
 #pragma unroll
-    for (int n = 0; n < 20; ++n) v[n] = __shfl_sync(kFull, q[c], n);
+    for (int n = 0; n < 20; ++n) v[n] = __shfl_sync(gmask, q[n >> 3][c], n & 7, kGroup);
     const float v000 = v[N000];
     c0[c] = v000;
     // Killing second differences (DisplacementField.cpp:326-331)
@@ -183,44 +190,65 @@ __device__ void gradient_warp(const FusedArgs &a, int x, int y, int z, int64_t i
     for (int c = 0; c < 3; ++c) kg[c] = kg[c] * sc / den;
   }
 
-  // one trilinear sample per lane: lanes 0-24 the cell-centre samples
-  // (SDF::getDistancef at i+0.5+h*o, SDF.cpp:577-582: the half voxel it adds is
-  // removed again by getDistance), lanes 25-31 the warped value at i + psi(i)
-  const int o0 = __ldg(&kOff25[lane][0]), o1 = __ldg(&kOff25[lane][1]), o2 = __ldg(&kOff25[lane][2]);
-  float t[3];
-  if (lane < 25) {
-    const float of[3] = {(float)o0, (float)o1, (float)o2};
-    const float base[3] = {(float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f};
+  // samples j = gl + 8r: j < 25 the cell-centre samples (SDF::getDistancef at
+  // i+0.5+h*o, SDF.cpp:577-582: the half voxel it adds is removed again by
+  // getDistance), j == 25 the warped value at i + psi(i)
+  float fs[4];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      float lin = of[0] * m[c][1] + of[1] * m[c][2] + of[2] * m[c][3];
-      float quad = of[0] * of[1] * m[c][4] + of[0] * of[2] * m[c][5] + of[1] * of[2] * m[c][6];
-      t[c] = (base[c] + h * of[c]) + (m[c][0] + h * (lin + h * quad));
+  for (int r = 0; r < 4; ++r) {
+    const int j = gl + 8 * r;
+    float t0, t1, t2;
+    if (j < 25) {
+      const float o0 = (float)__ldg(&kOff25[j][0]), o1 = (float)__ldg(&kOff25[j][1]),
+                  o2 = (float)__ldg(&kOff25[j][2]);
+      float t[3];
+      const float base[3] = {(float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f};
+      const float of[3] = {o0, o1, o2};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float lin = o0 * m[c][1] + o1 * m[c][2] + o2 * m[c][3];
+        float quad = o0 * o1 * m[c][4] + o0 * o2 * m[c][5] + o1 * o2 * m[c][6];
+        t[c] = (base[c] + h * of[c]) + (m[c][0] + h * (lin + h * quad));
+      }
+      t0 = t[0]; t1 = t[1]; t2 = t[2];
+    } else {
+      t0 = (((float)x + c0[0]) + 0.5f) - 0.5f;
+      t1 = (((float)y + c0[1]) + 0.5f) - 0.5f;
+      t2 = (((float)z + c0[2]) + 0.5f) - 0.5f;
     }
-  } else {
-    t[0] = (((float)x + c0[0]) + 0.5f) - 0.5f;
-    t[1] = (((float)y + c0[1]) + 0.5f) - 0.5f;
-    t[2] = (((float)z + c0[2]) + 0.5f) - 0.5f;
+    fs[r] = j <= 25 ? phi_tri(a, t0, t1, t2) : 0.f;
   }
-  const float f = phi_tri(a, t[0], t[1], t[2]);
-  const float f0 = __shfl_sync(kFull, f, 0);
-  const float s = __shfl_sync(kFull, f, 25);
-  const float cv = __shfl_sync(kFull, canv, 26);
+  const float f0 = __shfl_sync(gmask, fs[0], 0, kGroup);
+  const float s = __shfl_sync(gmask, fs[3], 1, kGroup);
+  const float cv = __shfl_sync(gmask, canv, 2, kGroup);
   // derivative stencils on sample differences (the constant f0 cancels):
   // gradient +-1 on +-e_k, Hessian +1 on +-2e_k, o_j*o_k on the diagonals
-  const float df = lane < 25 ? f - f0 : 0.f;
-  const int nzc = (o0 != 0) + (o1 != 0) + (o2 != 0);
-  const int amax = max(abs(o0), max(abs(o1), abs(o2)));
-  const bool first = nzc == 1 && amax == 1, second = nzc == 1 && amax == 2;
-  float gx = warp_sum(first ? (float)o0 * df : 0.f);
-  float gy = warp_sum(first ? (float)o1 * df : 0.f);
-  float gz = warp_sum(first ? (float)o2 * df : 0.f);
-  float hxx = warp_sum(second && o0 ? df : 0.f);
-  float hyy = warp_sum(second && o1 ? df : 0.f);
-  float hzz = warp_sum(second && o2 ? df : 0.f);
-  float hxy = warp_sum(nzc == 2 && !o2 ? (float)(o0 * o1) * df : 0.f);
-  float hxz = warp_sum(nzc == 2 && !o1 ? (float)(o0 * o2) * df : 0.f);
-  float hyz = warp_sum(nzc == 2 && !o0 ? (float)(o1 * o2) * df : 0.f);
+  float gx = 0.f, gy = 0.f, gz = 0.f, hxx = 0.f, hyy = 0.f, hzz = 0.f, hxy = 0.f, hxz = 0.f, hyz = 0.f;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int j = gl + 8 * r;
+    if (j >= 25) continue;
+    const int o0 = __ldg(&kOff25[j][0]), o1 = __ldg(&kOff25[j][1]), o2 = __ldg(&kOff25[j][2]);
+    const float df = fs[r] - f0;
+    const int nzc = (o0 != 0) + (o1 != 0) + (o2 != 0);
+    const int amax = max(abs(o0), max(abs(o1), abs(o2)));
+    if (nzc == 1 && amax == 1) {
+      gx += (float)o0 * df;
+      gy += (float)o1 * df;
+      gz += (float)o2 * df;
+    } else if (nzc == 1 && amax == 2) {
+      if (o0) hxx += df;
+      if (o1) hyy += df;
+      if (o2) hzz += df;
+    } else if (nzc == 2) {
+      if (!o2) hxy += (float)(o0 * o1) * df;
+      if (!o1) hxz += (float)(o0 * o2) * df;
+      if (!o0) hyz += (float)(o1 * o2) * df;
+    }
+  }
+  gx = group_sum(gx, gmask); gy = group_sum(gy, gmask); gz = group_sum(gz, gmask);
+  hxx = group_sum(hxx, gmask); hyy = group_sum(hyy, gmask); hzz = group_sum(hzz, gmask);
+  hxy = group_sum(hxy, gmask); hxz = group_sum(hxz, gmask); hyz = group_sum(hyz, gmask);
   const float inv2h = 1.f / (2.f * h), inv4hh = 1.f / (4.f * h * h);
   const float g[3] = {gx * inv2h, gy * inv2h, gz * inv2h};
   hxx *= inv4hh; hyy *= inv4hh; hzz *= inv4hh; hxy *= inv4hh; hxz *= inv4hh; hyz *= inv4hh;
@@ -246,8 +274,8 @@ __device__ void gradient_warp(const FusedArgs &a, int x, int y, int z, int64_t i
       }
     e += a.omega_k * (fr + a.gamma_k * tr);
   }
-  const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
   if (dp.use_levelset) {
+    const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
     float hg0 = hxx * g[0] + hxy * g[1] + hxz * g[2];
     float hg1 = hxy * g[0] + hyy * g[1] + hyz * g[2];
     float hg2 = hxz * g[0] + hyz * g[1] + hzz * g[2];
@@ -259,38 +287,35 @@ __device__ void gradient_warp(const FusedArgs &a, int x, int y, int z, int64_t i
     e += a.omega_s * 0.5f * r * r;
   }
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    d[k] = -a.alpha * grad[k];
-    g_out[k] = g[k];
-  }
+  for (int k = 0; k < 3; ++k) d[k] = -a.alpha * grad[k];
   s_out = s;
   e_out = e;
 }
 
 // Generic reference-order gradient for the outer shell (one thread).
 __device__ __noinline__ void gradient_generic(const FusedArgs &a, int x, int y, int z, float d[3],
-                                              float &s_out, float g_out[3], float &e_out) {
+                                              float &s_out, float &e_out) {
   const DevParams &dp = a.dp;
   PhiView<float> lv{a.live, dp.nx, dp.ny, dp.nz, a.oob};
   PhiView<float> cv{a.can, dp.nx, dp.ny, dp.nz, a.oob};
   PsiView<float, float> f{a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz};
   TParams<float> tp(dp);
-  float g[3];
+  float g[3], gd[3];
   energy_gradient(lv, cv, f, tp, x, y, z, g);
 #pragma unroll
   for (int k = 0; k < 3; ++k) d[k] = -tp.alpha * g[k];
   s_out = warped_distance(lv, f, x, y, z);
-  distance_gradient(lv, f, tp.delta_size, x, y, z, g_out);
-  e_out = monitor_energy(a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz, x, y, z, s_out, cv.at(x, y, z),
-                         g_out, dp);
+  distance_gradient(lv, f, tp.delta_size, x, y, z, gd);
+  e_out = monitor_energy(a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz, x, y, z, s_out, cv.at(x, y, z), gd,
+                         dp);
 }
 
-__device__ __forceinline__ void voxel_xyz(const DevParams &dp, int64_t i, int &x, int &y, int &z) {
-  const int64_t sz = (int64_t)dp.nx * dp.ny;
-  z = (int)(i / sz);
-  int64_t r = i - (int64_t)z * sz;
-  y = (int)(r / dp.nx);
-  x = (int)(r - (int64_t)y * dp.nx);
+__device__ __forceinline__ void voxel_xyz(const DevParams &dp, int i, int &x, int &y, int &z) {
+  const unsigned plane = (unsigned)dp.nx * (unsigned)dp.ny;
+  z = (int)((unsigned)i / plane);
+  const unsigned r = (unsigned)i - (unsigned)z * plane;
+  y = (int)(r / (unsigned)dp.nx);
+  x = (int)(r - (unsigned)y * (unsigned)dp.nx);
 }
 
 // Dense pass: stream the slab, pass psi through outside the band, list the
@@ -345,80 +370,76 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
   for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
 }
 
-// Band pass: one warp per listed voxel.  kCarry: re-test the band at the new
-// psi and list the survivors for the next iteration (list_out, counted in
-// st[iter+1].list); a listed entry ~i marks a voxel that left the band, whose
-// value is copied into the output buffer.
+// Band pass: a group of 8 lanes per listed voxel.  Every listed voxel is
+// re-tested with its warped value: one outside the band is passed through
+// (it left the band in the previous iteration; the dense pass lists only
+// voxels in the band).  kCarry: the voxels updated here form the next
+// iteration's list (list_out, counted in st[iter+1].list).
 template <bool kCarry>
-__global__ void __launch_bounds__(kBandThreads) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
+__global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
                                                              int *__restrict__ list_out) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.iter].skipped = 1;
     return;
   }
   const DevParams &dp = a.dp;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & (kGroup - 1);
+  const int group = threadIdx.x / kGroup;  // group within the block
+  const unsigned gmask = 0xffu << (lane & ~(kGroup - 1));
   const int nq = (int)a.st[a.iter].list;
-  const int total_warps = gridDim.x * kBandWarps;
-  const int rounds = (nq + total_warps - 1) / total_warps;
-  __shared__ int s_next[kBandWarps];
+  const int total_groups = gridDim.x * kGroupsPerBlock;
+  const int rounds = (nq + total_groups - 1) / total_groups;
+  __shared__ int s_next[kGroupsPerBlock];
   float maxd = 0.f;
   double energy = 0.0;
   unsigned active = 0;
   bool diverged = false;
   for (int r = 0; r < rounds; ++r) {
-    const int k = (r * gridDim.x + blockIdx.x) * kBandWarps + warp;
-    int next = INT32_MIN;  // entry this warp hands to the next iteration
+    const int k = (r * gridDim.x + blockIdx.x) * kGroupsPerBlock + group;
+    int next = -1;  // voxel this group hands to the next iteration
     if (k < nq) {
-      const int e = list_in[k];
-      if (e < 0) {
-        if (lane == 0) {  // left the band last iteration: settle both buffers
-          const int64_t i = ~e;
-          a.ox[i] = a.ix[i];
-          a.oy[i] = a.iy[i];
-          a.oz[i] = a.iz[i];
-        }
-      } else {
-        const int64_t i = e;
-        int x, y, z;
-        voxel_xyz(dp, i, x, y, z);
-        float d[3], s, g[3], en;
-        const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 &&
-                              z <= dp.nz - 2;
-        if (interior) {
-          gradient_warp(a, x, y, z, i, lane, d, s, g, en);
-        } else {
-          if (lane == 0) gradient_generic(a, x, y, z, d, s, g, en);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) d[c] = __shfl_sync(kFull, d[c], 0);
-        }
-        if (lane == 0) {
-          const float p0 = a.ix[i], p1 = a.iy[i], p2 = a.iz[i];
-          if (!isfinite(p0) || !isfinite(p1) || !isfinite(p2)) diverged = true;
-          const float n0 = p0 + d[0], n1 = p1 + d[1], n2 = p2 + d[2];
-          a.ox[i] = n0;
-          a.oy[i] = n1;
-          a.oz[i] = n2;
+      const int i = list_in[k];
+      int x, y, z;
+      voxel_xyz(dp, i, x, y, z);
+      float d[3] = {0.f, 0.f, 0.f}, s = 0.f, en = 0.f, c0[3] = {0.f, 0.f, 0.f};
+      const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 &&
+                            z <= dp.nz - 2;
+      if (interior) {
+        gradient_group(a, x, y, z, i, gl, gmask, d, s, en, c0);
+      } else if (gl == 0) {
+        gradient_generic(a, x, y, z, d, s, en);
+        c0[0] = a.ix[i];
+        c0[1] = a.iy[i];
+        c0[2] = a.iz[i];
+      }
+      if (gl == 0) {
+        if (in_band(s, a.band_hi, a.band_lo)) {
+          if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
+          a.ox[i] = c0[0] + d[0];
+          a.oy[i] = c0[1] + d[1];
+          a.oz[i] = c0[2] + d[2];
           maxd = fmaxf(maxd, sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
           energy += (double)en;
           ++active;
-          if (kCarry) {
-            const float s1 = warped_value(a, x, y, z, n0, n1, n2);
-            next = in_band(s1, a.band_hi, a.band_lo) ? e : ~e;
-          }
+          next = i;
+        } else {  // left the band: its psi is final, settle the output buffer
+          a.ox[i] = c0[0];
+          a.oy[i] = c0[1];
+          a.oz[i] = c0[2];
         }
       }
     }
     if (kCarry) {
-      if (lane == 0) s_next[warp] = next;
+      if (gl == 0) s_next[group] = next;
       __syncthreads();
       if (threadIdx.x == 0) {
         int cnt = 0;
-        for (int w = 0; w < kBandWarps; ++w) cnt += s_next[w] != INT32_MIN;
+        for (int w = 0; w < kGroupsPerBlock; ++w) cnt += s_next[w] >= 0;
         if (cnt) {
           int b = (int)atomicAdd(&a.st[a.iter + 1].list, (unsigned)cnt);
-          for (int w = 0; w < kBandWarps; ++w)
-            if (s_next[w] != INT32_MIN) list_out[b++] = s_next[w];
+          for (int w = 0; w < kGroupsPerBlock; ++w)
+            if (s_next[w] >= 0) list_out[b++] = s_next[w];
         }
       }
       __syncthreads();
