@@ -370,11 +370,115 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
   for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
 }
 
-// Band pass: a group of 8 lanes per listed voxel.  Every listed voxel is
-// re-tested with its warped value: one outside the band is passed through
-// (it left the band in the previous iteration; the dense pass lists only
-// voxels in the band).  kCarry: the voxels updated here form the next
-// iteration's list (list_out, counted in st[iter+1].list).
+// Update one band voxel with the group of 8 lanes it is assigned to.  The
+// voxel is re-tested with its warped value: one outside the band is passed
+// through (it left the band in the previous iteration).  Returns the voxel
+// for the next iteration's list (-1 if it left the band); the group leader
+// accumulates the statistics.
+__device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int gl, unsigned gmask,
+                                                 float &maxd, double &energy, unsigned &active,
+                                                 bool &diverged) {
+  const DevParams &dp = a.dp;
+  int x, y, z;
+  voxel_xyz(dp, i, x, y, z);
+  float d[3] = {0.f, 0.f, 0.f}, s = 0.f, en = 0.f, c0[3] = {0.f, 0.f, 0.f};
+  const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 &&
+                        z <= dp.nz - 2;
+  if (interior) {
+    gradient_group(a, x, y, z, i, gl, gmask, d, s, en, c0);
+  } else if (gl == 0) {
+    gradient_generic(a, x, y, z, d, s, en);
+    c0[0] = a.ix[i];
+    c0[1] = a.iy[i];
+    c0[2] = a.iz[i];
+  }
+  int next = -1;
+  if (gl == 0) {
+    if (in_band(s, a.band_hi, a.band_lo)) {
+      if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
+      a.ox[i] = c0[0] + d[0];
+      a.oy[i] = c0[1] + d[1];
+      a.oz[i] = c0[2] + d[2];
+      maxd = fmaxf(maxd, sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+      energy += (double)en;
+      ++active;
+      next = i;
+    } else {  // left the band: its psi is final, settle the output buffer
+      a.ox[i] = c0[0];
+      a.oy[i] = c0[1];
+      a.oz[i] = c0[2];
+    }
+  }
+  return next;
+}
+
+// One fused iteration in a single pass: each CTA streams its 32 x 8 x 8 slab
+// (psi passed through outside the band) and then updates the band voxels of
+// its own slab, 8 lanes per voxel.  The band work of one CTA overlaps the
+// streaming of the others.
+__global__ void __launch_bounds__(kThreads, 3) k_fused_step(FusedArgs a) {
+  if (iteration_gated(a.st, a.iter, a.dp)) {
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+      a.st[a.iter].skipped = 1;
+    return;
+  }
+  __shared__ int queue[kTile];
+  __shared__ int qn;
+  const DevParams &dp = a.dp;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  const int x = blockIdx.x * kTX + threadIdx.x;
+  const int y = blockIdx.y * kTY + threadIdx.y;
+  const int z0 = blockIdx.z * kZSlab;
+  if (tid == 0) qn = 0;
+  __syncthreads();
+  {
+    const bool col = x < dp.nx && y < dp.ny;
+    const int64_t sz = (int64_t)dp.nx * dp.ny;
+    const int64_t base = ((int64_t)z0 * dp.ny + y) * dp.nx + x;
+    float px[kZSlab], py[kZSlab], pz[kZSlab], ph[kZSlab];
+#pragma unroll
+    for (int j = 0; j < kZSlab; ++j) {
+      bool ok = col && (z0 + j) < dp.nz;
+      int64_t i = base + j * sz;
+      px[j] = ok ? __ldcs(a.ix + i) : 0.f;
+      py[j] = ok ? __ldcs(a.iy + i) : 0.f;
+      pz[j] = ok ? __ldcs(a.iz + i) : 0.f;
+      ph[j] = ok ? __ldg(a.live + i) : 0.f;
+    }
+#pragma unroll
+    for (int j = 0; j < kZSlab; ++j) {
+      int z = z0 + j;
+      if (!col || z >= dp.nz) continue;
+      int64_t i = base + j * sz;
+      float s = ph[j];
+      if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f) s = warped_value(a, x, y, z, px[j], py[j], pz[j]);
+      if (in_band(s, a.band_hi, a.band_lo)) {
+        queue[atomicAdd(&qn, 1)] = (int)i;
+      } else {
+        __stcs(a.ox + i, px[j]);
+        __stcs(a.oy + i, py[j]);
+        __stcs(a.oz + i, pz[j]);
+      }
+    }
+  }
+  __syncthreads();
+  const int nq = qn;
+  if (nq == 0) return;
+  const int lane = tid & 31, gl = lane & (kGroup - 1);
+  const unsigned gmask = 0xffu << (lane & ~(kGroup - 1));
+  float maxd = 0.f;
+  double energy = 0.0;
+  unsigned active = 0;
+  bool diverged = false;
+  for (int k = tid / kGroup; k < nq; k += kGroupsPerBlock)
+    update_band_voxel(a, queue[k], gl, gmask, maxd, energy, active, diverged);
+  reduce_iter_stats<kThreads>(a.st + a.iter, active, maxd, energy, diverged);
+}
+
+// Band pass of the band-only solver: a group of 8 lanes per listed voxel;
+// the voxels updated here form the next iteration's list (list_out, counted
+// in st[iter+1].list).  Launched as one resident wave that loops over the
+// list.
 template <bool kCarry>
 __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
                                                              int *__restrict__ list_out) {
@@ -382,7 +486,6 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.iter].skipped = 1;
     return;
   }
-  const DevParams &dp = a.dp;
   const int lane = threadIdx.x & 31;
   const int gl = lane & (kGroup - 1);
   const int group = threadIdx.x / kGroup;  // group within the block
@@ -398,38 +501,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
   for (int r = 0; r < rounds; ++r) {
     const int k = (r * gridDim.x + blockIdx.x) * kGroupsPerBlock + group;
     int next = -1;  // voxel this group hands to the next iteration
-    if (k < nq) {
-      const int i = list_in[k];
-      int x, y, z;
-      voxel_xyz(dp, i, x, y, z);
-      float d[3] = {0.f, 0.f, 0.f}, s = 0.f, en = 0.f, c0[3] = {0.f, 0.f, 0.f};
-      const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 &&
-                            z <= dp.nz - 2;
-      if (interior) {
-        gradient_group(a, x, y, z, i, gl, gmask, d, s, en, c0);
-      } else if (gl == 0) {
-        gradient_generic(a, x, y, z, d, s, en);
-        c0[0] = a.ix[i];
-        c0[1] = a.iy[i];
-        c0[2] = a.iz[i];
-      }
-      if (gl == 0) {
-        if (in_band(s, a.band_hi, a.band_lo)) {
-          if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
-          a.ox[i] = c0[0] + d[0];
-          a.oy[i] = c0[1] + d[1];
-          a.oz[i] = c0[2] + d[2];
-          maxd = fmaxf(maxd, sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
-          energy += (double)en;
-          ++active;
-          next = i;
-        } else {  // left the band: its psi is final, settle the output buffer
-          a.ox[i] = c0[0];
-          a.oy[i] = c0[1];
-          a.oz[i] = c0[2];
-        }
-      }
-    }
+    if (k < nq) next = update_band_voxel(a, list_in[k], gl, gmask, maxd, energy, active, diverged);
     if (kCarry) {
       if (gl == 0) s_next[group] = next;
       __syncthreads();
@@ -492,7 +564,7 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
                               int iterations, IterStats *st, int *lists, bool band_only,
                               cudaStream_t s) {
   dim3 block(kTX, kTY);
-  const unsigned band_blocks = (unsigned)kf_num_sms() * 8;
+  const unsigned band_blocks = (unsigned)kf_num_sms() * 3;  // one resident wave
   dim3 grid((dp.nx + kTX - 1) / kTX, (dp.ny + kTY - 1) / kTY, (dp.nz + kZSlab - 1) / kZSlab);
   FusedArgs a = make_args(live, can, dp, st);
   void *buf[2][3] = {{psi->p[0], psi->p[1], psi->p[2]}, {psi->q[0], psi->q[1], psi->q[2]}};
@@ -507,8 +579,7 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
     a.oz = (float *)out[2];
     a.iter = it;
     if (!band_only) {
-      k_fused_stream<<<grid, block, 0, s>>>(a, lst[0]);
-      k_fused_band<false><<<band_blocks, kBandThreads, 0, s>>>(a, lst[0], nullptr);
+      k_fused_step<<<grid, block, 0, s>>>(a);
     } else {
       if (it == 0) k_fused_stream<<<grid, block, 0, s>>>(a, lst[0]);
       k_fused_band<true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);

@@ -328,14 +328,15 @@ __device__ void reduce_iter_stats(IterStats *st, unsigned active, float max_delt
   __shared__ float s_m[kThreads / 32];
   __shared__ unsigned s_a[kThreads / 32];
   __shared__ int s_d;
-  if (threadIdx.x == 0) s_d = 0;
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  if (tid == 0) s_d = 0;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     energy += __shfl_xor_sync(0xffffffffu, energy, o);
     max_delta = fmaxf(max_delta, __shfl_xor_sync(0xffffffffu, max_delta, o));
     active += __shfl_xor_sync(0xffffffffu, active, o);
   }
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int lane = tid & 31, wid = tid >> 5;
   __syncthreads();
   if (diverged) s_d = 1;
   if (lane == 0) {
