@@ -145,6 +145,35 @@ int kf_field_upload(kf_field f, const void *xyz, void *stream);
 int kf_field_download(kf_field f, void *xyz, void *stream);
 int kf_field_device(kf_field f, void **px, void **py, void **pz);
 
+/* psi += other (DisplacementField::operator+, DisplacementField.cpp:73-80). */
+int kf_field_add(kf_field f, kf_field other, void *stream);
+/* psi = v everywhere (DisplacementField::initializeAllVoxels,
+ * DisplacementField.cpp:82-88). */
+int kf_field_fill(kf_field f, const double v[3], void *stream);
+/* psi at n voxels (host int32 xyz triples) into host double[n][3]
+ * (DisplacementField::getDisplacementAt, DisplacementField.cpp:22-38: a
+ * linear index outside the grid reads 0). */
+int kf_field_get_voxels(kf_field f, const int32_t *xyz, int n, double *out, void *stream);
+/* psi(i) += delta at n voxels (DisplacementField::update,
+ * DisplacementField.cpp:65-71); KF_ERR_INVALID for an index outside the
+ * grid (the reference's vector::at throws). */
+int kf_field_add_voxels(kf_field f, const int32_t *xyz, int n, const double *delta, void *stream);
+/* Trilinear samples of psi at n grid points (host double[n][3]) into host
+ * double[n][3] (DisplacementField::getDisplacementAtf, :40-58). */
+int kf_field_sample(kf_field f, const double *pts, int n, double *out, void *stream);
+
+/* Trilinear samples of phi and of the weights at n grid points (host
+ * double[n][3], grid units with the reference's half-voxel convention) into
+ * host double[n] (SDF::getDistance / SDF::getWeight, SDF.cpp:503-604;
+ * either output may be NULL). */
+int kf_grid_sample(kf_grid g, const kf_params *p, const double *pts, int n, double *phi,
+                   double *weight, void *stream);
+/* phi and weight at n voxels (host int32 xyz) into host arrays
+ * (SDF::getDistanceAtIndex / getWeightAtIndex, SDF.cpp:475-501: outside the
+ * grid phi = max_surface+epsilon, w = 0). */
+int kf_grid_get_voxels(kf_grid g, const kf_params *p, const int32_t *xyz, int n, double *phi,
+                       int64_t *weight, void *stream);
+
 /* ---- hot path --------------------------------------------------------- */
 /* SDF::integrateDepthFrame (SDF.cpp:137-197).  depth: float32 metres,
  * row-major [height][width] (host or device); c2w: row-major camera->world
@@ -189,6 +218,56 @@ int kf_fuse_warped(kf_grid dst, kf_grid other, kf_field psi, const kf_params *p,
  * capacity < count. */
 int kf_marching_cubes(kf_grid g, const kf_params *p, float *verts, int64_t capacity,
                       int64_t *ntri, void *stream);
+
+/* kf_marching_cubes into host memory (SDF::getMesh for callers without a
+ * CUDA runtime of their own): verts is a host buffer of `capacity`
+ * triangles (may be NULL to count). */
+int kf_mesh_host(kf_grid g, const kf_params *p, float *verts, int64_t capacity, int64_t *ntri,
+                 void *stream);
+
+/* ---- per-frame pipeline (KillingFusion::processNextFrame) -------------- */
+
+/* Meshes a frame can return (bit mask). */
+enum { KF_MESH_LIVE = 1, KF_MESH_REGISTERED = 2, KF_MESH_CANONICAL = 4 };
+
+typedef struct kf_fusion_config {
+  int dims[3];          /* grid size of the canonical and live SDFs          */
+  double voxel_size;    /* SDF voxel size (m)                                */
+  double min3d[3];      /* world position of the grid's min corner (m)       */
+  double K[9];          /* depth intrinsics, row-major                       */
+  int width, height;    /* depth frame size                                  */
+  double min_depth;     /* valid depth range (DatasetReader thresholds)      */
+  double max_depth;
+  kf_params params;     /* solver parameters                                 */
+  int iterations;       /* psi iterations per frame (KILLING_MAX_ITERATIONS) */
+  kf_solver solver;     /* KF_SOLVER_FUSED, _BAND, _PLAIN or _EXACT          */
+} kf_fusion_config;
+
+typedef struct kf_frame_result {
+  int32_t frame;              /* frames processed so far, this one included  */
+  int32_t reserved;
+  kf_solve_stats solve;       /* zero for the first frame                    */
+  int64_t ntri[3];            /* live, registered, canonical triangle counts */
+  const float *mesh[3];       /* host (pinned) triangle soups, 9 floats per
+                                 triangle, valid until the next call; NULL
+                                 when not requested                          */
+  double device_ms;           /* device time of the whole frame              */
+} kf_frame_result;
+
+/* The state of KillingFusion (KillingFusion.h:13-100): canonical SDF, the
+ * live frame's SDF and psi, on the device. */
+int kf_fusion_create(const kf_fusion_config *cfg, kf_fusion *out);
+int kf_fusion_destroy(kf_fusion f);
+/* KillingFusion::processNextFrame (KillingFusion.cpp:109-175).  The first
+ * frame becomes the canonical SDF; every later frame is integrated into a
+ * fresh live SDF, registered onto the canonical SDF from a zero psi
+ * (UseZeroDisplacementFieldForNextFrame), meshed, warped by psi and fused.
+ * depth: float32 metres (host or device); c2w may be NULL (identity, as
+ * KillingFusion::computeSDF uses).  meshes: KF_MESH_* bits. */
+int kf_fusion_process_frame(kf_fusion f, const float *depth, const double c2w[16], int meshes,
+                            kf_frame_result *res, void *stream);
+/* Handles of the pipeline's state (owned by the pipeline). */
+int kf_fusion_state(kf_fusion f, kf_grid *canonical, kf_grid *live, kf_field *psi);
 
 /* Marching cubes that allocates nothing.  No counterpart in the reference:
  * it exists for callers that cannot allocate device memory on their own --

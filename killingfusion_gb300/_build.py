@@ -41,7 +41,7 @@ CUDA_UNITS = [
     ("kf_batch.cu", []),
     ("kf_fusion.cu", []),
 ]
-HOST_UNITS = ["SDF.cpp", "DisplacementField.cpp", "KillingFusion.cpp"]
+HOST_UNITS = ["SDF.cpp", "DisplacementField.cpp", "DatasetReader.cpp", "KillingFusion.cpp"]
 
 
 def nvcc() -> str:
@@ -109,7 +109,7 @@ def _build_host(force: bool) -> None:
     deps += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
     if not (force or _stale(HOST_LIB, deps)):
         return
-    _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", INCLUDE, "-I", HOST, "-o", HOST_LIB]
+    _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-I", INCLUDE, "-I", HOST, "-o", HOST_LIB]
          + srcs + ["-L", LIB_DIR, "-lkillingfusion", "-Wl,-rpath,$ORIGIN"])
 
 

@@ -130,6 +130,18 @@ SIGNATURES = {
     "kf_marching_cubes": (C.c_int, [_vp, _PP, _vp, C.c_int64, C.POINTER(C.c_int64), _vp]),
     "kf_marching_cubes_noalloc": (C.c_int, [_vp, _ip3, _PP, _vp, C.c_int64, C.POINTER(C.c_int64),
                                             _vp]),
+    "kf_mesh_host": (C.c_int, [_vp, _PP, _vp, C.c_int64, C.POINTER(C.c_int64), _vp]),
+    "kf_field_add": (C.c_int, [_vp, _vp, _vp]),
+    "kf_field_fill": (C.c_int, [_vp, _dp, _vp]),
+    "kf_field_get_voxels": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
+    "kf_field_add_voxels": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
+    "kf_field_sample": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
+    "kf_grid_sample": (C.c_int, [_vp, _PP, _vp, C.c_int, _vp, _vp, _vp]),
+    "kf_grid_get_voxels": (C.c_int, [_vp, _PP, _vp, C.c_int, _vp, _vp, _vp]),
+    "kf_fusion_create": (C.c_int, [C.c_void_p, C.POINTER(_vp)]),
+    "kf_fusion_destroy": (C.c_int, [_vp]),
+    "kf_fusion_process_frame": (C.c_int, [_vp, _vp, _dp, C.c_int, C.c_void_p, _vp]),
+    "kf_fusion_state": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
 }
 
 _lib = None
@@ -320,3 +332,133 @@ def mc_case(cube: int):
     row = (C.c_int * 16)()
     check(load().kf_mc_case(cube, C.byref(em), row))
     return em.value, list(row)
+
+
+# ---------------------------------------------------------------------------
+# point queries (SDF / DisplacementField accessors)
+# ---------------------------------------------------------------------------
+
+def grid_sample(g: Grid, params: Params, pts):
+    """SDF::getDistance / SDF::getWeight at grid points [n, 3] -> (phi, w)."""
+    p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    phi = np.empty(len(p))
+    w = np.empty(len(p))
+    check(load().kf_grid_sample(g.h, C.byref(params.c()), p.ctypes.data, len(p), phi.ctypes.data,
+                                w.ctypes.data, None))
+    return phi, w
+
+
+def grid_get_voxels(g: Grid, params: Params, xyz):
+    v = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+    phi = np.empty(len(v))
+    w = np.empty(len(v), dtype=np.int64)
+    check(load().kf_grid_get_voxels(g.h, C.byref(params.c()), v.ctypes.data, len(v), phi.ctypes.data,
+                                    w.ctypes.data, None))
+    return phi, w
+
+
+def field_get_voxels(f: Field, xyz):
+    v = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+    out = np.empty((len(v), 3))
+    check(load().kf_field_get_voxels(f.h, v.ctypes.data, len(v), out.ctypes.data, None))
+    return out
+
+
+def field_sample(f: Field, pts):
+    p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    out = np.empty((len(p), 3))
+    check(load().kf_field_sample(f.h, p.ctypes.data, len(p), out.ctypes.data, None))
+    return out
+
+
+def field_add_voxels(f: Field, xyz, delta):
+    v = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+    d = np.ascontiguousarray(delta, dtype=np.float64).reshape(-1, 3)
+    check(load().kf_field_add_voxels(f.h, v.ctypes.data, len(v), d.ctypes.data, None))
+
+
+def field_add(f: Field, other: Field):
+    check(load().kf_field_add(f.h, other.h, None))
+
+
+def field_fill(f: Field, v):
+    check(load().kf_field_fill(f.h, _d(v), None))
+
+
+# ---------------------------------------------------------------------------
+# per-frame pipeline (KillingFusion::processNextFrame)
+# ---------------------------------------------------------------------------
+
+KF_MESH_LIVE, KF_MESH_REGISTERED, KF_MESH_CANONICAL = 1, 2, 4
+
+
+class FusionConfig(C.Structure):
+    _fields_ = [("dims", C.c_int * 3), ("voxel_size", C.c_double), ("min3d", C.c_double * 3),
+                ("K", C.c_double * 9), ("width", C.c_int), ("height", C.c_int),
+                ("min_depth", C.c_double), ("max_depth", C.c_double), ("params", _Params),
+                ("iterations", C.c_int), ("solver", C.c_int)]
+
+
+class FrameResult(C.Structure):
+    _fields_ = [("frame", C.c_int32), ("reserved", C.c_int32), ("solve", SolveStats),
+                ("ntri", C.c_int64 * 3), ("mesh", C.POINTER(C.c_float) * 3), ("device_ms", C.c_double)]
+
+
+class Fusion:
+    """KillingFusion's state on the device; process_frame is one
+    processNextFrame call through the C ABI."""
+
+    def __init__(self, dims, voxel_size, origin, params: Params, K=None, width=640, height=480,
+                 min_depth=0.05, max_depth=1.2, iterations=100, solver="fused"):
+        from . import synth
+        cfg = FusionConfig()
+        cfg.dims = (C.c_int * 3)(*[int(d) for d in dims])
+        cfg.voxel_size = float(voxel_size)
+        cfg.min3d = (C.c_double * 3)(*[float(v) for v in origin])
+        K = synth.K if K is None else np.asarray(K, dtype=np.float64)
+        cfg.K = (C.c_double * 9)(*[float(v) for v in K.ravel()])
+        cfg.width, cfg.height = int(width), int(height)
+        cfg.min_depth, cfg.max_depth = float(min_depth), float(max_depth)
+        cfg.params = params.c()
+        cfg.iterations = int(iterations)
+        cfg.solver = SOLVERS[solver]
+        self.cfg = cfg
+        self.params = params
+        h = _vp()
+        check(load().kf_fusion_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().kf_fusion_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def process_frame(self, depth, meshes=KF_MESH_LIVE | KF_MESH_REGISTERED | KF_MESH_CANONICAL,
+                      c2w=None, copy=True):
+        """depth: numpy float32 [h, w] (host) or a CUDA tensor.  Returns a
+        dict with the solve statistics and the requested meshes as float32
+        [T, 3, 3] arrays (copies unless copy=False)."""
+        if isinstance(depth, np.ndarray):
+            d = np.ascontiguousarray(depth, dtype=np.float32)
+            ptr = d.ctypes.data
+        else:
+            ptr = depth.data_ptr()
+        res = FrameResult()
+        pose = _d(np.asarray(c2w, dtype=np.float64).ravel()) if c2w is not None else None
+        check(load().kf_fusion_process_frame(self.h, ptr, pose, int(meshes), C.byref(res), None))
+        out = {"frame": res.frame, "solve": res.solve.as_dict(), "device_ms": res.device_ms,
+               "ntri": list(res.ntri)}
+        names = ("live", "registered", "canonical")
+        for k in range(3):
+            if meshes & (1 << k) and res.mesh[k]:
+                n = res.ntri[k]
+                a = np.ctypeslib.as_array(res.mesh[k], shape=(max(n, 1) * 9,))[: n * 9].reshape(n, 3, 3)
+                out[names[k]] = a.copy() if copy else a
+        return out
+
+    def state(self):
+        c, l, f = _vp(), _vp(), _vp()
+        check(load().kf_fusion_state(self.h, C.byref(c), C.byref(l), C.byref(f)))
+        return c.value, l.value, f.value

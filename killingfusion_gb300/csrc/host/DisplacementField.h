@@ -1,0 +1,64 @@
+// The displacement field psi with the reference's interface
+// (DisplacementField.h:9-66), stored on the device as a kf_field.  Point
+// accessors are device queries; they keep the reference's semantics (linear
+// index range check, trilinear sampling without a half-voxel shift) but each
+// call is a round trip, so hot loops belong to the C ABI.
+#pragma once
+
+#include <string>
+
+#include "kf_types.h"
+
+class DisplacementField {
+ public:
+  DisplacementField() = delete;
+  // Zero-initialised (DisplacementField.cpp:8-16).  KF_F64 fields feed the
+  // float64 exact solver.
+  DisplacementField(kf::Vec3i gridSize, double voxelSize, kf_precision precision = KF_F32);
+  DisplacementField(const DisplacementField &) = delete;
+  DisplacementField &operator=(const DisplacementField &) = delete;
+  DisplacementField(DisplacementField &&o) noexcept;
+  ~DisplacementField();
+
+  kf::Vec3d getDisplacementAt(const kf::Vec3i &spatialIndex) const;
+  kf::Vec3d getDisplacementAt(int x, int y, int z) const;
+  kf::Vec3d getDisplacementAtf(const kf::Vec3d &gridLocation) const;
+  kf::Vec3d getDisplacementAtf(double x, double y, double z) const;
+
+  // Adds deltaUpdate at spatialIndex (DisplacementField.cpp:65-71).
+  void update(const kf::Vec3i &spatialIndex, const kf::Vec3d &deltaUpdate);
+
+  // In-place addition returning *this, as the reference's operator+
+  // (DisplacementField.cpp:73-80).
+  DisplacementField &operator+(const DisplacementField &other);
+
+  void initializeAllVoxels(kf::Vec3d displacement);
+
+  // Central differences of psi~ at (x,y,z), column k = d psi / d x_k
+  // (DisplacementField.cpp:90-140).
+  kf::Mat3d computeJacobian(double x, double y, double z) const;
+  // |J|^2 + gamma <J, J^T>, 0 for a non-finite Jacobian (DisplacementField.cpp:171-193).
+  double computeKillingEnergy(double x, double y, double z) const;
+  // Finite difference of the Killing energy (DisplacementField.cpp:274-299).
+  kf::Vec3d computeKillingEnergyGradient(const kf::Vec3i &spatialIndex) const;
+  // The clamped Euler-Lagrange form the solver uses (DisplacementField.cpp:301-347).
+  kf::Vec3d computeKillingEnergyGradient2(const kf::Vec3i &spatialIndex) const;
+
+  // int32 dims[3], double voxel size, double[3N] (x,y,z per voxel)
+  // (DisplacementField.cpp:349-366).
+  void dumpToBinFile(std::string outputFilePath) const;
+  // Reads a file written by dumpToBinFile (no counterpart in the reference).
+  static DisplacementField loadFromBinFile(const std::string &path, kf_precision precision = KF_F32);
+
+  kf::Vec3i getGridSize() const { return m_gridSize; }
+  double getVoxelSize() const { return m_voxelSize; }
+  kf_precision getPrecision() const { return m_precision; }
+  kf_field handle() const { return m_field; }
+
+ private:
+  kf::Vec3d sample(const kf::Vec3d &p) const;
+  kf_field m_field = nullptr;
+  double m_voxelSize;
+  kf::Vec3i m_gridSize;
+  kf_precision m_precision;
+};

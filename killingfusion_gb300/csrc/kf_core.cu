@@ -545,6 +545,33 @@ extern "C" int kf_marching_cubes(kf_grid g, const kf_params *p, float *verts, in
   return kf_mc_run(g, dp, verts, capacity, ntri, kf_stream(stream));
 }
 
+extern "C" int kf_mesh_host(kf_grid g, const kf_params *p, float *verts, int64_t capacity,
+                            int64_t *ntri, void *stream) {
+  KF_REQUIRE(g && ntri, "NULL argument");
+  KF_REQUIRE(capacity >= 0, "capacity must be >= 0");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  cudaStream_t s = kf_stream(stream);
+  DevParams dp = kf_make_dev_params(g->n, p);
+  if (!verts || capacity == 0) return kf_mc_run(g, dp, nullptr, 0, ntri, s);
+  float *dev = nullptr;
+  KF_CHECK_CUDA(cudaMallocAsync((void **)&dev, (size_t)capacity * 9 * sizeof(float), s));
+  rc = kf_mc_run(g, dp, dev, capacity, ntri, s);
+  if (rc == KF_OK || rc == KF_ERR_CAPACITY) {
+    int64_t n = *ntri < capacity ? *ntri : capacity;
+    if (n > 0) {
+      cudaError_t e = cudaMemcpyAsync(verts, dev, (size_t)n * 9 * sizeof(float), cudaMemcpyDefault, s);
+      if (e != cudaSuccess) rc = kf_cuda_fail(e, "mesh copy to host");
+    }
+  }
+  cudaFreeAsync(dev, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess && rc == KF_OK) rc = kf_cuda_fail(e, "kf_mesh_host");
+  if (rc == KF_ERR_CAPACITY)
+    return kf_fail(KF_ERR_CAPACITY, "vertex buffer holds fewer triangles than the mesh has");
+  return rc;
+}
+
 // ---------------------------------------------------------------------------
 // psi solve
 // ---------------------------------------------------------------------------

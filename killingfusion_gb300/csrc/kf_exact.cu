@@ -13,6 +13,9 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <cstring>
+#include <vector>
+
 #include "kf_internal.h"
 #include "kf_ref_math.cuh"
 
@@ -479,5 +482,267 @@ int kf_gradient_ref_launch(kf_grid live, kf_grid can, kf_field psi, const DevPar
         f, dp, voxels, count, out, active);
   }
   KF_CHECK_LAUNCH("k_gradient_ref");
+  return KF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// point queries and field updates of the host classes (float64, reference
+// order): SDF::getDistance / getWeight / getDistanceAtIndex / getWeightAtIndex
+// (SDF.cpp:475-604), DisplacementField::getDisplacementAt / getDisplacementAtf
+// / update / operator+ / initializeAllVoxels (DisplacementField.cpp:22-88).
+// ---------------------------------------------------------------------------
+namespace {
+
+// weights through the same sampler: a PhiView over int32 weights
+struct WeightView {
+  const int32_t *w;
+  int nx, ny, nz;
+  __device__ __forceinline__ double at(int x, int y, int z) const {
+    if (x < 0 || x >= nx || y < 0 || y >= ny || z < 0 || z >= nz) return 0.0;
+    return (double)w[((int64_t)z * ny + y) * nx + x];
+  }
+};
+
+__global__ void k_grid_sample(PhiView<double> pv, WeightView wv, const double *__restrict__ pts, int n,
+                              double *__restrict__ phi, double *__restrict__ weight) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double p0 = pts[3 * i], p1 = pts[3 * i + 1], p2 = pts[3 * i + 2];
+  if (phi) phi[i] = phi_sample(pv, p0, p1, p2);
+  if (weight) {
+    double t0 = p0 - 0.5, t1 = p1 - 0.5, t2 = p2 - 0.5;
+    int b0 = (int)t0, b1 = (int)t1, b2 = (int)t2;
+    double v[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] = wv.at(b0 + (c & 1), b1 + ((c >> 1) & 1), b2 + (c >> 2));
+    weight[i] = lerp3(v, t0 - (double)b0, t1 - (double)b1, t2 - (double)b2);
+  }
+}
+
+__global__ void k_grid_get(PhiView<double> pv, WeightView wv, const int32_t *__restrict__ xyz, int n,
+                           double *__restrict__ phi, int64_t *__restrict__ weight) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  if (phi) phi[i] = pv.at(x, y, z);
+  if (weight) weight[i] = (int64_t)wv.at(x, y, z);
+}
+
+template <typename P>
+__global__ void k_field_get(PsiView<double, P> f, const int32_t *__restrict__ xyz, int n,
+                            double *__restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v[3];
+  f.at(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], v);
+  out[3 * i] = v[0];
+  out[3 * i + 1] = v[1];
+  out[3 * i + 2] = v[2];
+}
+
+template <typename P>
+__global__ void k_field_sample(PsiView<double, P> f, const double *__restrict__ pts, int n,
+                               double *__restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v[3];
+  psi_sample(f, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], v);
+  out[3 * i] = v[0];
+  out[3 * i + 1] = v[1];
+  out[3 * i + 2] = v[2];
+}
+
+// serial in list order, so repeated voxels accumulate as in the reference
+template <typename P>
+__global__ void k_field_add_voxels(P *px, P *py, P *pz, int nx, int ny, const int32_t *__restrict__ xyz,
+                                   int n, const double *__restrict__ delta) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int i = 0; i < n; ++i) {
+    const int64_t j = (int64_t)xyz[3 * i + 2] * nx * ny + (int64_t)xyz[3 * i + 1] * nx + xyz[3 * i];
+    px[j] = (P)((double)px[j] + delta[3 * i]);
+    py[j] = (P)((double)py[j] + delta[3 * i + 1]);
+    pz[j] = (P)((double)pz[j] + delta[3 * i + 2]);
+  }
+}
+
+template <typename P>
+__global__ void k_field_add(P *px, P *py, P *pz, const P *qx, const P *qy, const P *qz, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  px[i] = px[i] + qx[i];
+  py[i] = py[i] + qy[i];
+  pz[i] = pz[i] + qz[i];
+}
+
+template <typename P>
+__global__ void k_field_fill(P *px, P *py, P *pz, P a, P b, P c, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  px[i] = a;
+  py[i] = b;
+  pz[i] = c;
+}
+
+// Host staging of a small query: copy `bytes_in` of host input to the
+// device, run `launch(dev_in, dev_out)`, copy `bytes_out` back.
+template <typename F>
+int small_query(const void *in, size_t bytes_in, void *out, size_t bytes_out, cudaStream_t s, F launch) {
+  char *d = nullptr;
+  KF_CHECK_CUDA(cudaMallocAsync((void **)&d, bytes_in + bytes_out + 256, s));
+  char *dout = d + ((bytes_in + 255) & ~(size_t)255);
+  if (bytes_in) KF_CHECK_CUDA(cudaMemcpyAsync(d, in, bytes_in, cudaMemcpyDefault, s));
+  launch(d, dout);
+  cudaError_t le = cudaGetLastError();
+  if (bytes_out && le == cudaSuccess)
+    KF_CHECK_CUDA(cudaMemcpyAsync(out, dout, bytes_out, cudaMemcpyDefault, s));
+  KF_CHECK_CUDA(cudaFreeAsync(d, s));
+  KF_CHECK_CUDA(cudaStreamSynchronize(s));
+  if (le != cudaSuccess) return kf_cuda_fail(le, "query kernel");
+  return KF_OK;
+}
+
+}  // namespace
+
+extern "C" int kf_grid_sample(kf_grid g, const kf_params *p, const double *pts, int n, double *phi,
+                              double *weight, void *stream) {
+  KF_REQUIRE(g && p && (pts || n == 0), "NULL argument");
+  KF_REQUIRE(n >= 0, "n must be >= 0");
+  if (n == 0) return KF_OK;
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  DevParams dp = kf_make_dev_params(g->n, p);
+  PhiView<double> pv = phi_view<double>(g, g->phi, dp.oob_phi);
+  WeightView wv{g->w, g->n[0], g->n[1], g->n[2]};
+  const size_t bi = (size_t)n * 3 * sizeof(double), bo = (size_t)n * sizeof(double);
+  std::vector<double> buf(2 * (size_t)n);
+  rc = small_query(pts, bi, buf.data(), 2 * bo, kf_stream(stream), [&](char *din, char *dout) {
+    double *o = (double *)dout;
+    k_grid_sample<<<(n + 127) / 128, 128, 0, kf_stream(stream)>>>(pv, wv, (const double *)din, n, o,
+                                                                 o + n);
+  });
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i) {
+    if (phi) phi[i] = buf[i];
+    if (weight) weight[i] = buf[n + i];
+  }
+  return KF_OK;
+}
+
+extern "C" int kf_grid_get_voxels(kf_grid g, const kf_params *p, const int32_t *xyz, int n,
+                                  double *phi, int64_t *weight, void *stream) {
+  KF_REQUIRE(g && p && (xyz || n == 0), "NULL argument");
+  KF_REQUIRE(n >= 0, "n must be >= 0");
+  if (n == 0) return KF_OK;
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  DevParams dp = kf_make_dev_params(g->n, p);
+  PhiView<double> pv = phi_view<double>(g, g->phi, dp.oob_phi);
+  WeightView wv{g->w, g->n[0], g->n[1], g->n[2]};
+  std::vector<char> buf((size_t)n * 16);
+  rc = small_query(xyz, (size_t)n * 3 * sizeof(int32_t), buf.data(), buf.size(), kf_stream(stream),
+                   [&](char *din, char *dout) {
+                     k_grid_get<<<(n + 127) / 128, 128, 0, kf_stream(stream)>>>(
+                         pv, wv, (const int32_t *)din, n, (double *)dout, (int64_t *)(dout + (size_t)n * 8));
+                   });
+  if (rc) return rc;
+  if (phi) memcpy(phi, buf.data(), (size_t)n * 8);
+  if (weight) memcpy(weight, buf.data() + (size_t)n * 8, (size_t)n * 8);
+  return KF_OK;
+}
+
+template <typename P>
+static PsiView<double, P> psi_view(kf_field f) {
+  return PsiView<double, P>{(const P *)f->p[0], (const P *)f->p[1], (const P *)f->p[2], f->n[0], f->n[1],
+                            f->n[2]};
+}
+
+extern "C" int kf_field_get_voxels(kf_field f, const int32_t *xyz, int n, double *out, void *stream) {
+  KF_REQUIRE(f && (xyz || n == 0) && (out || n == 0), "NULL argument");
+  KF_REQUIRE(n >= 0, "n must be >= 0");
+  if (n == 0) return KF_OK;
+  return small_query(xyz, (size_t)n * 3 * sizeof(int32_t), out, (size_t)n * 3 * sizeof(double),
+                     kf_stream(stream), [&](char *din, char *dout) {
+                       unsigned nb = (n + 127) / 128;
+                       if (f->prec == KF_F32)
+                         k_field_get<float><<<nb, 128, 0, kf_stream(stream)>>>(psi_view<float>(f),
+                                                                             (const int32_t *)din, n,
+                                                                             (double *)dout);
+                       else
+                         k_field_get<double><<<nb, 128, 0, kf_stream(stream)>>>(psi_view<double>(f),
+                                                                              (const int32_t *)din, n,
+                                                                              (double *)dout);
+                     });
+}
+
+extern "C" int kf_field_sample(kf_field f, const double *pts, int n, double *out, void *stream) {
+  KF_REQUIRE(f && (pts || n == 0) && (out || n == 0), "NULL argument");
+  KF_REQUIRE(n >= 0, "n must be >= 0");
+  if (n == 0) return KF_OK;
+  return small_query(pts, (size_t)n * 3 * sizeof(double), out, (size_t)n * 3 * sizeof(double),
+                     kf_stream(stream), [&](char *din, char *dout) {
+                       unsigned nb = (n + 127) / 128;
+                       if (f->prec == KF_F32)
+                         k_field_sample<float><<<nb, 128, 0, kf_stream(stream)>>>(
+                             psi_view<float>(f), (const double *)din, n, (double *)dout);
+                       else
+                         k_field_sample<double><<<nb, 128, 0, kf_stream(stream)>>>(
+                             psi_view<double>(f), (const double *)din, n, (double *)dout);
+                     });
+}
+
+extern "C" int kf_field_add_voxels(kf_field f, const int32_t *xyz, int n, const double *delta,
+                                   void *stream) {
+  KF_REQUIRE(f && (xyz || n == 0) && (delta || n == 0), "NULL argument");
+  KF_REQUIRE(n >= 0, "n must be >= 0");
+  for (int i = 0; i < n; ++i) {
+    int64_t j = (int64_t)xyz[3 * i + 2] * f->n[0] * f->n[1] + (int64_t)xyz[3 * i + 1] * f->n[0] + xyz[3 * i];
+    KF_REQUIRE(j >= 0 && j < f->count, "voxel index outside the displacement field");
+  }
+  if (n == 0) return KF_OK;
+  std::vector<char> in((size_t)n * (12 + 24));
+  memcpy(in.data(), xyz, (size_t)n * 12);
+  memcpy(in.data() + (size_t)n * 12, delta, (size_t)n * 24);
+  return small_query(in.data(), in.size(), nullptr, 0, kf_stream(stream), [&](char *din, char *) {
+    const int32_t *dx = (const int32_t *)din;
+    const double *dd = (const double *)(din + (size_t)n * 12);
+    if (f->prec == KF_F32)
+      k_field_add_voxels<float><<<1, 1, 0, kf_stream(stream)>>>((float *)f->p[0], (float *)f->p[1],
+                                                                (float *)f->p[2], f->n[0], f->n[1], dx, n, dd);
+    else
+      k_field_add_voxels<double><<<1, 1, 0, kf_stream(stream)>>>(
+          (double *)f->p[0], (double *)f->p[1], (double *)f->p[2], f->n[0], f->n[1], dx, n, dd);
+  });
+}
+
+extern "C" int kf_field_add(kf_field f, kf_field other, void *stream) {
+  KF_REQUIRE(f && other, "NULL argument");
+  KF_REQUIRE(f->count == other->count && f->n[0] == other->n[0] && f->n[1] == other->n[1],
+             "field sizes differ");
+  KF_REQUIRE(f->prec == other->prec, "field precisions differ");
+  unsigned nb = blocks_for(f->count);
+  cudaStream_t s = kf_stream(stream);
+  if (f->prec == KF_F32)
+    k_field_add<float><<<nb, kBlock, 0, s>>>((float *)f->p[0], (float *)f->p[1], (float *)f->p[2],
+                                             (const float *)other->p[0], (const float *)other->p[1],
+                                             (const float *)other->p[2], f->count);
+  else
+    k_field_add<double><<<nb, kBlock, 0, s>>>((double *)f->p[0], (double *)f->p[1], (double *)f->p[2],
+                                              (const double *)other->p[0], (const double *)other->p[1],
+                                              (const double *)other->p[2], f->count);
+  KF_CHECK_LAUNCH("k_field_add");
+  return KF_OK;
+}
+
+extern "C" int kf_field_fill(kf_field f, const double v[3], void *stream) {
+  KF_REQUIRE(f && v, "NULL argument");
+  unsigned nb = blocks_for(f->count);
+  cudaStream_t s = kf_stream(stream);
+  if (f->prec == KF_F32)
+    k_field_fill<float><<<nb, kBlock, 0, s>>>((float *)f->p[0], (float *)f->p[1], (float *)f->p[2],
+                                              (float)v[0], (float)v[1], (float)v[2], f->count);
+  else
+    k_field_fill<double><<<nb, kBlock, 0, s>>>((double *)f->p[0], (double *)f->p[1], (double *)f->p[2],
+                                               v[0], v[1], v[2], f->count);
+  KF_CHECK_LAUNCH("k_field_fill");
   return KF_OK;
 }

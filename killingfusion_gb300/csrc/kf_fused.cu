@@ -412,73 +412,10 @@ __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int 
   return next;
 }
 
-// One fused iteration in a single pass: each CTA streams its 32 x 8 x 8 slab
-// (psi passed through outside the band) and then updates the band voxels of
-// its own slab, 8 lanes per voxel.  The band work of one CTA overlaps the
-// streaming of the others.
-__global__ void __launch_bounds__(kThreads, 3) k_fused_step(FusedArgs a) {
-  if (iteration_gated(a.st, a.iter, a.dp)) {
-    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
-      a.st[a.iter].skipped = 1;
-    return;
-  }
-  __shared__ int queue[kTile];
-  __shared__ int qn;
-  const DevParams &dp = a.dp;
-  const int tid = threadIdx.y * kTX + threadIdx.x;
-  const int x = blockIdx.x * kTX + threadIdx.x;
-  const int y = blockIdx.y * kTY + threadIdx.y;
-  const int z0 = blockIdx.z * kZSlab;
-  if (tid == 0) qn = 0;
-  __syncthreads();
-  {
-    const bool col = x < dp.nx && y < dp.ny;
-    const int64_t sz = (int64_t)dp.nx * dp.ny;
-    const int64_t base = ((int64_t)z0 * dp.ny + y) * dp.nx + x;
-    float px[kZSlab], py[kZSlab], pz[kZSlab], ph[kZSlab];
-#pragma unroll
-    for (int j = 0; j < kZSlab; ++j) {
-      bool ok = col && (z0 + j) < dp.nz;
-      int64_t i = base + j * sz;
-      px[j] = ok ? __ldcs(a.ix + i) : 0.f;
-      py[j] = ok ? __ldcs(a.iy + i) : 0.f;
-      pz[j] = ok ? __ldcs(a.iz + i) : 0.f;
-      ph[j] = ok ? __ldg(a.live + i) : 0.f;
-    }
-#pragma unroll
-    for (int j = 0; j < kZSlab; ++j) {
-      int z = z0 + j;
-      if (!col || z >= dp.nz) continue;
-      int64_t i = base + j * sz;
-      float s = ph[j];
-      if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f) s = warped_value(a, x, y, z, px[j], py[j], pz[j]);
-      if (in_band(s, a.band_hi, a.band_lo)) {
-        queue[atomicAdd(&qn, 1)] = (int)i;
-      } else {
-        __stcs(a.ox + i, px[j]);
-        __stcs(a.oy + i, py[j]);
-        __stcs(a.oz + i, pz[j]);
-      }
-    }
-  }
-  __syncthreads();
-  const int nq = qn;
-  if (nq == 0) return;
-  const int lane = tid & 31, gl = lane & (kGroup - 1);
-  const unsigned gmask = 0xffu << (lane & ~(kGroup - 1));
-  float maxd = 0.f;
-  double energy = 0.0;
-  unsigned active = 0;
-  bool diverged = false;
-  for (int k = tid / kGroup; k < nq; k += kGroupsPerBlock)
-    update_band_voxel(a, queue[k], gl, gmask, maxd, energy, active, diverged);
-  reduce_iter_stats<kThreads>(a.st + a.iter, active, maxd, energy, diverged);
-}
-
-// Band pass of the band-only solver: a group of 8 lanes per listed voxel;
-// the voxels updated here form the next iteration's list (list_out, counted
-// in st[iter+1].list).  Launched as one resident wave that loops over the
-// list.
+// Band pass: a group of 8 lanes per listed voxel, launched as one resident
+// wave that loops over the list.  kCarry (band-only solver): the voxels
+// updated here form the next iteration's list (list_out, counted in
+// st[iter+1].list).
 template <bool kCarry>
 __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
                                                              int *__restrict__ list_out) {
@@ -579,7 +516,8 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
     a.oz = (float *)out[2];
     a.iter = it;
     if (!band_only) {
-      k_fused_step<<<grid, block, 0, s>>>(a);
+      k_fused_stream<<<grid, block, 0, s>>>(a, lst[0]);
+      k_fused_band<false><<<band_blocks, kBandThreads, 0, s>>>(a, lst[0], nullptr);
     } else {
       if (it == 0) k_fused_stream<<<grid, block, 0, s>>>(a, lst[0]);
       k_fused_band<true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);

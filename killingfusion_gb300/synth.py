@@ -55,14 +55,15 @@ def counter_normal(seed: int, stream: int, count: int) -> np.ndarray:
     return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
 
 
-def pixel_rays(width: int = WIDTH, height: int = HEIGHT) -> np.ndarray:
+def pixel_rays(width: int = WIDTH, height: int = HEIGHT, K: np.ndarray | None = None) -> np.ndarray:
     """Unnormalised ray directions (z = 1) per pixel, float64[h, w, 3]."""
+    fx, fy, cx, cy = (FX, FY, CX, CY) if K is None else (K[0, 0], K[1, 1], K[0, 2], K[1, 2])
     col = np.arange(width, dtype=np.float64) - 0.5
     row = np.arange(height, dtype=np.float64) - 0.5
     u, v = np.meshgrid(col, row)
     d = np.empty((height, width, 3))
-    d[..., 0] = (u - CX) / FX
-    d[..., 1] = (v - CY) / FY
+    d[..., 0] = (u - cx) / fx
+    d[..., 1] = (v - cy) / fy
     d[..., 2] = 1.0
     return d
 
@@ -360,3 +361,54 @@ def shape_problem(seed: int, n: int, trunc_voxels: float = 5.0):
     c = np.where(can > trunc, trunc + 1e-5, np.maximum(can, -trunc - 1e-3))
     lv = np.where(live > trunc, trunc + 1e-5, np.maximum(live, -trunc - 1e-3))
     return c.astype(np.float32), lv.astype(np.float32), voxel
+
+
+def write_dataset(root: str, frames, K: np.ndarray, min_depth: float, max_depth: float) -> None:
+    """Write float32 depth frames in the layout the C++ DatasetReader reads:
+    intrinsics.txt (row-major K), meta.txt ("width height frames minDepth
+    maxDepth") and depth_%06d.f32 (float32 metres, row-major)."""
+    import os
+
+    os.makedirs(root, exist_ok=True)
+    frames = [np.ascontiguousarray(f, dtype=np.float32) for f in frames]
+    h, w = frames[0].shape
+    with open(os.path.join(root, "intrinsics.txt"), "w") as f:
+        f.write(" ".join(repr(float(v)) for v in np.asarray(K, dtype=np.float64).reshape(-1)) + "\n")
+    with open(os.path.join(root, "meta.txt"), "w") as f:
+        f.write("%d %d %d %r %r\n" % (w, h, len(frames), float(min_depth), float(max_depth)))
+    for i, d in enumerate(frames):
+        d.tofile(os.path.join(root, "depth_%06d.f32" % i))
+
+
+def frustum_bounds(K: np.ndarray, width: int, height: int, min_depth: float, max_depth: float):
+    """KillingFusion::computeBounds (KillingFusion.cpp:478-519): min and max
+    corner of the camera frustum between the two depths at pose = identity."""
+    Ki = _inverse3(K)
+    cu = [0, 0, width - 1, width - 1] * 2
+    cv = [0, height - 1, height - 1, 0] * 2
+    pts = []
+    for j in range(8):
+        d = min_depth if j < 4 else max_depth
+        p = [(Ki[r][0] * cu[j] + Ki[r][1] * cv[j] + Ki[r][2] * 1.0) * d for r in range(2)] + [d]
+        pts.append(p)
+    pts = np.array(pts)
+    return pts.min(axis=0), pts.max(axis=0)
+
+
+def _inverse3(m):
+    """3x3 inverse by cofactors, det expanded along column 0."""
+    m = np.asarray(m, dtype=np.float64)
+
+    def cof(i, j):
+        i1, i2, j1, j2 = (i + 1) % 3, (i + 2) % 3, (j + 1) % 3, (j + 2) % 3
+        return float(m[i1, j1] * m[i2, j2] - m[i1, j2] * m[i2, j1])
+
+    det = cof(0, 0) * m[0, 0] + cof(1, 0) * m[1, 0] + cof(2, 0) * m[2, 0]
+    inv_det = 1.0 / float(det)
+    return [[cof(j, i) * inv_det for j in range(3)] for i in range(3)]
+
+
+def grid_from_bounds(lo, hi, voxel: float):
+    """SDF::computeVoxelGridSize (SDF.cpp:117-124): int(bound / voxel) + 1."""
+    return tuple(int((float(hi[k]) - float(lo[k])) / voxel) + 1 for k in range(3))
+

@@ -72,3 +72,38 @@ def test_invalid_arguments_fail_cleanly(capi):
     bad = capi.Params(delta_size=0.5).c()
     assert L.kf_grid_create((C.c_int * 3)(4, 4, 4), 0.01, None, 0.05, C.byref(bad), C.byref(h)) == capi.KF_ERR_INVALID
     assert L.kf_psi_solve(None, None, None, C.byref(p), 1, 0, None, None) == capi.KF_ERR_INVALID
+
+
+def test_host_classes_compile_and_link(capi, tmp_path):
+    """The C++ class layer (SDF, DisplacementField, KillingFusion,
+    DatasetReader, SimpleMesh) builds and the test driver links against it;
+    nothing is run (that needs a GPU)."""
+    import subprocess
+    from killingfusion_gb300 import _build
+    _build.build()
+    assert os.path.exists(_build.HOST_LIB)
+    lib = os.path.dirname(_build.HOST_LIB)
+    exe = str(tmp_path / "host_driver")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    "-I", os.path.join(ROOT, "killingfusion_gb300", "csrc", "host"),
+                    os.path.join(ROOT, "tests", "cpp", "host_driver.cpp"), "-L", lib, "-lkf_host",
+                    "-lkillingfusion", "-Wl,-rpath," + lib, "-o", exe], check=True)
+    host = C.CDLL(_build.HOST_LIB)
+    assert host is not None
+
+
+def test_dataset_writer_and_bounds(tmp_path):
+    """synth.write_dataset writes the layout the C++ DatasetReader reads, and
+    the frustum bounds follow KillingFusion::computeBounds."""
+    from killingfusion_gb300 import synth
+    K = np.array([[52.5, 0.0, 31.5], [0.0, 52.5, 23.5], [0.0, 0.0, 1.0]])
+    frames = [np.full((48, 64), 0.4, np.float32), np.zeros((48, 64), np.float32)]
+    synth.write_dataset(str(tmp_path), frames, K, 0.3, 0.5)
+    assert open(tmp_path / "meta.txt").read().split() == ["64", "48", "2", "0.3", "0.5"]
+    np.testing.assert_array_equal(np.loadtxt(tmp_path / "intrinsics.txt").reshape(3, 3), K)
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "depth_000000.f32", np.float32).reshape(48, 64),
+                                  frames[0])
+    lo, hi = synth.frustum_bounds(K, 64, 48, 0.3, 0.5)
+    np.testing.assert_allclose(lo, [-0.3, -23.5 / 52.5 * 0.5, 0.3], rtol=1e-15)
+    np.testing.assert_allclose(hi, [0.3, 23.5 / 52.5 * 0.5, 0.5], rtol=1e-15)
+    assert synth.grid_from_bounds(lo, hi, 0.008) == (76, 56, 26)
