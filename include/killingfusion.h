@@ -197,6 +197,35 @@ int kf_psi_gradient_ref(kf_grid live, kf_grid canonical, kf_field psi,
                         const kf_params *p, const int32_t *voxels, int count,
                         double *out, uint8_t *active, void *stream);
 
+/* ---- project energy and its adjoint ----------------------------------- */
+/* No counterpart in the reference, whose solver descends the Euler-Lagrange
+ * gradients of KillingFusion::computeEnergyGradient (KillingFusion.cpp:399-476)
+ * without ever evaluating an energy.  This is a discrete energy with the same
+ * three terms, differentiable exactly:
+ *   E = sum over active i of 1/2((phi_w(i) - phi_can(i))/v)^2
+ *       + omega_s 1/2(sqrt(g.g + (v eps)^2)/v - 1)^2
+ *       + omega_k(|J|^2 + gamma <J, J^T>)
+ * with phi_w(j) = live sampled at j + psi(j) (grid units), g and J clamped
+ * central differences of phi_w and psi.  active: device uint8[N] mask, NULL =
+ * every voxel. */
+/* Energy terms {data, level set, Killing} of the active voxels inside box
+ * (x0, y0, z0, x1, y1, z1, half-open; NULL = whole grid), evaluated in
+ * `arith` precision and summed in float64 in a fixed order (deterministic);
+ * terms is a host double[3]; the call waits for the result. */
+int kf_energy(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
+              const uint8_t *active, const int box[6], kf_precision arith, double terms[3],
+              void *stream);
+/* dE/dpsi, float64, into device double[N][3] (deterministic gather). */
+int kf_energy_adjoint(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
+                      const uint8_t *active, double *grad, void *stream);
+/* Float64 central differences (E(psi + h e) - E(psi - h e)) / 2h for each of
+ * `count` voxels (device int32 xyz) and each psi component, into device
+ * double[count][3]; only the 3x3x3 window whose energy depends on psi(j) is
+ * evaluated. */
+int kf_energy_fd(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
+                 const uint8_t *active, const int32_t *voxels, int count, double h, double *out,
+                 void *stream);
+
 /* SDF::update(psi) (SDF.cpp:300-328): resample g at i+0.5+psi(i), weights
  * truncated to integers. */
 int kf_warp(kf_grid g, kf_field psi, const kf_params *p, void *stream);

@@ -37,7 +37,7 @@ CUDA_UNITS = [
     ("kf_fused.cu", []),
     ("kf_plain.cu", []),
     ("kf_mc.cu", []),
-    ("kf_energy.cu", []),
+    ("kf_energy.cu", ["-fmad=false"]),
     ("kf_batch.cu", []),
     ("kf_fusion.cu", []),
 ]

@@ -96,6 +96,7 @@ class Params:
 
 _vp = C.c_void_p
 _ip3 = C.POINTER(C.c_int)
+_ip6 = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
 _PP = C.POINTER(_Params)
 
@@ -123,6 +124,9 @@ SIGNATURES = {
                                      C.c_double, _vp]),
     "kf_psi_solve": (C.c_int, [_vp, _vp, _vp, _PP, C.c_int, C.c_int, C.POINTER(SolveStats), _vp]),
     "kf_psi_gradient_ref": (C.c_int, [_vp, _vp, _vp, _PP, _vp, C.c_int, _vp, _vp, _vp]),
+    "kf_energy": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _ip6, C.c_int, _dp, _vp]),
+    "kf_energy_adjoint": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _vp, _vp]),
+    "kf_energy_fd": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _vp, C.c_int, C.c_double, _vp, _vp]),
     "kf_warp": (C.c_int, [_vp, _vp, _PP, _vp]),
     "kf_fuse": (C.c_int, [_vp, _vp, _vp]),
     "kf_warp_fuse": (C.c_int, [_vp, _vp, _vp, _PP, _vp]),
@@ -297,6 +301,56 @@ def psi_gradient_ref(live: Grid, can: Grid, psi: Field, params: Params, voxels_x
                                      n, out.data_ptr(), act.data_ptr(), None))
     torch.cuda.synchronize()
     return out.cpu().numpy(), act.cpu().numpy()
+
+
+def _active_tensor(active, count):
+    import torch
+    if active is None:
+        return None
+    a = torch.as_tensor(np.ascontiguousarray(active, dtype=np.uint8).reshape(-1)).cuda()
+    assert a.numel() == count
+    return a
+
+
+def energy(live: Grid, can: Grid, psi: Field, params: Params, active=None, box=None,
+           arith: str = "f64") -> np.ndarray:
+    """Project energy terms (data, level set, Killing) over the active voxels
+    (uint8 mask of the grid, None = all) inside box (x0, y0, z0, x1, y1, z1,
+    half-open; None = the grid)."""
+    a = _active_tensor(active, int(np.prod(live.dims)))
+    terms = np.zeros(3)
+    b = (C.c_int * 6)(*[int(v) for v in box]) if box is not None else None
+    check(load().kf_energy(live.h, can.h, psi.h, C.byref(params.c()), a.data_ptr() if a is not None else None,
+                           b, KF_F64 if arith == "f64" else KF_F32,
+                           terms.ctypes.data_as(C.POINTER(C.c_double)), None))
+    return terms
+
+
+def energy_adjoint(live: Grid, can: Grid, psi: Field, params: Params, active=None) -> np.ndarray:
+    """Exact gradient of the project energy with respect to psi, float64
+    [nz, ny, nx, 3]."""
+    import torch
+    a = _active_tensor(active, int(np.prod(live.dims)))
+    out = torch.empty(live.shape + (3,), dtype=torch.float64, device="cuda")
+    check(load().kf_energy_adjoint(live.h, can.h, psi.h, C.byref(params.c()),
+                                   a.data_ptr() if a is not None else None, out.data_ptr(), None))
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def energy_fd(live: Grid, can: Grid, psi: Field, params: Params, voxels_xyz, h: float, active=None):
+    """Central differences (float64) of the project energy at voxels (int
+    [n, 3] of x, y, z), one column per psi component."""
+    import torch
+    a = _active_tensor(active, int(np.prod(live.dims)))
+    v = torch.as_tensor(np.ascontiguousarray(voxels_xyz, dtype=np.int32)).cuda()
+    n = v.shape[0]
+    out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    check(load().kf_energy_fd(live.h, can.h, psi.h, C.byref(params.c()),
+                              a.data_ptr() if a is not None else None, v.data_ptr(), n, float(h),
+                              out.data_ptr(), None))
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
 
 
 def warp(g: Grid, psi: Field, params: Params, stream=None):
