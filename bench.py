@@ -30,7 +30,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "voxel-updates/s at 256³ fused vs plain GPU (ψ err≤1e-4 vox); ms/frame; HBM %"
-ALGO_BYTES_PER_VOXEL = 32  # psi read 12 + write 12, phi_live 4, phi_can 4 per voxel-update
+# Compulsory DRAM bytes of one dense Jacobi iteration: every voxel reads psi
+# (12) and phi_live (4) for the band test; a voxel outside the band keeps its
+# psi, so only the band voxels also read phi_can and write psi (through the
+# side buffer and the scatter: 4 + 12 + 12 + 4 + 12 + 4 with the list).
+ALGO_BYTES_PER_VOXEL = 16
+ALGO_BYTES_PER_BAND_VOXEL = 48
 MESH_CAP = 4_000_000       # triangles per mesh buffer
 
 
@@ -156,7 +161,9 @@ def run_ours(args, rank, world, local):
     solver = capi.SOLVERS[args.solver]
     stats = capi.SolveStats()
     stream = torch.cuda.current_stream(dev)
-    launches_per_frame = 1 + 1 + 2 * args.iters + 1 + 3 * 3 if args.solver == "fused" else \
+    # reset, integrate, the solve (fused: stream + band + scatter per
+    # iteration; plain: 7 kernels), warp+fuse, 3 meshes of 3 kernels each
+    launches_per_frame = 1 + 1 + 3 * args.iters + 1 + 3 * 3 if args.solver == "fused" else \
         1 + 1 + 7 * args.iters + 1 + 3 * 3
 
     def frame(depth, e2e=False):
@@ -364,7 +371,8 @@ def run_main(args, rank, world, local):
     solve_ms = statistics.mean(res["solve_ms"])
     iter_ms = solve_ms / args.iters
     peak, peak_kind = peaks()
-    achieved = ALGO_BYTES_PER_VOXEL * N3 / (iter_ms / 1e3) / 1e9
+    algo_bytes = ALGO_BYTES_PER_VOXEL * N3 + ALGO_BYTES_PER_BAND_VOXEL * res["active"]
+    achieved = algo_bytes / (iter_ms / 1e3) / 1e9
     prof = profile_traffic()
     traffic = None
     if prof and prof.get("dram_bytes_per_voxel"):
@@ -388,15 +396,17 @@ def run_main(args, rank, world, local):
             "weights": "paper", "solver": args.solver, "frames": "1 canonical + warmup + steps",
             "step": "one processNextFrame: integrate, zero psi, %d psi iterations, 3 meshes, warp+fuse"
                     % args.iters,
-            "l2": "inputs larger than L2 (psi 2x201 MB, phi 2x67 MB per grid)",
+            "l2": "inputs larger than L2 (psi 201 MB + phi_live 67 MB read per iteration)",
             "parallelism": "replicas" if world > 1 else "1 GPU",
         },
         "e2e": {"value": e2e_value, "unit": "voxel-updates/s",
                 "h2d_bytes_per_step": 640 * 480 * 4, "d2h_bytes_per_step": res["d2h_bytes_per_step"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "fused psi iteration (k_fused_stream + k_fused_band)",
-                     "algorithmic_bytes_per_voxel": ALGO_BYTES_PER_VOXEL, "peak_source": peak_kind},
+                     "kernel": "fused psi iteration (k_fused_stream + k_fused_band + k_fused_scatter)",
+                     "algorithmic_bytes_per_iteration": algo_bytes,
+                     "algorithmic_bytes_per_voxel": ALGO_BYTES_PER_VOXEL,
+                     "algorithmic_bytes_per_band_voxel": ALGO_BYTES_PER_BAND_VOXEL, "peak_source": peak_kind},
         "clocks": res["clocks"],
         "gpu_launches": res["launches"],
         "solve_ms_per_frame": solve_ms,

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_stream(const BatchEntry *__r
   const int bx = (int)(local % e.gx);
   const int by = (int)((local / e.gx) % e.gy);
   const int bz = (int)(local / ((int64_t)e.gx * e.gy));
-  stream_tile(e.a[0], bx, by, bz, e.band, &e.a[0].st[0].list);
+  stream_tile<true>(e.a[0], bx, by, bz, e.band, &e.a[0].st[0].list);
 }
 
 template <int kMaxB>
@@ -148,7 +148,8 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_batch_band(const BatchEntry
       double energy = 0.0;
       unsigned active = 0;
       bool diverged = false;
-      next = update_band_voxel(a, list_in[k - s_pre[p]], gl, gmask, maxd, energy, active, diverged);
+      const int v = list_in[k - s_pre[p]];
+      next = update_band_voxel(a, v, v, gl, gmask, maxd, energy, active, diverged);
       if (gl == 0) {
         if (active) {
           atomicAdd(&s_active[p], active);

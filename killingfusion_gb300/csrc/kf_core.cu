@@ -631,9 +631,10 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
       break;
     }
   }
-  // Iteration k reads buffer k%2 and writes (k+1)%2; a diverged iteration
-  // still wrote its output.  Put the result into the primary planes.
-  if (executed & 1)
+  // Iteration k reads buffer k%2 and writes (k+1)%2 (the dense fused solver
+  // updates in place); a diverged iteration still wrote its output.  Put
+  // the result into the primary planes.
+  if (solver != KF_SOLVER_FUSED && (executed & 1))
     for (int k = 0; k < 3; ++k) {
       void *t = psi->p[k];
       psi->p[k] = psi->q[k];

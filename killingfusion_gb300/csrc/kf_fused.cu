@@ -3,24 +3,28 @@
 // KillingFusion::computeEnergyGradient, :399-476) and the CUDA-graph capture
 // of the fixed-iteration loop.
 //
-// An iteration is two passes:
-//   k_fused_stream (dense)  streams psi and phi_live and applies the band test
+// An iteration (KF_SOLVER_FUSED) is three passes over psi held in place:
+//   k_fused_stream (dense)  reads psi and phi_live and applies the band test
 //     of KillingFusion.cpp:272-274.  The warped value phi_live(i + psi(i)) is
 //     phi_live(i) itself when psi(i) == 0 (zero interpolation weights), so only
-//     voxels that have moved gather their 8 corners.  Voxels outside the band
-//     pass psi through; voxels inside are compacted into a list.
+//     voxels that have moved gather their 8 corners.  A voxel outside the
+//     band keeps its psi, which therefore need not be written; the voxels
+//     inside are compacted into a list.  16 bytes per voxel.
 //   k_fused_band  evaluates the full gradient of every listed voxel with a
 //     group of 8 lanes per voxel (4 voxels per warp): the group loads the 20
 //     psi neighbours of the stencil and shares them by shuffles, takes the 25
 //     warped-SDF samples of the gradient and Hessian plus the warped value
 //     (3-4 independent trilinear gathers per lane), and reduces the nine
-//     derivative sums of +-1-weighted sample differences.
+//     derivative sums of +-1-weighted sample differences.  The new psi goes
+//     to a side buffer indexed by list position, so every voxel still reads
+//     its neighbours' old values (Jacobi).
+//   k_fused_scatter  writes the band voxels' new psi back.
 // The band-only solver (KF_SOLVER_BAND) runs the dense pass once.  A voxel
 // outside the band keeps psi, so its band test keeps failing and the band can
 // only shrink: each band pass hands the voxels it updated to the next
 // iteration, which re-tests them with the warped value it samples anyway and
-// copies the ones that left the band into its output buffer.  Both solvers
-// produce the same psi.
+// copies the ones that left the band into its output buffer (ping-pong
+// buffers).  Both solvers produce the same psi.
 //
 // In the interior the psi samples that the reference takes at sub-voxel offsets
 // are closed-form linear combinations of the 3x3x3 neighbourhood:
@@ -35,22 +39,24 @@
 
 namespace {
 
-// Dense pass: stream the slab, pass psi through outside the band, list the
-// band voxels (st[iter].list counts them).
+// Dense pass: stream the slab, list the band voxels (st[iter].list counts
+// them); kPassThrough copies psi of the other voxels to the output buffer.
+template <bool kPassThrough>
 __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__restrict__ list) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
       a.st[a.iter].skipped = 1;
     return;
   }
-  stream_tile(a, blockIdx.x, blockIdx.y, blockIdx.z, list, &a.st[a.iter].list);
+  stream_tile<kPassThrough>(a, blockIdx.x, blockIdx.y, blockIdx.z, list, &a.st[a.iter].list);
 }
 
 // Band pass: a group of 8 lanes per listed voxel, launched as one resident
 // wave that loops over the list.  kCarry (band-only solver): the voxels
 // updated here form the next iteration's list (list_out, counted in
-// st[iter+1].list).
-template <bool kCarry>
+// st[iter+1].list).  kInPlace: the new psi of list entry k goes to entry k
+// of the output planes, for k_fused_scatter to write back.
+template <bool kCarry, bool kInPlace>
 __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
                                                              int *__restrict__ list_out) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
@@ -72,7 +78,10 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
   for (int r = 0; r < rounds; ++r) {
     const int k = (r * gridDim.x + blockIdx.x) * kGroupsPerBlock + group;
     int next = -1;  // voxel this group hands to the next iteration
-    if (k < nq) next = update_band_voxel(a, list_in[k], gl, gmask, maxd, energy, active, diverged);
+    if (k < nq) {
+      const int v = list_in[k];
+      next = update_band_voxel(a, v, kInPlace ? k : v, gl, gmask, maxd, energy, active, diverged);
+    }
     if (kCarry) {
       if (gl == 0) s_next[group] = next;
       __syncthreads();
@@ -89,6 +98,21 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
     }
   }
   reduce_iter_stats<kBandThreads>(a.st + a.iter, active, maxd, energy, diverged);
+}
+
+// In-place update: psi(list[k]) = entry k of the band pass's output planes,
+// once every band voxel has read its neighbours' old values.
+__global__ void __launch_bounds__(kThreads) k_fused_scatter(FusedArgs a, const int *__restrict__ list,
+                                                           float *__restrict__ px, float *__restrict__ py,
+                                                           float *__restrict__ pz) {
+  if (iteration_gated(a.st, a.iter, a.dp)) return;
+  const int nq = (int)a.st[a.iter].list;
+  for (int k = blockIdx.x * kThreads + threadIdx.x; k < nq; k += gridDim.x * kThreads) {
+    const int v = list[k];
+    px[v] = a.ox[k];
+    py[v] = a.oy[k];
+    pz[v] = a.oz[k];
+  }
 }
 
 }  // namespace
@@ -120,7 +144,9 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
   void *buf[2][3] = {{psi->p[0], psi->p[1], psi->p[2]}, {psi->q[0], psi->q[1], psi->q[2]}};
   int *lst[2] = {lists, lists + dp.count};
   for (int it = 0; it < iterations; ++it) {
-    void **in = buf[it & 1], **out = buf[(it + 1) & 1];
+    // dense: psi stays in the primary planes, the second planes hold the
+    // band voxels' new values by list position; band-only: ping-pong
+    void **in = band_only ? buf[it & 1] : buf[0], **out = band_only ? buf[(it + 1) & 1] : buf[1];
     a.ix = (const float *)in[0];
     a.iy = (const float *)in[1];
     a.iz = (const float *)in[2];
@@ -129,11 +155,13 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
     a.oz = (float *)out[2];
     a.iter = it;
     if (!band_only) {
-      k_fused_stream<<<grid, block, 0, s>>>(a, lst[0]);
-      k_fused_band<false><<<band_blocks, kBandThreads, 0, s>>>(a, lst[0], nullptr);
+      k_fused_stream<false><<<grid, block, 0, s>>>(a, lst[0]);
+      k_fused_band<false, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[0], nullptr);
+      k_fused_scatter<<<band_blocks, kThreads, 0, s>>>(a, lst[0], (float *)in[0], (float *)in[1],
+                                                      (float *)in[2]);
     } else {
-      if (it == 0) k_fused_stream<<<grid, block, 0, s>>>(a, lst[0]);
-      k_fused_band<true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
+      if (it == 0) k_fused_stream<true><<<grid, block, 0, s>>>(a, lst[0]);
+      k_fused_band<true, false><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
     }
   }
 }

@@ -294,8 +294,11 @@ __device__ __forceinline__ void voxel_xyz(const DevParams &dp, int i, int &x, in
 }
 
 // Dense pass over one tile (kTX x kTY columns, kZSlab planes) of block
-// coordinates (bx, by, bz): stream the slab, pass psi through outside the
-// band, append the band voxels to list (*count counts them).
+// coordinates (bx, by, bz): stream the slab, apply the band test, append the
+// band voxels to list (*count counts them).  kPassThrough (ping-pong
+// buffers): copy psi of the voxels outside the band to the output buffer;
+// without it (psi updated in place) they are only read.
+template <bool kPassThrough>
 __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, int bz,
                                             int *__restrict__ list, unsigned *count) {
   __shared__ int queue[kTile];
@@ -330,7 +333,7 @@ __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, 
     if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f) s = warped_value(a, x, y, z, px[j], py[j], pz[j]);
     if (in_band(s, a.band_hi, a.band_lo)) {
       queue[atomicAdd(&qn, 1)] = (int)i;
-    } else {
+    } else if (kPassThrough) {
       __stcs(a.ox + i, px[j]);
       __stcs(a.oy + i, py[j]);
       __stcs(a.oz + i, pz[j]);
@@ -342,12 +345,14 @@ __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, 
   for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
 }
 
-// Update one band voxel with the group of 8 lanes it is assigned to.  The
-// voxel is re-tested with its warped value: one outside the band is passed
-// through (it left the band in the previous iteration).  Returns the voxel
-// for the next iteration's list (-1 if it left the band); the group leader
+// Update one band voxel i with the group of 8 lanes it is assigned to and
+// write its new psi to entry `slot` of the output planes (slot == i for
+// ping-pong buffers; the voxel's list position for in-place updates).  The
+// voxel is re-tested with its warped value: one outside the band keeps its
+// psi (it left the band in the previous iteration).  Returns the voxel for
+// the next iteration's list (-1 if it left the band); the group leader
 // accumulates the statistics.
-__device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int gl, unsigned gmask,
+__device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int slot, int gl, unsigned gmask,
                                                  float &maxd, double &energy, unsigned &active,
                                                  bool &diverged) {
   const DevParams &dp = a.dp;
@@ -368,17 +373,17 @@ __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int 
   if (gl == 0) {
     if (in_band(s, a.band_hi, a.band_lo)) {
       if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
-      a.ox[i] = c0[0] + d[0];
-      a.oy[i] = c0[1] + d[1];
-      a.oz[i] = c0[2] + d[2];
+      a.ox[slot] = c0[0] + d[0];
+      a.oy[slot] = c0[1] + d[1];
+      a.oz[slot] = c0[2] + d[2];
       maxd = fmaxf(maxd, sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
       energy += (double)en;
       ++active;
       next = i;
     } else {  // left the band: its psi is final, settle the output buffer
-      a.ox[i] = c0[0];
-      a.oy[i] = c0[1];
-      a.oz[i] = c0[2];
+      a.ox[slot] = c0[0];
+      a.oy[slot] = c0[1];
+      a.oz[slot] = c0[2];
     }
   }
   return next;
