@@ -201,6 +201,7 @@ extern "C" int kf_grid_destroy(kf_grid g) {
   cudaFree(g->phi_alt);
   cudaFree(g->w_alt);
   cudaFree(g->depth);
+  cudaFree(g->integ);
   delete g;
   return KF_OK;
 }

@@ -13,6 +13,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -76,14 +77,69 @@ __device__ __forceinline__ int pixel_of(double u) {
   return (int)roundf(f);
 }
 
+// The running-mean update of SDF.cpp:185-193 once the pixel and the camera
+// depth zc are known.  With w == 0 and a finite phi the mean
+// (phi*0 + dist)/1 is dist itself, so the float64 multiply and divide are
+// skipped.
+__device__ __forceinline__ void integrate_update(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
+                                                 float df, double zc, const IntegrateArgs &a) {
+  const double dist = (double)df - zc;
+  if (dist < -a.unknown_clip) return;
+  const int32_t wi = w[i];
+  const float ph = phi[i];
+  if (wi == 0 && isfinite(ph)) {
+    phi[i] = (float)dist;
+  } else {
+    phi[i] = (float)(((double)ph * (double)wi + dist) / (double)(wi + 1));
+  }
+  w[i] = wi + 1;
+}
+
+// The whole float64 path of one voxel (SDF.cpp:151-193).
+__device__ void integrate_exact_voxel(float *__restrict__ phi, int32_t *__restrict__ w, int x, int y, int z,
+                                      int64_t i, const float *__restrict__ depth, const IntegrateArgs &a) {
+  double u, v, zc;
+  project_exact(a, x, y, z, u, v, zc);
+  const int col = pixel_of(u), row = pixel_of(v);
+  if (col < 0 || col >= a.width || row < 0 || row >= a.height) return;
+  const float df = depth[(int64_t)row * a.width + col];
+  if (df < a.min_depth_up || df > a.max_depth_down) return;
+  integrate_update(phi, w, i, df, zc, a);
+}
+
+// Per-axis products of the camera-depth row, W[8]*X(x), W[9]*Y(y) and
+// W[10]*Z(z), with X = voxel*(x+0.5)+min as SDF.cpp:151-157 computes it:
+// zc = ((tx + ty) + tz) + W[11] is then the reference's float64 value.
+__global__ void k_integrate_tables(double *__restrict__ tx, double *__restrict__ ty, double *__restrict__ tz,
+                                   int nx, int ny, int nz, IntegrateArgs a) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx + ny + nz; k += gridDim.x * blockDim.x) {
+    if (k < nx) {
+      tx[k] = a.W[8] * (a.voxel * ((double)k + 0.5) + a.min0);
+    } else if (k < nx + ny) {
+      const int j = k - nx;
+      ty[j] = a.W[9] * (a.voxel * ((double)j + 0.5) + a.min1);
+    } else {
+      const int j = k - nx - ny;
+      tz[j] = a.W[10] * (a.voxel * ((double)j + 0.5) + a.min2);
+    }
+  }
+}
+
 // SDF::integrateDepthFrame for one voxel per thread.  The pixel a voxel reads
 // flips only where u or v crosses an integer, so the projection runs in float
-// and is redone in float64 when either coordinate lies within 1/128 pixel of
-// an integer (the float error is below 1e-3 pixel) or is not finite.  The
-// distance and the running mean are float64 as in the reference.
+// and is left to the float64 path when either coordinate lies within 1/128
+// pixel of an integer (the float error is below 1e-3 pixel) or is not finite.
+// Those voxels are listed (warp-aggregated) for k_integrate_exact, so the
+// slow float64 projection runs on full warps instead of stalling the warps
+// they fall in; past the list's capacity a voxel takes the path in place.
+// The distance and the running mean are float64 as in the reference.
 __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, int32_t *__restrict__ w,
                                                       int nx, int ny, int nz,
                                                       const float *__restrict__ depth,
+                                                      const double *__restrict__ tx,
+                                                      const double *__restrict__ ty,
+                                                      const double *__restrict__ tz, int *__restrict__ list,
+                                                      unsigned *__restrict__ list_n, unsigned list_cap,
                                                       IntegrateArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -101,39 +157,112 @@ __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, i
   const float uf = a.Kf[0] * pa + a.Kf[1] * pb + a.Kf[2];
   const float vf = a.Kf[3] * pa + a.Kf[4] * pb + a.Kf[5];
   constexpr float kMargin = 1.0f / 128.0f;
-  int col, row;
-  bool exact_zc = false;
-  double zc = 0.0;
-  if (isfinite(uf) && isfinite(vf) && fabsf(uf - rintf(uf)) > kMargin &&
-      fabsf(vf - rintf(vf)) > kMargin && fabsf(uf) < 1e7f && fabsf(vf) < 1e7f) {
-    col = (int)floorf(uf + 1.0f);  // == roundf(u + 0.5) away from the flips
-    row = (int)floorf(vf + 1.0f);
-    if (uf < -1.0f) col = -1;      // roundf(u + 0.5) < 0: outside
-    if (vf < -1.0f) row = -1;
-  } else {
-    double u, v;
-    project_exact(a, x, y, z, u, v, zc);
-    exact_zc = true;
-    col = pixel_of(u);
-    row = pixel_of(v);
+  const bool sure = isfinite(uf) && isfinite(vf) && fabsf(uf - rintf(uf)) > kMargin &&
+                    fabsf(vf - rintf(vf)) > kMargin && fabsf(uf) < 1e7f && fabsf(vf) < 1e7f;
+  const unsigned act = __activemask();
+  const unsigned need = __ballot_sync(act, !sure);
+  if (!sure) {
+    const int lane = threadIdx.x & 31;  // blockDim.x == 32
+    const int leader = __ffs(need) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(list_n, (unsigned)__popc(need));
+    base = __shfl_sync(need, base, leader);
+    const unsigned slot = base + (unsigned)__popc(need & ((1u << lane) - 1u));
+    if (slot < list_cap)
+      list[slot] = (int)i;
+    else
+      integrate_exact_voxel(phi, w, x, y, z, i, depth, a);
+    return;
   }
+  int col = (int)floorf(uf + 1.0f);  // == roundf(u + 0.5) away from the flips
+  int row = (int)floorf(vf + 1.0f);
+  if (uf < -1.0f) col = -1;  // roundf(u + 0.5) < 0: outside
+  if (vf < -1.0f) row = -1;
   if (col < 0 || col >= a.width) return;
   if (row < 0 || row >= a.height) return;
   const float df = depth[(int64_t)row * a.width + col];
   // d < min_depth || d > max_depth on the float value compared as a double
   if (df < a.min_depth_up || df > a.max_depth_down) return;
-  if (!exact_zc) {
-    const double Z = a.voxel * ((double)z + 0.5) + a.min2;
-    const double Y = a.voxel * ((double)y + 0.5) + a.min1;
-    const double X = a.voxel * ((double)x + 0.5) + a.min0;
-    zc = a.W[8] * X + a.W[9] * Y + a.W[10] * Z + a.W[11] * 1.0;
-  }
-  const double dist = (double)df - zc;
-  if (dist < -a.unknown_clip) return;
-  int32_t wi = w[i];
-  phi[i] = (float)(((double)phi[i] * (double)wi + dist) / (double)(wi + 1));
-  w[i] = wi + 1;
+  const double zc = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
+  integrate_update(phi, w, i, df, zc, a);
 }
+
+// The listed voxels of k_integrate, each on the float64 path.
+__global__ void __launch_bounds__(kBlock) k_integrate_exact(float *__restrict__ phi, int32_t *__restrict__ w,
+                                                            int nx, int ny, const float *__restrict__ depth,
+                                                            const int *__restrict__ list,
+                                                            const unsigned *__restrict__ list_n,
+                                                            unsigned list_cap, IntegrateArgs a) {
+  const unsigned n = min(*list_n, list_cap);
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t i = list[k];
+    int x, y, z;
+    voxel_xyz(i, nx, ny, x, y, z);
+    integrate_exact_voxel(phi, w, x, y, z, i, depth, a);
+  }
+}
+
+}  // namespace
+
+int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height,
+                        const double w2c[16], const double K[9], double min_depth,
+                        double max_depth, cudaStream_t s) {
+  IntegrateArgs a;
+  for (int k = 0; k < 16; ++k) a.W[k] = w2c[k];
+  for (int k = 0; k < 9; ++k) a.K[k] = K[k];
+  for (int k = 0; k < 12; ++k) a.Wf[k] = (float)w2c[k];
+  for (int k = 0; k < 6; ++k) a.Kf[k] = (float)K[k];
+  a.voxel = g->voxel;
+  a.min0 = g->min3d[0];
+  a.min1 = g->min3d[1];
+  a.min2 = g->min3d[2];
+  a.vf = (float)g->voxel;
+  a.min0f = (float)g->min3d[0];
+  a.min1f = (float)g->min3d[1];
+  a.min2f = (float)g->min3d[2];
+  a.unknown_clip = g->unknown_clip;
+  a.min_depth = min_depth;
+  a.max_depth = max_depth;
+  // float x < min_depth  <=>  x < smallest float >= min_depth, and likewise
+  float lo = (float)min_depth, hi = (float)max_depth;
+  if ((double)lo < min_depth) lo = nextafterf(lo, INFINITY);
+  if ((double)hi > max_depth) hi = nextafterf(hi, -INFINITY);
+  a.min_depth_up = lo;
+  a.max_depth_down = hi;
+  a.width = width;
+  a.height = height;
+  // scratch: list counter, the three coordinate tables, the list
+  const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+  const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(g->count / 8, 65536), 0x7fffffff);
+  const size_t tab_off = 256, list_off = tab_off + (((size_t)(nx + ny + nz) * 8 + 255) & ~(size_t)255);
+  const size_t bytes = list_off + (size_t)cap * sizeof(int);
+  if (g->integ_bytes < bytes) {
+    cudaFree(g->integ);
+    g->integ = nullptr;
+    g->integ_bytes = 0;
+    if (cudaMalloc(&g->integ, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      g->integ = nullptr;
+      return kf_fail(KF_ERR_OOM, "cudaMalloc of the integration scratch failed");
+    }
+    g->integ_bytes = bytes;
+  }
+  char *base = (char *)g->integ;
+  unsigned *list_n = (unsigned *)base;
+  double *tx = (double *)(base + tab_off), *ty = tx + nx, *tz = ty + ny;
+  int *list = (int *)(base + list_off);
+  KF_CHECK_CUDA(cudaMemsetAsync(list_n, 0, sizeof(unsigned), s));
+  k_integrate_tables<<<blocks_for(nx + ny + nz), kBlock, 0, s>>>(tx, ty, tz, nx, ny, nz, a);
+  dim3 block(32, kBlock / 32);
+  dim3 grid((nx + 31) / 32, (ny + block.y - 1) / block.y, nz);
+  k_integrate<<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, list, list_n, cap, a);
+  k_integrate_exact<<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list, list_n,
+                                                                  cap, a);
+  KF_CHECK_LAUNCH("k_integrate");
+  return KF_OK;
+}
+
+namespace {
 
 // ---------------------------------------------------------------------------
 // warp / fuse
@@ -346,40 +475,6 @@ int kf_grid_ensure_alt(kf_grid g) {
     g->phi_alt = nullptr;
     return kf_fail(KF_ERR_OOM, "cudaMalloc of the resampling buffer failed");
   }
-  return KF_OK;
-}
-
-int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height,
-                        const double w2c[16], const double K[9], double min_depth,
-                        double max_depth, cudaStream_t s) {
-  IntegrateArgs a;
-  for (int k = 0; k < 16; ++k) a.W[k] = w2c[k];
-  for (int k = 0; k < 9; ++k) a.K[k] = K[k];
-  for (int k = 0; k < 12; ++k) a.Wf[k] = (float)w2c[k];
-  for (int k = 0; k < 6; ++k) a.Kf[k] = (float)K[k];
-  a.voxel = g->voxel;
-  a.min0 = g->min3d[0];
-  a.min1 = g->min3d[1];
-  a.min2 = g->min3d[2];
-  a.vf = (float)g->voxel;
-  a.min0f = (float)g->min3d[0];
-  a.min1f = (float)g->min3d[1];
-  a.min2f = (float)g->min3d[2];
-  a.unknown_clip = g->unknown_clip;
-  a.min_depth = min_depth;
-  a.max_depth = max_depth;
-  // float x < min_depth  <=>  x < smallest float >= min_depth, and likewise
-  float lo = (float)min_depth, hi = (float)max_depth;
-  if ((double)lo < min_depth) lo = nextafterf(lo, INFINITY);
-  if ((double)hi > max_depth) hi = nextafterf(hi, -INFINITY);
-  a.min_depth_up = lo;
-  a.max_depth_down = hi;
-  a.width = width;
-  a.height = height;
-  dim3 block(32, kBlock / 32);
-  dim3 grid((g->n[0] + 31) / 32, (g->n[1] + block.y - 1) / block.y, g->n[2]);
-  k_integrate<<<grid, block, 0, s>>>(g->phi, g->w, g->n[0], g->n[1], g->n[2], depth_dev, a);
-  KF_CHECK_LAUNCH("k_integrate");
   return KF_OK;
 }
 

@@ -42,7 +42,7 @@ namespace {
 // Dense pass: stream the slab, list the band voxels (st[iter].list counts
 // them); kPassThrough copies psi of the other voxels to the output buffer.
 template <bool kPassThrough>
-__global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__restrict__ list) {
+__global__ void __launch_bounds__(kThreads, 5) k_fused_stream(FusedArgs a, int *__restrict__ list) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
       a.st[a.iter].skipped = 1;

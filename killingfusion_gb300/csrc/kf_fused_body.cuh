@@ -323,20 +323,37 @@ __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, 
     pz[j] = ok ? __ldcs(a.iz + i) : 0.f;
     ph[j] = ok ? __ldg(a.live + i) : 0.f;
   }
+  // psi == 0 samples its own cell with zero weights: the warped value is
+  // phi_live(i) exactly.  Voxels that have moved are tested after the
+  // streamed values are dead (their trilinear gather is the rare, long path).
+  unsigned moved = 0;
 #pragma unroll
   for (int j = 0; j < kZSlab; ++j) {
     int z = z0 + j;
     if (!col || z >= dp.nz) continue;
     int64_t i = base + j * sz;
-    float s = ph[j];
-    // psi == 0 samples its own cell with zero weights: phi_live(i) exactly
-    if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f) s = warped_value(a, x, y, z, px[j], py[j], pz[j]);
+    if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f) {
+      moved |= 1u << j;
+    } else if (in_band(ph[j], a.band_hi, a.band_lo)) {
+      queue[atomicAdd(&qn, 1)] = (int)i;
+    } else if (kPassThrough) {
+      __stcs(a.ox + i, 0.f);
+      __stcs(a.oy + i, 0.f);
+      __stcs(a.oz + i, 0.f);
+    }
+  }
+  while (moved) {
+    const int j = __ffs(moved) - 1;
+    moved &= moved - 1;
+    const int64_t i = base + j * sz;
+    const float qx = a.ix[i], qy = a.iy[i], qz = a.iz[i];
+    const float s = warped_value(a, x, y, z0 + j, qx, qy, qz);
     if (in_band(s, a.band_hi, a.band_lo)) {
       queue[atomicAdd(&qn, 1)] = (int)i;
     } else if (kPassThrough) {
-      __stcs(a.ox + i, px[j]);
-      __stcs(a.oy + i, py[j]);
-      __stcs(a.oz + i, pz[j]);
+      __stcs(a.ox + i, qx);
+      __stcs(a.oy + i, qy);
+      __stcs(a.oz + i, qz);
     }
   }
   __syncthreads();

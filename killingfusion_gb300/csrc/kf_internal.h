@@ -23,6 +23,8 @@ struct kf_grid_s {
   int32_t *w_alt;
   float *depth;    // device staging for host depth frames (lazily sized)
   size_t depth_cap;
+  void *integ;     // integration scratch: counter, coordinate tables, list
+  size_t integ_bytes;
 };
 
 struct IterStats;

@@ -3,11 +3,17 @@
 //
 // Three passes keep the triangle soup in the reference's order (cells in
 // z, y, x order; triangles of a cell in table order):
-//   1. k_mc_count: each CTA classifies a contiguous run of cells and writes
-//      its triangle total;
-//   2. k_mc_scan:  one CTA turns the totals into exclusive offsets;
-//   3. k_mc_emit:  each CTA re-classifies its run, scans the per-thread
-//      totals and writes every triangle at its final position.
+//   1. k_mc_count: each CTA classifies a contiguous run of kCellsPerBlock
+//      cells and writes its triangle total;
+//   2. k_mc_scan:  one CTA turns the totals into exclusive offsets, a chunk
+//      of kScanChunk totals at a time through registers;
+//   3. k_mc_emit:  each CTA re-classifies its run round by round (thread t
+//      takes cell r*kThreads + t of round r, so the reads coalesce), scans
+//      the round's triangle counts and writes every triangle at its final
+//      position.
+// A cell whose own value is outside [lo, hi] is skipped after one read
+// (SDF.cpp:407), before any index arithmetic; only the band cells gather
+// their corners.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -20,8 +26,10 @@
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kCellsPerThread = 4;
-constexpr int kCellsPerBlock = kThreads * kCellsPerThread;
+constexpr int kRounds = 8;
+constexpr int kCellsPerBlock = kThreads * kRounds;
+constexpr int kScanPerThread = 32;
+constexpr int kScanChunk = kThreads * kScanPerThread;
 
 struct McTables {
   signed char tri[256][16];
@@ -70,16 +78,17 @@ __device__ __forceinline__ float at(const McGrid &g, int x, int y, int z) {
   return __ldg(g.phi + ((int64_t)z * g.ny + y) * g.nx + x);
 }
 
-// Cube configuration of cell i, or -1 when the cell is skipped.
-__device__ __forceinline__ int classify(const McGrid &g, int64_t i, int &x, int &y, int &z,
-                                        float val[8]) {
-  int64_t plane = (int64_t)g.nx * g.ny;
+// Cube configuration of cell i, or -1 when the cell is skipped (outside the
+// grid, or its own value outside [lo, hi]).
+__device__ __forceinline__ int classify(const McGrid &g, int64_t i, int &x, int &y, int &z, float val[8]) {
+  if (i >= g.count) return -1;
+  const float d = __ldg(g.phi + i);
+  if (d > g.hi || d < g.lo) return -1;
+  const int64_t plane = (int64_t)g.nx * g.ny;
   z = (int)(i / plane);
-  int64_t r = i - (int64_t)z * plane;
+  const int64_t r = i - (int64_t)z * plane;
   y = (int)(r / g.nx);
   x = (int)(r - (int64_t)y * g.nx);
-  float d = __ldg(g.phi + i);
-  if (d > g.hi || d < g.lo) return -1;
   int cube = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
@@ -89,13 +98,8 @@ __device__ __forceinline__ int classify(const McGrid &g, int64_t i, int &x, int 
   return cube;
 }
 
-__device__ __forceinline__ int cell_tris(const McGrid &g, int64_t i) {
-  if (i >= g.count) return 0;
-  int x, y, z;
-  float val[8];
-  int cube = classify(g, i, x, y, z, val);
-  if (cube < 0 || c_mc.edge[cube] == 0) return 0;
-  return c_mc.ntri[cube];
+__device__ __forceinline__ int cube_tris(int cube) {
+  return (cube < 0 || c_mc.edge[cube] == 0) ? 0 : (int)c_mc.ntri[cube];
 }
 
 template <typename T>
@@ -127,29 +131,45 @@ __device__ T block_exclusive_scan(T v, T *total) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block_tris) {
-  int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + (int64_t)threadIdx.x * kCellsPerThread;
+  const int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + threadIdx.x;
   uint32_t n = 0;
 #pragma unroll
-  for (int j = 0; j < kCellsPerThread; ++j) n += cell_tris(g, base + j);
+  for (int r = 0; r < kRounds; ++r) {
+    int x, y, z;
+    float val[8];
+    n += cube_tris(classify(g, base + (int64_t)r * kThreads, x, y, z, val));
+  }
   uint32_t total;
   block_exclusive_scan<uint32_t>(n, &total);
   if (threadIdx.x == 0) block_tris[blockIdx.x] = total;
 }
 
-// Exclusive scan of the per-block totals into 64-bit offsets (one CTA).
+// Exclusive scan of the per-block totals into 64-bit offsets (one CTA), a
+// chunk of kScanChunk totals per step: each thread sums kScanPerThread
+// consecutive totals, the block scans the sums, each thread writes its
+// offsets.
 __global__ void __launch_bounds__(kThreads) k_mc_scan(const uint32_t *block_tris, int64_t nblocks,
                                                       int64_t *block_off, int64_t *grand_total) {
-  int64_t per = (nblocks + kThreads - 1) / kThreads;
-  int64_t b0 = (int64_t)threadIdx.x * per;
-  int64_t s = 0;
-  for (int64_t b = b0; b < b0 + per && b < nblocks; ++b) s += block_tris[b];
-  int64_t total;
-  int64_t off = block_exclusive_scan<int64_t>(s, &total);
-  for (int64_t b = b0; b < b0 + per && b < nblocks; ++b) {
-    block_off[b] = off;
-    off += block_tris[b];
+  int64_t carry = 0;
+  for (int64_t c0 = 0; c0 < nblocks; c0 += kScanChunk) {
+    const int64_t b0 = c0 + (int64_t)threadIdx.x * kScanPerThread;
+    uint32_t v[kScanPerThread];
+    int64_t s = 0;
+#pragma unroll
+    for (int j = 0; j < kScanPerThread; ++j) {
+      v[j] = b0 + j < nblocks ? block_tris[b0 + j] : 0u;
+      s += v[j];
+    }
+    int64_t total;
+    int64_t off = carry + block_exclusive_scan<int64_t>(s, &total);
+#pragma unroll
+    for (int j = 0; j < kScanPerThread; ++j) {
+      if (b0 + j < nblocks) block_off[b0 + j] = off;
+      off += v[j];
+    }
+    carry += total;
   }
-  if (threadIdx.x == 0) *grand_total = total;
+  if (threadIdx.x == 0) *grand_total = carry;
 }
 
 __device__ __forceinline__ void vinterp(const float p1[3], const float p2[3], float v1, float v2,
@@ -161,21 +181,18 @@ __device__ __forceinline__ void vinterp(const float p1[3], const float p2[3], fl
 
 __global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *block_off,
                                                       float *__restrict__ verts, int64_t capacity) {
-  int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + (int64_t)threadIdx.x * kCellsPerThread;
-  uint32_t n = 0;
-#pragma unroll
-  for (int j = 0; j < kCellsPerThread; ++j) n += cell_tris(g, base + j);
-  int64_t out = block_off[blockIdx.x] + (int64_t)block_exclusive_scan<uint32_t>(n, nullptr);
-  if (n == 0) return;
-  for (int j = 0; j < kCellsPerThread; ++j) {
-    int64_t i = base + j;
-    if (i >= g.count) break;
+  int64_t out0 = block_off[blockIdx.x];
+  const int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + threadIdx.x;
+  for (int r = 0; r < kRounds; ++r) {
     int x, y, z;
     float val[8];
-    int cube = classify(g, i, x, y, z, val);
-    if (cube < 0) continue;
-    int em = c_mc.edge[cube];
-    if (em == 0) continue;
+    const int cube = classify(g, base + (int64_t)r * kThreads, x, y, z, val);
+    const uint32_t n = (uint32_t)cube_tris(cube);
+    uint32_t round_total;
+    int64_t out = out0 + (int64_t)block_exclusive_scan<uint32_t>(n, &round_total);
+    out0 += round_total;
+    if (n == 0) continue;
+    const int em = c_mc.edge[cube];
     float p[8][3];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -187,11 +204,9 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *b
 #pragma unroll
     for (int e = 0; e < 12; ++e)
       if (em & (1 << e))
-        vinterp(p[c_mc.ends[e][0]], p[c_mc.ends[e][1]], val[c_mc.ends[e][0]],
-                val[c_mc.ends[e][1]], vl[e]);
-    int nt = c_mc.ntri[cube];
-    for (int t = 0; t < nt; ++t, ++out) {
-      if (out >= capacity) return;
+        vinterp(p[c_mc.ends[e][0]], p[c_mc.ends[e][1]], val[c_mc.ends[e][0]], val[c_mc.ends[e][1]], vl[e]);
+    for (uint32_t t = 0; t < n; ++t, ++out) {
+      if (out >= capacity) break;
       float *o = verts + 9 * out;
 #pragma unroll
       for (int j2 = 0; j2 < 3; ++j2) {
