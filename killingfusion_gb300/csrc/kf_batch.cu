@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_batch_band(const BatchEntry
       const FusedArgs &a = e.a[par];
       const int *list_in = e.band + (par ? e.count : 0);
       float maxd = 0.f;
-      double energy = 0.0;
+      float energy = 0.f;
       unsigned active = 0;
       bool diverged = false;
       const int v = list_in[k - s_pre[p]];
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_batch_band(const BatchEntry
         if (active) {
           atomicAdd(&s_active[p], active);
           atomicMax(&s_maxd[p], __float_as_uint(maxd));
-          atomicAdd(&s_energy[p], energy);
+          atomicAdd(&s_energy[p], (double)energy);
         }
         if (diverged) s_div[p] = 1;
       }

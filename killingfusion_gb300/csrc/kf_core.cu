@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 
 #include "kf_internal.h"
@@ -144,11 +145,19 @@ static bool dims_ok(const int n[3]) {
   return (int64_t)n[0] * n[1] * n[2] < (int64_t)INT32_MAX;
 }
 
+// phi = v, w = 0 with 16-byte stores (the planes come from cudaMalloc,
+// 256-byte aligned); the last n % 4 entries one by one.
 __global__ void k_fill(float *phi, int32_t *w, int64_t n, float v) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    phi[i] = v;
-    w[i] = 0;
+  const int64_t n4 = n >> 2;
+  const float4 v4 = make_float4(v, v, v, v);
+  const int4 z4 = make_int4(0, 0, 0, 0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    reinterpret_cast<float4 *>(phi)[i] = v4;
+    reinterpret_cast<int4 *>(w)[i] = z4;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
+    phi[4 * n4 + threadIdx.x] = v;
+    w[4 * n4 + threadIdx.x] = 0;
   }
 }
 
@@ -157,7 +166,8 @@ extern "C" int kf_grid_reset(kf_grid g, const kf_params *p, void *stream) {
   int rc = kf_check_params(p);
   if (rc) return rc;
   float v = (float)(p->max_surface + p->epsilon);
-  k_fill<<<(unsigned)((g->count + 255) / 256), 256, 0, kf_stream(stream)>>>(g->phi, g->w, g->count, v);
+  const int64_t blocks = std::min<int64_t>((g->count / 4 + 255) / 256 + 1, (int64_t)kf_num_sms() * 16);
+  k_fill<<<(unsigned)blocks, 256, 0, kf_stream(stream)>>>(g->phi, g->w, g->count, v);
   KF_CHECK_LAUNCH("k_fill");
   return KF_OK;
 }

@@ -30,7 +30,17 @@ inline unsigned blocks_for(int64_t n, int per = kBlock) {
   return (unsigned)((n + per - 1) / per);
 }
 
+// Coordinates of voxel i; 32-bit division when the index fits (several
+// times cheaper than the 64-bit one).
 __device__ __forceinline__ void voxel_xyz(int64_t i, int nx, int ny, int &x, int &y, int &z) {
+  if (i <= 0xffffffffLL) {
+    const unsigned plane = (unsigned)nx * (unsigned)ny, ui = (unsigned)i;
+    z = (int)(ui / plane);
+    const unsigned r = ui - (unsigned)z * plane;
+    y = (int)(r / (unsigned)nx);
+    x = (int)(r - (unsigned)y * (unsigned)nx);
+    return;
+  }
   int64_t plane = (int64_t)nx * ny;
   z = (int)(i / plane);
   int64_t r = i - (int64_t)z * plane;

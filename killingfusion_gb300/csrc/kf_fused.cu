@@ -42,7 +42,7 @@ namespace {
 // Dense pass: stream the slab, list the band voxels (st[iter].list counts
 // them); kPassThrough copies psi of the other voxels to the output buffer.
 template <bool kPassThrough>
-__global__ void __launch_bounds__(kThreads, 5) k_fused_stream(FusedArgs a, int *__restrict__ list) {
+__global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__restrict__ list) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
       a.st[a.iter].skipped = 1;
@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
   const int rounds = (nq + total_groups - 1) / total_groups;
   __shared__ int s_next[kGroupsPerBlock];
   float maxd = 0.f;
-  double energy = 0.0;
+  float energy = 0.f;  // this thread's voxels; the block and grid sums are float64
   unsigned active = 0;
   bool diverged = false;
   for (int r = 0; r < rounds; ++r) {
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
       __syncthreads();
     }
   }
-  reduce_iter_stats<kBandThreads>(a.st + a.iter, active, maxd, energy, diverged);
+  reduce_iter_stats<kBandThreads>(a.st + a.iter, active, maxd, (double)energy, diverged);
 }
 
 // In-place update: psi(list[k]) = entry k of the band pass's output planes,

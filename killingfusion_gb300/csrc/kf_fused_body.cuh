@@ -51,11 +51,27 @@ __device__ __forceinline__ float phi_at(const FusedArgs &a, int x, int y, int z)
 // phi_live at grid coordinate t (SDF::getDistance after its -0.5 shift,
 // SDF.cpp:503-524): truncating base, outside corners read MaxSurface+eps.
 __device__ __forceinline__ float phi_tri(const FusedArgs &a, float t0, float t1, float t2) {
+  const DevParams &d = a.dp;
   int b0 = (int)t0, b1 = (int)t1, b2 = (int)t2;
   float f0 = t0 - (float)b0, f1 = t1 - (float)b1, f2 = t2 - (float)b2;
   float v[8];
+  if ((unsigned)b0 < (unsigned)(d.nx - 1) && (unsigned)b1 < (unsigned)(d.ny - 1) &&
+      (unsigned)b2 < (unsigned)(d.nz - 1)) {
+    // all eight corners inside: one address, constant strides
+    const float *p = a.live + ((int64_t)b2 * d.ny + b1) * d.nx + b0;
+    const int64_t sy = d.nx, sz = (int64_t)d.nx * d.ny;
+    v[0] = __ldg(p);
+    v[1] = __ldg(p + 1);
+    v[2] = __ldg(p + sy);
+    v[3] = __ldg(p + sy + 1);
+    v[4] = __ldg(p + sz);
+    v[5] = __ldg(p + sz + 1);
+    v[6] = __ldg(p + sz + sy);
+    v[7] = __ldg(p + sz + sy + 1);
+  } else {
 #pragma unroll
-  for (int c = 0; c < 8; ++c) v[c] = phi_at(a, b0 + (c & 1), b1 + ((c >> 1) & 1), b2 + (c >> 2));
+    for (int c = 0; c < 8; ++c) v[c] = phi_at(a, b0 + (c & 1), b1 + ((c >> 1) & 1), b2 + (c >> 2));
+  }
   return lerp3(v, f0, f1, f2);
 }
 
@@ -370,7 +386,7 @@ __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, 
 // the next iteration's list (-1 if it left the band); the group leader
 // accumulates the statistics.
 __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int slot, int gl, unsigned gmask,
-                                                 float &maxd, double &energy, unsigned &active,
+                                                 float &maxd, float &energy, unsigned &active,
                                                  bool &diverged) {
   const DevParams &dp = a.dp;
   int x, y, z;
@@ -394,7 +410,7 @@ __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int 
       a.oy[slot] = c0[1] + d[1];
       a.oz[slot] = c0[2] + d[2];
       maxd = fmaxf(maxd, sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
-      energy += (double)en;
+      energy += en;
       ++active;
       next = i;
     } else {  // left the band: its psi is final, settle the output buffer

@@ -84,11 +84,19 @@ __device__ __forceinline__ int classify(const McGrid &g, int64_t i, int &x, int 
   if (i >= g.count) return -1;
   const float d = __ldg(g.phi + i);
   if (d > g.hi || d < g.lo) return -1;
-  const int64_t plane = (int64_t)g.nx * g.ny;
-  z = (int)(i / plane);
-  const int64_t r = i - (int64_t)z * plane;
-  y = (int)(r / g.nx);
-  x = (int)(r - (int64_t)y * g.nx);
+  if (g.count <= 0xffffffffLL) {  // 32-bit division, several times cheaper
+    const unsigned plane = (unsigned)g.nx * (unsigned)g.ny, ui = (unsigned)i;
+    z = (int)(ui / plane);
+    const unsigned r = ui - (unsigned)z * plane;
+    y = (int)(r / (unsigned)g.nx);
+    x = (int)(r - (unsigned)y * (unsigned)g.nx);
+  } else {
+    const int64_t plane = (int64_t)g.nx * g.ny;
+    z = (int)(i / plane);
+    const int64_t r = i - (int64_t)z * plane;
+    y = (int)(r / g.nx);
+    x = (int)(r - (int64_t)y * g.nx);
+  }
   int cube = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
@@ -188,6 +196,7 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *b
     float val[8];
     const int cube = classify(g, base + (int64_t)r * kThreads, x, y, z, val);
     const uint32_t n = (uint32_t)cube_tris(cube);
+    if (!__syncthreads_or(n != 0)) continue;  // no triangle in this round
     uint32_t round_total;
     int64_t out = out0 + (int64_t)block_exclusive_scan<uint32_t>(n, &round_total);
     out0 += round_total;
