@@ -35,6 +35,8 @@
 //     from eight moments of the cell [i, i+1]^3.
 // Voxels on the grid's outer shell take the generic reference-order path
 // (truncating casts, linear-index wrap, outside values).
+#include <algorithm>
+
 #include "kf_fused_body.cuh"
 
 namespace {
@@ -44,11 +46,10 @@ namespace {
 template <bool kPassThrough>
 __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__restrict__ list) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
-    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
-      a.st[a.iter].skipped = 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.iter].skipped = 1;
     return;
   }
-  stream_tile<kPassThrough>(a, blockIdx.x, blockIdx.y, blockIdx.z, list, &a.st[a.iter].list);
+  stream_flat<kPassThrough>(a, blockIdx.x, list, &a.st[a.iter].list);
 }
 
 // Band pass: a group of 8 lanes per listed voxel, launched as one resident
@@ -137,9 +138,10 @@ void kf_fused_graph_destroy(FusedGraph *g) {
 static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
                               int iterations, IterStats *st, int *lists, bool band_only,
                               cudaStream_t s) {
-  dim3 block(kTX, kTY);
   const unsigned band_blocks = (unsigned)kf_num_sms() * 3;  // one resident wave
-  dim3 grid((dp.nx + kTX - 1) / kTX, (dp.ny + kTY - 1) / kTY, (dp.nz + kZSlab - 1) / kZSlab);
+  const unsigned grid = (unsigned)std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) /
+                                                        (kThreads * kFlatGroups), 1);
+  const unsigned block = kThreads;
   FusedArgs a = make_args(live, can, dp, st);
   void *buf[2][3] = {{psi->p[0], psi->p[1], psi->p[2]}, {psi->q[0], psi->q[1], psi->q[2]}};
   int *lst[2] = {lists, lists + dp.count};

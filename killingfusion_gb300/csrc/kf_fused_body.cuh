@@ -378,6 +378,94 @@ __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, 
   for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
 }
 
+// Dense pass over one run of kFlatVoxels consecutive voxels (flat index
+// order): thread t streams the float4 groups t and t + kThreads of the run
+// from each psi plane and from phi_live, applies the band test and appends
+// the band voxels to list (*count counts them).  kPassThrough copies psi of
+// all voxels to the output buffer (the band pass overwrites the band
+// voxels').  The last count % 4 voxels of the grid are taken by run 0.
+constexpr int kFlatGroups = 2;
+constexpr int kFlatVoxels = kThreads * kFlatGroups * 4;
+
+__device__ __forceinline__ void flat_test(const FusedArgs &a, int64_t i, float qx, float qy, float qz, float ph,
+                                          int *queue, int *qn, unsigned &moved, int bit) {
+  if (qx != 0.f || qy != 0.f || qz != 0.f)
+    moved |= 1u << bit;
+  else if (in_band(ph, a.band_hi, a.band_lo))
+    queue[atomicAdd(qn, 1)] = (int)i;
+}
+
+template <bool kPassThrough>
+__device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int *__restrict__ list,
+                                            unsigned *count) {
+  __shared__ int queue[kFlatVoxels + 4];
+  __shared__ int qn, qbase;
+  const DevParams &dp = a.dp;
+  const int tid = threadIdx.x;
+  if (tid == 0) qn = 0;
+  __syncthreads();
+  const int64_t n4 = dp.count >> 2;
+  const float4 *ix = reinterpret_cast<const float4 *>(a.ix), *iy = reinterpret_cast<const float4 *>(a.iy),
+               *iz = reinterpret_cast<const float4 *>(a.iz), *lv = reinterpret_cast<const float4 *>(a.live);
+  float4 px[kFlatGroups], py[kFlatGroups], pz[kFlatGroups], ph[kFlatGroups];
+  int64_t q[kFlatGroups];
+#pragma unroll
+  for (int g = 0; g < kFlatGroups; ++g) {
+    q[g] = run * (kThreads * kFlatGroups) + g * kThreads + tid;
+    const bool ok = q[g] < n4;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    px[g] = ok ? __ldcs(ix + q[g]) : zero;
+    py[g] = ok ? __ldcs(iy + q[g]) : zero;
+    pz[g] = ok ? __ldcs(iz + q[g]) : zero;
+    ph[g] = ok ? __ldg(lv + q[g]) : zero;
+  }
+  unsigned moved = 0;  // bit 4g + e: element e of group g has moved
+#pragma unroll
+  for (int g = 0; g < kFlatGroups; ++g) {
+    if (q[g] >= n4) continue;
+    const int64_t i = 4 * q[g];
+    flat_test(a, i, px[g].x, py[g].x, pz[g].x, ph[g].x, queue, &qn, moved, 4 * g);
+    flat_test(a, i + 1, px[g].y, py[g].y, pz[g].y, ph[g].y, queue, &qn, moved, 4 * g + 1);
+    flat_test(a, i + 2, px[g].z, py[g].z, pz[g].z, ph[g].z, queue, &qn, moved, 4 * g + 2);
+    flat_test(a, i + 3, px[g].w, py[g].w, pz[g].w, ph[g].w, queue, &qn, moved, 4 * g + 3);
+    if (kPassThrough) {
+      __stcs(reinterpret_cast<float4 *>(a.ox) + q[g], px[g]);
+      __stcs(reinterpret_cast<float4 *>(a.oy) + q[g], py[g]);
+      __stcs(reinterpret_cast<float4 *>(a.oz) + q[g], pz[g]);
+    }
+  }
+  // the ragged end of the grid, by run 0
+  if (run == 0 && tid < (int)(dp.count & 3)) {
+    const int64_t i = 4 * n4 + tid;
+    const float qx = a.ix[i], qy = a.iy[i], qz = a.iz[i];
+    flat_test(a, i, qx, qy, qz, __ldg(a.live + i), queue, &qn, moved, 4 * kFlatGroups);
+    if (kPassThrough) {
+      a.ox[i] = qx;
+      a.oy[i] = qy;
+      a.oz[i] = qz;
+    }
+  }
+  // voxels that have moved: the warped value is a trilinear gather
+  while (moved) {
+    const int bit = __ffs(moved) - 1;
+    moved &= moved - 1;
+    const int64_t i = bit < 4 * kFlatGroups
+                          ? 4 * (run * (kThreads * kFlatGroups) + (bit >> 2) * kThreads + tid) + (bit & 3)
+                          : 4 * n4 + tid;
+    const unsigned plane = (unsigned)dp.nx * (unsigned)dp.ny, ui = (unsigned)i;
+    const int z = (int)(ui / plane);
+    const unsigned r = ui - (unsigned)z * plane;
+    const int y = (int)(r / (unsigned)dp.nx);
+    const int x = (int)(r - (unsigned)y * (unsigned)dp.nx);
+    const float s = warped_value(a, x, y, z, a.ix[i], a.iy[i], a.iz[i]);
+    if (in_band(s, a.band_hi, a.band_lo)) queue[atomicAdd(&qn, 1)] = (int)i;
+  }
+  __syncthreads();
+  if (tid == 0 && qn) qbase = (int)atomicAdd(count, (unsigned)qn);
+  __syncthreads();
+  for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
+}
+
 // Update one band voxel i with the group of 8 lanes it is assigned to and
 // write its new psi to entry `slot` of the output planes (slot == i for
 // ping-pong buffers; the voxel's list position for in-place updates).  The
