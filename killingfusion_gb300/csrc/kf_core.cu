@@ -190,7 +190,8 @@ extern "C" int kf_grid_create(const int dims[3], double voxel_size, const double
   g->voxel = voxel_size;
   g->unknown_clip = unknown_clip;
   if (cudaMalloc(&g->phi, g->count * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&g->w, g->count * sizeof(int32_t)) != cudaSuccess) {
+      cudaMalloc(&g->w, g->count * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&g->ctr, 256) != cudaSuccess) {
     cudaGetLastError();
     kf_grid_destroy(g);
     return kf_fail(KF_ERR_OOM, "cudaMalloc of the SDF grid failed");
@@ -212,6 +213,7 @@ extern "C" int kf_grid_destroy(kf_grid g) {
   cudaFree(g->w_alt);
   cudaFree(g->depth);
   cudaFree(g->integ);
+  cudaFree(g->ctr);
   delete g;
   return KF_OK;
 }

@@ -316,37 +316,119 @@ __device__ __forceinline__ void warp_sample(const float *__restrict__ phi, const
   out_phi = lerp3(vp, f0, f1, f2);
 }
 
-// SDF::update followed by canonical->fuse(live) (KillingFusion.cpp:158-159,
-// SDF.cpp:199-241, 300-328).  When `can` is null only the warp is done.
-template <typename P>
-__global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ lphi,
-                                                      const int32_t *__restrict__ lw,
-                                                      float *__restrict__ lphi_out,
-                                                      int32_t *__restrict__ lw_out,
-                                                      float *__restrict__ cphi, int32_t *__restrict__ cw,
-                                                      PsiPlanes<P> f, int nx, int ny, int nz,
-                                                      double oob) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)nx * ny * nz) return;
-  int x, y, z;
-  voxel_xyz(i, nx, ny, x, y, z);
-  double dphi, dw;
-  bool moved;
-  warp_sample(lphi, lw, nx, ny, nz, oob, f, i, x, y, z, dphi, dw, moved);
-  float nphi = moved ? (float)dphi : lphi[i];
-  int32_t nw = moved ? (int32_t)(int64_t)dw : lw[i];
-  lphi_out[i] = nphi;
-  lw_out[i] = nw;
-  if (!cphi) return;
+// FUSE_BY_MERGE of (nphi, nw) into canonical voxel i (SDF.cpp:212-236).
+__device__ __forceinline__ void fuse_voxel(float *__restrict__ cphi, int32_t *__restrict__ cw, int64_t i,
+                                           float nphi, int32_t nw) {
   if (nw == 0) return;
-  int32_t w1 = cw[i];
+  const int32_t w1 = cw[i];
   if (w1 == 0) {
     cphi[i] = nphi;
     cw[i] = nw;
   } else {
-    double d1 = (double)cphi[i];
+    const double d1 = (double)cphi[i];
     cphi[i] = (float)(((double)w1 * d1 + (double)nw * (double)nphi) / (double)(w1 + nw));
     cw[i] = w1 + nw;
+  }
+}
+
+// SDF::update followed by canonical->fuse(live) (KillingFusion.cpp:158-159,
+// SDF.cpp:199-241, 300-328), in place.  A voxel with psi == 0 keeps its
+// values (zero interpolation weights), so only the moved voxels -- the band
+// the solver updated -- change: their resampled values go to a side list
+// (warp-aggregated slots) and k_warp_scatter writes them back once every
+// moved voxel has read its neighbours' old values.  Each thread takes four
+// consecutive voxels with 16-byte loads.  When `cphi` is null only the warp
+// is done.
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ lphi,
+                                                      const int32_t *__restrict__ lw,
+                                                      float *__restrict__ cphi, int32_t *__restrict__ cw,
+                                                      PsiPlanes<P> f, int nx, int ny, int nz, double oob,
+                                                      float *__restrict__ side_phi,
+                                                      int32_t *__restrict__ side_w,
+                                                      int32_t *__restrict__ side_i,
+                                                      unsigned *__restrict__ ctr) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i0 = 4 * q;
+  float ph[4] = {0.f, 0.f, 0.f, 0.f};
+  int32_t wv[4] = {0, 0, 0, 0};
+  unsigned moved = 0;
+  int valid = 0;
+  if (i0 + 3 < N) {
+    valid = 4;
+    const float4 a = __ldcs(reinterpret_cast<const float4 *>(lphi) + q);
+    const int4 b = __ldcs(reinterpret_cast<const int4 *>(lw) + q);
+    ph[0] = a.x; ph[1] = a.y; ph[2] = a.z; ph[3] = a.w;
+    wv[0] = b.x; wv[1] = b.y; wv[2] = b.z; wv[3] = b.w;
+    if (sizeof(P) == 4) {
+      const float4 x = __ldcs(reinterpret_cast<const float4 *>(f.x) + q);
+      const float4 y = __ldcs(reinterpret_cast<const float4 *>(f.y) + q);
+      const float4 z = __ldcs(reinterpret_cast<const float4 *>(f.z) + q);
+      moved = (x.x != 0.f || y.x != 0.f || z.x != 0.f) | (x.y != 0.f || y.y != 0.f || z.y != 0.f) << 1 |
+              (x.z != 0.f || y.z != 0.f || z.z != 0.f) << 2 | (x.w != 0.f || y.w != 0.f || z.w != 0.f) << 3;
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (f.x[i0 + e] != P(0) || f.y[i0 + e] != P(0) || f.z[i0 + e] != P(0)) moved |= 1u << e;
+    }
+  } else if (i0 < N) {
+    valid = (int)(N - i0);
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      if (e >= valid) break;
+      ph[e] = lphi[i0 + e];
+      wv[e] = lw[i0 + e];
+      if (f.x[i0 + e] != P(0) || f.y[i0 + e] != P(0) || f.z[i0 + e] != P(0)) moved |= 1u << e;
+    }
+  }
+  // one slot range per warp for its moved voxels
+  const int lane = threadIdx.x & 31;
+  const unsigned nm = (unsigned)__popc(moved);
+  unsigned incl = nm;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const unsigned wtotal = __shfl_sync(0xffffffffu, incl, 31);
+  unsigned base = 0;
+  if (lane == 0 && wtotal) base = atomicAdd(ctr, wtotal);
+  unsigned slot = __shfl_sync(0xffffffffu, base, 0) + incl - nm;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    if (e >= valid) break;
+    const int64_t i = i0 + e;
+    float nphi = ph[e];
+    int32_t nw = wv[e];
+    if (moved & (1u << e)) {
+      int x, y, z;
+      voxel_xyz(i, nx, ny, x, y, z);
+      double dphi, dw;
+      bool m;
+      warp_sample(lphi, lw, nx, ny, nz, oob, f, i, x, y, z, dphi, dw, m);
+      nphi = (float)dphi;
+      nw = (int32_t)(int64_t)dw;
+      side_phi[slot] = nphi;
+      side_w[slot] = nw;
+      side_i[slot] = (int32_t)i;
+      ++slot;
+    }
+    if (cphi) fuse_voxel(cphi, cw, i, nphi, nw);
+  }
+}
+
+// Writes the moved voxels' resampled values back (after k_warp_fuse).
+__global__ void __launch_bounds__(kBlock) k_warp_scatter(float *__restrict__ lphi, int32_t *__restrict__ lw,
+                                                         const float *__restrict__ side_phi,
+                                                         const int32_t *__restrict__ side_w,
+                                                         const int32_t *__restrict__ side_i,
+                                                         const unsigned *__restrict__ ctr) {
+  const unsigned n = *ctr;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int32_t i = side_i[k];
+    lphi[i] = side_phi[k];
+    lw[i] = side_w[k];
   }
 }
 
@@ -495,25 +577,28 @@ static PsiPlanes<P> planes(kf_field f) {
 
 static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevParams &dp,
                           cudaStream_t s) {
-  int st = kf_grid_ensure_alt(live);
+  // the moved-voxel list lives in psi's second (ping-pong) buffer, which
+  // holds nothing between solves: values, weights and indices, N each
+  int st = kf_field_ensure_pair(psi);
   if (st) return st;
+  float *side_phi = (float *)psi->q[0];
+  int32_t *side_w = (int32_t *)psi->q[1];
+  int32_t *side_i = (int32_t *)psi->q[2];
   float *cphi = can ? can->phi : nullptr;
   int32_t *cw = can ? can->w : nullptr;
+  KF_CHECK_CUDA(cudaMemsetAsync(live->ctr, 0, sizeof(unsigned), s));
+  const unsigned blocks = blocks_for((live->count + 3) / 4);
   if (psi->prec == KF_F32)
-    k_warp_fuse<float><<<blocks_for(live->count), kBlock, 0, s>>>(
-        live->phi, live->w, live->phi_alt, live->w_alt, cphi, cw, planes<float>(psi),
-        live->n[0], live->n[1], live->n[2], dp.oob_phi);
+    k_warp_fuse<float><<<blocks, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<float>(psi), live->n[0],
+                                                 live->n[1], live->n[2], dp.oob_phi, side_phi, side_w, side_i,
+                                                 live->ctr);
   else
-    k_warp_fuse<double><<<blocks_for(live->count), kBlock, 0, s>>>(
-        live->phi, live->w, live->phi_alt, live->w_alt, cphi, cw, planes<double>(psi),
-        live->n[0], live->n[1], live->n[2], dp.oob_phi);
+    k_warp_fuse<double><<<blocks, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<double>(psi), live->n[0],
+                                                  live->n[1], live->n[2], dp.oob_phi, side_phi, side_w, side_i,
+                                                  live->ctr);
+  k_warp_scatter<<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(live->phi, live->w, side_phi, side_w, side_i,
+                                                               live->ctr);
   KF_CHECK_LAUNCH("k_warp_fuse");
-  float *tp = live->phi;
-  live->phi = live->phi_alt;
-  live->phi_alt = tp;
-  int32_t *tw = live->w;
-  live->w = live->w_alt;
-  live->w_alt = tw;
   return KF_OK;
 }
 

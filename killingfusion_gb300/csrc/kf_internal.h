@@ -25,6 +25,7 @@ struct kf_grid_s {
   size_t depth_cap;
   void *integ;     // integration scratch: counter, coordinate tables, list
   size_t integ_bytes;
+  unsigned *ctr;   // device counter of the warp's moved-voxel list
 };
 
 struct IterStats;

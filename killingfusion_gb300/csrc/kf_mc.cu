@@ -80,10 +80,15 @@ __device__ __forceinline__ float at(const McGrid &g, int x, int y, int z) {
 
 // Cube configuration of cell i, or -1 when the cell is skipped (outside the
 // grid, or its own value outside [lo, hi]).
-__device__ __forceinline__ int classify(const McGrid &g, int64_t i, int &x, int &y, int &z, float val[8]) {
-  if (i >= g.count) return -1;
-  const float d = __ldg(g.phi + i);
-  if (d > g.hi || d < g.lo) return -1;
+__device__ __forceinline__ float own_value(const McGrid &g, int64_t i) {
+  return i < g.count ? __ldg(g.phi + i) : g.hi + 1.0f;  // past the end: skipped
+}
+
+// d: the cell's own value, own_value(g, i), loaded ahead by the caller so the
+// loads of all rounds are in flight together.
+__device__ __forceinline__ int classify(const McGrid &g, int64_t i, float d, int &x, int &y, int &z,
+                                        float val[8]) {
+  if (d > g.hi || d < g.lo) return -1;  // SDF.cpp:407 (a NaN is not skipped)
   if (g.count <= 0xffffffffLL) {  // 32-bit division, several times cheaper
     const unsigned plane = (unsigned)g.nx * (unsigned)g.ny, ui = (unsigned)i;
     z = (int)(ui / plane);
@@ -140,12 +145,15 @@ __device__ T block_exclusive_scan(T v, T *total) {
 
 __global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block_tris) {
   const int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + threadIdx.x;
+  float d[kRounds];
+#pragma unroll
+  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, base + (int64_t)r * kThreads);
   uint32_t n = 0;
 #pragma unroll
   for (int r = 0; r < kRounds; ++r) {
     int x, y, z;
     float val[8];
-    n += cube_tris(classify(g, base + (int64_t)r * kThreads, x, y, z, val));
+    n += cube_tris(classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val));
   }
   uint32_t total;
   block_exclusive_scan<uint32_t>(n, &total);
@@ -191,10 +199,18 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *b
                                                       float *__restrict__ verts, int64_t capacity) {
   int64_t out0 = block_off[blockIdx.x];
   const int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + threadIdx.x;
+  float d[kRounds];
+#pragma unroll
+  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, base + (int64_t)r * kThreads);
+#pragma unroll 1
   for (int r = 0; r < kRounds; ++r) {
     int x, y, z;
     float val[8];
-    const int cube = classify(g, base + (int64_t)r * kThreads, x, y, z, val);
+    float dr = d[0];
+#pragma unroll
+    for (int k = 1; k < kRounds; ++k)
+      if (k == r) dr = d[k];
+    const int cube = classify(g, base + (int64_t)r * kThreads, dr, x, y, z, val);
     const uint32_t n = (uint32_t)cube_tris(cube);
     if (!__syncthreads_or(n != 0)) continue;  // no triangle in this round
     uint32_t round_total;
