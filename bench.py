@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--solver", default="fused", choices=["fused", "plain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-iters", type=int, default=2, help="Jacobi iterations in the CPU sample")
+    ap.add_argument("--workload", default="ellipsoid", choices=["ellipsoid", "batch", "large"],
+                    help="ellipsoid: 256^3 sequence (the bench line); batch: 64 registration problems of "
+                         "32-160^3, 150 iterations; large: 512^3 capsule sequence, 300 iterations")
     return ap.parse_args()
 
 
@@ -98,8 +101,9 @@ class Clocks:
             os.close(fd)
             self.out = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.out, stderr=subprocess.DEVNULL)
+            time.sleep(0.5)  # the first samples come after the tool has started
         except Exception:
             self.proc = None
 
@@ -263,6 +267,162 @@ def run_ours(args, rank, world, local):
     return res, seq, P
 
 
+def batch_sizes(count=64, seed=4):
+    """Edges of the batched workload: log-uniform in [32, 160]."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return [int(round(float(np.exp(rng.uniform(np.log(32), np.log(160)))))) for _ in range(count)]
+
+
+def run_batch(args, local):
+    """64 independent two-frame registrations (sphere, ellipsoid or torus,
+    rigid offset + bend, edges 32-160), 150 band-only iterations each, all in
+    one batch; beside it the same problems solved one after another."""
+    import numpy as np
+    import torch
+
+    from killingfusion_gb300 import capi, synth
+
+    torch.cuda.set_device(local)
+    iters = 150
+    sizes = batch_sizes()
+    probs = []
+    for k, n in enumerate(sizes):
+        can, live, voxel = synth.shape_problem(1000 + k, n)
+        P = capi.Params.paper(voxel)
+        gl = capi.Grid((n, n, n), voxel, (0, 0, 0), P.unknown_clip, P)
+        gc = capi.Grid((n, n, n), voxel, (0, 0, 0), P.unknown_clip, P)
+        gl.upload(live, (live <= P.max_surface).astype(np.int32))
+        gc.upload(can, (can <= P.max_surface).astype(np.int32))
+        probs.append((gl, gc, capi.Field((n, n, n), capi.KF_F32), P))
+    voxels = sum(n ** 3 for n in sizes)
+    batch = capi.Batch(probs, iters)
+    blocks = batch.autotune()
+
+    def zero_all():
+        for _, _, f, _ in probs:
+            f.zero()
+
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        zero_all()
+        batch.run()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    band_total = 0
+    for _ in range(args.steps):
+        zero_all()
+        st = batch.run()
+        band_total = sum(x["active_first"] for x in st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    # the same problems one after another (band-only and dense fused solves)
+    seq_ms = {}
+    for solver in ("band", "fused"):
+        for rep in range(2):
+            zero_all()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for gl, gc, f, P in probs:
+                capi.psi_solve(gl, gc, f, P, iters, solver)
+            b.record(stream)
+            torch.cuda.synchronize()
+            seq_ms[solver] = a.elapsed_time(b)
+    batch.close()
+    value = voxels * iters / (ms / 1e3)
+    return {
+        "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batch-64", "problems": len(sizes), "edges": [min(sizes), max(sizes)],
+                   "voxels": voxels, "iterations": iters, "weights": "paper", "solver": "batched band-only",
+                   "band_blocks_per_sm": blocks,
+                   "step": "zero psi of all 64 problems, one kf_batch_run (150 iterations each)"},
+        "band_voxels_first_iteration": band_total,
+        "sequential_band_ms": seq_ms["band"], "sequential_fused_ms": seq_ms["fused"],
+        "batched_over_sequential_band": seq_ms["band"] / ms,
+        "clocks": clk, "gpu_launches": (1 + iters) * args.steps,
+    }
+
+
+def run_large(args, local):
+    """512^3 / 2 mm capsule sequence: per frame integrate, zero psi, 300
+    dense fused iterations; warp + fuse and the three meshes every 10th
+    frame."""
+    import numpy as np
+    import torch
+
+    from killingfusion_gb300 import capi, synth
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = capi.load()
+    iters = 300
+    seq = synth.CapsuleSequence(seed=5, frames=100, n=512)
+    grid = seq.grid
+    P = capi.Params.paper(grid.voxel)
+    steps = max(args.steps, 10)
+    nframes = 1 + args.warmup + steps
+    dev_frames = [torch.from_numpy(seq.frame(f)).to(dev) for f in range(nframes)]
+    can = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
+    live = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
+    psi = capi.Field(grid.dims, capi.KF_F32)
+    can.integrate(dev_frames[0], min_depth=0.05, max_depth=1.6)
+    mesh = torch.empty((MESH_CAP, 9), dtype=torch.float32, device=dev)
+    N3 = int(np.prod(grid.dims))
+    stream = torch.cuda.current_stream(dev)
+    stats = capi.SolveStats()
+
+    def frame(f, fuse):
+        live.reset(P)
+        live.integrate(dev_frames[f], min_depth=0.05, max_depth=1.6)
+        psi.zero()
+        capi.check(L.kf_psi_solve(live.h, can.h, psi.h, C.byref(P.c()), iters, capi.KF_SOLVER_FUSED,
+                                  C.byref(stats), None))
+        if fuse:
+            mesh_once(capi, L, live, P, mesh.data_ptr(), MESH_CAP)
+            capi.check(L.kf_warp_fuse(can.h, live.h, psi.h, C.byref(P.c()), None))
+            mesh_once(capi, L, live, P, mesh.data_ptr(), MESH_CAP)
+            mesh_once(capi, L, can, P, mesh.data_ptr(), MESH_CAP)
+
+    for f in range(1, 1 + args.warmup):
+        frame(f, f == args.warmup)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k, f in enumerate(range(1 + args.warmup, nframes)):
+        frame(f, (k + 1) % 10 == 0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / steps
+    solve_ms = stats.device_ms
+    peak, peak_kind = peaks()
+    algo = ALGO_BYTES_PER_VOXEL * N3 + ALGO_BYTES_PER_BAND_VOXEL * stats.active_first
+    achieved = algo / (solve_ms / iters / 1e3) / 1e9
+    return {
+        "metric": METRIC, "value": N3 * iters / (ms / 1e3), "unit": "voxel-updates/s", "n_gpus": 1,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "capsule-sequence-512", "grid": [512] * 3, "voxel_mm": 2.0,
+                   "iterations_per_frame": iters, "weights": "paper", "solver": "fused",
+                   "step": "one frame: integrate, zero psi, 300 iterations; warp+fuse and 3 meshes "
+                           "every 10th frame"},
+        "solve_ms_last_frame": solve_ms, "band_voxels": stats.active_first,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "fused psi iteration", "peak_source": peak_kind},
+        "clocks": clk,
+    }
+
+
 def cpu_sample(seq, P, iters, nthreads=0):
     """Bounded FP64 sample of one frame on the host cores: integrate, `iters`
     Jacobi iterations, update + fuse, three meshes; extrapolated to the
@@ -313,6 +473,16 @@ def main():
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
 
     if args.impl == "reference" and rank != 0:
+        return
+    if args.workload != "ellipsoid":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the CPU port is timed on the 256^3 "
+                                  "ellipsoid workload only"}))
+            return
+        line = run_batch(args, local) if args.workload == "batch" else run_large(args, local)
+        if rank == 0:
+            print(json.dumps(line))
         return
     run_main(args, rank, world, local)
 
