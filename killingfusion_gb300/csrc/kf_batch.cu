@@ -106,6 +106,11 @@ __device__ __forceinline__ int find_work(const unsigned *pre, int n, unsigned k)
   return lo;
 }
 
+// Band pass of iteration `it` over all problems.  The work is cut into
+// chunks of kGroupsPerBlock voxels that never cross a problem, so a CTA works
+// on one problem at a time: it stages that problem's argument block in shared
+// memory (the gradient reads it as often as the single-grid kernel reads its
+// constant parameters) and appends the chunk's carried voxels with one atomic.
 __global__ void __launch_bounds__(kBandThreads, 3) k_batch_band(const BatchEntry *__restrict__ tab, int nprob,
                                                                int it) {
   __shared__ unsigned s_cnt[kMaxBatch];
@@ -115,7 +120,8 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_batch_band(const BatchEntry
   __shared__ double s_energy[kMaxBatch];
   __shared__ int s_div[kMaxBatch];
   __shared__ int s_next[kGroupsPerBlock];
-  __shared__ int s_prob[kGroupsPerBlock];
+  __shared__ FusedArgs s_a;
+  __shared__ int *s_list_in, *s_list_out;
   const int par = it & 1;
   for (int q = threadIdx.x; q < nprob; q += blockDim.x) {
     const FusedArgs &a = tab[q].a[par];
@@ -128,28 +134,41 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_batch_band(const BatchEntry
     s_div[q] = 0;
   }
   __syncthreads();
-  scan_counts<kMaxBatch>(s_cnt, s_pre, nprob);
+  // chunks per problem, scanned in place of the counts' copy
+  unsigned chunks = threadIdx.x < nprob ? (s_cnt[threadIdx.x] + kGroupsPerBlock - 1) / kGroupsPerBlock : 0u;
+  __shared__ unsigned s_chunks[kMaxBatch];
+  if (threadIdx.x < nprob) s_chunks[threadIdx.x] = chunks;
+  __syncthreads();
+  scan_counts<kMaxBatch>(s_chunks, s_pre, nprob);
   const unsigned total = s_pre[nprob];
   const int lane = threadIdx.x & 31;
   const int gl = lane & (kGroup - 1);
   const int group = threadIdx.x / kGroup;
   const unsigned gmask = 0xffu << (lane & ~(kGroup - 1));
-  const unsigned total_groups = gridDim.x * kGroupsPerBlock;
-  const unsigned rounds = (total + total_groups - 1) / total_groups;
-  for (unsigned r = 0; r < rounds; ++r) {
-    const unsigned k = (r * gridDim.x + blockIdx.x) * kGroupsPerBlock + group;
-    int next = -1, p = -1;
-    if (k < total) {
-      p = find_work(s_pre, nprob, k);
-      const BatchEntry &e = tab[p];
-      const FusedArgs &a = e.a[par];
-      const int *list_in = e.band + (par ? e.count : 0);
+  int cur = -1;  // problem staged in s_a (the same in every thread)
+  for (unsigned c = blockIdx.x; c < total; c += gridDim.x) {
+    const int p = find_work(s_pre, nprob, c);
+    if (p != cur) {
+      __syncthreads();  // the previous problem's arguments are no longer read
+      const int *src = reinterpret_cast<const int *>(&tab[p].a[par]);
+      int *dst = reinterpret_cast<int *>(&s_a);
+      for (int w = threadIdx.x; w < (int)(sizeof(FusedArgs) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
+      if (threadIdx.x == 0) {
+        s_list_in = tab[p].band + (par ? tab[p].count : 0);
+        s_list_out = tab[p].band + (par ? 0 : tab[p].count);
+      }
+      cur = p;
+      __syncthreads();
+    }
+    const unsigned k = (c - s_pre[p]) * kGroupsPerBlock + group;
+    int next = -1;
+    if (k < s_cnt[p]) {
       float maxd = 0.f;
       float energy = 0.f;
       unsigned active = 0;
       bool diverged = false;
-      const int v = list_in[k - s_pre[p]];
-      next = update_band_voxel(a, v, v, gl, gmask, maxd, energy, active, diverged);
+      const int v = s_list_in[k];
+      next = update_band_voxel(s_a, v, v, gl, gmask, maxd, energy, active, diverged);
       if (gl == 0) {
         if (active) {
           atomicAdd(&s_active[p], active);
@@ -159,32 +178,16 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_batch_band(const BatchEntry
         if (diverged) s_div[p] = 1;
       }
     }
-    if (gl == 0) {
-      s_next[group] = next;
-      s_prob[group] = p;
-    }
+    if (gl == 0) s_next[group] = next;
     __syncthreads();
     if (threadIdx.x == 0) {
-      // hand the updated voxels to the next iteration, one atomic per run of
-      // groups working on the same problem
-      int w = 0;
-      while (w < kGroupsPerBlock) {
-        if (s_next[w] < 0) {
-          ++w;
-          continue;
-        }
-        const int q = s_prob[w];
-        int end = w, cnt = 0;
-        while (end < kGroupsPerBlock && (s_next[end] < 0 || s_prob[end] == q)) {
-          cnt += s_next[end] >= 0;
-          ++end;
-        }
-        const BatchEntry &e = tab[q];
-        int *list_out = e.band + (par ? 0 : e.count);
-        unsigned b = atomicAdd(&e.a[par].st[it + 1].list, (unsigned)cnt);
-        for (int u = w; u < end; ++u)
-          if (s_next[u] >= 0) list_out[b++] = s_next[u];
-        w = end;
+      // hand the chunk's updated voxels to the next iteration
+      int cnt = 0;
+      for (int w = 0; w < kGroupsPerBlock; ++w) cnt += s_next[w] >= 0;
+      if (cnt) {
+        unsigned b = atomicAdd(&s_a.st[it + 1].list, (unsigned)cnt);
+        for (int w = 0; w < kGroupsPerBlock; ++w)
+          if (s_next[w] >= 0) s_list_out[b++] = s_next[w];
       }
     }
     __syncthreads();

@@ -195,52 +195,64 @@ __device__ __forceinline__ void vinterp(const float p1[3], const float p2[3], fl
   for (int k = 0; k < 3; ++k) out[k] = p1[k] + t * (p1[k] - p2[k]);
 }
 
+// Writes the n triangles of cell i (configuration `cube`) from position out
+// on; re-gathers the corners (band cells only, off the common path).
+__device__ __noinline__ void emit_cell(const McGrid &g, int64_t i, int cube, int64_t out,
+                                       float *__restrict__ verts, int64_t capacity) {
+  int x, y, z;
+  float val[8];
+  classify(g, i, __ldg(g.phi + i), x, y, z, val);
+  const int em = c_mc.edge[cube];
+  float p[8][3];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    p[k][0] = (float)(x + c_mc.corner[k][0]) / g.hx - 1.0f;
+    p[k][1] = (float)(y + c_mc.corner[k][1]) / g.hy - 1.0f;
+    p[k][2] = (float)(z + c_mc.corner[k][2]) / g.hz - 1.0f;
+  }
+  float vl[12][3];
+#pragma unroll
+  for (int e = 0; e < 12; ++e)
+    if (em & (1 << e))
+      vinterp(p[c_mc.ends[e][0]], p[c_mc.ends[e][1]], val[c_mc.ends[e][0]], val[c_mc.ends[e][1]], vl[e]);
+  const int n = c_mc.ntri[cube];
+  for (int t = 0; t < n; ++t, ++out) {
+    if (out >= capacity) break;
+    float *o = verts + 9 * out;
+#pragma unroll
+    for (int j2 = 0; j2 < 3; ++j2) {
+      const float *v = vl[c_mc.tri[cube][3 * t + j2]];
+      o[3 * j2 + 0] = v[0];
+      o[3 * j2 + 1] = -v[1];
+      o[3 * j2 + 2] = v[2];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *block_off,
                                                       float *__restrict__ verts, int64_t capacity) {
   int64_t out0 = block_off[blockIdx.x];
   const int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + threadIdx.x;
+  // classify every round first (the loads in flight together), then scan
+  // and emit the rounds that have triangles
   float d[kRounds];
 #pragma unroll
   for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, base + (int64_t)r * kThreads);
-#pragma unroll 1
+  int cube[kRounds];
+#pragma unroll
   for (int r = 0; r < kRounds; ++r) {
     int x, y, z;
     float val[8];
-    float dr = d[0];
+    cube[r] = classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val);
+  }
 #pragma unroll
-    for (int k = 1; k < kRounds; ++k)
-      if (k == r) dr = d[k];
-    const int cube = classify(g, base + (int64_t)r * kThreads, dr, x, y, z, val);
-    const uint32_t n = (uint32_t)cube_tris(cube);
+  for (int r = 0; r < kRounds; ++r) {
+    const uint32_t n = (uint32_t)cube_tris(cube[r]);
     if (!__syncthreads_or(n != 0)) continue;  // no triangle in this round
     uint32_t round_total;
-    int64_t out = out0 + (int64_t)block_exclusive_scan<uint32_t>(n, &round_total);
+    const int64_t out = out0 + (int64_t)block_exclusive_scan<uint32_t>(n, &round_total);
     out0 += round_total;
-    if (n == 0) continue;
-    const int em = c_mc.edge[cube];
-    float p[8][3];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      p[k][0] = (float)(x + c_mc.corner[k][0]) / g.hx - 1.0f;
-      p[k][1] = (float)(y + c_mc.corner[k][1]) / g.hy - 1.0f;
-      p[k][2] = (float)(z + c_mc.corner[k][2]) / g.hz - 1.0f;
-    }
-    float vl[12][3];
-#pragma unroll
-    for (int e = 0; e < 12; ++e)
-      if (em & (1 << e))
-        vinterp(p[c_mc.ends[e][0]], p[c_mc.ends[e][1]], val[c_mc.ends[e][0]], val[c_mc.ends[e][1]], vl[e]);
-    for (uint32_t t = 0; t < n; ++t, ++out) {
-      if (out >= capacity) break;
-      float *o = verts + 9 * out;
-#pragma unroll
-      for (int j2 = 0; j2 < 3; ++j2) {
-        const float *v = vl[c_mc.tri[cube][3 * t + j2]];
-        o[3 * j2 + 0] = v[0];
-        o[3 * j2 + 1] = -v[1];
-        o[3 * j2 + 2] = v[2];
-      }
-    }
+    if (n) emit_cell(g, base + (int64_t)r * kThreads, cube[r], out, verts, capacity);
   }
 }
 
