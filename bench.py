@@ -297,7 +297,7 @@ def run_batch(args, local):
         probs.append((gl, gc, capi.Field((n, n, n), capi.KF_F32), P))
     voxels = sum(n ** 3 for n in sizes)
     batch = capi.Batch(probs, iters)
-    blocks = batch.autotune()
+    blocks, regs = batch.autotune()
 
     def zero_all():
         for _, _, f, _ in probs:
@@ -335,6 +335,7 @@ def run_batch(args, local):
             torch.cuda.synchronize()
             seq_ms[solver] = a.elapsed_time(b)
     batch.close()
+    small = small_batch(capi, synth, torch, iters)
     value = voxels * iters / (ms / 1e3)
     return {
         "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": 1, "steps": args.steps,
@@ -342,13 +343,59 @@ def run_batch(args, local):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "batch-64", "problems": len(sizes), "edges": [min(sizes), max(sizes)],
                    "voxels": voxels, "iterations": iters, "weights": "paper", "solver": "batched band-only",
-                   "band_blocks_per_sm": blocks,
+                   "band_blocks_per_sm": blocks, "band_registers": regs,
                    "step": "zero psi of all 64 problems, one kf_batch_run (150 iterations each)"},
         "band_voxels_first_iteration": band_total,
         "sequential_band_ms": seq_ms["band"], "sequential_fused_ms": seq_ms["fused"],
         "batched_over_sequential_band": seq_ms["band"] / ms,
+        "small_problems": small,
         "clocks": clk, "gpu_launches": (1 + iters) * args.steps,
     }
+
+
+def small_batch(capi, synth, torch, iters, count=192):
+    """Many small problems (edges 16-40), where one launch per problem and
+    iteration is latency-bound: batched vs one after another."""
+    import numpy as np
+    rng = np.random.default_rng(9)
+    sizes = [int(v) for v in rng.integers(16, 41, count)]
+    probs = []
+    for k, n in enumerate(sizes):
+        can, live, voxel = synth.shape_problem(5000 + k, n)
+        P = capi.Params.paper(voxel)
+        gl = capi.Grid((n, n, n), voxel, (0, 0, 0), P.unknown_clip, P)
+        gc = capi.Grid((n, n, n), voxel, (0, 0, 0), P.unknown_clip, P)
+        gl.upload(live, (live <= P.max_surface).astype(np.int32))
+        gc.upload(can, (can <= P.max_surface).astype(np.int32))
+        probs.append((gl, gc, capi.Field((n, n, n), capi.KF_F32), P))
+    batch = capi.Batch(probs, iters)
+    shape = batch.autotune()
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _, _, f, _ in probs:
+            f.zero()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    def sequential():
+        for gl, gc, f, P in probs:
+            capi.psi_solve(gl, gc, f, P, iters, "band")
+
+    timed(batch.run)
+    tb = min(timed(batch.run) for _ in range(3))
+    timed(sequential)
+    ts = min(timed(sequential) for _ in range(2))
+    batch.close()
+    vox = sum(n ** 3 for n in sizes)
+    return {"problems": count, "edges": [min(sizes), max(sizes)], "voxels": vox, "iterations": iters,
+            "batched_ms": tb, "sequential_band_ms": ts, "batched_over_sequential_band": ts / tb,
+            "batched_voxel_updates_per_s": vox * iters / (tb / 1e3), "shape": list(shape)}
 
 
 def run_large(args, local):

@@ -274,10 +274,11 @@ typedef struct kf_batch_item {
 
 int kf_batch_create(const kf_batch_item *items, int count, int iterations, kf_batch *out);
 int kf_batch_destroy(kf_batch b);
-/* Times the band pass of the first iteration at 1, 2 and 3 resident blocks
- * per SM on this batch's data and keeps the fastest for kf_batch_run (psi is
- * not changed).  blocks_per_sm (may be NULL) receives the choice. */
-int kf_batch_autotune(kf_batch b, int *blocks_per_sm, void *stream);
+/* Times the band pass of the first iteration on this batch's data for each
+ * launch shape -- a register budget of 80 (1, 2 or 3 resident CTAs per SM)
+ * or 128 (1 or 2) -- and keeps the fastest for kf_batch_run (psi is not
+ * changed).  blocks_per_sm and registers (may be NULL) receive the choice. */
+int kf_batch_autotune(kf_batch b, int *blocks_per_sm, int *registers, void *stream);
 /* Runs the batch's iterations on every problem from its current psi.  stats:
  * one record per problem (may be NULL).  KF_ERR_DIVERGED when any problem
  * diverged (its record says which); the others are still solved. */

@@ -129,7 +129,7 @@ SIGNATURES = {
     "kf_energy_fd": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _vp, C.c_int, C.c_double, _vp, _vp]),
     "kf_batch_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
     "kf_batch_destroy": (C.c_int, [_vp]),
-    "kf_batch_autotune": (C.c_int, [_vp, C.POINTER(C.c_int), _vp]),
+    "kf_batch_autotune": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), _vp]),
     "kf_batch_run": (C.c_int, [_vp, _vp, _vp]),
     "kf_warp": (C.c_int, [_vp, _vp, _PP, _vp]),
     "kf_fuse": (C.c_int, [_vp, _vp, _vp]),
@@ -473,10 +473,11 @@ class Batch:
 
     __del__ = close
 
-    def autotune(self, stream=None) -> int:
-        k = C.c_int(0)
-        check(load().kf_batch_autotune(self.h, C.byref(k), _stream(stream)))
-        return k.value
+    def autotune(self, stream=None) -> tuple:
+        """(blocks per SM, register budget) of the fastest band-pass shape."""
+        k, r = C.c_int(0), C.c_int(0)
+        check(load().kf_batch_autotune(self.h, C.byref(k), C.byref(r), _stream(stream)))
+        return k.value, r.value
 
     def run(self, stream=None, raise_on_divergence=True) -> list:
         st = (SolveStats * self.n)()

@@ -111,8 +111,9 @@ __device__ __forceinline__ int find_work(const unsigned *pre, int n, unsigned k)
 // on one problem at a time: it stages that problem's argument block in shared
 // memory (the gradient reads it as often as the single-grid kernel reads its
 // constant parameters) and appends the chunk's carried voxels with one atomic.
-__global__ void __launch_bounds__(kBandThreads, 3) k_batch_band(const BatchEntry *__restrict__ tab, int nprob,
-                                                               int it) {
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const BatchEntry *__restrict__ tab,
+                                                                        int nprob, int it) {
   __shared__ unsigned s_cnt[kMaxBatch];
   __shared__ unsigned s_pre[kMaxBatch + 1];
   __shared__ unsigned s_active[kMaxBatch];
@@ -209,6 +210,7 @@ struct kf_batch_s {
   std::vector<kf_batch_item> items;
   int iterations = 0;
   int band_blocks_per_sm = 3;
+  int band_regs = 80;  // 80: variant for 3 CTAs per SM; 128: for 2
   int64_t tiles = 0;
   BatchEntry *tab = nullptr;        // device
   BatchEntry *tab_host = nullptr;   // pinned
@@ -217,6 +219,7 @@ struct kf_batch_s {
   IterStats *stats_host = nullptr;  // pinned
   cudaGraphExec_t exec = nullptr;
   int exec_blocks = 0;
+  int exec_regs = 0;
   cudaStream_t capture = nullptr;
 };
 
@@ -262,24 +265,34 @@ static int batch_upload_table(kf_batch b, cudaStream_t s) {
   return KF_OK;
 }
 
-static void batch_launch(kf_batch b, int iterations, int blocks_per_sm, cudaStream_t s) {
+// One band pass with `blocks_per_sm` CTAs per SM of the 80- or 128-register
+// variant.
+static void band_launch(kf_batch b, int regs, int blocks_per_sm, int it, cudaStream_t s) {
+  const unsigned blocks = (unsigned)(kf_num_sms() * blocks_per_sm);
+  const int n = (int)b->items.size();
+  if (regs > 80)
+    k_batch_band<2><<<blocks, kBandThreads, 0, s>>>(b->tab, n, it);
+  else
+    k_batch_band<3><<<blocks, kBandThreads, 0, s>>>(b->tab, n, it);
+}
+
+static void batch_launch(kf_batch b, int iterations, int regs, int blocks_per_sm, cudaStream_t s) {
   const int n = (int)b->items.size();
   const int64_t tiles = b->tiles;
   dim3 sgrid((unsigned)std::min<int64_t>(tiles, 65535), (unsigned)((tiles + 65534) / 65535));
   k_batch_stream<<<sgrid, dim3(kTX, kTY), 0, s>>>(b->tab, b->tile_pre, n);
-  const unsigned blocks = (unsigned)(kf_num_sms() * blocks_per_sm);
-  for (int it = 0; it < iterations; ++it) k_batch_band<<<blocks, kBandThreads, 0, s>>>(b->tab, n, it);
+  for (int it = 0; it < iterations; ++it) band_launch(b, regs, blocks_per_sm, it, s);
 }
 
-static int batch_capture(kf_batch b, int blocks_per_sm) {
-  if (b->exec && b->exec_blocks == blocks_per_sm) return KF_OK;
+static int batch_capture(kf_batch b, int regs, int blocks_per_sm) {
+  if (b->exec && b->exec_blocks == blocks_per_sm && b->exec_regs == regs) return KF_OK;
   if (b->exec) {
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
   }
   cudaGraph_t graph;
   KF_CHECK_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal));
-  batch_launch(b, b->iterations, blocks_per_sm, b->capture);
+  batch_launch(b, b->iterations, regs, blocks_per_sm, b->capture);
   cudaError_t le = cudaGetLastError();
   KF_CHECK_CUDA(cudaStreamEndCapture(b->capture, &graph));
   if (le != cudaSuccess) {
@@ -290,6 +303,7 @@ static int batch_capture(kf_batch b, int blocks_per_sm) {
   cudaGraphDestroy(graph);
   if (ie != cudaSuccess) return kf_cuda_fail(ie, "cudaGraphInstantiate");
   b->exec_blocks = blocks_per_sm;
+  b->exec_regs = regs;
   return KF_OK;
 }
 
@@ -355,22 +369,23 @@ extern "C" int kf_batch_destroy(kf_batch b) {
 // Launches the captured loop (band pass at blocks_per_sm) into the ping-pong
 // buffers and the statistics; which buffer holds each field's psi is settled
 // by the caller from the statistics.
-static int batch_execute(kf_batch b, int blocks_per_sm, cudaStream_t s) {
+static int batch_execute(kf_batch b, int regs, int blocks_per_sm, cudaStream_t s) {
   const int n = (int)b->items.size();
   int rc = batch_upload_table(b, s);
   if (rc) return rc;
   KF_CHECK_CUDA(cudaMemsetAsync(b->stats, 0, sizeof(IterStats) * (size_t)n * stats_stride(b), s));
-  rc = batch_capture(b, blocks_per_sm);
+  rc = batch_capture(b, regs, blocks_per_sm);
   if (rc) return rc;
   KF_CHECK_CUDA(cudaGraphLaunch(b->exec, s));
   return KF_OK;
 }
 
-// Times the band pass of the first iteration (the longest band list) at 1, 2
-// and 3 blocks per SM and keeps the fastest.  Each trial reruns the dense
-// first pass, which reads psi and writes only the second ping-pong buffer,
-// so the fields keep their psi.
-extern "C" int kf_batch_autotune(kf_batch b, int *blocks_per_sm, void *stream) {
+// Times the band pass of the first iteration (the longest band list) for
+// each launch shape -- the 80-register variant at 1, 2 and 3 CTAs per SM,
+// the 128-register variant at 1 and 2 -- and keeps the fastest.  Each trial
+// reruns the dense first pass, which reads psi and writes only the second
+// ping-pong buffer, so the fields keep their psi.
+extern "C" int kf_batch_autotune(kf_batch b, int *blocks_per_sm, int *registers, void *stream) {
   KF_REQUIRE(b, "NULL batch");
   cudaStream_t s = kf_stream(stream);
   const int n = (int)b->items.size();
@@ -381,16 +396,17 @@ extern "C" int kf_batch_autotune(kf_batch b, int *blocks_per_sm, void *stream) {
   KF_CHECK_CUDA(cudaEventCreate(&e1));
   const int64_t tiles = b->tiles;
   dim3 sgrid((unsigned)std::min<int64_t>(tiles, 65535), (unsigned)((tiles + 65534) / 65535));
+  const int shapes[5][2] = {{80, 1}, {80, 2}, {80, 3}, {128, 1}, {128, 2}};
   float best = 0.f;
-  int best_k = b->band_blocks_per_sm;
+  int best_s = -1;
   cudaError_t err = cudaSuccess;
-  for (int k = 1; k <= 3 && err == cudaSuccess; ++k) {
+  for (int sh = 0; sh < 5 && err == cudaSuccess; ++sh) {
     float kbest = 0.f;
     for (int rep = 0; rep < 3 && err == cudaSuccess; ++rep) {
       cudaMemsetAsync(b->stats, 0, sizeof(IterStats) * (size_t)n * stats_stride(b), s);
       k_batch_stream<<<sgrid, dim3(kTX, kTY), 0, s>>>(b->tab, b->tile_pre, n);
       cudaEventRecord(e0, s);
-      k_batch_band<<<(unsigned)(kf_num_sms() * k), kBandThreads, 0, s>>>(b->tab, n, 0);
+      band_launch(b, shapes[sh][0], shapes[sh][1], 0, s);
       cudaEventRecord(e1, s);
       err = cudaEventSynchronize(e1);
       if (err == cudaSuccess) err = cudaGetLastError();
@@ -398,16 +414,18 @@ extern "C" int kf_batch_autotune(kf_batch b, int *blocks_per_sm, void *stream) {
       cudaEventElapsedTime(&ms, e0, e1);
       if (rep == 1 || (rep > 1 && ms < kbest)) kbest = ms;  // rep 0 warms up
     }
-    if (err == cudaSuccess && (k == 1 || kbest < best)) {
+    if (err == cudaSuccess && (best_s < 0 || kbest < best)) {
       best = kbest;
-      best_k = k;
+      best_s = sh;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (err != cudaSuccess) return kf_cuda_fail(err, "kf_batch_autotune");
-  b->band_blocks_per_sm = best_k;
-  if (blocks_per_sm) *blocks_per_sm = best_k;
+  b->band_regs = shapes[best_s][0];
+  b->band_blocks_per_sm = shapes[best_s][1];
+  if (blocks_per_sm) *blocks_per_sm = b->band_blocks_per_sm;
+  if (registers) *registers = b->band_regs;
   return KF_OK;
 }
 
@@ -420,7 +438,7 @@ extern "C" int kf_batch_run(kf_batch b, kf_solve_stats *stats, void *stream) {
   KF_CHECK_CUDA(cudaEventCreate(&e0));
   KF_CHECK_CUDA(cudaEventCreate(&e1));
   cudaEventRecord(e0, s);
-  int rc = batch_execute(b, b->band_blocks_per_sm, s);
+  int rc = batch_execute(b, b->band_regs, b->band_blocks_per_sm, s);
   if (rc) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
