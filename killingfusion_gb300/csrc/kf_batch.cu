@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
   const int lane = threadIdx.x & 31;
   const int gl = lane & (kGroup - 1);
   const int group = threadIdx.x / kGroup;
-  const unsigned gmask = 0xffu << (lane & ~(kGroup - 1));
+  const unsigned gmask = group_mask(lane);
   int cur = -1;  // problem staged in s_a (the same in every thread)
   for (unsigned c = blockIdx.x; c < total; c += gridDim.x) {
     const int p = find_work(s_pre, nprob, c);

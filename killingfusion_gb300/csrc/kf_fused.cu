@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
   const int lane = threadIdx.x & 31;
   const int gl = lane & (kGroup - 1);
   const int group = threadIdx.x / kGroup;  // group within the block
-  const unsigned gmask = 0xffu << (lane & ~(kGroup - 1));
+  const unsigned gmask = group_mask(lane);
   const int nq = (int)a.st[a.iter].list;
   const int total_groups = gridDim.x * kGroupsPerBlock;
   const int rounds = (nq + total_groups - 1) / total_groups;

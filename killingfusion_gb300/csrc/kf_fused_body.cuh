@@ -23,8 +23,14 @@ constexpr int kZSlab = 8;
 constexpr int kTile = kThreads * kZSlab;
 constexpr int kBandWarps = 8;
 constexpr int kBandThreads = 32 * kBandWarps;
-constexpr int kGroup = 8;                       // lanes per band voxel
+constexpr int kGroup = 8;                       // lanes per band voxel (4, 8 or 16)
 constexpr int kGroupsPerBlock = kBandThreads / kGroup;
+constexpr int kNbPerLane = (20 + kGroup - 1) / kGroup;   // psi neighbours per lane
+constexpr int kSmpPerLane = (26 + kGroup - 1) / kGroup;  // warped samples per lane
+constexpr unsigned kGroupBits = kGroup == 32 ? 0xffffffffu : (1u << kGroup) - 1u;
+
+// The lanes of the group that lane `lane` belongs to.
+__device__ __forceinline__ unsigned group_mask(int lane) { return kGroupBits << (lane & ~(kGroup - 1)); }
 
 struct FusedArgs {
   const float *__restrict__ live;
@@ -101,9 +107,8 @@ enum { N000 = 0, NXP, NXM, NYP, NYM, NZP, NZM, NXPYP, NXPYM, NXMYP, NXMYM, NXPZP
        NXMZM, NYPZP, NYPZM, NYMZP, NYMZM, N111 };
 
 __device__ __forceinline__ float group_sum(float v, unsigned mask) {
-  v += __shfl_xor_sync(mask, v, 4, kGroup);
-  v += __shfl_xor_sync(mask, v, 2, kGroup);
-  v += __shfl_xor_sync(mask, v, 1, kGroup);
+#pragma unroll
+  for (int o = kGroup / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, kGroup);
   return v;
 }
 
@@ -116,11 +121,11 @@ __device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t 
   const int64_t sy = dp.nx, sz = (int64_t)dp.nx * dp.ny;
   const float h = a.h;
 
-  // psi neighbours gl, gl+8, gl+16 (those < 20); phi_can on lane 2
-  float q[3][3];
+  // psi neighbours gl, gl+kGroup, ... (those < 20); phi_can on lane 2
+  float q[kNbPerLane][3];
 #pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    const int n = gl + 8 * r;
+  for (int r = 0; r < kNbPerLane; ++r) {
+    const int n = gl + kGroup * r;
     if (n < 20) {
       const int64_t j = idx + __ldg(&kNb20[n][0]) + __ldg(&kNb20[n][1]) * sy + __ldg(&kNb20[n][2]) * sz;
       q[r][0] = __ldg(a.ix + j);
@@ -138,7 +143,7 @@ __device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t 
   for (int c = 0; c < 3; ++c) {
     float v[20];
 #pragma unroll
-    for (int n = 0; n < 20; ++n) v[n] = __shfl_sync(gmask, q[n >> 3][c], n & 7, kGroup);
+    for (int n = 0; n < 20; ++n) v[n] = __shfl_sync(gmask, q[n / kGroup][c], n % kGroup, kGroup);
     const float v000 = v[N000];
     c0[c] = v000;
     // Killing second differences (DisplacementField.cpp:326-331)
@@ -181,13 +186,13 @@ __device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t 
     for (int c = 0; c < 3; ++c) kg[c] = kg[c] * sc / den;
   }
 
-  // samples j = gl + 8r: j < 25 the cell-centre samples (SDF::getDistancef at
+  // samples j = gl + kGroup*r: j < 25 the cell-centre samples (SDF::getDistancef at
   // i+0.5+h*o, SDF.cpp:577-582: the half voxel it adds is removed again by
   // getDistance), j == 25 the warped value at i + psi(i)
-  float fs[4];
+  float fs[kSmpPerLane];
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int j = gl + 8 * r;
+  for (int r = 0; r < kSmpPerLane; ++r) {
+    const int j = gl + kGroup * r;
     float t0, t1, t2;
     if (j < 25) {
       const float o0 = (float)__ldg(&kOff25[j][0]), o1 = (float)__ldg(&kOff25[j][1]),
@@ -210,14 +215,14 @@ __device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t 
     fs[r] = j <= 25 ? phi_tri(a, t0, t1, t2) : 0.f;
   }
   const float f0 = __shfl_sync(gmask, fs[0], 0, kGroup);
-  const float s = __shfl_sync(gmask, fs[3], 1, kGroup);
+  const float s = __shfl_sync(gmask, fs[25 / kGroup], 25 % kGroup, kGroup);
   const float cv = __shfl_sync(gmask, canv, 2, kGroup);
   // derivative stencils on sample differences (the constant f0 cancels):
   // gradient +-1 on +-e_k, Hessian +1 on +-2e_k, o_j*o_k on the diagonals
   float gx = 0.f, gy = 0.f, gz = 0.f, hxx = 0.f, hyy = 0.f, hzz = 0.f, hxy = 0.f, hxz = 0.f, hyz = 0.f;
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int j = gl + 8 * r;
+  for (int r = 0; r < kSmpPerLane; ++r) {
+    const int j = gl + kGroup * r;
     if (j >= 25) continue;
     const int o0 = __ldg(&kOff25[j][0]), o1 = __ldg(&kOff25[j][1]), o2 = __ldg(&kOff25[j][2]);
     const float df = fs[r] - f0;
