@@ -11,10 +11,10 @@
 //     band keeps its psi, which therefore need not be written; the voxels
 //     inside are compacted into a list.  16 bytes per voxel.
 //   k_fused_band  evaluates the full gradient of every listed voxel with a
-//     group of 8 lanes per voxel (4 voxels per warp): the group loads the 20
+//     group of kGroup = 4 lanes per voxel (8 voxels per warp): the group loads the 20
 //     psi neighbours of the stencil and shares them by shuffles, takes the 25
 //     warped-SDF samples of the gradient and Hessian plus the warped value
-//     (3-4 independent trilinear gathers per lane), and reduces the nine
+//     (6-7 independent trilinear gathers per lane), and reduces the nine
 //     derivative sums of +-1-weighted sample differences.  The new psi goes
 //     to a side buffer indexed by list position, so every voxel still reads
 //     its neighbours' old values (Jacobi).
@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
   stream_flat<kPassThrough>(a, blockIdx.x, list, &a.st[a.iter].list);
 }
 
-// Band pass: a group of 8 lanes per listed voxel, launched as one resident
+// Band pass: a group of kGroup lanes per listed voxel, launched as one resident
 // wave that loops over the list.  kCarry (band-only solver): the voxels
 // updated here form the next iteration's list (list_out, counted in
 // st[iter+1].list).  kInPlace: the new psi of list entry k goes to entry k

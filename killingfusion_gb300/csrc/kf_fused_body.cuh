@@ -23,7 +23,11 @@ constexpr int kZSlab = 8;
 constexpr int kTile = kThreads * kZSlab;
 constexpr int kBandWarps = 8;
 constexpr int kBandThreads = 32 * kBandWarps;
-constexpr int kGroup = 8;                       // lanes per band voxel (4, 8 or 16)
+// Lanes per band voxel.  The group's shared work (20 psi neighbours, the
+// Killing stencil, the cell moments) is replicated on its lanes and the 26
+// warped samples are split among them: 4 lanes (7 samples each) measured
+// 1.32x the band voxels/s of 8 and 2x of 16 on band-heavy grids; 2 lanes spill.
+constexpr int kGroup = 4;
 constexpr int kGroupsPerBlock = kBandThreads / kGroup;
 constexpr int kNbPerLane = (20 + kGroup - 1) / kGroup;   // psi neighbours per lane
 constexpr int kSmpPerLane = (26 + kGroup - 1) / kGroup;  // warped samples per lane
@@ -112,7 +116,7 @@ __device__ __forceinline__ float group_sum(float v, unsigned mask) {
   return v;
 }
 
-// One interior voxel (1 <= x,y,z <= n-2) by a group of 8 lanes.  Every lane
+// One interior voxel (1 <= x,y,z <= n-2) by a group of kGroup lanes.  Every lane
 // of the group returns the step d = -alpha * g, the warped value s at
 // i + psi(i), and the monitored energy e.
 __device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t idx, int gl,
@@ -471,7 +475,7 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
   for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
 }
 
-// Update one band voxel i with the group of 8 lanes it is assigned to and
+// Update one band voxel i with the group of kGroup lanes it is assigned to and
 // write its new psi to entry `slot` of the output planes (slot == i for
 // ping-pong buffers; the voxel's list position for in-place updates).  The
 // voxel is re-tested with its warped value: one outside the band keeps its
