@@ -120,7 +120,6 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
   __shared__ unsigned s_maxd[kMaxBatch];
   __shared__ double s_energy[kMaxBatch];
   __shared__ int s_div[kMaxBatch];
-  __shared__ int s_next[kGroupsPerBlock];
   __shared__ FusedArgs s_a;
   __shared__ int *s_list_in, *s_list_out;
   const int par = it & 1;
@@ -179,19 +178,8 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
         if (diverged) s_div[p] = 1;
       }
     }
-    if (gl == 0) s_next[group] = next;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      // hand the chunk's updated voxels to the next iteration
-      int cnt = 0;
-      for (int w = 0; w < kGroupsPerBlock; ++w) cnt += s_next[w] >= 0;
-      if (cnt) {
-        unsigned b = atomicAdd(&s_a.st[it + 1].list, (unsigned)cnt);
-        for (int w = 0; w < kGroupsPerBlock; ++w)
-          if (s_next[w] >= 0) s_list_out[b++] = s_next[w];
-      }
-    }
-    __syncthreads();
+    // hand the chunk's updated voxels to the next iteration
+    block_append(next, gl == 0, &s_a.st[it + 1].list, s_list_out);
   }
   for (int q = threadIdx.x; q < nprob; q += blockDim.x) {
     IterStats *st = tab[q].a[par].st + it;

@@ -71,7 +71,6 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
   const int nq = (int)a.st[a.iter].list;
   const int total_groups = gridDim.x * kGroupsPerBlock;
   const int rounds = (nq + total_groups - 1) / total_groups;
-  __shared__ int s_next[kGroupsPerBlock];
   float maxd = 0.f;
   float energy = 0.f;  // this thread's voxels; the block and grid sums are float64
   unsigned active = 0;
@@ -83,20 +82,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
       const int v = list_in[k];
       next = update_band_voxel(a, v, kInPlace ? k : v, gl, gmask, maxd, energy, active, diverged);
     }
-    if (kCarry) {
-      if (gl == 0) s_next[group] = next;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        int cnt = 0;
-        for (int w = 0; w < kGroupsPerBlock; ++w) cnt += s_next[w] >= 0;
-        if (cnt) {
-          int b = (int)atomicAdd(&a.st[a.iter + 1].list, (unsigned)cnt);
-          for (int w = 0; w < kGroupsPerBlock; ++w)
-            if (s_next[w] >= 0) list_out[b++] = s_next[w];
-        }
-      }
-      __syncthreads();
-    }
+    if (kCarry) block_append(next, gl == 0, &a.st[a.iter + 1].list, list_out);
   }
   reduce_iter_stats<kBandThreads>(a.st + a.iter, active, maxd, (double)energy, diverged);
 }

@@ -475,6 +475,29 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
   for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
 }
 
+// Appends the voxels `next` (>= 0 on the group leaders that carry one) of the
+// whole block to list_out with one atomic on *count, in group order; every
+// thread of the block calls it.
+__device__ __forceinline__ void block_append(int next, bool leader, unsigned *count, int *__restrict__ list_out) {
+  __shared__ unsigned s_wcnt[kBandWarps], s_wbase[kBandWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool has = leader && next >= 0;
+  const unsigned ball = __ballot_sync(0xffffffffu, has);
+  if (lane == 0) s_wcnt[warp] = (unsigned)__popc(ball);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = 0;
+    for (int w = 0; w < kBandWarps; ++w) {
+      s_wbase[w] = t;
+      t += s_wcnt[w];
+    }
+    const unsigned b = t ? atomicAdd(count, t) : 0u;
+    for (int w = 0; w < kBandWarps; ++w) s_wbase[w] += b;
+  }
+  __syncthreads();
+  if (has) list_out[s_wbase[warp] + (unsigned)__popc(ball & ((1u << lane) - 1u))] = next;
+}
+
 // Update one band voxel i with the group of kGroup lanes it is assigned to and
 // write its new psi to entry `slot` of the output planes (slot == i for
 // ping-pong buffers; the voxel's list position for in-place updates).  The
