@@ -534,6 +534,15 @@ def main():
     run_main(args, rank, world, local)
 
 
+def max_over_ranks(values, device="cuda"):
+    """Element-wise maximum of per-rank times over all ranks (the slowest
+    replica sets the whole job's time)."""
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def run_main(args, rank, world, local):
     import numpy as np
 
@@ -576,9 +585,7 @@ def run_main(args, rank, world, local):
     el = res["elapsed_ms"]
     e2e_ms = res["e2e_ms"]
     if world > 1:
-        t = torch.tensor([el, e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el, e2e_ms = float(t[0]), float(t[1])
+        el, e2e_ms = max_over_ranks([el, e2e_ms], "cuda")
     if rank != 0:
         return
     N3 = res["N3"]

@@ -58,11 +58,19 @@ typedef enum kf_solver {
   KF_SOLVER_FUSED = 0, /* one stencil pass per iteration, CUDA-graph loop  */
   KF_SOLVER_PLAIN = 1, /* one kernel per energy term, fields through HBM   */
   KF_SOLVER_EXACT = 2, /* float64 replay of the reference (needs KF_F64 psi) */
-  KF_SOLVER_BAND = 3   /* the fused stencil on the band only: a voxel outside
+  KF_SOLVER_BAND = 3,  /* the fused stencil on the band only: a voxel outside
                           the band keeps psi, so its band test keeps failing
                           and the band can only shrink; after the first dense
                           pass each iteration visits the previous iteration's
                           band.  Same psi as KF_SOLVER_FUSED.               */
+  KF_SOLVER_PERVOXEL = 4 /* the reference's default schedule
+                          (KillingFusion.cpp:353-396): every voxel inside the
+                          symmetric band steps psi in place until its step or
+                          gradient is at most params.threshold or `iterations`
+                          steps were taken.  All voxels run at once, reading
+                          their neighbours' current psi (asynchronous
+                          relaxation; the reference's OpenMP threads race the
+                          same way), so psi is not reproducible bit for bit. */
 } kf_solver;
 
 /* The reference's config.h globals that the hot path reads. */
@@ -185,7 +193,11 @@ int kf_integrate_depth(kf_grid g, const float *depth, int width, int height,
 /* KillingFusion::computeDisplacementField, Jacobi schedule
  * (KillingFusion.cpp:240-352): `iterations` gradient-descent steps of psi
  * registering `live` onto `canonical`.  Returns KF_ERR_DIVERGED when psi
- * turned non-finite inside the band.  stats may be NULL. */
+ * turned non-finite inside the band.  stats may be NULL.  With
+ * KF_SOLVER_PERVOXEL `iterations` caps each voxel's steps and the statistics
+ * read: iterations_run = most steps a voxel took, converged = no voxel hit
+ * the cap, active_first = active_last = voxels visited, energy_last = their
+ * monitored energy at their last step, max_delta_last = largest last step. */
 int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
                  int iterations, kf_solver solver, kf_solve_stats *stats, void *stream);
 
@@ -299,7 +311,7 @@ typedef struct kf_fusion_config {
   double max_depth;
   kf_params params;     /* solver parameters                                 */
   int iterations;       /* psi iterations per frame (KILLING_MAX_ITERATIONS) */
-  kf_solver solver;     /* KF_SOLVER_FUSED, _BAND, _PLAIN or _EXACT          */
+  kf_solver solver;     /* KF_SOLVER_FUSED, _BAND, _PLAIN, _EXACT, _PERVOXEL */
 } kf_fusion_config;
 
 typedef struct kf_frame_result {

@@ -106,6 +106,7 @@ DevParams kf_make_dev_params(const int n[3], const kf_params *p) {
   d.band_hi = p->max_surface - p->epsilon;
   d.band_hi_f = float_down(d.band_hi);
   d.band_lo_f = float_up(-p->unknown_clip);
+  d.pv_lo_f = float_up(-p->max_surface + p->epsilon);
   d.mc_hi_f = float_down(p->max_surface);
   d.oob_phi_f = (float)d.oob_phi;
   d.use_data = p->use_data;
@@ -598,7 +599,7 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
   int rc = kf_check_params(p);
   if (rc) return rc;
   KF_REQUIRE(solver == KF_SOLVER_FUSED || solver == KF_SOLVER_PLAIN || solver == KF_SOLVER_EXACT ||
-                 solver == KF_SOLVER_BAND,
+                 solver == KF_SOLVER_BAND || solver == KF_SOLVER_PERVOXEL,
              "unknown solver");
   KF_REQUIRE((solver == KF_SOLVER_EXACT) == (psi->prec == KF_F64),
              "KF_SOLVER_EXACT runs on KF_F64 fields and the other solvers on KF_F32 fields");
@@ -615,7 +616,9 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
   KF_CHECK_CUDA(cudaEventCreate(&e0));
   KF_CHECK_CUDA(cudaEventCreate(&e1));
   KF_CHECK_CUDA(cudaEventRecord(e0, s));
-  if (solver == KF_SOLVER_FUSED || solver == KF_SOLVER_BAND)
+  if (solver == KF_SOLVER_PERVOXEL)
+    rc = kf_solve_pervoxel(live, canonical, psi, dp, iterations, st, s);
+  else if (solver == KF_SOLVER_FUSED || solver == KF_SOLVER_BAND)
     rc = kf_solve_fused(live, canonical, psi, dp, iterations, st, solver == KF_SOLVER_BAND, s);
   else if (solver == KF_SOLVER_PLAIN)
     rc = kf_solve_plain(live, canonical, psi, dp, iterations, st, s);
@@ -628,12 +631,33 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
   }
   KF_CHECK_CUDA(cudaEventRecord(e1, s));
   IterStats *host = psi->stats_host;
-  KF_CHECK_CUDA(cudaMemcpyAsync(host, st, sizeof(IterStats) * iterations, cudaMemcpyDeviceToHost, s));
+  KF_CHECK_CUDA(cudaMemcpyAsync(host, st, sizeof(IterStats) * (iterations + 1), cudaMemcpyDeviceToHost, s));
   KF_CHECK_CUDA(cudaStreamSynchronize(s));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (solver == KF_SOLVER_PERVOXEL) {
+    // record 0: voxels visited (list), their last monitored energy and
+    // step, divergence; record 1: voxels that hit the cap (active), most
+    // steps of a voxel (list)
+    const int diverged = host[0].diverged;
+    if (stats) {
+      float md;
+      unsigned bits = host[0].max_delta;
+      memcpy(&md, &bits, sizeof(md));
+      stats->iterations_run = (int32_t)host[1].list;
+      stats->converged = (!diverged && host[1].active == 0) ? 1 : 0;
+      stats->diverged = diverged;
+      stats->active_first = stats->active_last = host[0].list;
+      stats->energy_last = host[0].energy;
+      stats->max_delta_last = md;
+      stats->device_ms = ms;
+    }
+    if (diverged)
+      return kf_fail(KF_ERR_DIVERGED, "deformation field diverged (non-finite psi inside the band)");
+    return KF_OK;
+  }
   int executed = 0;
   int diverged = 0;
   for (int k = 0; k < iterations; ++k) {

@@ -102,6 +102,88 @@ __global__ void __launch_bounds__(kThreads) k_fused_scatter(FusedArgs a, const i
   }
 }
 
+// KillingFusion::computeDisplacementField, default per-voxel schedule
+// (KillingFusion.cpp:353-396) as asynchronous relaxation: every listed voxel
+// (inside the symmetric band) is taken by one group, which steps its psi in
+// place -- a.ix and a.ox are the same planes -- until the step or the
+// gradient is at most the threshold or max_iters steps were taken.  The
+// neighbours it reads are whatever the other groups have written so far (the
+// reference's OpenMP threads race the same way).  Statistics: record 0
+// voxels (list, from the band pass), last step, last monitored energy,
+// divergence; record 1 voxels that hit the cap (active) and the most steps
+// of one voxel (list).
+__global__ void __launch_bounds__(kBandThreads, 3) k_pervoxel(FusedArgs a, const int *__restrict__ list,
+                                                            int max_iters) {
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & (kGroup - 1);
+  const int group = threadIdx.x / kGroup;
+  const unsigned gmask = group_mask(lane);
+  const DevParams &dp = a.dp;
+  const int nq = (int)a.st[0].list;
+  const float thr = (float)dp.threshold;
+  float maxd = 0.f, energy = 0.f;
+  unsigned capped = 0, most = 0;
+  bool diverged = false;
+  for (int k = blockIdx.x * kGroupsPerBlock + group; k < nq; k += gridDim.x * kGroupsPerBlock) {
+    const int i = list[k];
+    int x, y, z;
+    voxel_xyz(dp, i, x, y, z);
+    const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 && z <= dp.nz - 2;
+    int iter = 0;
+    unsigned steps = 0;
+    float dn = 0.f, en = 0.f;
+    bool div = false;
+    while (true) {
+      float d[3] = {0.f, 0.f, 0.f}, sv = 0.f, e = 0.f, c0[3] = {0.f, 0.f, 0.f};
+      if (interior) {
+        gradient_group<true>(a, x, y, z, i, gl, gmask, d, sv, e, c0);
+      } else {
+        if (gl == 0) {
+          gradient_generic(a, x, y, z, d, sv, e);
+          c0[0] = __ldcg(a.ix + i);
+          c0[1] = __ldcg(a.iy + i);
+          c0[2] = __ldcg(a.iz + i);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          d[c] = __shfl_sync(gmask, d[c], 0, kGroup);
+          c0[c] = __shfl_sync(gmask, c0[c], 0, kGroup);
+        }
+        e = __shfl_sync(gmask, e, 0, kGroup);
+      }
+      const float n0 = c0[0] + d[0], n1 = c0[1] + d[1], n2 = c0[2] + d[2];
+      if (gl == 0) {  // DisplacementField::update (DisplacementField.cpp:65-71)
+        a.ox[i] = n0;
+        a.oy[i] = n1;
+        a.oz[i] = n2;
+      }
+      __syncwarp(gmask);
+      ++steps;
+      dn = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      en = e;
+      if (dn <= thr) break;
+      if (!isfinite(n0) || !isfinite(n1) || !isfinite(n2)) {
+        div = true;
+        break;
+      }
+      ++iter;
+      // |gradient| = |step| / alpha
+      if (!(dn / a.alpha > thr) || iter >= max_iters) break;
+    }
+    if (gl == 0) {
+      maxd = fmaxf(maxd, dn);
+      energy += en;
+      capped += iter >= max_iters;
+      most = max(most, steps);
+      diverged |= div;
+    }
+  }
+  // voxels processed are counted by the band pass (record 0's list)
+  reduce_iter_stats<kBandThreads>(a.st, 0u, maxd, (double)energy, diverged);
+  if (gl == 0 && capped) atomicAdd(&a.st[1].active, capped);
+  if (gl == 0 && most) atomicMax(&a.st[1].list, most);
+}
+
 }  // namespace
 
 // A captured iteration loop, valid for one set of buffers and parameters.
@@ -189,3 +271,29 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
   KF_CHECK_CUDA(cudaGraphLaunch(g->exec, s));
   return KF_OK;
 }
+
+int kf_solve_pervoxel(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp, int max_iters,
+                      IterStats *st, cudaStream_t s) {
+  int rc = kf_field_band_list(psi, &psi->band);
+  if (rc) return rc;
+  // the symmetric band of KillingFusion.cpp:369 and psi read and written in
+  // place
+  DevParams pd = dp;
+  pd.early_exit = 0;
+  FusedArgs a = make_args(live, can, pd, st);
+  a.band_lo = dp.pv_lo_f;
+  a.ix = (const float *)psi->p[0];
+  a.iy = (const float *)psi->p[1];
+  a.iz = (const float *)psi->p[2];
+  a.ox = (float *)psi->p[0];
+  a.oy = (float *)psi->p[1];
+  a.oz = (float *)psi->p[2];
+  a.iter = 0;
+  const unsigned grid = (unsigned)std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) /
+                                                        (kThreads * kFlatGroups), 1);
+  k_fused_stream<false><<<grid, kThreads, 0, s>>>(a, psi->band);
+  k_pervoxel<<<(unsigned)kf_num_sms() * 3, kBandThreads, 0, s>>>(a, psi->band, max_iters);
+  KF_CHECK_LAUNCH("per-voxel solve");
+  return KF_OK;
+}
+

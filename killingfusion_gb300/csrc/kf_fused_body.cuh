@@ -119,6 +119,7 @@ __device__ __forceinline__ float group_sum(float v, unsigned mask) {
 // One interior voxel (1 <= x,y,z <= n-2) by a group of kGroup lanes.  Every lane
 // of the group returns the step d = -alpha * g, the warped value s at
 // i + psi(i), and the monitored energy e.
+template <bool kCoherent = false>
 __device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t idx, int gl,
                                unsigned gmask, float d[3], float &s_out, float &e_out, float c0[3]) {
   const DevParams &dp = a.dp;
@@ -132,9 +133,11 @@ __device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t 
     const int n = gl + kGroup * r;
     if (n < 20) {
       const int64_t j = idx + __ldg(&kNb20[n][0]) + __ldg(&kNb20[n][1]) * sy + __ldg(&kNb20[n][2]) * sz;
-      q[r][0] = __ldg(a.ix + j);
-      q[r][1] = __ldg(a.iy + j);
-      q[r][2] = __ldg(a.iz + j);
+      // psi updated in place by other groups (per-voxel schedule): read it
+      // through L2, never from a stale L1 or read-only line
+      q[r][0] = kCoherent ? __ldcg(a.ix + j) : __ldg(a.ix + j);
+      q[r][1] = kCoherent ? __ldcg(a.iy + j) : __ldg(a.iy + j);
+      q[r][2] = kCoherent ? __ldcg(a.iz + j) : __ldg(a.iz + j);
     } else {
       q[r][0] = q[r][1] = q[r][2] = 0.f;
     }

@@ -87,6 +87,8 @@ struct DevParams {
   float band_lo_f;       // smallest float >= -unknown_clip (s < lo <=> s < band_lo_f)
   float mc_hi_f;         // largest float <= max_surface
   float oob_phi_f;       // (float)(max_surface + epsilon)
+  float pv_lo_f;         // smallest float >= -(max_surface - epsilon), the lower
+                         // band edge of the per-voxel schedule
   int use_data, use_levelset, use_killing;
   int early_exit;
   double threshold;
@@ -113,6 +115,10 @@ int kf_solve_plain(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
                    int iterations, IterStats *stats_dev, cudaStream_t s);
 int kf_solve_exact(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
                    int iterations, IterStats *stats_dev, cudaStream_t s);
+// Per-voxel schedule (KF_SOLVER_PERVOXEL); stats_dev[0] and [1] as
+// documented at kf_psi_solve.
+int kf_solve_pervoxel(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
+                      int max_iters, IterStats *stats_dev, cudaStream_t s);
 int kf_gradient_ref_launch(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
                            const int32_t *voxels, int count, double *out, uint8_t *active,
                            cudaStream_t s);

@@ -463,6 +463,49 @@ int orc_solve_jacobi(const double *live, const double *can, double *psi,
   return 0;
 }
 
+/* KillingFusion::computeDisplacementField, default per-voxel schedule
+ * (KillingFusion.cpp:353-396) on one thread, cells in z, y, x order: a voxel
+ * whose warped value lies inside the symmetric band +-(MaxSurface - epsilon)
+ * (:369) steps psi in place, -alpha * gradient at a time, until the step or
+ * the gradient is at most threshold or max_iters steps were taken (:374-394).
+ * Returns 0, or -1 when psi turned non-finite (the reference throws -1).
+ * counts (may be NULL): voxels visited, steps taken, voxels that hit
+ * max_iters. */
+int orc_solve_pervoxel(const double *live, const double *can, double *psi,
+                       const int n[3], const orc_params *P, int max_iters,
+                       int64_t counts[3]) {
+  int64_t visited = 0, steps = 0, capped = 0;
+  for (int z = 0; z < n[2]; ++z)
+    for (int y = 0; y < n[1]; ++y)
+      for (int x = 0; x < n[0]; ++x) {
+        double s = orc_warped_distance(live, psi, n, P, x, y, z);
+        if (s > P->max_surface - P->epsilon || s < -P->max_surface + P->epsilon)
+          continue;
+        ++visited;
+        const int64_t i = lin(n, x, y, z);
+        double g[3];
+        int iter = 0;
+        do {
+          orc_energy_gradient(live, can, psi, n, P, x, y, z, g);
+          double d[3];
+          for (int k = 0; k < 3; ++k) d[k] = -P->alpha * g[k];
+          for (int k = 0; k < 3; ++k) psi[3 * i + k] = psi[3 * i + k] + d[k];
+          ++steps;
+          if (norm3(d) <= P->threshold) break;
+          if (!isfinite(psi[3 * i]) || !isfinite(psi[3 * i + 1]) || !isfinite(psi[3 * i + 2]))
+            return -1;
+          iter += 1;
+        } while (norm3(g) > P->threshold && iter < max_iters);
+        if (iter >= max_iters) ++capped;
+      }
+  if (counts) {
+    counts[0] = visited;
+    counts[1] = steps;
+    counts[2] = capped;
+  }
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* TSDF integration (SDF.cpp:137-197)                                       */
 /* ------------------------------------------------------------------------ */

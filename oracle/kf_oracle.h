@@ -102,6 +102,9 @@ int orc_is_active(const double *live, const double *psi, const int n[3],
  * reference's `throw -1`).  active_counts (may be NULL) receives the number of
  * voxels inside the band for each iteration.  nthreads<=0 uses OpenMP's
  * default. */
+int orc_solve_pervoxel(const double *live, const double *can, double *psi,
+                       const int n[3], const orc_params *P, int max_iters,
+                       int64_t counts[3]);
 int orc_solve_jacobi(const double *live, const double *can, double *psi,
                      const int n[3], const orc_params *P, int iters,
                      int nthreads, int64_t *active_counts);
