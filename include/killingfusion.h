@@ -100,7 +100,7 @@ typedef struct kf_solve_stats {
   int32_t iterations_run; /* iterations executed                           */
   int32_t converged;      /* 1 if max |dpsi| fell to params.threshold      */
   int32_t diverged;       /* 1 if psi turned non-finite inside the band    */
-  int32_t reserved;
+  int32_t capped;         /* KF_SOLVER_PERVOXEL: voxels that hit the cap   */
   int64_t active_first;   /* voxels inside the band, first iteration       */
   int64_t active_last;    /* ... last executed iteration                   */
   double energy_first;    /* monitored energy (FP64 reduction)             */

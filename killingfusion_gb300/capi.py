@@ -46,12 +46,12 @@ class _Params(C.Structure):
 
 class SolveStats(C.Structure):
     _fields_ = [("iterations_run", C.c_int32), ("converged", C.c_int32), ("diverged", C.c_int32),
-                ("reserved", C.c_int32), ("active_first", C.c_int64), ("active_last", C.c_int64),
+                ("capped", C.c_int32), ("active_first", C.c_int64), ("active_last", C.c_int64),
                 ("energy_first", C.c_double), ("energy_last", C.c_double),
                 ("max_delta_last", C.c_double), ("device_ms", C.c_double)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 @dataclass(frozen=True)

@@ -648,6 +648,7 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
       memcpy(&md, &bits, sizeof(md));
       stats->iterations_run = (int32_t)host[1].list;
       stats->converged = (!diverged && host[1].active == 0) ? 1 : 0;
+      stats->capped = (int32_t)host[1].active;
       stats->diverged = diverged;
       stats->active_first = stats->active_last = host[0].list;
       stats->energy_last = host[0].energy;
