@@ -189,6 +189,14 @@ int kf_grid_get_voxels(kf_grid g, const kf_params *p, const int32_t *xyz, int n,
 int kf_integrate_depth(kf_grid g, const float *depth, int width, int height,
                        const double c2w[16], const double K[9], double min_depth,
                        double max_depth, void *stream);
+/* The same with 16-bit depth (the reference's PNG frames, millimetres for
+ * the Kinect datasets): each value becomes (double)v * scale, as
+ * cv::Mat::convertTo(CV_64FC1, 1.0 / 1000) produces it in the reference
+ * (DatasetReader.cpp:131-132), so integration matches the reference's
+ * double depth exactly.  Masked-out pixels are 0 (below any minimum depth). */
+int kf_integrate_depth_u16(kf_grid g, const uint16_t *depth, int width, int height, double scale,
+                           const double c2w[16], const double K[9], double min_depth,
+                           double max_depth, void *stream);
 
 /* KillingFusion::computeDisplacementField, Jacobi schedule
  * (KillingFusion.cpp:240-352): `iterations` gradient-descent steps of psi

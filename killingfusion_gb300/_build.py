@@ -41,7 +41,7 @@ CUDA_UNITS = [
     ("kf_batch.cu", []),
     ("kf_fusion.cu", []),
 ]
-HOST_UNITS = ["SDF.cpp", "DisplacementField.cpp", "DatasetReader.cpp", "KillingFusion.cpp"]
+HOST_UNITS = ["SDF.cpp", "DisplacementField.cpp", "DatasetReader.cpp", "KillingFusion.cpp", "png.cpp"]
 
 
 def nvcc() -> str:

@@ -122,6 +122,8 @@ SIGNATURES = {
     "kf_field_device": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
     "kf_integrate_depth": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _dp, _dp, C.c_double,
                                      C.c_double, _vp]),
+    "kf_integrate_depth_u16": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_double,
+                                         C.c_double, _vp]),
     "kf_psi_solve": (C.c_int, [_vp, _vp, _vp, _PP, C.c_int, C.c_int, C.POINTER(SolveStats), _vp]),
     "kf_psi_gradient_ref": (C.c_int, [_vp, _vp, _vp, _PP, _vp, C.c_int, _vp, _vp, _vp]),
     "kf_energy": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _ip6, C.c_int, _dp, _vp]),
@@ -249,6 +251,20 @@ class Grid:
             ptr, (hh, ww) = depth.data_ptr(), tuple(depth.shape)
         check(load().kf_integrate_depth(self.h, ptr, ww, hh, _d(c2w.ravel()), _d(K.ravel()),
                                         min_depth, max_depth, _stream(stream)))
+
+    def integrate_u16(self, depth, scale=0.001, c2w=None, K=None, min_depth=0.05, max_depth=1.2, stream=None):
+        """SDF::integrateDepthFrame on 16-bit depth (numpy uint16 [h, w] or a
+        CUDA tensor); each value is (double)v * scale."""
+        from . import synth
+        c2w = np.eye(4) if c2w is None else np.asarray(c2w, dtype=np.float64)
+        K = synth.K if K is None else np.asarray(K, dtype=np.float64)
+        if isinstance(depth, np.ndarray):
+            d = np.ascontiguousarray(depth, dtype=np.uint16)
+            ptr, (hh, ww) = d.ctypes.data, d.shape
+        else:
+            ptr, (hh, ww) = depth.data_ptr(), tuple(depth.shape)
+        check(load().kf_integrate_depth_u16(self.h, ptr, ww, hh, float(scale), _d(c2w.ravel()),
+                                            _d(K.ravel()), min_depth, max_depth, _stream(stream)))
 
 
 class Field:

@@ -105,9 +105,14 @@ std::vector<SDF> SDF::getDataEnergyTestSample(double voxelSize, double unknownCl
 
 void SDF::integrateDepthFrame(const kf::DepthImage &depth, const kf::Mat4d &c2w, const Mat3d &K,
                               double minDepth, double maxDepth) {
-  kf::check(kf_integrate_depth(m_grid, depth.ptr(), depth.cols, depth.rows, c2w.data(), K.data(),
-                               minDepth, maxDepth, nullptr),
-            "kf_integrate_depth");
+  if (depth.is_raw())
+    kf::check(kf_integrate_depth_u16(m_grid, depth.raw.data(), depth.cols, depth.rows, depth.scale, c2w.data(),
+                                     K.data(), minDepth, maxDepth, nullptr),
+              "kf_integrate_depth_u16");
+  else
+    kf::check(kf_integrate_depth(m_grid, depth.ptr(), depth.cols, depth.rows, c2w.data(), K.data(), minDepth,
+                                 maxDepth, nullptr),
+              "kf_integrate_depth");
 }
 
 bool SDF::indexInGridBounds(int x, int y, int z) const {

@@ -12,12 +12,17 @@
 #include "kf_types.h"
 
 namespace kf {
-// A depth image in metres (row-major float32), standing in for the cv::Mat
-// the reference integrates (SDF.cpp:137-177).
+// A depth image, standing in for the cv::Mat the reference integrates
+// (SDF.cpp:137-177): float32 metres in `data`, or -- as the reference's PNG
+// frames arrive -- 16-bit values in `raw` that are (double)v * scale metres
+// (DatasetReader.cpp:131-132).  Row-major.
 struct DepthImage {
   int rows = 0, cols = 0;
   std::vector<float> data;
+  std::vector<uint16_t> raw;
+  double scale = 0.0;
   const float *ptr() const { return data.data(); }
+  bool is_raw() const { return !raw.empty(); }
 };
 }  // namespace kf
 

@@ -81,8 +81,15 @@ struct Config {
   double omegaLevelSet = 0.1;
   double epsilon = 0.00001;
   // solver of computeDisplacementField (the reference's Jacobi schedule in
-  // one of its GPU forms)
+  // one of its GPU forms, or its per-voxel schedule)
   kf_solver solver = KF_SOLVER_FUSED;
+  // the dataset of the reference's directory layout (config.cpp:10-19):
+  // 0 Duck, 1 Snoopy
+  int datasetType = 1;
+  const char *imageDir[2] = {"Duck/", "Snoopy/"};
+  int numImageFiles[2] = {447, 630};
+  const char *intrinsicParamsFile = "intrinsics_kinect1.txt";
+  double datasetDepthMinMaxValues[2][2] = {{0.0497470, 1.2}, {0.0495164, 1.2}};
 
   kf_params params() const {
     kf_params p;

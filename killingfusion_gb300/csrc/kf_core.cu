@@ -469,20 +469,14 @@ static bool invert4(const double m[16], double out[16]) {
   return true;
 }
 
-extern "C" int kf_integrate_depth(kf_grid g, const float *depth, int width, int height,
-                                  const double c2w[16], const double K[9], double min_depth,
-                                  double max_depth, void *stream) {
-  KF_REQUIRE(g && depth && c2w && K, "NULL argument");
-  KF_REQUIRE(width > 0 && height > 0, "depth frame size must be positive");
-  cudaStream_t s = kf_stream(stream);
-  double w2c[16];
-  KF_REQUIRE(invert4(c2w, w2c), "camera pose is singular");
+// The depth frame on the device: itself when it is device (or managed)
+// memory, else copied into the grid's staging buffer.
+static int stage_depth(kf_grid g, const void *depth, size_t bytes, cudaStream_t s, const void **dev) {
   cudaPointerAttributes attr;
-  const float *dev = depth;
+  *dev = depth;
   if (cudaPointerGetAttributes(&attr, depth) != cudaSuccess || attr.type == cudaMemoryTypeUnregistered ||
       attr.type == cudaMemoryTypeHost) {
     cudaGetLastError();
-    size_t bytes = (size_t)width * height * sizeof(float);
     if (g->depth_cap < bytes) {
       cudaFree(g->depth);
       g->depth = nullptr;
@@ -494,9 +488,39 @@ extern "C" int kf_integrate_depth(kf_grid g, const float *depth, int width, int 
       g->depth_cap = bytes;
     }
     KF_CHECK_CUDA(cudaMemcpyAsync(g->depth, depth, bytes, cudaMemcpyHostToDevice, s));
-    dev = g->depth;
+    *dev = g->depth;
   }
-  return kf_launch_integrate(g, dev, width, height, w2c, K, min_depth, max_depth, s);
+  return KF_OK;
+}
+
+extern "C" int kf_integrate_depth(kf_grid g, const float *depth, int width, int height,
+                                  const double c2w[16], const double K[9], double min_depth,
+                                  double max_depth, void *stream) {
+  KF_REQUIRE(g && depth && c2w && K, "NULL argument");
+  KF_REQUIRE(width > 0 && height > 0, "depth frame size must be positive");
+  cudaStream_t s = kf_stream(stream);
+  double w2c[16];
+  KF_REQUIRE(invert4(c2w, w2c), "camera pose is singular");
+  const void *dev = nullptr;
+  int rc = stage_depth(g, depth, (size_t)width * height * sizeof(float), s, &dev);
+  if (rc) return rc;
+  return kf_launch_integrate(g, (const float *)dev, width, height, w2c, K, min_depth, max_depth, s);
+}
+
+extern "C" int kf_integrate_depth_u16(kf_grid g, const uint16_t *depth, int width, int height, double scale,
+                                      const double c2w[16], const double K[9], double min_depth,
+                                      double max_depth, void *stream) {
+  KF_REQUIRE(g && depth && c2w && K, "NULL argument");
+  KF_REQUIRE(width > 0 && height > 0, "depth frame size must be positive");
+  KF_REQUIRE(scale > 0.0, "depth scale must be positive");
+  cudaStream_t s = kf_stream(stream);
+  double w2c[16];
+  KF_REQUIRE(invert4(c2w, w2c), "camera pose is singular");
+  const void *dev = nullptr;
+  int rc = stage_depth(g, depth, (size_t)width * height * sizeof(uint16_t), s, &dev);
+  if (rc) return rc;
+  return kf_launch_integrate_u16(g, (const uint16_t *)dev, scale, width, height, w2c, K, min_depth, max_depth,
+                                 s);
 }
 
 extern "C" int kf_warp(kf_grid g, kf_field psi, const kf_params *p, void *stream) {

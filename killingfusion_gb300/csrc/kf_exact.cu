@@ -58,6 +58,7 @@ struct IntegrateArgs {
   float vf, min0f, min1f, min2f;
   double voxel, min0, min1, min2, unknown_clip, min_depth, max_depth;
   float min_depth_up, max_depth_down;  // float neighbours of the depth range
+  double depth_scale;                  // metres per unit of 16-bit depth
   int width, height;
 };
 
@@ -92,8 +93,8 @@ __device__ __forceinline__ int pixel_of(double u) {
 // (phi*0 + dist)/1 is dist itself, so the float64 multiply and divide are
 // skipped.
 __device__ __forceinline__ void integrate_update(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
-                                                 float df, double zc, const IntegrateArgs &a) {
-  const double dist = (double)df - zc;
+                                                 double depth, double zc, const IntegrateArgs &a) {
+  const double dist = depth - zc;
   if (dist < -a.unknown_clip) return;
   const int32_t wi = w[i];
   const float ph = phi[i];
@@ -105,16 +106,35 @@ __device__ __forceinline__ void integrate_update(float *__restrict__ phi, int32_
   w[i] = wi + 1;
 }
 
+// The depth at pixel k as the reference reads it (a double) and its range
+// test `depth < minDepth || depth > maxDepth` (SDF.cpp:176-179; a NaN passes,
+// as there).  Float metres: compared through the float neighbours of the
+// bounds.  16-bit units: (double)v * scale, as cv::Mat::convertTo with a
+// scale produces them (DatasetReader.cpp:131-132).
+__device__ __forceinline__ bool depth_at(const float *__restrict__ depth, int64_t k, const IntegrateArgs &a,
+                                         double &d) {
+  const float df = depth[k];
+  d = (double)df;
+  return !(df < a.min_depth_up || df > a.max_depth_down);
+}
+
+__device__ __forceinline__ bool depth_at(const uint16_t *__restrict__ depth, int64_t k, const IntegrateArgs &a,
+                                         double &d) {
+  d = (double)depth[k] * a.depth_scale;
+  return !(d < a.min_depth || d > a.max_depth);
+}
+
 // The whole float64 path of one voxel (SDF.cpp:151-193).
+template <typename D>
 __device__ void integrate_exact_voxel(float *__restrict__ phi, int32_t *__restrict__ w, int x, int y, int z,
-                                      int64_t i, const float *__restrict__ depth, const IntegrateArgs &a) {
+                                      int64_t i, const D *__restrict__ depth, const IntegrateArgs &a) {
   double u, v, zc;
   project_exact(a, x, y, z, u, v, zc);
   const int col = pixel_of(u), row = pixel_of(v);
   if (col < 0 || col >= a.width || row < 0 || row >= a.height) return;
-  const float df = depth[(int64_t)row * a.width + col];
-  if (df < a.min_depth_up || df > a.max_depth_down) return;
-  integrate_update(phi, w, i, df, zc, a);
+  double dd;
+  if (!depth_at(depth, (int64_t)row * a.width + col, a, dd)) return;
+  integrate_update(phi, w, i, dd, zc, a);
 }
 
 // Per-axis products of the camera-depth row, W[8]*X(x), W[9]*Y(y) and
@@ -143,9 +163,10 @@ __global__ void k_integrate_tables(double *__restrict__ tx, double *__restrict__
 // slow float64 projection runs on full warps instead of stalling the warps
 // they fall in; past the list's capacity a voxel takes the path in place.
 // The distance and the running mean are float64 as in the reference.
+template <typename D>
 __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, int32_t *__restrict__ w,
                                                       int nx, int ny, int nz,
-                                                      const float *__restrict__ depth,
+                                                      const D *__restrict__ depth,
                                                       const double *__restrict__ tx,
                                                       const double *__restrict__ ty,
                                                       const double *__restrict__ tz, int *__restrict__ list,
@@ -190,16 +211,16 @@ __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, i
   if (vf < -1.0f) row = -1;
   if (col < 0 || col >= a.width) return;
   if (row < 0 || row >= a.height) return;
-  const float df = depth[(int64_t)row * a.width + col];
-  // d < min_depth || d > max_depth on the float value compared as a double
-  if (df < a.min_depth_up || df > a.max_depth_down) return;
+  double dd;
+  if (!depth_at(depth, (int64_t)row * a.width + col, a, dd)) return;
   const double zc = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
-  integrate_update(phi, w, i, df, zc, a);
+  integrate_update(phi, w, i, dd, zc, a);
 }
 
 // The listed voxels of k_integrate, each on the float64 path.
+template <typename D>
 __global__ void __launch_bounds__(kBlock) k_integrate_exact(float *__restrict__ phi, int32_t *__restrict__ w,
-                                                            int nx, int ny, const float *__restrict__ depth,
+                                                            int nx, int ny, const D *__restrict__ depth,
                                                             const int *__restrict__ list,
                                                             const unsigned *__restrict__ list_n,
                                                             unsigned list_cap, IntegrateArgs a) {
@@ -214,9 +235,10 @@ __global__ void __launch_bounds__(kBlock) k_integrate_exact(float *__restrict__ 
 
 }  // namespace
 
-int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height,
-                        const double w2c[16], const double K[9], double min_depth,
-                        double max_depth, cudaStream_t s) {
+template <typename D>
+static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, int width, int height,
+                            const double w2c[16], const double K[9], double min_depth, double max_depth,
+                            cudaStream_t s) {
   IntegrateArgs a;
   for (int k = 0; k < 16; ++k) a.W[k] = w2c[k];
   for (int k = 0; k < 9; ++k) a.K[k] = K[k];
@@ -241,6 +263,7 @@ int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height
   a.max_depth_down = hi;
   a.width = width;
   a.height = height;
+  a.depth_scale = depth_scale;
   // scratch: list counter, the three coordinate tables, the list
   const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
   const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(g->count / 8, 65536), 0x7fffffff);
@@ -265,11 +288,22 @@ int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height
   k_integrate_tables<<<blocks_for(nx + ny + nz), kBlock, 0, s>>>(tx, ty, tz, nx, ny, nz, a);
   dim3 block(32, kBlock / 32);
   dim3 grid((nx + 31) / 32, (ny + block.y - 1) / block.y, nz);
-  k_integrate<<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, list, list_n, cap, a);
-  k_integrate_exact<<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list, list_n,
-                                                                  cap, a);
+  k_integrate<D><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, list, list_n, cap, a);
+  k_integrate_exact<D><<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list,
+                                                                     list_n, cap, a);
   KF_CHECK_LAUNCH("k_integrate");
   return KF_OK;
+}
+
+int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height, const double w2c[16],
+                        const double K[9], double min_depth, double max_depth, cudaStream_t s) {
+  return launch_integrate(g, depth_dev, 0.0, width, height, w2c, K, min_depth, max_depth, s);
+}
+
+int kf_launch_integrate_u16(kf_grid g, const uint16_t *depth_dev, double scale, int width, int height,
+                            const double w2c[16], const double K[9], double min_depth, double max_depth,
+                            cudaStream_t s) {
+  return launch_integrate(g, depth_dev, scale, width, height, w2c, K, min_depth, max_depth, s);
 }
 
 namespace {

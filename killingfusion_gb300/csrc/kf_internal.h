@@ -140,6 +140,9 @@ int kf_num_sms();
 // launches implemented in kf_exact.cu (float64 arithmetic without fused
 // multiply-add where the reference's rounding decides a discrete outcome)
 int kf_grid_ensure_alt(kf_grid g);
+int kf_launch_integrate_u16(kf_grid g, const uint16_t *depth_dev, double scale, int width, int height,
+                            const double w2c[16], const double K[9], double min_depth, double max_depth,
+                            cudaStream_t s);
 int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height,
                         const double w2c[16], const double K[9], double min_depth,
                         double max_depth, cudaStream_t s);

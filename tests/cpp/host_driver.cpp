@@ -8,6 +8,8 @@
 //   host_driver dataset <root> <outdir> <solver> <iterations> <frames> <voxel>
 //       processNextFrame over <frames> frames; writes the three meshes of each
 //       frame (OFF), psi of each frame and the final canonical SDF (.bin)
+//   host_driver refdataset <root> <outdir> <solver> <iterations> <frames>
+//       the same on the reference's PNG dataset layout and default config
 //   host_driver points <outdir>
 //       point queries of SDF and DisplacementField on a small seeded grid
 #include <cstdio>
@@ -79,6 +81,40 @@ static int run_dataset(int argc, char **argv) {
   }
   fusion.getCanonicalSdf()->dumpToBinFile(out + "canonical.bin", c.UnknownClipDistance, 1.0);
   std::cout << "frame index " << fusion.getCurrentFrameIndex() << std::endl;
+  return 0;
+}
+
+// The reference's own dataset layout (Snoopy/, PNG depth and mask,
+// intrinsics_kinect1.txt) with the reference's default configuration:
+//   host_driver refdataset <root> <outdir> <solver> <iterations> <frames>
+static int run_refdataset(int argc, char **argv) {
+  if (argc < 7) return 2;
+  std::string root = argv[2], out = std::string(argv[3]) + "/";
+  kf::Config &c = kf::config();
+  c.solver = solver_of(argv[4]);
+  c.KILLING_MAX_ITERATIONS = std::atoi(argv[5]);
+  const int frames = std::atoi(argv[6]);
+  c.datasetType = 1;
+  SDF::outputDir() = out;
+  DatasetReader reader(root);
+  if (!reader.referenceLayout()) throw std::runtime_error("expected the reference's layout");
+  std::cout << "frames " << reader.getNumImageFiles() << " depth " << reader.getMinimumDepthThreshold() << " "
+            << reader.getMaximumDepthThreshold() << std::endl;
+  KillingFusion fusion{reader};
+  fusion.setFrameRange(0, frames);
+  const char *names[3] = {"live", "registered", "canonical"};
+  for (int f = 0; f < frames; ++f) {
+    std::vector<SimpleMesh *> meshes = fusion.processNextFrame();
+    for (int k = 0; k < 3; ++k) {
+      char name[256];
+      std::snprintf(name, sizeof name, "%s%s_%03d.off", out.c_str(), names[k], f);
+      write_mesh(meshes[k], name);
+    }
+    char name[256];
+    std::snprintf(name, sizeof name, "%spsi_%03d.bin", out.c_str(), f);
+    fusion.getCurrentFrameDisplacementField()->dumpToBinFile(name);
+  }
+  fusion.getCanonicalSdf()->dumpToBinFile(out + "canonical.bin", c.UnknownClipDistance, 1.0);
   return 0;
 }
 
@@ -158,6 +194,7 @@ int main(int argc, char **argv) {
   try {
     if (!std::strcmp(argv[1], "spheres")) return run_spheres(argc, argv);
     if (!std::strcmp(argv[1], "dataset")) return run_dataset(argc, argv);
+    if (!std::strcmp(argv[1], "refdataset")) return run_refdataset(argc, argv);
     if (!std::strcmp(argv[1], "points")) return run_points(argc, argv);
   } catch (const std::exception &e) {
     std::cerr << "error: " << e.what() << std::endl;

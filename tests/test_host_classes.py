@@ -246,3 +246,51 @@ def test_point_queries(driver, oracle, tmp_path):
             oracle.voxel_query("hess", phi64, None, psi64, [v], P)[0],
             dv, oracle.voxel_query("killing", phi64, None, psi64, [v], P)[0]])
         np.testing.assert_array_equal(rv[i], expect, err_msg="voxel %d %s" % (i, v))
+
+
+def test_reference_dataset_layout(driver, oracle, tmp_path):
+    """DatasetReader on the reference's own layout (Snoopy/depth_%06d.png in
+    millimetres, omask_%06d.png, intrinsics_kinect1.txt; DatasetReader.cpp:15-66)
+    with the reference's default configuration: the masked 16-bit depth is
+    integrated as the reference's double metres, bit for bit."""
+    import pngio
+    grid, frames = synth.sphere_pair()
+    root = tmp_path / "data"
+    (root / "Snoopy").mkdir(parents=True)
+    with open(root / "intrinsics_kinect1.txt", "w") as f:
+        f.write(" ".join(repr(float(v)) for v in synth.K.ravel()) + "\n")
+    depth_m = []
+    for k, fr in enumerate(frames):
+        mm = np.round(fr.astype(np.float64) * 1000.0).astype(np.uint16)
+        mask = (mm > 0).astype(np.uint8) * 255
+        mask[:, :200] = 0  # the left of the frame is masked out
+        pngio.write(root / "Snoopy" / ("depth_%06d.png" % k), mm)
+        pngio.write(root / "Snoopy" / ("omask_%06d.png" % k), mask)
+        depth_m.append(np.where(mask > 0, mm.astype(np.float64) * (1.0 / 1000), 0.0))
+    out = tmp_path / "out"
+    out.mkdir()
+    log = driver("refdataset", root, out, "exact", 4, 2)
+    assert "frames 630 depth 0.0495164 1.2" in log
+    P = OParams()  # config.cpp values
+    lo, hi = synth.frustum_bounds(synth.K, 640, 480, 0.0495164, 1.2)
+    dims = synth.grid_from_bounds(lo, hi, P.voxel_size)
+    shape = dims[::-1]
+    init = f32(np.full(shape, P.max_surface + P.epsilon))
+
+    def integrate(d):
+        phi, w = oracle.integrate(init, np.zeros(shape, np.int64), P.voxel_size, lo, P.unknown_clip, d,
+                                  np.eye(4), synth.K, 0.0495164, 1.2)
+        return f32(phi), w
+
+    can, cw = integrate(depth_m[0])
+    assert (cw > 0).sum() > 100
+    live, lw = integrate(depth_m[1])
+    st, psi = oracle.solve(live, can, np.zeros(shape + (3,)), 4, P)
+    assert st == 0
+    np.testing.assert_array_equal(read_psi_bin(out / "psi_001.bin")[1], psi)
+    uphi, uw = oracle.update(live, lw, psi, P)
+    fphi, _ = oracle.fuse(can, cw, f32(uphi), uw)
+    d, head, phi = read_sdf_bin(out / "canonical.bin")
+    assert tuple(d) == dims
+    np.testing.assert_array_equal(phi, f32(fphi))
+    assert_mesh(out / "live_001.off", oracle.mesh(live, P))
