@@ -67,10 +67,12 @@ typedef enum kf_solver {
                           (KillingFusion.cpp:353-396): every voxel inside the
                           symmetric band steps psi in place until its step or
                           gradient is at most params.threshold or `iterations`
-                          steps were taken.  All voxels run at once, reading
-                          their neighbours' current psi (asynchronous
-                          relaxation; the reference's OpenMP threads race the
-                          same way), so psi is not reproducible bit for bit. */
+                          steps were taken, its neighbours fixed meanwhile.
+                          Voxels go in 8 colours (parity of x, y, z) instead
+                          of the reference's z, y, x order, so the result is
+                          deterministic but not the reference's bit for bit
+                          (nor is the reference's with more than one OpenMP
+                          thread).                                          */
 } kf_solver;
 
 /* The reference's config.h globals that the hot path reads. */

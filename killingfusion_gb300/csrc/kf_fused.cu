@@ -103,17 +103,18 @@ __global__ void __launch_bounds__(kThreads) k_fused_scatter(FusedArgs a, const i
 }
 
 // KillingFusion::computeDisplacementField, default per-voxel schedule
-// (KillingFusion.cpp:353-396) as asynchronous relaxation: every listed voxel
-// (inside the symmetric band) is taken by one group, which steps its psi in
-// place -- a.ix and a.ox are the same planes -- until the step or the
-// gradient is at most the threshold or max_iters steps were taken.  The
-// neighbours it reads are whatever the other groups have written so far (the
-// reference's OpenMP threads race the same way).  Statistics: record 0
-// voxels (list, from the band pass), last step, last monitored energy,
-// divergence; record 1 voxels that hit the cap (active) and the most steps
-// of one voxel (list).
+// (KillingFusion.cpp:353-396), for the listed voxels (inside the symmetric
+// band) of one colour (x&1) | (y&1)<<1 | (z&1)<<2: each is taken by one
+// group, which steps its psi in place -- a.ix and a.ox are the same planes --
+// until the step or the gradient is at most the threshold or max_iters steps
+// were taken.  A voxel's gradient reads psi only in its 3x3x3 neighbourhood,
+// where no other voxel has its colour, so its neighbours stay fixed while it
+// iterates, as in the reference's sequential loop, and the result does not
+// depend on scheduling.  Statistics: record 0 voxels (list, from the band
+// pass), last step, last monitored energy, divergence; record 1 voxels that
+// hit the cap (active) and the most steps of one voxel (list).
 __global__ void __launch_bounds__(kBandThreads, 3) k_pervoxel(FusedArgs a, const int *__restrict__ list,
-                                                            int max_iters) {
+                                                            int max_iters, int color) {
   const int lane = threadIdx.x & 31;
   const int gl = lane & (kGroup - 1);
   const int group = threadIdx.x / kGroup;
@@ -128,6 +129,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_pervoxel(FusedArgs a, const
     const int i = list[k];
     int x, y, z;
     voxel_xyz(dp, i, x, y, z);
+    if (((x & 1) | (y & 1) << 1 | (z & 1) << 2) != color) continue;
     const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 && z <= dp.nz - 2;
     int iter = 0;
     unsigned steps = 0;
@@ -292,7 +294,8 @@ int kf_solve_pervoxel(kf_grid live, kf_grid can, kf_field psi, const DevParams &
   const unsigned grid = (unsigned)std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) /
                                                         (kThreads * kFlatGroups), 1);
   k_fused_stream<false><<<grid, kThreads, 0, s>>>(a, psi->band);
-  k_pervoxel<<<(unsigned)kf_num_sms() * 3, kBandThreads, 0, s>>>(a, psi->band, max_iters);
+  for (int color = 0; color < 8; ++color)
+    k_pervoxel<<<(unsigned)kf_num_sms() * 3, kBandThreads, 0, s>>>(a, psi->band, max_iters, color);
   KF_CHECK_LAUNCH("per-voxel solve");
   return KF_OK;
 }

@@ -464,20 +464,24 @@ int orc_solve_jacobi(const double *live, const double *can, double *psi,
 }
 
 /* KillingFusion::computeDisplacementField, default per-voxel schedule
- * (KillingFusion.cpp:353-396) on one thread, cells in z, y, x order: a voxel
- * whose warped value lies inside the symmetric band +-(MaxSurface - epsilon)
- * (:369) steps psi in place, -alpha * gradient at a time, until the step or
- * the gradient is at most threshold or max_iters steps were taken (:374-394).
- * Returns 0, or -1 when psi turned non-finite (the reference throws -1).
- * counts (may be NULL): voxels visited, steps taken, voxels that hit
- * max_iters. */
+ * (KillingFusion.cpp:353-396) on one thread: a voxel whose warped value lies
+ * inside the symmetric band +-(MaxSurface - epsilon) (:369) steps psi in
+ * place, -alpha * gradient at a time, until the step or the gradient is at
+ * most threshold or max_iters steps were taken (:374-394).  Order: cells in
+ * z, y, x order (the reference's, colored == 0), or colour by colour
+ * ((x&1) | (y&1)<<1 | (z&1)<<2 = 0..7, z, y, x within a colour; colored != 0)
+ * as the GPU solver runs them.  Returns 0, or -1 when psi turned non-finite
+ * (the reference throws -1).  counts (may be NULL): voxels visited, steps
+ * taken, voxels that hit max_iters. */
 int orc_solve_pervoxel(const double *live, const double *can, double *psi,
                        const int n[3], const orc_params *P, int max_iters,
-                       int64_t counts[3]) {
+                       int colored, int64_t counts[3]) {
   int64_t visited = 0, steps = 0, capped = 0;
+  for (int color = 0; color < (colored ? 8 : 1); ++color)
   for (int z = 0; z < n[2]; ++z)
     for (int y = 0; y < n[1]; ++y)
       for (int x = 0; x < n[0]; ++x) {
+        if (colored && ((x & 1) | (y & 1) << 1 | (z & 1) << 2) != color) continue;
         double s = orc_warped_distance(live, psi, n, P, x, y, z);
         if (s > P->max_surface - P->epsilon || s < -P->max_surface + P->epsilon)
           continue;

@@ -104,7 +104,7 @@ int orc_is_active(const double *live, const double *psi, const int n[3],
  * default. */
 int orc_solve_pervoxel(const double *live, const double *can, double *psi,
                        const int n[3], const orc_params *P, int max_iters,
-                       int64_t counts[3]);
+                       int colored, int64_t counts[3]);
 int orc_solve_jacobi(const double *live, const double *can, double *psi,
                      const int n[3], const orc_params *P, int iters,
                      int nthreads, int64_t *active_counts);

@@ -103,7 +103,7 @@ class Oracle:
             "orc_warped_distance": (C.c_double, [_dp, _dp, _i32p, P, C.c_int, C.c_int, C.c_int]),
             "orc_is_active": (C.c_int, [_dp, _dp, _i32p, P, C.c_int, C.c_int, C.c_int]),
             "orc_solve_jacobi": (C.c_int, [_dp, _dp, _dp, _i32p, P, C.c_int, C.c_int, C.c_void_p]),
-            "orc_solve_pervoxel": (C.c_int, [_dp, _dp, _dp, _i32p, P, C.c_int, C.c_void_p]),
+            "orc_solve_pervoxel": (C.c_int, [_dp, _dp, _dp, _i32p, P, C.c_int, C.c_int, C.c_void_p]),
             "orc_integrate": (None, [_dp, _ip, _i32p, C.c_double, _dp, C.c_double, _dp, C.c_int,
                                      C.c_int, _dp, _dp, C.c_double, C.c_double]),
             "orc_update": (None, [_dp, _ip, _dp, _i32p, P]),
@@ -205,14 +205,16 @@ class Oracle:
                                      counts.ctypes.data)
         return (st, psi, counts[:iters]) if active_counts else (st, psi)
 
-    def solve_pervoxel(self, live, can, psi, max_iters, P: Params):
-        """The reference's default per-voxel schedule, one thread in z, y, x
-        order; returns (status, psi, (visited, steps, capped))."""
+    def solve_pervoxel(self, live, can, psi, max_iters, P: Params, colored=False):
+        """The reference's default per-voxel schedule on one thread, in z, y, x
+        order or colour by colour; returns (status, psi, (visited, steps,
+        capped))."""
         live = _c(live, np.float64)
         psi = np.array(psi, dtype=np.float64, order="C", copy=True)
         counts = np.zeros(3, dtype=np.int64)
         st = self.L.orc_solve_pervoxel(live, _c(can, np.float64), psi, _dims(live),
-                                       C.byref(_OrcParams.of(P)), max_iters, counts.ctypes.data)
+                                       C.byref(_OrcParams.of(P)), max_iters, int(bool(colored)),
+                                       counts.ctypes.data)
         return st, psi, tuple(int(c) for c in counts)
 
     def integrate(self, phi, w, voxel, min3, unknown_clip, depth, w2c, K, min_depth, max_depth):

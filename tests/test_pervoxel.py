@@ -1,9 +1,11 @@
 """KF_SOLVER_PERVOXEL, the reference's default per-voxel schedule
-(KillingFusion.cpp:353-396), against the oracle's single-thread run of the
-same schedule.  The GPU runs every voxel at once on its neighbours' current
-psi (the reference's OpenMP threads race the same way), so parity is
-statistical: the same voxels visited, every one converged or capped as in
-the oracle, and the registration's data residual within a few per cent."""
+(KillingFusion.cpp:353-396), against the oracle's single-thread runs of the
+same schedule.  The GPU takes the voxels colour by colour (parity of x, y, z:
+no two voxels of one colour share a neighbourhood, so each iterates with its
+neighbours fixed, as in the reference's loop); the oracle runs that order in
+float64 (psi within float32 rounding) and the reference's z, y, x order
+(same voxels, same convergence, registration residual within a few per cent
+of its improvement)."""
 import numpy as np
 import pytest
 
@@ -43,14 +45,18 @@ def test_pervoxel_matches_oracle_statistically(gpu, oracle):
     psi = f.download().astype(np.float64)
     l64, c64 = live.astype(np.float64), can.astype(np.float64)
     ost, opsi, (visited, steps, capped) = oracle.solve_pervoxel(l64, c64, np.zeros(psi.shape), 1024, OP)
-    assert ost == 0
+    cst, cpsi, (cvisited, csteps, ccapped) = oracle.solve_pervoxel(l64, c64, np.zeros(psi.shape), 1024, OP,
+                                                                   colored=True)
+    assert ost == 0 and cst == 0
     print("gpu: visited %d, capped %d, most steps %d; oracle: visited %d, capped %d, steps %d"
           % (st["active_first"], st["capped"], st["iterations_run"], visited, capped, steps))
-    assert st["active_first"] == visited > 1000
-    assert capped == 0
-    # a voxel whose neighbours keep moving may not settle within the cap
-    assert st["capped"] <= 0.05 * visited
+    assert st["active_first"] == visited == cvisited > 1000
+    assert capped == ccapped == st["capped"] == 0 and st["converged"] == 1
     assert 1 <= st["iterations_run"] <= 1024
+    # the GPU's order, in float64: float32 rounding apart
+    print("psi: max |gpu - oracle (colour order)| %.2e voxel, max |psi| %.2e"
+          % (np.abs(psi - cpsi).max(), np.abs(cpsi).max()))
+    assert np.abs(psi - cpsi).max() <= 2e-5
     # the voxels visited: symmetric band of the zero field
     lo = -(OP.max_surface - OP.epsilon)
     z, y, x = np.nonzero((l64 <= OP.max_surface - OP.epsilon) & (l64 >= lo))
@@ -63,7 +69,6 @@ def test_pervoxel_matches_oracle_statistically(gpu, oracle):
     r_gpu = residual(oracle, l64, c64, psi, OP, vox)
     r_orc = residual(oracle, l64, c64, opsi, OP, vox)
     print("residual: start %.5f  oracle %.5f  gpu %.5f" % (r0, r_orc, r_gpu))
-    print("psi: max |gpu - oracle| %.2e voxel, max |oracle| %.2e" % (np.abs(psi - opsi).max(), np.abs(opsi).max()))
     assert r_orc < r0 and r_gpu < r0
     assert abs(r_gpu - r_orc) <= 0.05 * (r0 - r_orc) + 1e-9
 
@@ -80,7 +85,7 @@ def test_pervoxel_cap_and_paper_weights(gpu, oracle):
     cap = 64
     st = gpu.psi_solve(gl, gc, f, P, cap, "pervoxel")
     _, _, (visited, steps, capped) = oracle.solve_pervoxel(live.astype(np.float64), can.astype(np.float64),
-                                                           np.zeros(live.shape + (3,)), cap, OP)
+                                                           np.zeros(live.shape + (3,)), cap, OP, colored=True)
     print("paper weights: gpu capped %d of %d, oracle capped %d" % (st["capped"], st["active_first"], capped))
     assert st["active_first"] == visited
     assert st["iterations_run"] <= cap
