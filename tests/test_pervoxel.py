@@ -68,9 +68,12 @@ def test_pervoxel_matches_oracle_statistically(gpu, oracle):
     r0 = residual(oracle, l64, c64, np.zeros(psi.shape), OP, vox)
     r_gpu = residual(oracle, l64, c64, psi, OP, vox)
     r_orc = residual(oracle, l64, c64, opsi, OP, vox)
-    print("residual: start %.5f  oracle %.5f  gpu %.5f" % (r0, r_orc, r_gpu))
-    assert r_orc < r0 and r_gpu < r0
-    assert abs(r_gpu - r_orc) <= 0.05 * (r0 - r_orc) + 1e-9
+    r_col = residual(oracle, l64, c64, cpsi, OP, vox)
+    print("residual: start %.6f  reference order %.6f  colour order %.6f  gpu %.6f" % (r0, r_orc, r_col, r_gpu))
+    assert r_orc < r0 and r_col < r0 and r_gpu < r0
+    # the GPU is the colour order; the two orders improve the residual alike
+    assert abs(r_gpu - r_col) <= 1e-6 * r_col
+    assert abs(r_col - r_orc) <= 0.25 * (r0 - r_orc)
 
 
 def test_pervoxel_cap_and_paper_weights(gpu, oracle):
