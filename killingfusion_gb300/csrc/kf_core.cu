@@ -332,6 +332,9 @@ int kf_field_band_list(kf_field f, int **out) {
 
 void kf_field_release_solver(kf_field f) {
   cudaFree(f->band);
+  cudaFree(f->runs);
+  f->runs = nullptr;
+  f->runs_cap = 0;
   f->band = nullptr;
   cudaFree(f->stats);
   cudaFreeHost(f->stats_host);

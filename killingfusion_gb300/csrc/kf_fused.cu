@@ -3,7 +3,7 @@
 // KillingFusion::computeEnergyGradient, :399-476) and the CUDA-graph capture
 // of the fixed-iteration loop.
 //
-// An iteration (KF_SOLVER_FUSED) is three passes over psi held in place:
+// An iteration (KF_SOLVER_FUSED) is two passes over psi held in place:
 //   k_fused_stream (dense)  reads psi and phi_live and applies the band test
 //     of KillingFusion.cpp:272-274.  The warped value phi_live(i + psi(i)) is
 //     phi_live(i) itself when psi(i) == 0 (zero interpolation weights), so only
@@ -18,7 +18,8 @@
 //     derivative sums of +-1-weighted sample differences.  The new psi goes
 //     to a side buffer indexed by list position, so every voxel still reads
 //     its neighbours' old values (Jacobi).
-//   k_fused_scatter  writes the band voxels' new psi back.
+//   The next iteration's dense pass writes the band voxels' new psi back,
+//     each run of voxels its own (k_fused_scatter after the last iteration).
 // The band-only solver (KF_SOLVER_BAND) runs the dense pass once.  A voxel
 // outside the band keeps psi, so its band test keeps failing and the band can
 // only shrink: each band pass hands the voxels it updated to the next
@@ -43,13 +44,30 @@ namespace {
 
 // Dense pass: stream the slab, list the band voxels (st[iter].list counts
 // them); kPassThrough copies psi of the other voxels to the output buffer.
+// In place (runs != NULL): the run first writes back the new psi that the
+// previous iteration's band pass left for its own band voxels -- the entries
+// runs[run] of prev_list and of the second planes (a.ox..a.oz) -- and then
+// streams; it records where its band voxels land in `list`.
 template <bool kPassThrough>
-__global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__restrict__ list) {
+__global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__restrict__ list,
+                                                          const int *__restrict__ prev_list,
+                                                          int2 *__restrict__ runs) {
+  if (runs && a.iter > 0 && !a.st[a.iter - 1].skipped) {
+    const int2 r = runs[blockIdx.x];
+    float *px = const_cast<float *>(a.ix), *py = const_cast<float *>(a.iy), *pz = const_cast<float *>(a.iz);
+    for (int j = threadIdx.x; j < r.y; j += kThreads) {
+      const int slot = r.x + j, v = prev_list[slot];
+      px[v] = a.ox[slot];
+      py[v] = a.oy[slot];
+      pz[v] = a.oz[slot];
+    }
+    __syncthreads();
+  }
   if (iteration_gated(a.st, a.iter, a.dp)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.iter].skipped = 1;
     return;
   }
-  stream_flat<kPassThrough>(a, blockIdx.x, list, &a.st[a.iter].list);
+  stream_flat<kPassThrough>(a, blockIdx.x, list, &a.st[a.iter].list, runs ? runs + blockIdx.x : nullptr);
 }
 
 // Band pass: a group of kGroup lanes per listed voxel, launched as one resident
@@ -87,8 +105,8 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
   reduce_iter_stats<kBandThreads>(a.st + a.iter, active, maxd, (double)energy, diverged);
 }
 
-// In-place update: psi(list[k]) = entry k of the band pass's output planes,
-// once every band voxel has read its neighbours' old values.
+// In-place update after the last iteration: psi(list[k]) = entry k of the
+// band pass's output planes (the dense passes write back the others).
 __global__ void __launch_bounds__(kThreads) k_fused_scatter(FusedArgs a, const int *__restrict__ list,
                                                            float *__restrict__ px, float *__restrict__ py,
                                                            float *__restrict__ pz) {
@@ -192,7 +210,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_pervoxel(FusedArgs a, const
 struct FusedGraph {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t capture = nullptr;
-  const void *key_ptr[10] = {};
+  const void *key_ptr[11] = {};
   int iterations = 0;
   bool band_only = false;
   DevParams dp;
@@ -206,7 +224,7 @@ void kf_fused_graph_destroy(FusedGraph *g) {
 }
 
 static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
-                              int iterations, IterStats *st, int *lists, bool band_only,
+                              int iterations, IterStats *st, int *lists, int2 *runs, bool band_only,
                               cudaStream_t s) {
   const unsigned band_blocks = (unsigned)kf_num_sms() * 3;  // one resident wave
   const unsigned grid = (unsigned)std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) /
@@ -227,12 +245,14 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
     a.oz = (float *)out[2];
     a.iter = it;
     if (!band_only) {
-      k_fused_stream<false><<<grid, block, 0, s>>>(a, lst[0]);
-      k_fused_band<false, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[0], nullptr);
-      k_fused_scatter<<<band_blocks, kThreads, 0, s>>>(a, lst[0], (float *)in[0], (float *)in[1],
-                                                      (float *)in[2]);
+      // lists alternate so that a run can still read the previous iteration's
+      k_fused_stream<false><<<grid, block, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1], runs);
+      k_fused_band<false, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], nullptr);
+      if (it == iterations - 1)
+        k_fused_scatter<<<band_blocks, kThreads, 0, s>>>(a, lst[it & 1], (float *)in[0], (float *)in[1],
+                                                        (float *)in[2]);
     } else {
-      if (it == 0) k_fused_stream<true><<<grid, block, 0, s>>>(a, lst[0]);
+      if (it == 0) k_fused_stream<true><<<grid, block, 0, s>>>(a, lst[0], nullptr, nullptr);
       k_fused_band<true, false><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
     }
   }
@@ -244,8 +264,20 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
   if (rc) return rc;
   rc = kf_field_band_list(psi, &psi->band);
   if (rc) return rc;
-  const void *key[10] = {live->phi, can->phi, psi->p[0], psi->p[1], psi->p[2],
-                         psi->q[0], psi->q[1], psi->q[2], st, psi->band};
+  const int64_t nruns =
+      std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) / (kThreads * kFlatGroups), 1);
+  if (psi->runs_cap < nruns) {
+    cudaFree(psi->runs);
+    psi->runs = nullptr;
+    psi->runs_cap = 0;
+    if (cudaMalloc(&psi->runs, nruns * sizeof(int2)) != cudaSuccess) {
+      cudaGetLastError();
+      return kf_fail(KF_ERR_OOM, "cudaMalloc of the dense pass's run table failed");
+    }
+    psi->runs_cap = nruns;
+  }
+  const void *key[11] = {live->phi, can->phi, psi->p[0], psi->p[1], psi->p[2],
+                         psi->q[0], psi->q[1], psi->q[2], st, psi->band, psi->runs};
   FusedGraph *g = psi->graph;
   bool hit = g && g->iterations == iterations && g->band_only == band_only &&
              memcmp(g->key_ptr, key, sizeof(key)) == 0 && memcmp(&g->dp, &dp, sizeof(dp)) == 0;
@@ -255,7 +287,7 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
     KF_CHECK_CUDA(cudaStreamCreateWithFlags(&g->capture, cudaStreamNonBlocking));
     cudaGraph_t graph;
     KF_CHECK_CUDA(cudaStreamBeginCapture(g->capture, cudaStreamCaptureModeThreadLocal));
-    launch_iterations(live, can, psi, dp, iterations, st, psi->band, band_only, g->capture);
+    launch_iterations(live, can, psi, dp, iterations, st, psi->band, psi->runs, band_only, g->capture);
     cudaError_t le = cudaGetLastError();
     KF_CHECK_CUDA(cudaStreamEndCapture(g->capture, &graph));
     if (le != cudaSuccess) {
@@ -293,7 +325,7 @@ int kf_solve_pervoxel(kf_grid live, kf_grid can, kf_field psi, const DevParams &
   a.iter = 0;
   const unsigned grid = (unsigned)std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) /
                                                         (kThreads * kFlatGroups), 1);
-  k_fused_stream<false><<<grid, kThreads, 0, s>>>(a, psi->band);
+  k_fused_stream<false><<<grid, kThreads, 0, s>>>(a, psi->band, nullptr, nullptr);
   for (int color = 0; color < 8; ++color)
     k_pervoxel<<<(unsigned)kf_num_sms() * 3, kBandThreads, 0, s>>>(a, psi->band, max_iters, color);
   KF_CHECK_LAUNCH("per-voxel solve");

@@ -409,7 +409,7 @@ __device__ __forceinline__ void flat_test(const FusedArgs &a, int64_t i, float q
 
 template <bool kPassThrough>
 __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int *__restrict__ list,
-                                            unsigned *count) {
+                                            unsigned *count, int2 *__restrict__ range = nullptr) {
   __shared__ int queue[kFlatVoxels + 4];
   __shared__ int qn, qbase;
   const DevParams &dp = a.dp;
@@ -476,6 +476,9 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
   if (tid == 0 && qn) qbase = (int)atomicAdd(count, (unsigned)qn);
   __syncthreads();
   for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
+  // where this run's band voxels sit in the list (for the next iteration's
+  // write-back of their new psi)
+  if (range && tid == 0) *range = make_int2(qn ? qbase : 0, qn);
 }
 
 // Appends the voxels `next` (>= 0 on the group leaders that carry one) of the

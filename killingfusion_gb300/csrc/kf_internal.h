@@ -45,6 +45,8 @@ struct kf_field_s {
   size_t plain_bytes;
   FusedGraph *graph;      // captured fused iteration loop
   int *band;              // band-voxel lists (two, of one int per voxel each)
+  int2 *runs;             // per run of the dense pass: its entries of the list
+  int64_t runs_cap;
 };
 
 // ---------------------------------------------------------------------------
