@@ -282,15 +282,18 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   uint32_t *tris = (uint32_t *)(total_dev + 1);
   k_mc_count<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris);
   k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev);
-  // the emit pass stops at `capacity` by itself, so it is queued before the
-  // count is read back: one wait per mesh
-  if (verts && capacity > 0) k_mc_emit<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, off, verts, capacity);
-  KF_CHECK_LAUNCH("marching-cubes kernels");
+  KF_CHECK_LAUNCH("k_mc_count/k_mc_scan");
+  // wait for the count only; the emit pass runs on while the caller queues
+  // its next work
   int64_t total = 0;
   KF_CHECK_CUDA(cudaMemcpyAsync(&total, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-  KF_CHECK_CUDA(cudaFreeAsync(scratch, s));
   KF_CHECK_CUDA(cudaStreamSynchronize(s));
   *ntri = total;
+  if (verts && total > 0 && capacity > 0) {
+    k_mc_emit<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, off, verts, capacity);
+    KF_CHECK_LAUNCH("k_mc_emit");
+  }
+  KF_CHECK_CUDA(cudaFreeAsync(scratch, s));
   if (verts && capacity < total)
     return kf_fail(KF_ERR_CAPACITY, "vertex buffer holds fewer triangles than the mesh has");
   return KF_OK;
