@@ -156,7 +156,8 @@ def test_mc_tables_match_reference_header(oracle):
     """The oracle's marching-cubes tables equal the reference's edgeTable and
     triTable (MarchingCubes.h:26-318), read from the reference checkout."""
     import re
-    path = "/root/reference/KillingFusion/include/MarchingCubes.h"
+    from oracle import build as obuild
+    path = os.path.join(obuild.DEFAULT_REF_ROOT, "KillingFusion", "include", "MarchingCubes.h")
     if not os.path.exists(path):
         pytest.skip("reference checkout absent")
     src = open(path).read()
