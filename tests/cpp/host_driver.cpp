@@ -8,6 +8,8 @@
 //   host_driver dataset <root> <outdir> <solver> <iterations> <frames> <voxel>
 //       processNextFrame over <frames> frames; writes the three meshes of each
 //       frame (OFF), psi of each frame and the final canonical SDF (.bin)
+//   host_driver process <root> <outdir> <solver> <iterations> <voxel>
+//       KillingFusion::process: psi carried over, fusion through psi
 //   host_driver refdataset <root> <outdir> <solver> <iterations> <frames>
 //       the same on the reference's PNG dataset layout and default config
 //   host_driver points <outdir>
@@ -84,8 +86,27 @@ static int run_dataset(int argc, char **argv) {
   return 0;
 }
 
+// KillingFusion::process over a raw dataset (frames 4 .. numFrames-1, psi
+// carried from frame to frame, fused through psi):
+//   host_driver process <root> <outdir> <solver> <iterations> <voxel>
+static int run_process(int argc, char **argv) {
+  if (argc < 7) return 2;
+  std::string root = argv[2], out = std::string(argv[3]) + "/";
+  kf::Config &c = kf::config();
+  c.solver = solver_of(argv[4]);
+  c.KILLING_MAX_ITERATIONS = std::atoi(argv[5]);
+  c.VoxelSize = std::atof(argv[6]);
+  c.UnknownClipDistance = c.MaxSurfaceVoxelDistance = c.VoxelSize * 5;
+  SDF::outputDir() = out;
+  KillingFusion fusion{DatasetReader(root)};
+  fusion.process();
+  return 0;
+}
+
 // The reference's own dataset layout (Snoopy/, PNG depth and mask,
 // intrinsics_kinect1.txt) with the reference's default configuration:
+//   host_driver process <root> <outdir> <solver> <iterations> <voxel>
+//       KillingFusion::process: psi carried over, fusion through psi
 //   host_driver refdataset <root> <outdir> <solver> <iterations> <frames>
 static int run_refdataset(int argc, char **argv) {
   if (argc < 7) return 2;
@@ -195,6 +216,7 @@ int main(int argc, char **argv) {
     if (!std::strcmp(argv[1], "spheres")) return run_spheres(argc, argv);
     if (!std::strcmp(argv[1], "dataset")) return run_dataset(argc, argv);
     if (!std::strcmp(argv[1], "refdataset")) return run_refdataset(argc, argv);
+    if (!std::strcmp(argv[1], "process")) return run_process(argc, argv);
     if (!std::strcmp(argv[1], "points")) return run_points(argc, argv);
   } catch (const std::exception &e) {
     std::cerr << "error: " << e.what() << std::endl;

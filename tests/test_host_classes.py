@@ -294,3 +294,48 @@ def test_reference_dataset_layout(driver, oracle, tmp_path):
     assert tuple(d) == dims
     np.testing.assert_array_equal(phi, f32(fphi))
     assert_mesh(out / "live_001.off", oracle.mesh(live, P))
+
+
+def test_process_carries_psi_and_fuses_through_it(driver, oracle, tmp_path):
+    """KillingFusion::process (KillingFusion.cpp:41-107): frames 4.. of the
+    sequence, psi carried from frame to frame, SDF::fuse(other, psi) into the
+    canonical SDF and the registered meshes through SDF::save_mesh(.., psi);
+    FinalCanonicalModel.bin at the end."""
+    K, frames = small_camera_frames(7)
+    min_d, max_d, voxel, iters = 0.3, 0.5, 0.008, 6
+    root = tmp_path / "data"
+    synth.write_dataset(str(root), frames, K, min_d, max_d)
+    out = tmp_path / "out"
+    out.mkdir()
+    driver("process", root, out, "exact", iters, voxel)
+    lo, hi = synth.frustum_bounds(K, 64, 48, min_d, max_d)
+    dims = synth.grid_from_bounds(lo, hi, voxel)
+    P = OParams(voxel_size=voxel, unknown_clip=5 * voxel, max_surface=5 * voxel)
+    shape = dims[::-1]
+    init = f32(np.full(shape, P.max_surface + P.epsilon))
+    zero_w = np.zeros(shape, np.int64)
+
+    def integrate(frame):
+        phi, w = oracle.integrate(init, zero_w, voxel, lo, P.unknown_clip, frame.astype(np.float64),
+                                  np.eye(4), K, min_d, max_d)
+        return f32(phi), w
+
+    prev, pw = integrate(frames[4])
+    can, cw = oracle.fuse(init, zero_w, prev, pw)
+    can = f32(can)
+    for name in ("InputFrameSDF", "RegisteredFrameSDF", "CanonicalSDF", "LiveCanonicalSdf"):
+        assert_mesh(out / ("%s004.off" % name), oracle.mesh(prev, P))
+    psi = np.zeros(shape + (3,))
+    for i in (5, 6):
+        cur, curw = integrate(frames[i])
+        assert_mesh(out / ("InputFrameSDF%03d.off" % i), oracle.mesh(cur, P))
+        st, psi = oracle.solve(cur, can, psi, iters, P)
+        assert st == 0
+        reg, _ = oracle.fuse_psi(init, zero_w, cur, curw, psi, P)
+        assert_mesh(out / ("RegisteredFrameSDF%03d.off" % i), oracle.mesh(f32(reg), P))
+        can, cw = oracle.fuse_psi(can, cw, cur, curw, psi, P)
+        can = f32(can)
+        assert_mesh(out / ("CanonicalSDF%03d.off" % i), oracle.mesh(can, P))
+    d, head, phi = read_sdf_bin(out / "FinalCanonicalModel.bin")
+    assert tuple(d) == dims
+    np.testing.assert_array_equal(phi, can)
