@@ -12,10 +12,11 @@
 //                   search over the tile prefix) building each problem's
 //                   band list;
 //   k_batch_band    per iteration, the band voxels of all problems as one
-//                   work list: a block scans the per-problem list counts into
-//                   a prefix, each 8-lane group maps its work item to
-//                   (problem, voxel) and updates it; statistics are gathered
-//                   per problem in shared memory and flushed once per block.
+//                   work list cut into chunks that never cross a problem: a
+//                   block scans the per-problem chunk counts into a prefix,
+//                   finds each chunk's problem and hands each kGroup-lane
+//                   group one voxel; statistics are gathered per problem in
+//                   shared memory and flushed once per block.
 // Each problem converges on its own (params.early_exit): once its previous
 // iteration moved psi by at most params.threshold it is skipped, and its
 // voxels are no longer listed.  The whole loop is captured in one CUDA graph
