@@ -96,6 +96,14 @@ typedef struct kf_params {
                            reference's Jacobi schedule does; 1: stop once
                            max |dpsi| <= threshold, the criterion of its
                            per-voxel schedule (KillingFusion.cpp:381)      */
+  int use_trust;        /* UseTrustStrategy (config.cpp:27): the trust-region
+                           step of the Jacobi schedule (KillingFusion.cpp:
+                           288-314), taken only with the data term alone
+                           (use_data set, use_levelset and use_killing
+                           clear), as the reference takes it.  Run by
+                           KF_SOLVER_FUSED, _BAND and _EXACT; _PLAIN and
+                           kf_batch_create reject it; _PERVOXEL ignores it,
+                           as the reference's per-voxel schedule does.    */
 } kf_params;
 
 typedef struct kf_solve_stats {

@@ -41,7 +41,7 @@ class _Params(C.Structure):
         "voxel_size", "unknown_clip", "max_surface", "epsilon", "delta_size", "alpha",
         "omega_k", "gamma_k", "omega_s", "threshold", "killing_clamp")] + [
         ("use_data", C.c_int), ("use_levelset", C.c_int), ("use_killing", C.c_int),
-        ("early_exit", C.c_int)]
+        ("early_exit", C.c_int), ("use_trust", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -73,6 +73,7 @@ class Params:
     use_levelset: bool = True
     use_killing: bool = True
     early_exit: bool = False
+    use_trust: bool = False
 
     @staticmethod
     def reference(voxel_size: float = 0.012, trunc_voxels: float = 4.0) -> "Params":

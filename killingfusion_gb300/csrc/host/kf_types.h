@@ -72,6 +72,9 @@ struct Config {
   double MaxSurfaceVoxelDistance = 0.012 * 4;
   bool EnergyTypeUsed[3] = {true, true, true};  // data, level set, Killing
   bool UseZeroDisplacementFieldForNextFrame = true;
+  // the trust-region step of the Jacobi schedule, data term alone
+  // (config.cpp:27, KillingFusion.cpp:288-314)
+  bool UseTrustStrategy = false;
   int KILLING_MAX_ITERATIONS = 1024;
   double deltaSize = 0.05;
   double alpha = 0.025;
@@ -107,6 +110,7 @@ struct Config {
     p.use_data = EnergyTypeUsed[0];
     p.use_levelset = EnergyTypeUsed[1];
     p.use_killing = EnergyTypeUsed[2];
+    p.use_trust = UseTrustStrategy;
     return p;
   }
 };

@@ -313,6 +313,8 @@ extern "C" int kf_batch_create(const kf_batch_item *items, int count, int iterat
     KF_REQUIRE(it.live->count <= 0x7fffffff, "grid too large for a batch item");
     int rc = kf_check_params(&it.params);
     if (rc) return rc;
+    KF_REQUIRE(!kf_make_dev_params(it.live->n, &it.params).trust,
+               "batched solves have no trust-region step (use_trust with the data term alone)");
     for (int q = 0; q < p; ++q) KF_REQUIRE(items[q].psi != it.psi, "a field appears twice in a batch");
   }
   kf_batch b = new kf_batch_s();

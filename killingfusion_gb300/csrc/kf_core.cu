@@ -114,6 +114,7 @@ DevParams kf_make_dev_params(const int n[3], const kf_params *p) {
   d.use_killing = p->use_killing;
   d.early_exit = p->early_exit;
   d.threshold = p->threshold;
+  d.trust = p->use_trust && p->use_data && !p->use_levelset && !p->use_killing;
   return d;
 }
 
@@ -330,11 +331,24 @@ int kf_field_band_list(kf_field f, int **out) {
   return KF_OK;
 }
 
+int kf_field_trust_rows(kf_field f, int **out) {
+  if (!f->rows &&
+      cudaMalloc(&f->rows, 2 * (size_t)f->n[1] * f->n[2] * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    f->rows = nullptr;
+    return kf_fail(KF_ERR_OOM, "cudaMalloc of the trust-region row table failed");
+  }
+  *out = f->rows;
+  return KF_OK;
+}
+
 void kf_field_release_solver(kf_field f) {
   cudaFree(f->band);
   cudaFree(f->runs);
   f->runs = nullptr;
   f->runs_cap = 0;
+  cudaFree(f->rows);
+  f->rows = nullptr;
   f->band = nullptr;
   cudaFree(f->stats);
   cudaFreeHost(f->stats_host);
@@ -630,6 +644,9 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
              "unknown solver");
   KF_REQUIRE((solver == KF_SOLVER_EXACT) == (psi->prec == KF_F64),
              "KF_SOLVER_EXACT runs on KF_F64 fields and the other solvers on KF_F32 fields");
+  KF_REQUIRE(!(p->use_trust && p->use_data && !p->use_levelset && !p->use_killing &&
+               solver == KF_SOLVER_PLAIN),
+             "the trust-region step (use_trust) runs in KF_SOLVER_FUSED, _BAND and _EXACT, not _PLAIN");
   if (stats) memset(stats, 0, sizeof(*stats));
   if (iterations == 0) return KF_OK;
   cudaStream_t s = kf_stream(stream);

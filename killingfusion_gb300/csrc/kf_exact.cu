@@ -516,12 +516,15 @@ __global__ void __launch_bounds__(kBlock) k_fuse_warped(float *__restrict__ phi1
 // ---------------------------------------------------------------------------
 // float64 replay of the Jacobi psi update (KillingFusion.cpp:248-352)
 // ---------------------------------------------------------------------------
+// With dp.trust each step goes through trust_step; a voxel whose step
+// failed keeps its psi and records its x in rows[z * ny + y] (the smallest
+// such x of the row wins), for k_exact_trust_rows.
 __global__ void __launch_bounds__(kBlock) k_exact_step(PhiView<double> live, PhiView<double> can,
                                                        PsiView<double, double> fin,
                                                        double *__restrict__ ox,
                                                        double *__restrict__ oy,
                                                        double *__restrict__ oz, DevParams dp,
-                                                       IterStats *st, int iter) {
+                                                       IterStats *st, int iter, int *__restrict__ rows) {
   if (iteration_gated(st, iter, dp)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) st[iter].skipped = 1;
     return;
@@ -538,10 +541,18 @@ __global__ void __launch_bounds__(kBlock) k_exact_step(PhiView<double> live, Phi
     if (in_band(s, dp.band_hi, -dp.unknown_clip)) {
       active = true;
       TParams<double> tp(dp);
-      double g[3];
+      double g[3], u[3];
       energy_gradient(live, can, fin, tp, x, y, z, g);
 #pragma unroll
-      for (int k = 0; k < 3; ++k) d[k] = d[k] + -tp.alpha * g[k];
+      for (int k = 0; k < 3; ++k) u[k] = -tp.alpha * g[k];
+      const double c[3] = {p0, p1, p2};
+      if (dp.trust && !trust_step(live, can.at(x, y, z), s, x, y, z, c, g, tp.alpha, u)) {
+        atomicMin(rows + ((int64_t)z * dp.ny + y), x);
+      } else {
+        // the update field starts at zero (KillingFusion.cpp:256, 316)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) d[k] = d[k] + u[k];
+      }
       if (!isfinite(p0) || !isfinite(p1) || !isfinite(p2)) st[iter].diverged = 1;
       dn = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     }
@@ -557,6 +568,31 @@ __global__ void __launch_bounds__(kBlock) k_exact_step(PhiView<double> live, Phi
     atomicAdd(&st[iter].active, (unsigned)__popc(ballot));
     atomicMax(&st[iter].max_delta, __float_as_uint(m));
   }
+}
+
+// Trust-region step, after k_exact_step: the voxels of a row from its first
+// failed step on keep their psi (the reference's break out of the x loop,
+// KillingFusion.cpp:312-313).  One warp per row; the warp clears the row's
+// entry for the next iteration.
+__global__ void __launch_bounds__(kBlock) k_exact_trust_rows(const double *__restrict__ ix,
+                                                             const double *__restrict__ iy,
+                                                             const double *__restrict__ iz,
+                                                             double *__restrict__ ox, double *__restrict__ oy,
+                                                             double *__restrict__ oz, int *__restrict__ rows,
+                                                             int nx, int nrows) {
+  const int row = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= nrows) return;
+  const int first = rows[row];
+  if (first >= nx) return;
+  const int64_t base = (int64_t)row * nx;
+  for (int x = first + 1 + lane; x < nx; x += 32) {  // psi + the zero update
+    ox[base + x] = ix[base + x] + 0.0;
+    oy[base + x] = iy[base + x] + 0.0;
+    oz[base + x] = iz[base + x] + 0.0;
+  }
+  __syncwarp();
+  if (lane == 0) rows[row] = kRowClear;
 }
 
 // Reference gradient at a list of voxels (KillingFusion.cpp:399-442).
@@ -675,13 +711,24 @@ int kf_solve_exact(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
   PhiView<double> lv = phi_view<double>(live, live->phi, dp.oob_phi);
   PhiView<double> cv = phi_view<double>(can, can->phi, dp.oob_phi);
   void *buf[2][3] = {{psi->p[0], psi->p[1], psi->p[2]}, {psi->q[0], psi->q[1], psi->q[2]}};
+  int *rows = nullptr;
+  const int nrows = dp.ny * dp.nz;
+  if (dp.trust) {
+    rc = kf_field_trust_rows(psi, &rows);
+    if (rc) return rc;
+    KF_CHECK_CUDA(cudaMemsetAsync(rows, 0x7f, (size_t)nrows * sizeof(int), s));
+  }
   for (int it = 0; it < iterations; ++it) {
     void **in = buf[it & 1], **out = buf[(it + 1) & 1];
     PsiView<double, double> fin{(const double *)in[0], (const double *)in[1],
                                 (const double *)in[2], dp.nx, dp.ny, dp.nz};
     k_exact_step<<<blocks_for(dp.count), kBlock, 0, s>>>(lv, cv, fin, (double *)out[0],
                                                          (double *)out[1], (double *)out[2], dp,
-                                                         st, it);
+                                                         st, it, rows);
+    if (dp.trust)
+      k_exact_trust_rows<<<(unsigned)(((int64_t)nrows * 32 + kBlock - 1) / kBlock), kBlock, 0, s>>>(
+          (const double *)in[0], (const double *)in[1], (const double *)in[2], (double *)out[0],
+          (double *)out[1], (double *)out[2], rows, dp.nx, nrows);
     KF_CHECK_LAUNCH("k_exact_step");
   }
   return KF_OK;

@@ -74,8 +74,9 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
 // wave that loops over the list.  kCarry (band-only solver): the voxels
 // updated here form the next iteration's list (list_out, counted in
 // st[iter+1].list).  kInPlace: the new psi of list entry k goes to entry k
-// of the output planes, for k_fused_scatter to write back.
-template <bool kCarry, bool kInPlace>
+// of the output planes, for k_fused_scatter to write back.  kTrust: the
+// trust-region step (dp.trust), followed by k_trust_fix.
+template <bool kCarry, bool kInPlace, bool kTrust = false>
 __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
                                                              int *__restrict__ list_out) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, con
     int next = -1;  // voxel this group hands to the next iteration
     if (k < nq) {
       const int v = list_in[k];
-      next = update_band_voxel(a, v, kInPlace ? k : v, gl, gmask, maxd, energy, active, diverged);
+      next = update_band_voxel<kTrust>(a, v, kInPlace ? k : v, gl, gmask, maxd, energy, active, diverged);
     }
     if (kCarry) block_append(next, gl == 0, &a.st[a.iter + 1].list, list_out);
   }
@@ -117,6 +118,32 @@ __global__ void __launch_bounds__(kThreads) k_fused_scatter(FusedArgs a, const i
     px[v] = a.ox[k];
     py[v] = a.oy[k];
     pz[v] = a.oz[k];
+  }
+}
+
+// Trust-region step, after the band pass of iteration a.iter: the reference
+// breaks out of a row's x loop at the first voxel whose step failed
+// (KillingFusion.cpp:312-313), so listed voxels at or after that x (a.rows)
+// get their old psi back in the output planes (entry k in place, voxel v
+// ping-pong).  Also clears next_rows, the table of the next band pass.
+__global__ void __launch_bounds__(kThreads) k_trust_fix(FusedArgs a, const int *__restrict__ list, bool in_place,
+                                                       int *__restrict__ next_rows) {
+  const int nrows = a.dp.ny * a.dp.nz;
+  const int stride = gridDim.x * kThreads;
+  const int t0 = blockIdx.x * kThreads + threadIdx.x;
+  for (int r = t0; r < nrows; r += stride) next_rows[r] = kRowClear;
+  if (a.st[a.iter].skipped) return;
+  const int nq = (int)a.st[a.iter].list;
+  for (int k = t0; k < nq; k += stride) {
+    const int v = list[k];
+    int x, y, z;
+    voxel_xyz(a.dp, v, x, y, z);
+    if (x >= a.rows[z * a.dp.ny + y]) {
+      const int slot = in_place ? k : v;
+      a.ox[slot] = a.ix[v];
+      a.oy[slot] = a.iy[v];
+      a.oz[slot] = a.iz[v];
+    }
   }
 }
 
@@ -210,7 +237,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_pervoxel(FusedArgs a, const
 struct FusedGraph {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t capture = nullptr;
-  const void *key_ptr[11] = {};
+  const void *key_ptr[12] = {};
   int iterations = 0;
   bool band_only = false;
   DevParams dp;
@@ -224,8 +251,8 @@ void kf_fused_graph_destroy(FusedGraph *g) {
 }
 
 static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
-                              int iterations, IterStats *st, int *lists, int2 *runs, bool band_only,
-                              cudaStream_t s) {
+                              int iterations, IterStats *st, int *lists, int2 *runs, int *rows,
+                              bool band_only, cudaStream_t s) {
   const unsigned band_blocks = (unsigned)kf_num_sms() * 3;  // one resident wave
   const unsigned grid = (unsigned)std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) /
                                                         (kThreads * kFlatGroups), 1);
@@ -233,6 +260,8 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
   FusedArgs a = make_args(live, can, dp, st);
   void *buf[2][3] = {{psi->p[0], psi->p[1], psi->p[2]}, {psi->q[0], psi->q[1], psi->q[2]}};
   int *lst[2] = {lists, lists + dp.count};
+  const int nrows = dp.ny * dp.nz;
+  if (dp.trust) cudaMemsetAsync(rows, 0x7f, (size_t)nrows * sizeof(int), s);
   for (int it = 0; it < iterations; ++it) {
     // dense: psi stays in the primary planes, the second planes hold the
     // band voxels' new values by list position; band-only: ping-pong
@@ -244,16 +273,28 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
     a.oy = (float *)out[1];
     a.oz = (float *)out[2];
     a.iter = it;
+    a.rows = dp.trust ? rows + (it & 1) * nrows : nullptr;
+    int *next_rows = dp.trust ? rows + ((it + 1) & 1) * nrows : nullptr;
     if (!band_only) {
       // lists alternate so that a run can still read the previous iteration's
       k_fused_stream<false><<<grid, block, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1], runs);
-      k_fused_band<false, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], nullptr);
+      if (dp.trust) {
+        k_fused_band<false, true, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], nullptr);
+        k_trust_fix<<<band_blocks, kThreads, 0, s>>>(a, lst[it & 1], true, next_rows);
+      } else {
+        k_fused_band<false, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], nullptr);
+      }
       if (it == iterations - 1)
         k_fused_scatter<<<band_blocks, kThreads, 0, s>>>(a, lst[it & 1], (float *)in[0], (float *)in[1],
                                                         (float *)in[2]);
     } else {
       if (it == 0) k_fused_stream<true><<<grid, block, 0, s>>>(a, lst[0], nullptr, nullptr);
-      k_fused_band<true, false><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
+      if (dp.trust) {
+        k_fused_band<true, false, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
+        k_trust_fix<<<band_blocks, kThreads, 0, s>>>(a, lst[it & 1], false, next_rows);
+      } else {
+        k_fused_band<true, false><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
+      }
     }
   }
 }
@@ -276,8 +317,13 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
     }
     psi->runs_cap = nruns;
   }
-  const void *key[11] = {live->phi, can->phi, psi->p[0], psi->p[1], psi->p[2],
-                         psi->q[0], psi->q[1], psi->q[2], st, psi->band, psi->runs};
+  int *rows = nullptr;
+  if (dp.trust) {
+    rc = kf_field_trust_rows(psi, &rows);
+    if (rc) return rc;
+  }
+  const void *key[12] = {live->phi, can->phi, psi->p[0], psi->p[1], psi->p[2],
+                         psi->q[0], psi->q[1], psi->q[2], st, psi->band, psi->runs, rows};
   FusedGraph *g = psi->graph;
   bool hit = g && g->iterations == iterations && g->band_only == band_only &&
              memcmp(g->key_ptr, key, sizeof(key)) == 0 && memcmp(&g->dp, &dp, sizeof(dp)) == 0;
@@ -287,7 +333,8 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
     KF_CHECK_CUDA(cudaStreamCreateWithFlags(&g->capture, cudaStreamNonBlocking));
     cudaGraph_t graph;
     KF_CHECK_CUDA(cudaStreamBeginCapture(g->capture, cudaStreamCaptureModeThreadLocal));
-    launch_iterations(live, can, psi, dp, iterations, st, psi->band, psi->runs, band_only, g->capture);
+    launch_iterations(live, can, psi, dp, iterations, st, psi->band, psi->runs, rows, band_only,
+                      g->capture);
     cudaError_t le = cudaGetLastError();
     KF_CHECK_CUDA(cudaStreamEndCapture(g->capture, &graph));
     if (le != cudaSuccess) {
@@ -314,6 +361,7 @@ int kf_solve_pervoxel(kf_grid live, kf_grid can, kf_field psi, const DevParams &
   // place
   DevParams pd = dp;
   pd.early_exit = 0;
+  pd.trust = 0;  // the per-voxel schedule has no trust-region step
   FusedArgs a = make_args(live, can, pd, st);
   a.band_lo = dp.pv_lo_f;
   a.ix = (const float *)psi->p[0];

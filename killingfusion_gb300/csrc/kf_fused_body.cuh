@@ -46,6 +46,7 @@ struct FusedArgs {
   float *__restrict__ oy;
   float *__restrict__ oz;
   IterStats *st;
+  int *rows;  // trust-region step: first failed x per row, this iteration
   int iter;
   DevParams dp;
   // float copies of the parameters
@@ -511,6 +512,36 @@ __device__ __forceinline__ void block_append(int next, bool leader, unsigned *co
 // psi (it left the band in the previous iteration).  Returns the voxel for
 // the next iteration's list (-1 if it left the band); the group leader
 // accumulates the statistics.
+// The trust-region step (KillingFusion.cpp:288-314) for the float solvers:
+// d = -alpha * g (float) on entry, the accepted step on return; false when
+// the step size fell below 1e-7.  The search runs in double, as
+// kfref::trust_step: a float position cannot resolve the steps of 1e-7 * g
+// that the search reaches before it gives up (near x = 64 one float ulp is
+// 7.6e-6 voxel), so in float a step that is too small to move the sample
+// reads as "no worse" and the search would accept where the reference
+// breaks the row.
+__device__ __noinline__ bool trust_step_f(const FusedArgs &a, int x, int y, int z, int64_t i,
+                                          const float c[3], float d[3]) {
+  const DevParams &dp = a.dp;
+  PhiView<double> lv{a.live, dp.nx, dp.ny, dp.nz, dp.oob_phi};
+  const double cd[3] = {c[0], c[1], c[2]};
+  const double prev = phi_sample(lv, ((double)x + cd[0]) + 0.5, ((double)y + cd[1]) + 0.5,
+                                 ((double)z + cd[2]) + 0.5);
+  double g[3], dd[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    g[k] = (double)d[k] / -(double)a.alpha;
+    dd[k] = -dp.alpha * g[k];
+  }
+  const bool ok = trust_step(lv, (double)__ldg(a.can + i), prev, x, y, z, cd, g, dp.alpha, dd);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = (float)dd[k];
+  return ok;
+}
+
+// kTrust: the trust-region step (dp.trust set), a separate instantiation so
+// that the plain band pass carries no call to it.
+template <bool kTrust = false>
 __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int slot, int gl, unsigned gmask,
                                                  float &maxd, float &energy, unsigned &active,
                                                  bool &diverged) {
@@ -532,6 +563,11 @@ __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int 
   if (gl == 0) {
     if (in_band(s, a.band_hi, a.band_lo)) {
       if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
+      if (kTrust && !trust_step_f(a, x, y, z, i, c0, d)) {
+        // this voxel and the rest of its row keep psi (k_trust_fix)
+        atomicMin(a.rows + (z * dp.ny + y), x);
+        d[0] = d[1] = d[2] = 0.f;
+      }
       a.ox[slot] = c0[0] + d[0];
       a.oy[slot] = c0[1] + d[1];
       a.oz[slot] = c0[2] + d[2];

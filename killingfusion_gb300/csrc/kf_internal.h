@@ -47,6 +47,8 @@ struct kf_field_s {
   int *band;              // band-voxel lists (two, of one int per voxel each)
   int2 *runs;             // per run of the dense pass: its entries of the list
   int64_t runs_cap;
+  int *rows;              // trust-region step: the first x of each row (y, z)
+                          // whose step failed, two arrays of ny*nz
 };
 
 // ---------------------------------------------------------------------------
@@ -94,6 +96,9 @@ struct DevParams {
   int use_data, use_levelset, use_killing;
   int early_exit;
   double threshold;
+  int trust;             // the trust-region step applies: use_trust with the
+                         // data term alone (KillingFusion.cpp:289)
+  int pad_;
 };
 
 DevParams kf_make_dev_params(const int n[3], const kf_params *p);
@@ -131,6 +136,11 @@ int kf_field_ensure_pair(kf_field f);
 int kf_field_stats(kf_field f, int iterations, IterStats **dev);
 // two band-voxel lists (one int per voxel of the grid each)
 int kf_field_band_list(kf_field f, int **out);
+// Row table of the trust-region step: two arrays of ny*nz ints.
+int kf_field_trust_rows(kf_field f, int **out);
+// "No step failed in this row": larger than any x; also the value of every
+// byte, so that one memset initialises a table.
+constexpr int kRowClear = 0x7f7f7f7f;
 // free the solver workspace of a field (graph, scratch, statistics)
 void kf_field_release_solver(kf_field f);
 void kf_fused_graph_destroy(FusedGraph *g);

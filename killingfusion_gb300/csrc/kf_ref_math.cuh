@@ -254,6 +254,33 @@ __device__ void energy_gradient(const PhiView<T> &live, const PhiView<T> &can,
   for (int r = 0; r < 3; ++r) out[r] = (dg[r] + kg[r]) + lg[r];
 }
 
+// The trust-region step of the Jacobi sweep (KillingFusion.cpp:288-314),
+// taken with the data term alone.  On entry d = -alpha * g.  While the step
+// does not bring phi_live at ((i + psi(i)) + d) + 0.5 closer to dest =
+// phi_can(i) than prev = phi_live at the voxel's own warped position, the
+// step size a is divided by 1.5 and d = -a * g.  Returns false when a fell
+// below 1e-7: the reference then breaks out of the voxel's x loop, so this
+// voxel and the rest of its row keep their psi for the iteration.
+template <typename T>
+__device__ bool trust_step(const PhiView<T> &live, T dest, T prev, int x, int y, int z, const T c[3],
+                           const T g[3], T alpha, T d[3]) {
+  T a = alpha;
+  bool decreased = false;
+  do {
+    const T s = phi_sample(live, (((T)x + c[0]) + d[0]) + T(0.5), (((T)y + c[1]) + d[1]) + T(0.5),
+                           (((T)z + c[2]) + d[2]) + T(0.5));
+    const T worse = fabs(s - dest) - fabs(prev - dest);
+    if (worse > T(0)) {
+      a /= T(1.5);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) d[k] = -a * g[k];
+    } else {
+      decreased = true;
+    }
+  } while (!decreased && a > T(1e-7));
+  return !(a < T(1e-7));
+}
+
 // Band test of the Jacobi sweep (KillingFusion.cpp:272-274) in T.  The float
 // thresholds are the float neighbours of the double ones that make the float
 // comparison equivalent to comparing the value as a double.

@@ -416,15 +416,55 @@ int orc_is_active(const double *live, const double *psi, const int n[3],
   return 1;
 }
 
+/* The trust-region strategy of the Jacobi sweep (KillingFusion.cpp:288-314),
+ * taken only with the data term alone: while the step d = -a * g does not
+ * bring phi_live at ((i + psi(i)) + d) + 0.5 closer to phi_can(i) than
+ * phi_live at the voxel's own warped position, a /= 1.5.  Returns 1 with the
+ * accepted step in d, or 0 when a fell below 1e-7 (the reference then breaks
+ * out of the voxel's x loop: this voxel and the rest of its row keep their
+ * psi for this iteration). */
+static int trust_step(const double *live, const double *can, const double *psi,
+                      const int n[3], const orc_params *P, int x, int y, int z,
+                      const double g[3], double d[3]) {
+  double a = P->alpha;
+  int decreased = 0;
+  const double dest = orc_phi_at(can, n, P, x, y, z);
+  const double prev = orc_warped_distance(live, psi, n, P, x, y, z);
+  double cur[3];
+  orc_psi_at(psi, n, x, y, z, cur);
+  do {
+    double loc[3];
+    loc[0] = (((double)x + cur[0]) + d[0]) + 0.5;
+    loc[1] = (((double)y + cur[1]) + d[1]) + 0.5;
+    loc[2] = (((double)z + cur[2]) + d[2]) + 0.5;
+    double s = orc_phi_sample(live, n, P, loc);
+    double worse = fabs(s - dest) - fabs(prev - dest);
+    if (worse > 0) {
+      a /= 1.5;
+      for (int k = 0; k < 3; ++k) d[k] = -a * g[k];
+    } else {
+      decreased = 1;
+    }
+  } while (!decreased && a > 1e-7);
+  return !(a < 1e-7);
+}
+
+int orc_trust_active(const orc_params *P) {
+  return P->use_trust && P->use_data && !P->use_levelset && !P->use_killing;
+}
+
 /* KillingFusion::computeDisplacementField, Jacobi schedule
  * (UpdateAllVoxelsInEachIter && UsePreviousIterationDeformationField,
  * KillingFusion.cpp:248-352): every iteration allocates a zero update field,
  * fills it with -alpha*gradient at the voxels inside the band, then adds it
- * to psi. */
+ * to psi.  With P->use_trust and the data term alone, each step goes through
+ * the trust-region strategy (trust_step).  active_counts counts the voxels
+ * inside the band, including those a row break leaves unvisited. */
 int orc_solve_jacobi(const double *live, const double *can, double *psi,
                      const int n[3], const orc_params *P, int iters,
                      int nthreads, int64_t *active_counts) {
   const int64_t N = (int64_t)n[0] * n[1] * n[2];
+  const int trust = orc_trust_active(P);
   int diverged = 0;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -438,13 +478,20 @@ int orc_solve_jacobi(const double *live, const double *can, double *psi,
 #pragma omp parallel for schedule(dynamic) reduction(+ : act) reduction(| : diverged)
     for (int z = 0; z < n[2]; ++z) {
       for (int y = 0; y < n[1]; ++y) {
+        int broken = 0;
         for (int x = 0; x < n[0]; ++x) {
           if (!orc_is_active(live, psi, n, P, x, y, z)) continue;
           ++act;
-          double g[3];
+          if (broken) continue;
+          double g[3], d[3];
           orc_energy_gradient(live, can, psi, n, P, x, y, z, g);
           int64_t i = lin(n, x, y, z);
-          for (int k = 0; k < 3; ++k) delta[3 * i + k] += -P->alpha * g[k];
+          for (int k = 0; k < 3; ++k) d[k] = -P->alpha * g[k];
+          if (trust && !trust_step(live, can, psi, n, P, x, y, z, g, d)) {
+            broken = 1;
+            continue;
+          }
+          for (int k = 0; k < 3; ++k) delta[3 * i + k] += d[k];
           double cur[3];
           orc_psi_at(psi, n, x, y, z, cur);
           if (!isfinite(cur[0]) || !isfinite(cur[1]) || !isfinite(cur[2]))

@@ -44,7 +44,7 @@ typedef struct orc_params {
   int use_data;           /* EnergyTypeUsed[0] (config.cpp:23)           */
   int use_levelset;       /* EnergyTypeUsed[1]                           */
   int use_killing;        /* EnergyTypeUsed[2]                           */
-  int pad_;
+  int use_trust;          /* UseTrustStrategy (config.cpp:27)            */
 } orc_params;
 
 /* ---- samplers (SDF.cpp:475-524, 570-604; DisplacementField.cpp:22-58) ---- */
@@ -105,6 +105,9 @@ int orc_is_active(const double *live, const double *psi, const int n[3],
 int orc_solve_pervoxel(const double *live, const double *can, double *psi,
                        const int n[3], const orc_params *P, int max_iters,
                        int colored, int64_t counts[3]);
+/* 1 when the trust-region strategy applies: use_trust with the data term
+ * alone (KillingFusion.cpp:289). */
+int orc_trust_active(const orc_params *P);
 int orc_solve_jacobi(const double *live, const double *can, double *psi,
                      const int n[3], const orc_params *P, int iters,
                      int nthreads, int64_t *active_counts);

@@ -45,6 +45,7 @@ class Params:
     use_data: bool = True
     use_levelset: bool = True
     use_killing: bool = True
+    use_trust: bool = False
 
     @staticmethod
     def paper(voxel_size: float, trunc_voxels: float = 5.0) -> "Params":
@@ -62,7 +63,7 @@ class _OrcParams(C.Structure):
         "voxel_size", "unknown_clip", "max_surface", "epsilon", "delta_size", "alpha",
         "omega_k", "gamma_k", "omega_s", "threshold", "killing_clamp")] + [
         ("use_data", C.c_int), ("use_levelset", C.c_int), ("use_killing", C.c_int),
-        ("pad_", C.c_int)]
+        ("use_trust", C.c_int)]
 
     @classmethod
     def of(cls, p: Params) -> "_OrcParams":
@@ -303,7 +304,7 @@ def ref_env(P: Params, iterations: int) -> dict:
         "KF_REF_OMEGA_S": repr(P.omega_s), "KF_REF_THRESHOLD": repr(P.threshold),
         "KF_REF_USE_DATA": str(int(P.use_data)), "KF_REF_USE_LEVELSET": str(int(P.use_levelset)),
         "KF_REF_USE_KILLING": str(int(P.use_killing)), "KF_REF_ITERATIONS": str(int(iterations)),
-        "KF_REF_JACOBI": "1",
+        "KF_REF_JACOBI": "1", "KF_REF_TRUST": str(int(P.use_trust)),
     }
 
 

@@ -36,7 +36,7 @@ const bool EnergyTypeUsed[3] = {envi("KF_REF_USE_DATA", 1) != 0,
 const bool UseZeroDisplacementFieldForNextFrame = true;
 const bool UpdateAllVoxelsInEachIter = envi("KF_REF_JACOBI", 1) != 0;
 const bool UsePreviousIterationDeformationField = true;
-const bool UseTrustStrategy = false;
+const bool UseTrustStrategy = envi("KF_REF_TRUST", 0) != 0;
 const double deltaSize = envd("KF_REF_DELTA_SIZE", 0.05);
 const int KILLING_MAX_ITERATIONS = envi("KF_REF_ITERATIONS", 1024);
 const double threshold = envd("KF_REF_THRESHOLD", 0.000001);

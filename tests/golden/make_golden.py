@@ -7,7 +7,7 @@ restatement (oracle/kf_oracle.c) must reproduce every stored output bit for
 bit (tests/test_oracle_golden.py); the fixtures travel where the reference
 checkout does not.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [fixture ...]   (default: all)
 """
 import os
 import sys
@@ -168,9 +168,24 @@ def integrate_small():
     save("integrate_small", **out)
 
 
+def trust_region():
+    """The Jacobi schedule with the trust-region step (UseTrustStrategy,
+    KillingFusion.cpp:288-314), data term alone: 22^3 sphere pair, alpha 0.1,
+    8 iterations.  At the sphere centre's row the step size underflows and
+    the reference breaks out of the row's x loop."""
+    P = Params.paper(0.004).with_(use_levelset=False, use_killing=False, use_trust=True)
+    iters = 8
+    R = RefLib(P, iters)
+    can, live = small_pair(22, P.voxel_size, 5.0, seed=9)
+    can, live = can.astype(np.float64), live.astype(np.float64)
+    st, psi = R.solve(live, can, np.zeros(can.shape + (3,)))
+    assert st == 0
+    save("trust_region", can=can, live=live, iterations=np.array(iters), psi=psi)
+
+
+FIXTURES = {f.__name__: f for f in (linear_selftests, jacobian_killing, two_spheres,
+                                    sphere_pair_small, integrate_small, trust_region)}
+
 if __name__ == "__main__":
-    linear_selftests()
-    jacobian_killing()
-    two_spheres()
-    sphere_pair_small()
-    integrate_small()
+    for name in sys.argv[1:] or list(FIXTURES):
+        FIXTURES[name]()

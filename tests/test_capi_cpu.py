@@ -46,10 +46,25 @@ def test_version_and_params_presets(capi):
     L.kf_params_reference(C.byref(p))
     assert (p.voxel_size, p.alpha, p.omega_k, p.gamma_k, p.omega_s) == (0.012, 0.025, 0.04, 0.0, 0.1)
     assert (p.unknown_clip, p.max_surface, p.delta_size, p.epsilon) == (0.048, 0.048, 0.05, 1e-5)
-    assert p.killing_clamp == 0.1 and p.early_exit == 0
+    assert p.killing_clamp == 0.1 and p.early_exit == 0 and p.use_trust == 0
     L.kf_params_paper(C.byref(p), 0.004, 5.0)
     assert (p.alpha, p.omega_k, p.gamma_k, p.omega_s) == (0.1, 0.5, 0.1, 0.2)
     assert abs(p.unknown_clip - 0.02) < 1e-15
+
+
+def test_params_struct_matches_header(capi):
+    """The ctypes mirror of kf_params has the header's fields, in order and
+    with the same C types."""
+    src = open(os.path.join(ROOT, "include", "killingfusion.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"typedef struct kf_params \{(.*?)\} kf_params;", src, flags=re.S).group(1)
+    fields = []
+    for ctype, names in re.findall(r"(double|int)\s+([^;]+);", body):
+        fields += [(n.strip(), ctype) for n in names.split(",")]
+    mirror = [(n, "double" if t is C.c_double else "int") for n, t in capi._Params._fields_]
+    assert mirror == fields
+    # the Python dataclass carries every field
+    assert set(capi.Params.__dataclass_fields__) == {n for n, _ in fields}
 
 
 def test_mc_table_matches_oracle(capi, oracle):

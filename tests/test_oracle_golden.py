@@ -95,6 +95,33 @@ def test_two_spheres_fixture(oracle):
     np.testing.assert_array_equal(oracle.mesh(fphi, P), g["mesh_fused"])
 
 
+def test_trust_region_fixture(oracle):
+    """The Jacobi schedule with the trust-region step, data term alone
+    (KillingFusion.cpp:288-314): the restatement reproduces the reference's
+    psi, including the row whose step size underflows and whose remaining
+    voxels the reference's break leaves unchanged."""
+    g = load("trust_region")
+    P = Params.paper(0.004).with_(use_levelset=False, use_killing=False, use_trust=True)
+    zero = np.zeros(g["live"].shape + (3,))
+    st, psi = oracle.solve(g["live"], g["can"], zero, int(g["iterations"]), P)
+    assert st == 0
+    np.testing.assert_array_equal(psi, g["psi"])
+    # the fixture exercises the break: band voxels that never moved, all in
+    # rows where an earlier voxel's step failed
+    active = oracle.voxel_query("active", g["live"], g["can"], zero, _all_xyz(g["live"]), P)
+    active = active.reshape(g["live"].shape) > 0
+    still = active & ~np.any(g["psi"] != 0, axis=-1)
+    assert 5 <= still.sum() < 100
+    _, plain = oracle.solve(g["live"], g["can"], zero, int(g["iterations"]), P.with_(use_trust=False))
+    assert np.all(np.any(plain[still] != 0, axis=-1))
+
+
+def _all_xyz(phi):
+    nz, ny, nx = phi.shape
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    return np.stack([x, y, z], -1).reshape(-1, 3).astype(np.int32)
+
+
 def test_sphere_pair_fixture(oracle):
     """Per-voxel gradient terms at a random psi (every band voxel and the
     outer shell, where the reference's index wrap and out-of-grid values

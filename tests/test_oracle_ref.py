@@ -46,6 +46,26 @@ def test_solve_bitexact(oracle, name):
     np.testing.assert_array_equal(p1, p2)
 
 
+@pytest.mark.parametrize("alpha", [0.1, 0.5, 2.0])
+def test_solve_trust_region_bitexact(oracle, alpha):
+    """UseTrustStrategy with the data term alone (KillingFusion.cpp:288-314),
+    including the break out of a row's x loop when the step size underflows."""
+    P = Params.paper(0.004).with_(use_levelset=False, use_killing=False, use_trust=True, alpha=alpha)
+    iters = 5
+    R = RefLib(P, iters)
+    can, live = small_pair(22, P.voxel_size, 5.0, seed=9)
+    st1, p1 = oracle.solve(live, can, np.zeros(live.shape + (3,)), iters, P)
+    st2, p2 = R.solve(live, can, np.zeros(live.shape + (3,)))
+    assert st1 == st2 == 0
+    np.testing.assert_array_equal(p1, p2)
+    # with the level-set or Killing term the reference skips the strategy
+    Pk = P.with_(use_killing=True)
+    st3, p3 = oracle.solve(live, can, np.zeros(live.shape + (3,)), 2, Pk)
+    st4, p4 = RefLib(Pk, 2).solve(live, can, np.zeros(live.shape + (3,)))
+    assert st3 == st4 == 0
+    np.testing.assert_array_equal(p3, p4)
+
+
 def test_warp_fuse_mesh_bitexact(oracle):
     P = PARAMS["paper"]
     R = RefLib(P, 1)
