@@ -505,13 +505,6 @@ __device__ __forceinline__ void block_append(int next, bool leader, unsigned *co
   if (has) list_out[s_wbase[warp] + (unsigned)__popc(ball & ((1u << lane) - 1u))] = next;
 }
 
-// Update one band voxel i with the group of kGroup lanes it is assigned to and
-// write its new psi to entry `slot` of the output planes (slot == i for
-// ping-pong buffers; the voxel's list position for in-place updates).  The
-// voxel is re-tested with its warped value: one outside the band keeps its
-// psi (it left the band in the previous iteration).  Returns the voxel for
-// the next iteration's list (-1 if it left the band); the group leader
-// accumulates the statistics.
 // The trust-region step (KillingFusion.cpp:288-314) for the float solvers:
 // d = -alpha * g (float) on entry, the accepted step on return; false when
 // the step size fell below 1e-7.  The search runs in double, as
@@ -539,6 +532,13 @@ __device__ __noinline__ bool trust_step_f(const FusedArgs &a, int x, int y, int 
   return ok;
 }
 
+// Update one band voxel i with the group of kGroup lanes it is assigned to and
+// write its new psi to entry `slot` of the output planes (slot == i for
+// ping-pong buffers; the voxel's list position for in-place updates).  The
+// voxel is re-tested with its warped value: one outside the band keeps its
+// psi (it left the band in the previous iteration).  Returns the voxel for
+// the next iteration's list (-1 if it left the band); the group leader
+// accumulates the statistics.
 // kTrust: the trust-region step (dp.trust set), a separate instantiation so
 // that the plain band pass carries no call to it.
 template <bool kTrust = false>
