@@ -15,8 +15,10 @@
 //                   work list cut into chunks that never cross a problem: a
 //                   block scans the per-problem chunk counts into a prefix,
 //                   finds each chunk's problem and hands each kGroup-lane
-//                   group one voxel; statistics are gathered per problem in
-//                   shared memory and flushed once per block.
+//                   group one voxel; statistics stay in registers while the
+//                   block works on one problem, are warp-reduced into that
+//                   problem's shared totals when it moves on, and are
+//                   flushed once per block.
 // Each problem converges on its own (params.early_exit): once its previous
 // iteration moved psi by at most params.threshold it is skipped, and its
 // voxels are no longer listed.  The whole loop is captured in one CUDA graph
@@ -146,10 +148,39 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
   const int gl = lane & (kGroup - 1);
   const int group = threadIdx.x / kGroup;
   const unsigned gmask = group_mask(lane);
+  // statistics of the staged problem, per thread until the problem changes
+  float maxd = 0.f;
+  float energy = 0.f;
+  unsigned active = 0;
+  bool diverged = false;
+  // warp sums into the problem's shared totals (c, hence p, is the same in
+  // every thread of the block, so every warp reaches this together)
+  auto flush = [&](int q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      energy += __shfl_xor_sync(0xffffffffu, energy, o);
+      maxd = fmaxf(maxd, __shfl_xor_sync(0xffffffffu, maxd, o));
+      active += __shfl_xor_sync(0xffffffffu, active, o);
+    }
+    const bool any_div = __any_sync(0xffffffffu, diverged);
+    if (lane == 0) {
+      if (active) {
+        atomicAdd(&s_active[q], active);
+        atomicMax(&s_maxd[q], __float_as_uint(maxd));
+        atomicAdd(&s_energy[q], (double)energy);
+      }
+      if (any_div) s_div[q] = 1;
+    }
+    maxd = 0.f;
+    energy = 0.f;
+    active = 0;
+    diverged = false;
+  };
   int cur = -1;  // problem staged in s_a (the same in every thread)
   for (unsigned c = blockIdx.x; c < total; c += gridDim.x) {
     const int p = find_work(s_pre, nprob, c);
     if (p != cur) {
+      if (cur >= 0) flush(cur);
       __syncthreads();  // the previous problem's arguments are no longer read
       const int *src = reinterpret_cast<const int *>(&tab[p].a[par]);
       int *dst = reinterpret_cast<int *>(&s_a);
@@ -164,24 +195,14 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
     const unsigned k = (c - s_pre[p]) * kGroupsPerBlock + group;
     int next = -1;
     if (k < s_cnt[p]) {
-      float maxd = 0.f;
-      float energy = 0.f;
-      unsigned active = 0;
-      bool diverged = false;
       const int v = s_list_in[k];
       next = update_band_voxel(s_a, v, v, gl, gmask, maxd, energy, active, diverged);
-      if (gl == 0) {
-        if (active) {
-          atomicAdd(&s_active[p], active);
-          atomicMax(&s_maxd[p], __float_as_uint(maxd));
-          atomicAdd(&s_energy[p], (double)energy);
-        }
-        if (diverged) s_div[p] = 1;
-      }
     }
     // hand the chunk's updated voxels to the next iteration
     block_append(next, gl == 0, &s_a.st[it + 1].list, s_list_out);
   }
+  if (cur >= 0) flush(cur);
+  __syncthreads();
   for (int q = threadIdx.x; q < nprob; q += blockDim.x) {
     IterStats *st = tab[q].a[par].st + it;
     if (s_active[q]) {
