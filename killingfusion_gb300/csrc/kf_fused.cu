@@ -10,14 +10,13 @@
 //     voxels that have moved gather their 8 corners.  A voxel outside the
 //     band keeps its psi, which therefore need not be written; the voxels
 //     inside are compacted into a list.  16 bytes per voxel.
-//   k_fused_band  evaluates the full gradient of every listed voxel with a
-//     group of kGroup = 4 lanes per voxel (8 voxels per warp): the group loads the 20
-//     psi neighbours of the stencil and shares them by shuffles, takes the 25
-//     warped-SDF samples of the gradient and Hessian plus the warped value
-//     (6-7 independent trilinear gathers per lane), and reduces the nine
-//     derivative sums of +-1-weighted sample differences.  The new psi goes
-//     to a side buffer indexed by list position, so every voxel still reads
-//     its neighbours' old values (Jacobi).
+//   k_fused_band  evaluates the full gradient of every listed voxel, one
+//     thread per voxel (kGroup = 1): the thread loads the 20 psi neighbours
+//     of the stencil per component, takes the 25 warped-SDF samples of the
+//     gradient and Hessian at compile-time offsets plus the warped value (26
+//     independent trilinear gathers), and applies the reference's difference
+//     stencils.  The new psi goes to a side buffer indexed by list position,
+//     so every voxel still reads its neighbours' old values (Jacobi).
 //   The next iteration's dense pass writes the band voxels' new psi back,
 //     each run of voxels its own (k_fused_scatter after the last iteration).
 // The band-only solver (KF_SOLVER_BAND) runs the dense pass once.  A voxel
@@ -77,7 +76,7 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
 // of the output planes, for k_fused_scatter to write back.  kTrust: the
 // trust-region step (dp.trust), followed by k_trust_fix.
 template <bool kCarry, bool kInPlace, bool kTrust = false>
-__global__ void __launch_bounds__(kBandThreads, 3) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
+__global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
                                                              int *__restrict__ list_out) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.iter].skipped = 1;
@@ -158,7 +157,7 @@ __global__ void __launch_bounds__(kThreads) k_trust_fix(FusedArgs a, const int *
 // depend on scheduling.  Statistics: record 0 voxels (list, from the band
 // pass), last step, last monitored energy, divergence; record 1 voxels that
 // hit the cap (active) and the most steps of one voxel (list).
-__global__ void __launch_bounds__(kBandThreads, 3) k_pervoxel(FusedArgs a, const int *__restrict__ list,
+__global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_pervoxel(FusedArgs a, const int *__restrict__ list,
                                                             int max_iters, int color) {
   const int lane = threadIdx.x & 31;
   const int gl = lane & (kGroup - 1);
@@ -183,7 +182,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_pervoxel(FusedArgs a, const
     while (true) {
       float d[3] = {0.f, 0.f, 0.f}, sv = 0.f, e = 0.f, c0[3] = {0.f, 0.f, 0.f};
       if (interior) {
-        gradient_group<true>(a, x, y, z, i, gl, gmask, d, sv, e, c0);
+        gradient_band<true>(a, x, y, z, i, gl, gmask, d, sv, e, c0);
       } else {
         if (gl == 0) {
           gradient_generic(a, x, y, z, d, sv, e);
@@ -206,7 +205,7 @@ __global__ void __launch_bounds__(kBandThreads, 3) k_pervoxel(FusedArgs a, const
       }
       __syncwarp(gmask);
       ++steps;
-      dn = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      dn = sqrtf(ff(d[2], d[2], ff(d[1], d[1], fm(d[0], d[0]))));
       en = e;
       if (dn <= thr) break;
       if (!isfinite(n0) || !isfinite(n1) || !isfinite(n2)) {
@@ -253,7 +252,7 @@ void kf_fused_graph_destroy(FusedGraph *g) {
 static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
                               int iterations, IterStats *st, int *lists, int2 *runs, int *rows,
                               bool band_only, cudaStream_t s) {
-  const unsigned band_blocks = (unsigned)kf_num_sms() * 3;  // one resident wave
+  const unsigned band_blocks = (unsigned)kf_num_sms() * kBandBlocksPerSM;  // one resident wave
   const unsigned grid = (unsigned)std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) /
                                                         (kThreads * kFlatGroups), 1);
   const unsigned block = kThreads;
@@ -375,7 +374,7 @@ int kf_solve_pervoxel(kf_grid live, kf_grid can, kf_field psi, const DevParams &
                                                         (kThreads * kFlatGroups), 1);
   k_fused_stream<false><<<grid, kThreads, 0, s>>>(a, psi->band, nullptr, nullptr);
   for (int color = 0; color < 8; ++color)
-    k_pervoxel<<<(unsigned)kf_num_sms() * 3, kBandThreads, 0, s>>>(a, psi->band, max_iters, color);
+    k_pervoxel<<<(unsigned)kf_num_sms() * kBandBlocksPerSM, kBandThreads, 0, s>>>(a, psi->band, max_iters, color);
   KF_CHECK_LAUNCH("per-voxel solve");
   return KF_OK;
 }
