@@ -46,14 +46,29 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--iters", type=int, default=200)
+    ap.add_argument("--iters", type=int, default=None,
+                    help="psi iterations per frame (default: 200 ellipsoid, 100 sphere, 300 large)")
     ap.add_argument("--solver", default="fused", choices=["fused", "plain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-iters", type=int, default=2, help="Jacobi iterations in the CPU sample")
-    ap.add_argument("--workload", default="ellipsoid", choices=["ellipsoid", "batch", "large"],
-                    help="ellipsoid: 256^3 sequence (the bench line); batch: 64 registration problems of "
-                         "32-160^3, 150 iterations; large: 512^3 capsule sequence, 300 iterations")
-    return ap.parse_args()
+    ap.add_argument("--workload", default="ellipsoid", choices=["ellipsoid", "sphere", "batch", "large"],
+                    help="ellipsoid: 256^3 sequence (the bench line); sphere: the 64^3 two-frame sphere "
+                         "pair, 100 iterations; batch: 64 registration problems of 32-160^3, 150 "
+                         "iterations; large: 512^3 capsule sequence, 300 iterations")
+    args = ap.parse_args()
+    if args.iters is None:
+        args.iters = {"sphere": 100, "large": 300}.get(args.workload, 200)
+    return args
+
+
+def workload_sequence(args):
+    """(sequence, frames in it, max depth, workload name) of the per-frame
+    workloads."""
+    from killingfusion_gb300 import synth
+    if args.workload == "sphere":
+        return synth.SpherePairSequence(), 2, 1.2, "sphere-pair-64"
+    return (synth.EllipsoidSequence(seed=2, frames=30, n=args.size), 30, 1.6,
+            "ellipsoid-sequence-%d" % args.size)
 
 
 def dist_info():
@@ -147,18 +162,19 @@ def run_ours(args, rank, world, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     L = capi.load()
-    seq = synth.EllipsoidSequence(seed=2, frames=30, n=args.size)
+    seq, nseq, max_depth, _ = workload_sequence(args)
     grid = seq.grid
     P = capi.Params.paper(grid.voxel)
     nframes = 1 + args.warmup + args.steps
-    host_frames = [seq.frame(f % 30) for f in range(nframes)]
+    # frame 0 is the canonical frame; the live frames cycle through the rest
+    host_frames = [seq.frame(0 if f == 0 else 1 + (f - 1) % (nseq - 1)) for f in range(nframes)]
     dev_frames = [torch.from_numpy(f).to(dev) for f in host_frames]
     pinned = [torch.from_numpy(f).pin_memory() for f in host_frames]
 
     can = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
     live = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
     psi = capi.Field(grid.dims, capi.KF_F32)
-    can.integrate(dev_frames[0], min_depth=0.05, max_depth=1.6)
+    can.integrate(dev_frames[0], min_depth=0.05, max_depth=max_depth)
     meshes = [torch.empty((MESH_CAP, 9), dtype=torch.float32, device=dev) for _ in range(3)]
     host_mesh = [torch.empty((MESH_CAP, 9), dtype=torch.float32).pin_memory() for _ in range(3)]
     N3 = int(np.prod(grid.dims))
@@ -178,9 +194,9 @@ def run_ours(args, rank, world, local):
             d = depth  # pinned host tensor: the ABI copies it in
             capi.check(L.kf_integrate_depth(live.h, d.data_ptr(), d.shape[1], d.shape[0],
                                             capi._d(np.eye(4).ravel()), capi._d(synth.K.ravel()),
-                                            0.05, 1.6, None))
+                                            0.05, max_depth, None))
         else:
-            live.integrate(depth, min_depth=0.05, max_depth=1.6)
+            live.integrate(depth, min_depth=0.05, max_depth=max_depth)
         psi.zero()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -230,7 +246,7 @@ def run_ours(args, rank, world, local):
     # end to end through the C ABI with host buffers
     can_e2e = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
     capi.check(L.kf_integrate_depth(can_e2e.h, pinned[0].data_ptr(), 640, 480,
-                                    capi._d(np.eye(4).ravel()), capi._d(synth.K.ravel()), 0.05, 1.6,
+                                    capi._d(np.eye(4).ravel()), capi._d(synth.K.ravel()), 0.05, max_depth,
                                     None))
     can, can_e2e = can_e2e, can
     barrier()
@@ -247,7 +263,7 @@ def run_ours(args, rank, world, local):
     # plain per-term solver on the same frame (fewer iterations), for the ratio
     plain_it = 10
     live.reset(P)
-    live.integrate(dev_frames[-1], min_depth=0.05, max_depth=1.6)
+    live.integrate(dev_frames[-1], min_depth=0.05, max_depth=max_depth)
     psi.zero()
     st_plain = capi.psi_solve(live, can_e2e, psi, P, plain_it, "plain" if args.solver == "fused" else "fused")
     other_vups = N3 * plain_it / (st_plain["device_ms"] / 1e3)
@@ -471,7 +487,7 @@ def run_large(args, local):
     }
 
 
-def cpu_sample(seq, P, iters, nthreads=0):
+def cpu_sample(seq, P, iters, max_depth=1.6, nthreads=0):
     """Bounded FP64 sample of one frame on the host cores: integrate, `iters`
     Jacobi iterations, update + fuse, three meshes; extrapolated to the
     frame's full iteration count by the caller."""
@@ -488,10 +504,12 @@ def cpu_sample(seq, P, iters, nthreads=0):
     f1 = seq.frame(1).astype(np.float64)
     base = np.full(n, OP.max_surface + OP.epsilon)
     w0 = np.zeros(n, np.int64)
-    can, wc = O.integrate(base, w0, g.voxel, g.origin, OP.unknown_clip, f0, np.eye(4), synth.K, 0.05, 1.6)
+    can, wc = O.integrate(base, w0, g.voxel, g.origin, OP.unknown_clip, f0, np.eye(4), synth.K, 0.05,
+                          max_depth)
     t = {}
     a = time.perf_counter()
-    live, wl = O.integrate(base, w0, g.voxel, g.origin, OP.unknown_clip, f1, np.eye(4), synth.K, 0.05, 1.6)
+    live, wl = O.integrate(base, w0, g.voxel, g.origin, OP.unknown_clip, f1, np.eye(4), synth.K, 0.05,
+                           max_depth)
     t["integrate"] = time.perf_counter() - a
     a = time.perf_counter()
     st, psi = O.solve(live, can, np.zeros(n + (3,)), iters, OP, nthreads=nthreads)
@@ -504,6 +522,21 @@ def cpu_sample(seq, P, iters, nthreads=0):
     m2 = O.mesh(fphi, OP)
     t["fuse_mesh"] = time.perf_counter() - a
     return t
+
+
+def cpu_sample_iters(args):
+    """Jacobi iterations the CPU sample times: all of them on the small
+    sphere pair, --cpu-iters of the 256^3 frame's 200 (then extrapolated)."""
+    return args.iters if args.workload == "sphere" else args.cpu_iters
+
+
+def cpu_sample_text(args, name, cpu_iters, cores):
+    if cpu_iters == args.iters:
+        return ("one frame of the %s workload: integrate, %d Jacobi iterations, update+fuse, 3 meshes; "
+                "FP64 oracle port on %d threads" % (name, args.iters, cores))
+    return ("one frame of the %s workload: integrate, %d of %d Jacobi iterations, update+fuse, 3 meshes; "
+            "FP64 oracle port on %d threads; frame time extrapolated to %d iterations"
+            % (name, cpu_iters, args.iters, cores, args.iters))
 
 
 def cpu_threads():
@@ -522,7 +555,7 @@ def main():
 
     if args.impl == "reference" and rank != 0:
         return
-    if args.workload != "ellipsoid":
+    if args.workload not in ("ellipsoid", "sphere"):
         if args.impl == "reference":
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "the CPU port is timed on the 256^3 "
@@ -549,30 +582,28 @@ def run_main(args, rank, world, local):
 
     if args.impl == "reference":
         from killingfusion_gb300 import synth
-        seq = synth.EllipsoidSequence(seed=2, frames=30, n=args.size)
+        seq, _, max_depth, name = workload_sequence(args)
         from killingfusion_gb300.capi import Params
         P = Params.paper(seq.grid.voxel)
         N3 = int(np.prod(seq.grid.dims))
         cores = cpu_threads()
+        cpu_iters = cpu_sample_iters(args)
         per = []
         for s in range(args.warmup + args.steps):
-            t = cpu_sample(seq, P, args.cpu_iters)
-            frame_s = t["integrate"] + t["solve"] / args.cpu_iters * args.iters + t["fuse_mesh"]
+            t = cpu_sample(seq, P, cpu_iters, max_depth)
+            frame_s = t["integrate"] + t["solve"] / cpu_iters * args.iters + t["fuse_mesh"]
             if s >= args.warmup:
                 per.append(frame_s)
         frame_s = statistics.mean(per)
         value = N3 * args.iters / frame_s
-        sample = ("one frame of the %d^3 sequence: integrate, %d of %d Jacobi iterations, update+fuse, "
-                  "3 meshes; FP64 oracle port on %d threads; frame time extrapolated to %d iterations"
-                  % (args.size, args.cpu_iters, args.iters, cores, args.iters))
+        sample = cpu_sample_text(args, name, cpu_iters, cores)
         line = {
             "impl": "reference", "metric": METRIC, "value": value, "unit": "voxel-updates/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": frame_s * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "ellipsoid-sequence-%d" % args.size, "grid": [args.size] * 3,
-                       "voxel_mm": 5.0 * 256 / args.size, "iterations_per_frame": args.iters,
-                       "weights": "paper"},
+            "config": {"workload": name, "grid": list(seq.grid.dims), "voxel_mm": seq.grid.voxel * 1e3,
+                       "iterations_per_frame": args.iters, "weights": "paper"},
             "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0,
@@ -616,8 +647,8 @@ def run_main(args, rank, world, local):
         "dtype": "f32",
         "data": "synthetic",
         "config": {
-            "workload": "ellipsoid-sequence-%d" % args.size, "grid": [args.size] * 3,
-            "voxel_mm": 5.0 * 256 / args.size, "iterations_per_frame": args.iters,
+            "workload": workload_sequence(args)[3], "grid": list(seq.grid.dims),
+            "voxel_mm": seq.grid.voxel * 1e3, "iterations_per_frame": args.iters,
             "weights": "paper", "solver": args.solver, "frames": "1 canonical + warmup + steps",
             "step": "one processNextFrame: integrate, zero psi, %d psi iterations, 3 meshes, warp+fuse"
                     % args.iters,
@@ -640,6 +671,11 @@ def run_main(args, rank, world, local):
         "band_voxels": res["active"],
         "triangles_last_frame": res["tris"][-1],
     }
+    if args.workload == "sphere":
+        # 64^3: 4.2 MB of psi and phi per iteration stay in the 129 MB L2
+        line["config"]["l2"] = "inputs fit in L2 (16 B x 64^3 = 4.2 MB per iteration)"
+        line["roofline"] = None
+        line["roofline_note"] = "L2-resident workload: the HBM roofline applies to the 256^3 bench line"
     if args.solver == "fused":
         line["fused_over_plain"] = line["solve_voxel_updates_per_s"] / res["other_vups"]
     frame_other_ms = el / args.steps - solve_ms
@@ -652,13 +688,13 @@ def run_main(args, rank, world, local):
                 "which can only shrink (a voxel outside the band keeps psi)",
     }
     if world == 1 and not args.no_cpu_baseline:
-        t = cpu_sample(seq, P, args.cpu_iters)
-        frame_s = t["integrate"] + t["solve"] / args.cpu_iters * args.iters + t["fuse_mesh"]
+        cpu_iters = cpu_sample_iters(args)
+        t = cpu_sample(seq, P, cpu_iters, workload_sequence(args)[2])
+        frame_s = t["integrate"] + t["solve"] / cpu_iters * args.iters + t["fuse_mesh"]
         line["cpu_baseline"] = {
             "value": N3 * args.iters / frame_s, "unit": "voxel-updates/s", "cores": cpu_threads(),
-            "kind": "port",
-            "sample": "one frame, %d of %d Jacobi iterations timed, frame time extrapolated"
-                      % (args.cpu_iters, args.iters),
+            "kind": "port", "ms_per_frame": frame_s * 1e3,
+            "sample": cpu_sample_text(args, workload_sequence(args)[3], cpu_iters, cpu_threads()),
         }
     print(json.dumps(line))
 

@@ -187,6 +187,18 @@ def sphere_pair(seed: int = 1, sigma: float = 0.001):
     return grid, [f0, f1]
 
 
+class SpherePairSequence:
+    """sphere_pair as a sequence: frame 0 is the canonical sphere, every
+    later frame the moved and stretched one (the small two-frame workload)."""
+
+    def __init__(self, seed: int = 1, sigma: float = 0.001):
+        self.grid, self._frames = sphere_pair(seed, sigma)
+        self.frames = 2
+
+    def frame(self, f: int) -> np.ndarray:
+        return self._frames[0 if f == 0 else 1]
+
+
 class EllipsoidSequence:
     """256^3 / 5 mm: union of 5 ellipsoids bending about a seeded hinge."""
 
