@@ -187,8 +187,13 @@ def run_ours(args, rank, world, local):
     launches_per_frame = 1 + 3 + 2 * args.iters + 1 + 2 + 3 * 3 if args.solver == "fused" else \
         1 + 3 + 7 * args.iters + 2 + 3 * 3
 
+    counts = torch.zeros(3, dtype=torch.int64).pin_memory()  # triangle counts, written by the device
+    Pc = P.c()
+
     def frame(depth, e2e=False):
-        """One processNextFrame: returns (solve event pair, mesh triangle counts, d2h bytes)."""
+        """One processNextFrame, queued without the host waiting in between
+        (kf_psi_solve_async, kf_marching_cubes_async) and waited for once at
+        its end: returns (solve event pair, mesh triangle counts, d2h bytes)."""
         live.reset(P)
         if e2e:
             d = depth  # pinned host tensor: the ABI copies it in
@@ -200,20 +205,26 @@ def run_ours(args, rank, world, local):
         psi.zero()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        st = L.kf_psi_solve(live.h, can.h, psi.h, C.byref(P.c()), args.iters, solver,
-                            C.byref(stats), None)
+        capi.check(L.kf_psi_solve_async(live.h, can.h, psi.h, C.byref(Pc), args.iters, solver, None))
         e1.record(stream)
-        capi.check(st)
-        n0 = mesh_once(capi, L, live, P, meshes[0].data_ptr(), MESH_CAP)
-        capi.check(L.kf_warp_fuse(can.h, live.h, psi.h, C.byref(P.c()), None))
-        n1 = mesh_once(capi, L, live, P, meshes[1].data_ptr(), MESH_CAP)
-        n2 = mesh_once(capi, L, can, P, meshes[2].data_ptr(), MESH_CAP)
+        capi.check(L.kf_marching_cubes_async(live.h, C.byref(Pc), meshes[0].data_ptr(), MESH_CAP,
+                                             counts.data_ptr(), None))
+        capi.check(L.kf_warp_fuse(can.h, live.h, psi.h, C.byref(Pc), None))
+        capi.check(L.kf_marching_cubes_async(live.h, C.byref(Pc), meshes[1].data_ptr(), MESH_CAP,
+                                             counts.data_ptr() + 8, None))
+        capi.check(L.kf_marching_cubes_async(can.h, C.byref(Pc), meshes[2].data_ptr(), MESH_CAP,
+                                             counts.data_ptr() + 16, None))
+        capi.check(L.kf_psi_solve_wait(psi.h, C.byref(stats)))
+        stream.synchronize()
+        n = [int(v) for v in counts.tolist()]
+        if max(n) > MESH_CAP:
+            raise RuntimeError("mesh of %d triangles above the buffers' %d" % (max(n), MESH_CAP))
         d2h = 0
         if e2e:
-            for k, n in enumerate((n0, n1, n2)):
-                host_mesh[k][:n].copy_(meshes[k][:n], non_blocking=True)
-                d2h += n * 36
-        return (e0, e1), (n0, n1, n2), d2h
+            for k in range(3):
+                host_mesh[k][:n[k]].copy_(meshes[k][:n[k]], non_blocking=True)
+                d2h += n[k] * 36
+        return (e0, e1), tuple(n), d2h
 
     def barrier():
         torch.cuda.synchronize(dev)

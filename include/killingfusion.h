@@ -219,6 +219,19 @@ int kf_integrate_depth_u16(kf_grid g, const uint16_t *depth, int width, int heig
 int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
                  int iterations, kf_solver solver, kf_solve_stats *stats, void *stream);
 
+/* kf_psi_solve without waiting (no counterpart in the reference, whose
+ * solve returns when done): queues the solve on `stream` and returns, so
+ * that a frame's later work (meshes, warp + fuse) queues behind it without
+ * the host waiting in between.  psi's planes hold the result for everything
+ * queued after this call.  kf_psi_solve_wait then waits for the solve and
+ * returns its statistics and status (KF_ERR_DIVERGED as kf_psi_solve).
+ * With params.early_exit only KF_SOLVER_FUSED and _PERVOXEL are accepted
+ * (the others alternate two buffers, and which holds psi would depend on the
+ * iterations run).  Only the last solve queued on a field can be waited on. */
+int kf_psi_solve_async(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
+                       int iterations, kf_solver solver, void *stream);
+int kf_psi_solve_wait(kf_field psi, kf_solve_stats *stats);
+
 /* KillingFusion::computeEnergyGradient (KillingFusion.cpp:399-442) at
  * `count` voxels (device int32 xyz triples), in the field's precision;
  * out: device double[count][3].  Also the band test (KillingFusion.cpp:272)
@@ -277,6 +290,14 @@ int kf_fuse_warped(kf_grid dst, kf_grid other, kf_field psi, const kf_params *p,
  * capacity < count. */
 int kf_marching_cubes(kf_grid g, const kf_params *p, float *verts, int64_t capacity,
                       int64_t *ntri, void *stream);
+
+/* kf_marching_cubes without waiting: queues the count, the scan and the
+ * emit pass and returns.  The triangle count is written to *ntri on the
+ * stream (device, pinned host or managed memory; read it after the stream
+ * has passed this call); verts receives the first min(count, capacity)
+ * triangles, and a count above capacity is the caller's to check. */
+int kf_marching_cubes_async(kf_grid g, const kf_params *p, float *verts, int64_t capacity,
+                            int64_t *ntri, void *stream);
 
 /* kf_marching_cubes into host memory (SDF::getMesh for callers without a
  * CUDA runtime of their own): verts is a host buffer of `capacity`

@@ -126,6 +126,8 @@ SIGNATURES = {
     "kf_integrate_depth_u16": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_double,
                                          C.c_double, _vp]),
     "kf_psi_solve": (C.c_int, [_vp, _vp, _vp, _PP, C.c_int, C.c_int, C.POINTER(SolveStats), _vp]),
+    "kf_psi_solve_async": (C.c_int, [_vp, _vp, _vp, _PP, C.c_int, C.c_int, _vp]),
+    "kf_psi_solve_wait": (C.c_int, [_vp, C.POINTER(SolveStats)]),
     "kf_psi_gradient_ref": (C.c_int, [_vp, _vp, _vp, _PP, _vp, C.c_int, _vp, _vp, _vp]),
     "kf_energy": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _ip6, C.c_int, _dp, _vp]),
     "kf_energy_adjoint": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _vp, _vp]),
@@ -139,6 +141,7 @@ SIGNATURES = {
     "kf_warp_fuse": (C.c_int, [_vp, _vp, _vp, _PP, _vp]),
     "kf_fuse_warped": (C.c_int, [_vp, _vp, _vp, _PP, _vp]),
     "kf_marching_cubes": (C.c_int, [_vp, _PP, _vp, C.c_int64, C.POINTER(C.c_int64), _vp]),
+    "kf_marching_cubes_async": (C.c_int, [_vp, _PP, _vp, C.c_int64, _vp, _vp]),
     "kf_marching_cubes_noalloc": (C.c_int, [_vp, _ip3, _PP, _vp, C.c_int64, C.POINTER(C.c_int64),
                                             _vp]),
     "kf_mesh_host": (C.c_int, [_vp, _PP, _vp, C.c_int64, C.POINTER(C.c_int64), _vp]),
@@ -307,6 +310,19 @@ def psi_solve(live: Grid, can: Grid, psi: Field, params: Params, iterations: int
     st = SolveStats()
     check(load().kf_psi_solve(live.h, can.h, psi.h, C.byref(params.c()), int(iterations),
                               SOLVERS[solver], C.byref(st), _stream(stream)))
+    return st.as_dict()
+
+
+def psi_solve_async(live: Grid, can: Grid, psi: Field, params: Params, iterations: int,
+                    solver: str = "fused", stream=None) -> None:
+    """Queue a solve (kf_psi_solve_async); psi_solve_wait reads its stats."""
+    check(load().kf_psi_solve_async(live.h, can.h, psi.h, C.byref(params.c()), int(iterations),
+                                    SOLVERS[solver], _stream(stream)))
+
+
+def psi_solve_wait(psi: Field) -> dict:
+    st = SolveStats()
+    check(load().kf_psi_solve_wait(psi.h, C.byref(st)))
     return st.as_dict()
 
 

@@ -215,6 +215,7 @@ extern "C" int kf_grid_destroy(kf_grid g) {
   cudaFree(g->w_alt);
   cudaFree(g->depth);
   cudaFree(g->integ);
+  cudaFree(g->mc);
   cudaFree(g->ctr);
   delete g;
   return KF_OK;
@@ -349,6 +350,11 @@ void kf_field_release_solver(kf_field f) {
   f->runs_cap = 0;
   cudaFree(f->rows);
   f->rows = nullptr;
+  for (int k = 0; k < 3; ++k) {
+    if (f->ev[k]) cudaEventDestroy(f->ev[k]);
+    f->ev[k] = nullptr;
+  }
+  f->pending = 0;
   f->band = nullptr;
   cudaFree(f->stats);
   cudaFreeHost(f->stats_host);
@@ -600,6 +606,22 @@ extern "C" int kf_marching_cubes(kf_grid g, const kf_params *p, float *verts, in
   return kf_mc_run(g, dp, verts, capacity, ntri, kf_stream(stream));
 }
 
+extern "C" int kf_marching_cubes_async(kf_grid g, const kf_params *p, float *verts, int64_t capacity,
+                                       int64_t *ntri, void *stream) {
+  KF_REQUIRE(g && ntri, "NULL argument");
+  KF_REQUIRE(capacity >= 0, "capacity must be >= 0");
+  cudaPointerAttributes at;
+  KF_REQUIRE(cudaPointerGetAttributes(&at, ntri) == cudaSuccess &&
+                 (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeHost ||
+                  at.type == cudaMemoryTypeManaged),
+             "ntri must be device, pinned host or managed memory");
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  DevParams dp = kf_make_dev_params(g->n, p);
+  int64_t unused = 0;
+  return kf_mc_run(g, dp, verts, capacity, &unused, kf_stream(stream), ntri);
+}
+
 extern "C" int kf_mesh_host(kf_grid g, const kf_params *p, float *verts, int64_t capacity,
                             int64_t *ntri, void *stream) {
   KF_REQUIRE(g && ntri, "NULL argument");
@@ -630,9 +652,11 @@ extern "C" int kf_mesh_host(kf_grid g, const kf_params *p, float *verts, int64_t
 // ---------------------------------------------------------------------------
 // psi solve
 // ---------------------------------------------------------------------------
-extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
-                            int iterations, kf_solver solver, kf_solve_stats *stats,
-                            void *stream) {
+// Queues a solve and the copy of its statistics to the field's pinned
+// mirror; *launched = 0 when there was nothing to queue (iterations == 0).
+static int solve_launch(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p, int iterations,
+                        kf_solver solver, cudaStream_t s, int *launched) {
+  *launched = 0;
   KF_REQUIRE(live && canonical && psi, "NULL argument");
   KF_REQUIRE(live != canonical, "live and canonical must differ");
   KF_REQUIRE(same_dims(live->n, canonical->n) && same_dims(live->n, psi->n), "sizes differ");
@@ -647,19 +671,16 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
   KF_REQUIRE(!(p->use_trust && p->use_data && !p->use_levelset && !p->use_killing &&
                solver == KF_SOLVER_PLAIN),
              "the trust-region step (use_trust) runs in KF_SOLVER_FUSED, _BAND and _EXACT, not _PLAIN");
-  if (stats) memset(stats, 0, sizeof(*stats));
   if (iterations == 0) return KF_OK;
-  cudaStream_t s = kf_stream(stream);
   DevParams dp = kf_make_dev_params(live->n, p);
   IterStats *st = nullptr;
   // one extra record: the band solver counts the next iteration's list there
   rc = kf_field_stats(psi, iterations + 1, &st);
   if (rc) return rc;
   KF_CHECK_CUDA(cudaMemsetAsync(st, 0, sizeof(IterStats) * (iterations + 1), s));
-  cudaEvent_t e0, e1;
-  KF_CHECK_CUDA(cudaEventCreate(&e0));
-  KF_CHECK_CUDA(cudaEventCreate(&e1));
-  KF_CHECK_CUDA(cudaEventRecord(e0, s));
+  for (int k = 0; k < 3; ++k)
+    if (!psi->ev[k]) KF_CHECK_CUDA(cudaEventCreate(&psi->ev[k]));
+  KF_CHECK_CUDA(cudaEventRecord(psi->ev[0], s));
   if (solver == KF_SOLVER_PERVOXEL)
     rc = kf_solve_pervoxel(live, canonical, psi, dp, iterations, st, s);
   else if (solver == KF_SOLVER_FUSED || solver == KF_SOLVER_BAND)
@@ -668,19 +689,29 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
     rc = kf_solve_plain(live, canonical, psi, dp, iterations, st, s);
   else
     rc = kf_solve_exact(live, canonical, psi, dp, iterations, st, s);
-  if (rc) {
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    return rc;
-  }
-  KF_CHECK_CUDA(cudaEventRecord(e1, s));
-  IterStats *host = psi->stats_host;
-  KF_CHECK_CUDA(cudaMemcpyAsync(host, st, sizeof(IterStats) * (iterations + 1), cudaMemcpyDeviceToHost, s));
-  KF_CHECK_CUDA(cudaStreamSynchronize(s));
+  if (rc) return rc;
+  KF_CHECK_CUDA(cudaEventRecord(psi->ev[1], s));
+  KF_CHECK_CUDA(cudaMemcpyAsync(psi->stats_host, st, sizeof(IterStats) * (iterations + 1),
+                                cudaMemcpyDeviceToHost, s));
+  KF_CHECK_CUDA(cudaEventRecord(psi->ev[2], s));
+  psi->last_iterations = iterations;
+  psi->last_solver = solver;
+  psi->pending = 1;
+  *launched = 1;
+  return KF_OK;
+}
+
+// Waits for the statistics of the last solve launched on psi and reads
+// them.  presumed_swapped: the buffers were exchanged at launch on the
+// assumption that every iteration runs (kf_psi_solve_async).
+static int solve_finish(kf_field psi, kf_solve_stats *stats, bool presumed_swapped) {
+  KF_CHECK_CUDA(cudaEventSynchronize(psi->ev[2]));
+  psi->pending = 0;
+  const IterStats *host = psi->stats_host;
+  const int iterations = psi->last_iterations;
+  const kf_solver solver = psi->last_solver;
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  cudaEventElapsedTime(&ms, psi->ev[0], psi->ev[1]);
   if (solver == KF_SOLVER_PERVOXEL) {
     // record 0: voxels visited (list), their last monitored energy and
     // step, divergence; record 1: voxels that hit the cap (active), most
@@ -716,7 +747,7 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
   // Iteration k reads buffer k%2 and writes (k+1)%2 (the dense fused solver
   // updates in place); a diverged iteration still wrote its output.  Put
   // the result into the primary planes.
-  if (solver != KF_SOLVER_FUSED && (executed & 1))
+  if (solver != KF_SOLVER_FUSED && !presumed_swapped && (executed & 1))
     for (int k = 0; k < 3; ++k) {
       void *t = psi->p[k];
       psi->p[k] = psi->q[k];
@@ -741,4 +772,45 @@ extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const
   if (diverged)
     return kf_fail(KF_ERR_DIVERGED, "deformation field diverged (non-finite psi inside the band)");
   return KF_OK;
+}
+
+extern "C" int kf_psi_solve(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
+                            int iterations, kf_solver solver, kf_solve_stats *stats,
+                            void *stream) {
+  if (stats) memset(stats, 0, sizeof(*stats));
+  int launched = 0;
+  int rc = solve_launch(live, canonical, psi, p, iterations, solver, kf_stream(stream), &launched);
+  if (rc || !launched) return rc;
+  return solve_finish(psi, stats, false);
+}
+
+extern "C" int kf_psi_solve_async(kf_grid live, kf_grid canonical, kf_field psi, const kf_params *p,
+                                  int iterations, kf_solver solver, void *stream) {
+  KF_REQUIRE(p, "params is NULL");
+  KF_REQUIRE(!(p->early_exit && solver != KF_SOLVER_FUSED && solver != KF_SOLVER_PERVOXEL),
+             "kf_psi_solve_async with early_exit needs KF_SOLVER_FUSED or _PERVOXEL (the other solvers "
+             "alternate two buffers, and which one holds psi depends on the iterations run)");
+  int launched = 0;
+  int rc = solve_launch(live, canonical, psi, p, iterations, solver, kf_stream(stream), &launched);
+  if (rc || !launched) return rc;
+  // every iteration runs (no early exit): psi ends in buffer iterations % 2
+  if (solver != KF_SOLVER_FUSED && solver != KF_SOLVER_PERVOXEL && (iterations & 1))
+    for (int k = 0; k < 3; ++k) {
+      void *t = psi->p[k];
+      psi->p[k] = psi->q[k];
+      psi->q[k] = t;
+    }
+  psi->pending = 2;  // 2: launched by kf_psi_solve_async
+  return KF_OK;
+}
+
+extern "C" int kf_psi_solve_wait(kf_field psi, kf_solve_stats *stats) {
+  KF_REQUIRE(psi, "NULL argument");
+  if (stats) memset(stats, 0, sizeof(*stats));
+  KF_REQUIRE(psi->pending == 2, "no kf_psi_solve_async pending on this field");
+  int rc = solve_finish(psi, stats, true);
+  if (rc == KF_OK && psi->last_solver != KF_SOLVER_FUSED && psi->last_solver != KF_SOLVER_PERVOXEL &&
+      stats && stats->iterations_run != psi->last_iterations)
+    return kf_fail(KF_ERR_INVALID, "an asynchronous solve stopped early; psi is in the other buffer");
+  return rc;
 }

@@ -143,8 +143,19 @@ extern "C" int kf_fusion_process_frame(kf_fusion f, const float *depth, const do
     if (!rc) rc = kf_integrate_depth(f->live, depth, c.width, c.height, pose, c.K, c.min_depth,
                                      c.max_depth, s);
     if (!rc) rc = kf_field_zero(f->psi, s);
-    if (!rc) rc = kf_psi_solve(f->live, f->can, f->psi, p, c.iterations, c.solver, &r.solve, stream);
+    // the live mesh queues behind the solve without the host waiting in
+    // between; the solve's status is read before warp + fuse changes the
+    // canonical SDF, so a diverged solve leaves it untouched, as the
+    // reference's throw does
+    const bool async = !(p->early_exit && c.solver != KF_SOLVER_FUSED && c.solver != KF_SOLVER_PERVOXEL);
+    if (!rc)
+      rc = async ? kf_psi_solve_async(f->live, f->can, f->psi, p, c.iterations, c.solver, stream)
+                 : kf_psi_solve(f->live, f->can, f->psi, p, c.iterations, c.solver, &r.solve, stream);
     if (!rc && (meshes & KF_MESH_LIVE)) rc = mesh_to_host(f, f->live, 0, &r.ntri[0], s);
+    if (async && c.iterations > 0) {
+      const int wrc = kf_psi_solve_wait(f->psi, &r.solve);
+      if (!rc) rc = wrc;
+    }
     if (!rc) rc = kf_warp_fuse(f->can, f->live, f->psi, p, s);
     if (!rc && (meshes & KF_MESH_REGISTERED)) rc = mesh_to_host(f, f->live, 1, &r.ntri[1], s);
   }

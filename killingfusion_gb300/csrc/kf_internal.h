@@ -26,6 +26,8 @@ struct kf_grid_s {
   void *integ;     // integration scratch: counter, coordinate tables, list
   size_t integ_bytes;
   unsigned *ctr;   // device counter of the warp's moved-voxel list
+  void *mc;        // marching-cubes scratch: offsets, per-block totals and masks
+  size_t mc_bytes;
 };
 
 struct IterStats;
@@ -49,6 +51,13 @@ struct kf_field_s {
   int64_t runs_cap;
   int *rows;              // trust-region step: the first x of each row (y, z)
                           // whose step failed, two arrays of ny*nz
+  // the last solve launched on this field: its events (start, end, end of
+  // the statistics copy), iteration count, solver and whether its statistics
+  // are still to be read (kf_psi_solve_wait)
+  cudaEvent_t ev[3];
+  int last_iterations;
+  kf_solver last_solver;
+  int pending;
 };
 
 // ---------------------------------------------------------------------------
@@ -166,4 +175,4 @@ int kf_launch_fuse_warped(kf_grid dst, kf_grid other, kf_field psi, const DevPar
                           cudaStream_t s);
 // marching cubes (kf_mc.cu)
 int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, int64_t *ntri,
-              cudaStream_t s);
+              cudaStream_t s, int64_t *ntri_async = nullptr);

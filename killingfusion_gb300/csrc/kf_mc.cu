@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -143,7 +144,12 @@ __device__ T block_exclusive_scan(T v, T *total) {
   return prefix;
 }
 
-__global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block_tris) {
+// Words of the per-block mask of cells with triangles: one per warp and
+// round, bit t for the warp's lane t.
+constexpr int kMaskWords = kRounds * (kThreads / 32);
+
+template <bool kMask>
+__global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block_tris, uint32_t *mask) {
   const int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + threadIdx.x;
   float d[kRounds];
 #pragma unroll
@@ -153,7 +159,13 @@ __global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block
   for (int r = 0; r < kRounds; ++r) {
     int x, y, z;
     float val[8];
-    n += cube_tris(classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val));
+    const int c = cube_tris(classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val));
+    n += c;
+    if (kMask) {
+      const uint32_t ball = __ballot_sync(0xffffffffu, c != 0);
+      if ((threadIdx.x & 31) == 0)
+        mask[(int64_t)blockIdx.x * kMaskWords + r * (kThreads / 32) + (threadIdx.x >> 5)] = ball;
+    }
   }
   uint32_t total;
   block_exclusive_scan<uint32_t>(n, &total);
@@ -161,31 +173,83 @@ __global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block
 }
 
 // Exclusive scan of the per-block totals into 64-bit offsets (one CTA), a
-// chunk of kScanChunk totals per step: each thread sums kScanPerThread
-// consecutive totals, the block scans the sums, each thread writes its
-// offsets.
+// chunk of kScanChunk totals at a time: the chunk is staged in shared memory
+// with coalesced loads (padded by one word per 32, so that thread t's
+// kScanPerThread consecutive totals sit in distinct banks), each thread
+// sums its totals, the block scans the sums, and each thread writes its
+// offsets.  With `nonempty` it also lists the blocks that have triangles,
+// in order: the triangle count and a has-triangles flag travel in one
+// 64-bit scan (count << 24 | flag; fewer than 2^24 blocks).
 __global__ void __launch_bounds__(kThreads) k_mc_scan(const uint32_t *block_tris, int64_t nblocks,
-                                                      int64_t *block_off, int64_t *grand_total) {
-  int64_t carry = 0;
+                                                      int64_t *block_off, int64_t *grand_total,
+                                                      int *nonempty, int *n_nonempty) {
+  __shared__ uint32_t s_v[kScanChunk + kScanChunk / 32];
+  uint64_t carry = 0;
   for (int64_t c0 = 0; c0 < nblocks; c0 += kScanChunk) {
-    const int64_t b0 = c0 + (int64_t)threadIdx.x * kScanPerThread;
-    uint32_t v[kScanPerThread];
-    int64_t s = 0;
+    const int64_t n = nblocks - c0 < kScanChunk ? nblocks - c0 : kScanChunk;
+    for (int i = threadIdx.x; i < kScanChunk; i += kThreads) s_v[i + (i >> 5)] = i < n ? block_tris[c0 + i] : 0u;
+    __syncthreads();
+    const int first = threadIdx.x * kScanPerThread;
+    uint64_t sum = 0;
 #pragma unroll
     for (int j = 0; j < kScanPerThread; ++j) {
-      v[j] = b0 + j < nblocks ? block_tris[b0 + j] : 0u;
-      s += v[j];
+      const uint32_t v = s_v[first + j + ((first + j) >> 5)];
+      sum += ((uint64_t)v << 24) | (uint64_t)(v != 0);
     }
-    int64_t total;
-    int64_t off = carry + block_exclusive_scan<int64_t>(s, &total);
+    uint64_t total;
+    uint64_t excl = carry + block_exclusive_scan<uint64_t>(sum, &total);
 #pragma unroll
     for (int j = 0; j < kScanPerThread; ++j) {
-      if (b0 + j < nblocks) block_off[b0 + j] = off;
-      off += v[j];
+      const int i = first + j;
+      const uint32_t v = s_v[i + (i >> 5)];
+      if (i < n) {
+        block_off[c0 + i] = (int64_t)(excl >> 24);
+        if (nonempty && v) nonempty[excl & 0xffffffu] = (int)(c0 + i);
+      }
+      excl += ((uint64_t)v << 24) | (uint64_t)(v != 0);
     }
     carry += total;
+    __syncthreads();  // the chunk is read before the next one is staged
   }
-  if (threadIdx.x == 0) *grand_total = carry;
+  if (threadIdx.x == 0) {
+    *grand_total = (int64_t)(carry >> 24);
+    if (n_nonempty) *n_nonempty = (int)(carry & 0xffffffu);
+  }
+}
+
+// Exclusive prefix over the block of K values per thread at once, and the K
+// block totals; every thread calls it.
+template <int K>
+__device__ __forceinline__ void block_scan_vec(const uint32_t v[K], uint32_t excl[K], uint32_t tot[K]) {
+  __shared__ uint32_t s_w[kThreads / 32][K];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t inc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) inc[k] = v[k];
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc[k], o);
+      if (lane >= o) inc[k] += t;
+    }
+  if (lane == 31)
+#pragma unroll
+    for (int k = 0; k < K; ++k) s_w[wid][k] = inc[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    uint32_t before = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+      const uint32_t x = s_w[w][k];
+      if (w < wid) before += x;
+      all += x;
+    }
+    excl[k] = before + inc[k] - v[k];
+    tot[k] = all;
+  }
+  __syncthreads();  // s_w is free for the next call
 }
 
 __device__ __forceinline__ void vinterp(const float p1[3], const float p2[3], float v1, float v2,
@@ -229,21 +293,36 @@ __device__ __noinline__ void emit_cell(const McGrid &g, int64_t i, int cube, int
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *block_off,
-                                                      float *__restrict__ verts, int64_t capacity) {
-  int64_t out0 = block_off[blockIdx.x];
-  const int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + threadIdx.x;
+// The triangles of cell block b (cells b*kCellsPerBlock + r*kThreads + t),
+// from position out0 on.  kMask: mask holds k_mc_count's cells with
+// triangles and only those gather their corners; otherwise every cell is
+// classified again.
+template <bool kMask>
+__device__ __forceinline__ void emit_block(const McGrid &g, int64_t b, int64_t out0,
+                                           const uint32_t *__restrict__ mask, float *__restrict__ verts,
+                                           int64_t capacity) {
+  const int64_t base = b * kCellsPerBlock + threadIdx.x;
   // classify every round first (the loads in flight together), then scan
   // and emit the rounds that have triangles
   float d[kRounds];
+  bool has[kRounds];
 #pragma unroll
-  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, base + (int64_t)r * kThreads);
+  for (int r = 0; r < kRounds; ++r) {
+    if (kMask) {
+      const uint32_t w = __ldg(mask + b * kMaskWords + r * (kThreads / 32) + (threadIdx.x >> 5));
+      has[r] = (w >> (threadIdx.x & 31)) & 1u;
+      d[r] = has[r] ? __ldg(g.phi + base + (int64_t)r * kThreads) : g.hi + 1.0f;
+    } else {
+      has[r] = true;
+      d[r] = own_value(g, base + (int64_t)r * kThreads);
+    }
+  }
   int cube[kRounds];
 #pragma unroll
   for (int r = 0; r < kRounds; ++r) {
     int x, y, z;
     float val[8];
-    cube[r] = classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val);
+    cube[r] = has[r] ? classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val) : -1;
   }
 #pragma unroll
   for (int r = 0; r < kRounds; ++r) {
@@ -256,10 +335,65 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *b
   }
 }
 
+// Every cell block, one CTA each.
+__global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *block_off,
+                                                      float *__restrict__ verts, int64_t capacity) {
+  emit_block<false>(g, blockIdx.x, block_off[blockIdx.x], nullptr, verts, capacity);
+}
+
+// Only the blocks with triangles (k_mc_scan's list), a resident grid of CTAs
+// looping over them.  A block's cells with triangles (k_mc_count's mask)
+// gather their corners together, one scan orders the triangles of all its
+// rounds at once, and each cell then writes its own.
+__global__ void __launch_bounds__(kThreads) k_mc_emit_listed(McGrid g, const int64_t *block_off,
+                                                             const int *__restrict__ nonempty,
+                                                             const int *__restrict__ n_nonempty,
+                                                             const uint32_t *__restrict__ mask,
+                                                             float *__restrict__ verts, int64_t capacity) {
+  const int n = *n_nonempty;
+  for (int e = blockIdx.x; e < n; e += gridDim.x) {
+    const int64_t b = nonempty[e];
+    const int64_t base = b * kCellsPerBlock + threadIdx.x;
+    bool has[kRounds];
+    float d[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      const uint32_t w = __ldg(mask + b * kMaskWords + r * (kThreads / 32) + (threadIdx.x >> 5));
+      has[r] = (w >> (threadIdx.x & 31)) & 1u;
+      d[r] = has[r] ? __ldg(g.phi + base + (int64_t)r * kThreads) : g.hi + 1.0f;
+    }
+    int cube[kRounds];
+    uint32_t nt[kRounds], pre[kRounds], tot[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      int x, y, z;
+      float val[8];
+      cube[r] = has[r] ? classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val) : -1;
+      nt[r] = (uint32_t)cube_tris(cube[r]);
+    }
+    block_scan_vec<kRounds>(nt, pre, tot);
+    int64_t out = block_off[b];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      if (nt[r]) emit_cell(g, base + (int64_t)r * kThreads, cube[r], out + pre[r], verts, capacity);
+      out += tot[r];
+    }
+  }
+}
+
+// Resident CTAs of the listed emit pass (at most one per cell block).
+unsigned emit_grid(int64_t nblocks) {
+  return (unsigned)std::min<int64_t>(nblocks, (int64_t)kf_num_sms() * 8);
+}
+
 }  // namespace
 
+// ntri_async == NULL: waits for the count, returns it in *ntri and launches
+// the emit pass only when there are triangles.  Otherwise nothing waits: the
+// count is copied to ntri_async (device or pinned host memory) and the emit
+// pass writes the first `capacity` triangles.
 int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, int64_t *ntri,
-              cudaStream_t s) {
+              cudaStream_t s, int64_t *ntri_async) {
   McGrid mg;
   mg.phi = g->phi;
   mg.nx = g->n[0];
@@ -273,16 +407,39 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   mg.hy = (float)g->n[1] / 2.0f;
   mg.hz = (float)g->n[2] / 2.0f;
   int64_t nblocks = (g->count + kCellsPerBlock - 1) / kCellsPerBlock;
-  // scratch: per-block totals (u32), offsets (i64), grand total (i64)
-  size_t bytes = nblocks * sizeof(uint32_t) + (nblocks + 1) * sizeof(int64_t) + 16;
-  char *scratch = nullptr;
-  KF_CHECK_CUDA(cudaMallocAsync((void **)&scratch, bytes, s));
-  int64_t *off = (int64_t *)(((uintptr_t)scratch + 15) & ~(uintptr_t)15);
+  // scratch, kept with the grid (calls on one grid are stream-ordered):
+  // offsets (i64) and the grand total right after them, the per-block totals
+  // (u32) and the masks of cells with triangles (u32)
+  const size_t bytes = (nblocks + 1) * sizeof(int64_t) + nblocks * sizeof(uint32_t) * (2 + kMaskWords) + 16;
+  if (g->mc_bytes < bytes) {
+    cudaFree(g->mc);
+    g->mc = nullptr;
+    g->mc_bytes = 0;
+    if (cudaMalloc(&g->mc, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      g->mc = nullptr;
+      return kf_fail(KF_ERR_OOM, "cudaMalloc of the marching-cubes scratch failed");
+    }
+    g->mc_bytes = bytes;
+  }
+  int64_t *off = (int64_t *)g->mc;
   int64_t *total_dev = off + nblocks;
   uint32_t *tris = (uint32_t *)(total_dev + 1);
-  k_mc_count<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris);
-  k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev);
+  uint32_t *mask = tris + nblocks;
+  int *nonempty = (int *)(mask + nblocks * kMaskWords);
+  int *n_nonempty = nonempty + nblocks;
+  k_mc_count<true><<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris, mask);
+  k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev, nonempty, n_nonempty);
   KF_CHECK_LAUNCH("k_mc_count/k_mc_scan");
+  if (ntri_async) {
+    KF_CHECK_CUDA(cudaMemcpyAsync(ntri_async, total_dev, sizeof(int64_t), cudaMemcpyDefault, s));
+    if (verts && capacity > 0) {
+      k_mc_emit_listed<<<emit_grid(nblocks), kThreads, 0, s>>>(mg, off, nonempty, n_nonempty, mask, verts,
+                                                              capacity);
+      KF_CHECK_LAUNCH("k_mc_emit_listed");
+    }
+    return KF_OK;
+  }
   // wait for the count only; the emit pass runs on while the caller queues
   // its next work
   int64_t total = 0;
@@ -290,10 +447,10 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   KF_CHECK_CUDA(cudaStreamSynchronize(s));
   *ntri = total;
   if (verts && total > 0 && capacity > 0) {
-    k_mc_emit<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, off, verts, capacity);
-    KF_CHECK_LAUNCH("k_mc_emit");
+    k_mc_emit_listed<<<emit_grid(nblocks), kThreads, 0, s>>>(mg, off, nonempty, n_nonempty, mask, verts,
+                                                            capacity);
+    KF_CHECK_LAUNCH("k_mc_emit_listed");
   }
-  KF_CHECK_CUDA(cudaFreeAsync(scratch, s));
   if (verts && capacity < total)
     return kf_fail(KF_ERR_CAPACITY, "vertex buffer holds fewer triangles than the mesh has");
   return KF_OK;
@@ -377,9 +534,10 @@ extern "C" int kf_marching_cubes_noalloc(const float *phi, const int dims[3], co
   // Every word read below is written earlier in this call; the grand total is
   // cleared anyway so a failed launch cannot report a previous call's count.
   KF_CHECK_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(int64_t), s));
-  k_mc_count<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris);
-  k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev);
-  if (verts && capacity > 0) k_mc_emit<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, off, verts, capacity);
+  k_mc_count<false><<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris, nullptr);
+  k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev, nullptr, nullptr);
+  if (verts && capacity > 0)
+    k_mc_emit<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, off, verts, capacity);
   KF_CHECK_LAUNCH("kf_marching_cubes_noalloc kernels");
   int64_t total = 0;
   KF_CHECK_CUDA(cudaMemcpyAsync(&total, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s));

@@ -42,6 +42,13 @@ static int run_spheres(int argc, char **argv) {
   std::string out = std::string(argv[2]) + "/";
   kf::config().solver = solver_of(argv[3]);
   kf::config().KILLING_MAX_ITERATIONS = std::atoi(argv[4]);
+  if (argc > 5 && !std::strcmp(argv[5], "trust")) {
+    // the data term alone with the trust-region step (config.cpp:23, 27)
+    kf::Config &c = kf::config();
+    c.EnergyTypeUsed[1] = c.EnergyTypeUsed[2] = false;
+    c.UseTrustStrategy = true;
+    c.alpha = std::atof(argv[6]);
+  }
   SDF::outputDir() = out;
   KillingFusion fusion{DatasetReader(out + "dataset")};
   fusion.processTest(1);

@@ -123,6 +123,29 @@ def test_process_test_spheres(driver, oracle, tmp_path):
     np.testing.assert_allclose(merged, gold["fused_phi"], atol=1e-6)
 
 
+def test_process_test_spheres_trust_region(driver, oracle, tmp_path):
+    """kf::Config's UseTrustStrategy with the data term alone reaches the
+    solver: processTest(3) registers with the trust-region step
+    (KillingFusion.cpp:288-314), bit for bit with the oracle, and differs
+    from the plain data-term step."""
+    gold = np.load(os.path.join(HERE, "golden", "two_spheres.npz"))
+    iters, alpha = 40, 0.5
+    K = np.array(synth.K)
+    synth.write_dataset(str(tmp_path / "dataset"), [np.zeros((48, 64), np.float32)], K, 0.3, 0.5)
+    driver("spheres", tmp_path, "exact", iters, "trust", alpha)
+    P = OParams().with_(use_levelset=False, use_killing=False, use_trust=True, alpha=alpha)
+    phi0, w0 = f32(gold["phi0"]), gold["w0"]
+    phi1, w1 = f32(gold["phi1"]), gold["w1"]
+    st, psi = oracle.solve(phi1, phi0, np.zeros(phi0.shape + (3,)), iters, P)
+    assert st == 0
+    fphi, _ = oracle.fuse_psi(phi0, w0, phi1, w1, psi, P)
+    merged = read_sdf_bin(tmp_path / "testType-2-outputSphere1MergedTo0UsingKilling.bin")[2]
+    np.testing.assert_array_equal(merged, f32(fphi))
+    _, plain = oracle.solve(phi1, phi0, np.zeros(phi0.shape + (3,)), iters, P.with_(use_trust=False))
+    pphi, _ = oracle.fuse_psi(phi0, w0, phi1, w1, plain, P)
+    assert np.any(f32(pphi) != merged)
+
+
 def small_camera_frames(n_frames=3, seed=4):
     """A 64x48 camera (f = 52.5 px) looking at a sphere that moves and
     stretches along x, float32 metres."""
