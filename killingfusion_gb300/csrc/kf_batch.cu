@@ -14,8 +14,8 @@
 //   k_batch_band    per iteration, the band voxels of all problems as one
 //                   work list cut into chunks that never cross a problem: a
 //                   block scans the per-problem chunk counts into a prefix,
-//                   finds each chunk's problem and hands each kGroup-lane
-//                   group one voxel; statistics stay in registers while the
+//                   finds each chunk's problem and hands each thread one
+//                   voxel; statistics stay in registers while the
 //                   block works on one problem, are warp-reduced into that
 //                   problem's shared totals when it moves on, and are
 //                   flushed once per block.
@@ -110,7 +110,7 @@ __device__ __forceinline__ int find_work(const unsigned *pre, int n, unsigned k)
 }
 
 // Band pass of iteration `it` over all problems.  The work is cut into
-// chunks of kGroupsPerBlock voxels that never cross a problem, so a CTA works
+// chunks of kBandThreads voxels that never cross a problem, so a CTA works
 // on one problem at a time: it stages that problem's argument block in shared
 // memory (the gradient reads it as often as the single-grid kernel reads its
 // constant parameters) and appends the chunk's carried voxels with one atomic.
@@ -138,16 +138,13 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
   }
   __syncthreads();
   // chunks per problem, scanned in place of the counts' copy
-  unsigned chunks = threadIdx.x < nprob ? (s_cnt[threadIdx.x] + kGroupsPerBlock - 1) / kGroupsPerBlock : 0u;
+  unsigned chunks = threadIdx.x < nprob ? (s_cnt[threadIdx.x] + kBandThreads - 1) / kBandThreads : 0u;
   __shared__ unsigned s_chunks[kMaxBatch];
   if (threadIdx.x < nprob) s_chunks[threadIdx.x] = chunks;
   __syncthreads();
   scan_counts<kMaxBatch>(s_chunks, s_pre, nprob);
   const unsigned total = s_pre[nprob];
   const int lane = threadIdx.x & 31;
-  const int gl = lane & (kGroup - 1);
-  const int group = threadIdx.x / kGroup;
-  const unsigned gmask = group_mask(lane);
   // statistics of the staged problem, per thread until the problem changes
   float maxd = 0.f;
   float energy = 0.f;
@@ -192,14 +189,14 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
       cur = p;
       __syncthreads();
     }
-    const unsigned k = (c - s_pre[p]) * kGroupsPerBlock + group;
+    const unsigned k = (c - s_pre[p]) * kBandThreads + threadIdx.x;
     int next = -1;
     if (k < s_cnt[p]) {
       const int v = s_list_in[k];
-      next = update_band_voxel(s_a, v, v, gl, gmask, maxd, energy, active, diverged);
+      next = update_band_voxel(s_a, v, v, maxd, energy, active, diverged);
     }
     // hand the chunk's updated voxels to the next iteration
-    block_append(next, gl == 0, &s_a.st[it + 1].list, s_list_out);
+    block_append(next, &s_a.st[it + 1].list, s_list_out);
   }
   if (cur >= 0) flush(cur);
   __syncthreads();

@@ -11,7 +11,7 @@
 //     band keeps its psi, which therefore need not be written; the voxels
 //     inside are compacted into a list.  16 bytes per voxel.
 //   k_fused_band  evaluates the full gradient of every listed voxel, one
-//     thread per voxel (kGroup = 1): the thread loads the 20 psi neighbours
+//     thread per voxel: the thread loads the 20 psi neighbours
 //     of the stencil per component, takes the 25 warped-SDF samples of the
 //     gradient and Hessian at compile-time offsets plus the warped value (26
 //     independent trilinear gathers), and applies the reference's difference
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
   stream_flat<kPassThrough>(a, blockIdx.x, list, &a.st[a.iter].list, runs ? runs + blockIdx.x : nullptr);
 }
 
-// Band pass: a group of kGroup lanes per listed voxel, launched as one resident
+// Band pass: one thread per listed voxel, launched as one resident
 // wave that loops over the list.  kCarry (band-only solver): the voxels
 // updated here form the next iteration's list (list_out, counted in
 // st[iter+1].list).  kInPlace: the new psi of list entry k goes to entry k
@@ -82,25 +82,21 @@ __global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_fused_band(F
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.iter].skipped = 1;
     return;
   }
-  const int lane = threadIdx.x & 31;
-  const int gl = lane & (kGroup - 1);
-  const int group = threadIdx.x / kGroup;  // group within the block
-  const unsigned gmask = group_mask(lane);
   const int nq = (int)a.st[a.iter].list;
-  const int total_groups = gridDim.x * kGroupsPerBlock;
-  const int rounds = (nq + total_groups - 1) / total_groups;
+  const int total_threads = gridDim.x * kBandThreads;
+  const int rounds = (nq + total_threads - 1) / total_threads;
   float maxd = 0.f;
   float energy = 0.f;  // this thread's voxels; the block and grid sums are float64
   unsigned active = 0;
   bool diverged = false;
   for (int r = 0; r < rounds; ++r) {
-    const int k = (r * gridDim.x + blockIdx.x) * kGroupsPerBlock + group;
-    int next = -1;  // voxel this group hands to the next iteration
+    const int k = (r * gridDim.x + blockIdx.x) * kBandThreads + threadIdx.x;
+    int next = -1;  // voxel this thread hands to the next iteration
     if (k < nq) {
       const int v = list_in[k];
-      next = update_band_voxel<kTrust>(a, v, kInPlace ? k : v, gl, gmask, maxd, energy, active, diverged);
+      next = update_band_voxel<kTrust>(a, v, kInPlace ? k : v, maxd, energy, active, diverged);
     }
-    if (kCarry) block_append(next, gl == 0, &a.st[a.iter + 1].list, list_out);
+    if (kCarry) block_append(next, &a.st[a.iter + 1].list, list_out);
   }
   reduce_iter_stats<kBandThreads>(a.st + a.iter, active, maxd, (double)energy, diverged);
 }
@@ -159,17 +155,13 @@ __global__ void __launch_bounds__(kThreads) k_trust_fix(FusedArgs a, const int *
 // hit the cap (active) and the most steps of one voxel (list).
 __global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_pervoxel(FusedArgs a, const int *__restrict__ list,
                                                             int max_iters, int color) {
-  const int lane = threadIdx.x & 31;
-  const int gl = lane & (kGroup - 1);
-  const int group = threadIdx.x / kGroup;
-  const unsigned gmask = group_mask(lane);
   const DevParams &dp = a.dp;
   const int nq = (int)a.st[0].list;
   const float thr = (float)dp.threshold;
   float maxd = 0.f, energy = 0.f;
   unsigned capped = 0, most = 0;
   bool diverged = false;
-  for (int k = blockIdx.x * kGroupsPerBlock + group; k < nq; k += gridDim.x * kGroupsPerBlock) {
+  for (int k = blockIdx.x * kBandThreads + threadIdx.x; k < nq; k += gridDim.x * kBandThreads) {
     const int i = list[k];
     int x, y, z;
     voxel_xyz(dp, i, x, y, z);
@@ -182,28 +174,18 @@ __global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_pervoxel(Fus
     while (true) {
       float d[3] = {0.f, 0.f, 0.f}, sv = 0.f, e = 0.f, c0[3] = {0.f, 0.f, 0.f};
       if (interior) {
-        gradient_band<true>(a, x, y, z, i, gl, gmask, d, sv, e, c0);
+        gradient_lane<true>(a, x, y, z, i, d, sv, e, c0);
       } else {
-        if (gl == 0) {
-          gradient_generic(a, x, y, z, d, sv, e);
-          c0[0] = __ldcg(a.ix + i);
-          c0[1] = __ldcg(a.iy + i);
-          c0[2] = __ldcg(a.iz + i);
-        }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          d[c] = __shfl_sync(gmask, d[c], 0, kGroup);
-          c0[c] = __shfl_sync(gmask, c0[c], 0, kGroup);
-        }
-        e = __shfl_sync(gmask, e, 0, kGroup);
+        gradient_generic(a, x, y, z, d, sv, e);
+        c0[0] = __ldcg(a.ix + i);
+        c0[1] = __ldcg(a.iy + i);
+        c0[2] = __ldcg(a.iz + i);
       }
       const float n0 = c0[0] + d[0], n1 = c0[1] + d[1], n2 = c0[2] + d[2];
-      if (gl == 0) {  // DisplacementField::update (DisplacementField.cpp:65-71)
-        a.ox[i] = n0;
-        a.oy[i] = n1;
-        a.oz[i] = n2;
-      }
-      __syncwarp(gmask);
+      // DisplacementField::update (DisplacementField.cpp:65-71)
+      a.ox[i] = n0;
+      a.oy[i] = n1;
+      a.oz[i] = n2;
       ++steps;
       dn = sqrtf(ff(d[2], d[2], ff(d[1], d[1], fm(d[0], d[0]))));
       en = e;
@@ -216,18 +198,16 @@ __global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_pervoxel(Fus
       // |gradient| = |step| / alpha
       if (!(dn / a.alpha > thr) || iter >= max_iters) break;
     }
-    if (gl == 0) {
-      maxd = fmaxf(maxd, dn);
-      energy += en;
-      capped += iter >= max_iters;
-      most = max(most, steps);
-      diverged |= div;
-    }
+    maxd = fmaxf(maxd, dn);
+    energy += en;
+    capped += iter >= max_iters;
+    most = max(most, steps);
+    diverged |= div;
   }
   // voxels processed are counted by the band pass (record 0's list)
   reduce_iter_stats<kBandThreads>(a.st, 0u, maxd, (double)energy, diverged);
-  if (gl == 0 && capped) atomicAdd(&a.st[1].active, capped);
-  if (gl == 0 && most) atomicMax(&a.st[1].list, most);
+  if (capped) atomicAdd(&a.st[1].active, capped);
+  if (most) atomicMax(&a.st[1].list, most);
 }
 
 }  // namespace

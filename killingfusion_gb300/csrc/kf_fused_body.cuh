@@ -24,22 +24,6 @@ constexpr int kTile = kThreads * kZSlab;
 constexpr int kBandWarps = 8;
 constexpr int kBandThreads = 32 * kBandWarps;
 constexpr int kBandBlocksPerSM = 2;  // resident band-pass CTAs (launch bounds and grid)
-// Lanes per band voxel.  With one (gradient_lane) a thread loads its
-// voxel's psi neighbours and takes all 26 warped samples at compile-time
-// offsets; with a group (gradient_group) the neighbours are shared by
-// shuffles, the Killing stencil and the cell moments are replicated on the
-// lanes and the samples split among them.  One lane per voxel (two CTAs of
-// 256 threads per SM) measured 1.7x the band voxels/s of 4 lanes on
-// band-heavy grids and 2.3x on the 64-problem batch, and 3 % faster on the
-// dense 256^3 iteration; 4 lanes were 1.32x 8 lanes and 2x 16.
-constexpr int kGroup = 1;
-constexpr int kGroupsPerBlock = kBandThreads / kGroup;
-constexpr int kNbPerLane = (20 + kGroup - 1) / kGroup;   // psi neighbours per lane
-constexpr int kSmpPerLane = (26 + kGroup - 1) / kGroup;  // warped samples per lane
-constexpr unsigned kGroupBits = kGroup == 32 ? 0xffffffffu : (1u << kGroup) - 1u;
-
-// The lanes of the group that lane `lane` belongs to.
-__device__ __forceinline__ unsigned group_mask(int lane) { return kGroupBits << (lane & ~(kGroup - 1)); }
 
 struct FusedArgs {
   const float *__restrict__ live;
@@ -118,211 +102,15 @@ __device__ __noinline__ float warped_value(const FusedArgs &a, int x, int y, int
                  (((float)z + p2) + 0.5f) - 0.5f);
 }
 
-// The 25 sub-voxel offsets (units of h) of the cell-centre samples: 0, +-e_k
-// (gradient), +-2e_k and +-e_j+-e_k (Hessian).
-__device__ const signed char kOff25[25][3] = {
-    {0, 0, 0},   {1, 0, 0},   {-1, 0, 0},  {0, 1, 0},  {0, -1, 0},  {0, 0, 1},  {0, 0, -1},
-    {2, 0, 0},   {-2, 0, 0},  {0, 2, 0},   {0, -2, 0}, {0, 0, 2},   {0, 0, -2}, {1, 0, 1},
-    {-1, 0, 1},  {0, 1, 1},   {0, -1, 1},  {1, 1, 0},  {-1, 1, 0},  {-1, 0, -1}, {1, 0, -1},
-    {0, -1, -1}, {0, 1, -1},  {-1, -1, 0}, {1, -1, 0}};
-
-// The 20 psi neighbours of the interior stencil: the 19-point Killing
-// stencil and the far corner (1,1,1) of the cell-centre cell.
-__device__ const signed char kNb20[24][3] = {
-    {0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},   {0, -1, 0}, {0, 0, 1},  {0, 0, -1},
-    {1, 1, 0},  {1, -1, 0}, {-1, 1, 0}, {-1, -1, 0}, {1, 0, 1},  {1, 0, -1}, {-1, 0, 1},
-    {-1, 0, -1}, {0, 1, 1}, {0, 1, -1}, {0, -1, 1},  {0, -1, -1}, {1, 1, 1},  {0, 0, 0},
-    {0, 0, 0},  {0, 0, 0},  {0, 0, 0}};
+// The 20 psi neighbours of the interior stencil (nb20_off): the 19-point
+// Killing stencil and the far corner (1,1,1) of the cell-centre cell.
 enum { N000 = 0, NXP, NXM, NYP, NYM, NZP, NZM, NXPYP, NXPYM, NXMYP, NXMYM, NXPZP, NXPZM, NXMZP,
        NXMZM, NYPZP, NYPZM, NYMZP, NYMZM, N111 };
 
-__device__ __forceinline__ float group_sum(float v, unsigned mask) {
-#pragma unroll
-  for (int o = kGroup / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, kGroup);
-  return v;
-}
-
-// One interior voxel (1 <= x,y,z <= n-2) by a group of kGroup lanes.  Every lane
-// of the group returns the step d = -alpha * g, the warped value s at
-// i + psi(i), and the monitored energy e.
-template <bool kCoherent = false>
-__device__ void gradient_group(const FusedArgs &a, int x, int y, int z, int64_t idx, int gl,
-                               unsigned gmask, float d[3], float &s_out, float &e_out, float c0[3]) {
-  const DevParams &dp = a.dp;
-  const int64_t sy = dp.nx, sz = (int64_t)dp.nx * dp.ny;
-  const float h = a.h;
-
-  // psi neighbours gl, gl+kGroup, ... (those < 20); phi_can on lane 2
-  float q[kNbPerLane][3];
-#pragma unroll
-  for (int r = 0; r < kNbPerLane; ++r) {
-    const int n = gl + kGroup * r;
-    if (n < 20) {
-      const int64_t j = idx + __ldg(&kNb20[n][0]) + __ldg(&kNb20[n][1]) * sy + __ldg(&kNb20[n][2]) * sz;
-      // psi updated in place by other groups (per-voxel schedule): read it
-      // through L2, never from a stale L1 or read-only line
-      q[r][0] = kCoherent ? __ldcg(a.ix + j) : __ldg(a.ix + j);
-      q[r][1] = kCoherent ? __ldcg(a.iy + j) : __ldg(a.iy + j);
-      q[r][2] = kCoherent ? __ldcg(a.iz + j) : __ldg(a.iz + j);
-    } else {
-      q[r][0] = q[r][1] = q[r][2] = 0.f;
-    }
-  }
-  const float canv = gl == 2 ? __ldg(a.can + idx) : 0.f;
-
-  float kg[3], div[3] = {0.f, 0.f, 0.f}, m[3][7], J[3][3];
-  const float two_h = 2.f * h, hh = h * h;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    float v[20];
-#pragma unroll
-    for (int n = 0; n < 20; ++n) v[n] = __shfl_sync(gmask, q[n / kGroup][c], n % kGroup, kGroup);
-    const float v000 = v[N000];
-    c0[c] = v000;
-    // Killing second differences (DisplacementField.cpp:326-331)
-    float xx = two_h * ((v[NXP] - v000) + (v[NXM] - v000));
-    float yy = two_h * ((v[NYP] - v000) + (v[NYM] - v000));
-    float zz = two_h * ((v[NZP] - v000) + (v[NZM] - v000));
-    float xy = hh * ((v[NXPYP] - v[NXPYM]) - (v[NXMYP] - v[NXMYM]));
-    float xz = hh * ((v[NXPZP] - v[NXPZM]) - (v[NXMZP] - v[NXMZM]));
-    float yz = hh * ((v[NYPZP] - v[NYPZM]) - (v[NYMZP] - v[NYMZM]));
-    kg[c] = -2.f * (xx + yy + zz);
-    if (c == 0) { div[0] += xx; div[1] += xy; div[2] += xz; }
-    if (c == 1) { div[0] += xy; div[1] += yy; div[2] += yz; }
-    if (c == 2) { div[0] += xz; div[1] += yz; div[2] += zz; }
-    // central differences for the monitored Killing energy
-    J[c][0] = 0.5f * (v[NXP] - v[NXM]);
-    J[c][1] = 0.5f * (v[NYP] - v[NYM]);
-    J[c][2] = 0.5f * (v[NZP] - v[NZM]);
-    // moments of the cell [i, i+1]^3 (corner k_abc = psi(i + (a,b,c)))
-    float k000 = v000, k100 = v[NXP], k010 = v[NYP], k110 = v[NXPYP];
-    float k001 = v[NZP], k101 = v[NXPZP], k011 = v[NYPZP], k111 = v[N111];
-    float sx0 = (k000 + k010) + (k001 + k011), sx1 = (k100 + k110) + (k101 + k111);
-    float sy0 = (k000 + k100) + (k001 + k101), sy1 = (k010 + k110) + (k011 + k111);
-    float sz0 = (k000 + k100) + (k010 + k110), sz1 = (k001 + k101) + (k011 + k111);
-    m[c][0] = 0.125f * (sx0 + sx1);
-    m[c][1] = 0.25f * (sx1 - sx0);
-    m[c][2] = 0.25f * (sy1 - sy0);
-    m[c][3] = 0.25f * (sz1 - sz0);
-    m[c][4] = 0.5f * ((k110 - k010) - (k100 - k000) + (k111 - k011) - (k101 - k001));
-    m[c][5] = 0.5f * ((k101 - k001) - (k100 - k000) + (k111 - k011) - (k110 - k010));
-    m[c][6] = 0.5f * ((k011 - k001) - (k010 - k000) + (k111 - k101) - (k110 - k100));
-  }
-  // Killing gradient: damped divergence term, clamp |g| to killing_clamp, /4h^2
-#pragma unroll
-  for (int c = 0; c < 3; ++c) kg[c] += (-2.f * a.gamma_k) * div[c];
-  {
-    float nrm = sqrtf(kg[0] * kg[0] + kg[1] * kg[1] + kg[2] * kg[2]);
-    float sc = nrm > a.clamp ? a.clamp / nrm : 1.f;
-    float den = 4.f * h * h;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) kg[c] = kg[c] * sc / den;
-  }
-
-  // samples j = gl + kGroup*r: j < 25 the cell-centre samples (SDF::getDistancef at
-  // i+0.5+h*o, SDF.cpp:577-582: the half voxel it adds is removed again by
-  // getDistance), j == 25 the warped value at i + psi(i)
-  float fs[kSmpPerLane];
-#pragma unroll
-  for (int r = 0; r < kSmpPerLane; ++r) {
-    const int j = gl + kGroup * r;
-    float t0, t1, t2;
-    if (j < 25) {
-      const float o0 = (float)__ldg(&kOff25[j][0]), o1 = (float)__ldg(&kOff25[j][1]),
-                  o2 = (float)__ldg(&kOff25[j][2]);
-      float t[3];
-      const float base[3] = {(float)x + 0.5f, (float)y + 0.5f, (float)z + 0.5f};
-      const float of[3] = {o0, o1, o2};
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float lin = o0 * m[c][1] + o1 * m[c][2] + o2 * m[c][3];
-        float quad = o0 * o1 * m[c][4] + o0 * o2 * m[c][5] + o1 * o2 * m[c][6];
-        t[c] = (base[c] + h * of[c]) + (m[c][0] + h * (lin + h * quad));
-      }
-      t0 = t[0]; t1 = t[1]; t2 = t[2];
-    } else {
-      t0 = (((float)x + c0[0]) + 0.5f) - 0.5f;
-      t1 = (((float)y + c0[1]) + 0.5f) - 0.5f;
-      t2 = (((float)z + c0[2]) + 0.5f) - 0.5f;
-    }
-    fs[r] = j <= 25 ? phi_tri(a, t0, t1, t2) : 0.f;
-  }
-  const float f0 = __shfl_sync(gmask, fs[0], 0, kGroup);
-  const float s = __shfl_sync(gmask, fs[25 / kGroup], 25 % kGroup, kGroup);
-  const float cv = __shfl_sync(gmask, canv, 2, kGroup);
-  // derivative stencils on sample differences (the constant f0 cancels):
-  // gradient +-1 on +-e_k, Hessian +1 on +-2e_k, o_j*o_k on the diagonals
-  float gx = 0.f, gy = 0.f, gz = 0.f, hxx = 0.f, hyy = 0.f, hzz = 0.f, hxy = 0.f, hxz = 0.f, hyz = 0.f;
-#pragma unroll
-  for (int r = 0; r < kSmpPerLane; ++r) {
-    const int j = gl + kGroup * r;
-    if (j >= 25) continue;
-    const int o0 = __ldg(&kOff25[j][0]), o1 = __ldg(&kOff25[j][1]), o2 = __ldg(&kOff25[j][2]);
-    const float df = fs[r] - f0;
-    const int nzc = (o0 != 0) + (o1 != 0) + (o2 != 0);
-    const int amax = max(abs(o0), max(abs(o1), abs(o2)));
-    if (nzc == 1 && amax == 1) {
-      gx += (float)o0 * df;
-      gy += (float)o1 * df;
-      gz += (float)o2 * df;
-    } else if (nzc == 1 && amax == 2) {
-      if (o0) hxx += df;
-      if (o1) hyy += df;
-      if (o2) hzz += df;
-    } else if (nzc == 2) {
-      if (!o2) hxy += (float)(o0 * o1) * df;
-      if (!o1) hxz += (float)(o0 * o2) * df;
-      if (!o0) hyz += (float)(o1 * o2) * df;
-    }
-  }
-  gx = group_sum(gx, gmask); gy = group_sum(gy, gmask); gz = group_sum(gz, gmask);
-  hxx = group_sum(hxx, gmask); hyy = group_sum(hyy, gmask); hzz = group_sum(hzz, gmask);
-  hxy = group_sum(hxy, gmask); hxz = group_sum(hxz, gmask); hyz = group_sum(hyz, gmask);
-  const float inv2h = 1.f / (2.f * h), inv4hh = 1.f / (4.f * h * h);
-  const float g[3] = {gx * inv2h, gy * inv2h, gz * inv2h};
-  hxx *= inv4hh; hyy *= inv4hh; hzz *= inv4hh; hxy *= inv4hh; hxz *= inv4hh; hyz *= inv4hh;
-
-  float grad[3] = {0.f, 0.f, 0.f};
-  float e = 0.f;
-  if (dp.use_data) {
-    float r = (s - cv) / a.voxel;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) grad[k] += r * g[k];
-    e += 0.5f * r * r;
-  }
-  if (dp.use_killing) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) grad[k] += kg[k] * a.omega_k;
-    float fr = 0.f, tr = 0.f;
-#pragma unroll
-    for (int p = 0; p < 3; ++p)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        fr += J[p][k] * J[p][k];
-        tr += J[p][k] * J[k][p];
-      }
-    e += a.omega_k * (fr + a.gamma_k * tr);
-  }
-  if (dp.use_levelset) {
-    const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-    float hg0 = hxx * g[0] + hxy * g[1] + hxz * g[2];
-    float hg1 = hxy * g[0] + hyy * g[1] + hyz * g[2];
-    float hg2 = hxz * g[0] + hyz * g[1] + hzz * g[2];
-    float sc = (gn - 1.f) / (gn + a.eps) * a.omega_s;
-    grad[0] += hg0 * sc;
-    grad[1] += hg1 * sc;
-    grad[2] += hg2 * sc;
-    float r = gn / a.voxel - 1.f;
-    e += a.omega_s * 0.5f * r * r;
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) d[k] = -a.alpha * grad[k];
-  s_out = s;
-  e_out = e;
-}
-
-// The stencil offsets of gradient_group as compile-time functions, so that
-// a loop over them unrolls into constant-offset code (gradient_lane).
+// The stencil offsets as compile-time functions, so that a loop over them
+// unrolls into constant-offset code.  off25_at: the 25 sub-voxel offsets
+// (units of h) of the cell-centre samples: 0, +-e_k (gradient), +-2e_k and
+// +-e_j+-e_k (Hessian).
 __host__ __device__ constexpr int nb20_off(int n, int c) {
   constexpr signed char t[20][3] = {
       {0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},   {0, -1, 0}, {0, 0, 1},  {0, 0, -1},
@@ -339,12 +127,17 @@ __host__ __device__ constexpr int off25_at(int j, int c) {
   return t[j][c];
 }
 
-// One interior voxel (1 <= x,y,z <= n-2) by one thread: the arithmetic of
-// gradient_group without the group -- the thread loads the 20 psi
-// neighbours of each component itself and takes all 26 samples, whose
-// offsets are compile-time constants, and the derivative stencils are the
-// reference's (SDF.cpp:726-744, 867-881).  Nothing is replicated across
-// lanes, so a warp updates 32 voxels.
+// One interior voxel (1 <= x,y,z <= n-2) by one thread: returns the step
+// d = -alpha * g, the warped value s at i + psi(i), the monitored energy e
+// and psi(i) in c0.  The thread loads the 20 psi neighbours of each
+// component and takes all 26 samples, whose offsets are compile-time
+// constants; the derivative stencils are the reference's (SDF.cpp:726-744,
+// 867-881).  Measured against groups of lanes per voxel that shared the
+// neighbours by shuffles (and so replicated the Killing stencil and the
+// moments on every lane): one thread per voxel runs 112 warp instructions
+// per band voxel against 291 for 4 lanes, 1.7x the band voxels/s on
+// band-heavy grids, 2.3x on a 64-problem batch, 3 % faster on the dense
+// 256^3 iteration; 4 lanes had been 1.32x 8 lanes and 2x 16.
 template <bool kCoherent = false>
 __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, int z, int64_t idx, float d[3],
                                               float &s_out, float &e_out, float c0[3]) {
@@ -481,18 +274,6 @@ __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, 
   for (int k = 0; k < 3; ++k) d[k] = fm(-a.alpha, grad[k]);
   s_out = s;
   e_out = e;
-}
-
-// The interior gradient of the band passes: one thread per voxel
-// (kGroup == 1) or a group of kGroup lanes.
-template <bool kCoherent = false>
-__device__ __forceinline__ void gradient_band(const FusedArgs &a, int x, int y, int z, int64_t idx, int gl,
-                                              unsigned gmask, float d[3], float &s_out, float &e_out,
-                                              float c0[3]) {
-  if constexpr (kGroup == 1)
-    gradient_lane<kCoherent>(a, x, y, z, idx, d, s_out, e_out, c0);
-  else
-    gradient_group<kCoherent>(a, x, y, z, idx, gl, gmask, d, s_out, e_out, c0);
 }
 
 // Generic reference-order gradient for the outer shell (one thread).
@@ -681,13 +462,13 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
   if (range && tid == 0) *range = make_int2(qn ? qbase : 0, qn);
 }
 
-// Appends the voxels `next` (>= 0 on the group leaders that carry one) of the
-// whole block to list_out with one atomic on *count, in group order; every
+// Appends the voxels `next` (>= 0 on the threads that carry one) of the
+// whole block to list_out with one atomic on *count, in thread order; every
 // thread of the block calls it.
-__device__ __forceinline__ void block_append(int next, bool leader, unsigned *count, int *__restrict__ list_out) {
+__device__ __forceinline__ void block_append(int next, unsigned *count, int *__restrict__ list_out) {
   __shared__ unsigned s_wcnt[kBandWarps], s_wbase[kBandWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const bool has = leader && next >= 0;
+  const bool has = next >= 0;
   const unsigned ball = __ballot_sync(0xffffffffu, has);
   if (lane == 0) s_wcnt[warp] = (unsigned)__popc(ball);
   __syncthreads();
@@ -731,19 +512,17 @@ __device__ __noinline__ bool trust_step_f(const FusedArgs &a, int x, int y, int 
   return ok;
 }
 
-// Update one band voxel i with the group of kGroup lanes it is assigned to and
-// write its new psi to entry `slot` of the output planes (slot == i for
-// ping-pong buffers; the voxel's list position for in-place updates).  The
-// voxel is re-tested with its warped value: one outside the band keeps its
-// psi (it left the band in the previous iteration).  Returns the voxel for
-// the next iteration's list (-1 if it left the band); the group leader
-// accumulates the statistics.
+// Update band voxel i (one thread) and write its new psi to entry `slot` of
+// the output planes (slot == i for ping-pong buffers; the voxel's list
+// position for in-place updates).  The voxel is re-tested with its warped
+// value: one outside the band keeps its psi (it left the band in the
+// previous iteration).  Returns the voxel for the next iteration's list (-1
+// if it left the band) and accumulates the statistics.
 // kTrust: the trust-region step (dp.trust set), a separate instantiation so
 // that the plain band pass carries no call to it.
 template <bool kTrust = false>
-__device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int slot, int gl, unsigned gmask,
-                                                 float &maxd, float &energy, unsigned &active,
-                                                 bool &diverged) {
+__device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int slot, float &maxd,
+                                                 float &energy, unsigned &active, bool &diverged) {
   const DevParams &dp = a.dp;
   int x, y, z;
   voxel_xyz(dp, i, x, y, z);
@@ -751,34 +530,32 @@ __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int 
   const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 &&
                         z <= dp.nz - 2;
   if (interior) {
-    gradient_band(a, x, y, z, i, gl, gmask, d, s, en, c0);
-  } else if (gl == 0) {
+    gradient_lane(a, x, y, z, i, d, s, en, c0);
+  } else {
     gradient_generic(a, x, y, z, d, s, en);
     c0[0] = a.ix[i];
     c0[1] = a.iy[i];
     c0[2] = a.iz[i];
   }
   int next = -1;
-  if (gl == 0) {
-    if (in_band(s, a.band_hi, a.band_lo)) {
-      if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
-      if (kTrust && !trust_step_f(a, x, y, z, i, c0, d)) {
-        // this voxel and the rest of its row keep psi (k_trust_fix)
-        atomicMin(a.rows + (z * dp.ny + y), x);
-        d[0] = d[1] = d[2] = 0.f;
-      }
-      a.ox[slot] = c0[0] + d[0];
-      a.oy[slot] = c0[1] + d[1];
-      a.oz[slot] = c0[2] + d[2];
-      maxd = fmaxf(maxd, sqrtf(ff(d[2], d[2], ff(d[1], d[1], fm(d[0], d[0])))));
-      energy += en;
-      ++active;
-      next = i;
-    } else {  // left the band: its psi is final, settle the output buffer
-      a.ox[slot] = c0[0];
-      a.oy[slot] = c0[1];
-      a.oz[slot] = c0[2];
+  if (in_band(s, a.band_hi, a.band_lo)) {
+    if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
+    if (kTrust && !trust_step_f(a, x, y, z, i, c0, d)) {
+      // this voxel and the rest of its row keep psi (k_trust_fix)
+      atomicMin(a.rows + (z * dp.ny + y), x);
+      d[0] = d[1] = d[2] = 0.f;
     }
+    a.ox[slot] = c0[0] + d[0];
+    a.oy[slot] = c0[1] + d[1];
+    a.oz[slot] = c0[2] + d[2];
+    maxd = fmaxf(maxd, sqrtf(ff(d[2], d[2], ff(d[1], d[1], fm(d[0], d[0])))));
+    energy += en;
+    ++active;
+    next = i;
+  } else {  // left the band: its psi is final, settle the output buffer
+    a.ox[slot] = c0[0];
+    a.oy[slot] = c0[1];
+    a.oz[slot] = c0[2];
   }
   return next;
 }
