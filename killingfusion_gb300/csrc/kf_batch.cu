@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
       next = update_band_voxel(s_a, v, v, maxd, energy, active, diverged);
     }
     // hand the chunk's updated voxels to the next iteration
-    block_append(next, &s_a.st[it + 1].list, s_list_out);
+    block_append<kBandWarps>(next, &s_a.st[it + 1].list, s_list_out);
   }
   if (cur >= 0) flush(cur);
   __syncthreads();

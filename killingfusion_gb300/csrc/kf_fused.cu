@@ -76,29 +76,29 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
 // of the output planes, for k_fused_scatter to write back.  kTrust: the
 // trust-region step (dp.trust), followed by k_trust_fix.
 template <bool kCarry, bool kInPlace, bool kTrust = false>
-__global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
+__global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(FusedArgs a, const int *__restrict__ list_in,
                                                              int *__restrict__ list_out) {
   if (iteration_gated(a.st, a.iter, a.dp)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.iter].skipped = 1;
     return;
   }
   const int nq = (int)a.st[a.iter].list;
-  const int total_threads = gridDim.x * kBandThreads;
+  const int total_threads = gridDim.x * kLaneThreads;
   const int rounds = (nq + total_threads - 1) / total_threads;
   float maxd = 0.f;
   float energy = 0.f;  // this thread's voxels; the block and grid sums are float64
   unsigned active = 0;
   bool diverged = false;
   for (int r = 0; r < rounds; ++r) {
-    const int k = (r * gridDim.x + blockIdx.x) * kBandThreads + threadIdx.x;
+    const int k = (r * gridDim.x + blockIdx.x) * kLaneThreads + threadIdx.x;
     int next = -1;  // voxel this thread hands to the next iteration
     if (k < nq) {
       const int v = list_in[k];
       next = update_band_voxel<kTrust>(a, v, kInPlace ? k : v, maxd, energy, active, diverged);
     }
-    if (kCarry) block_append(next, &a.st[a.iter + 1].list, list_out);
+    if (kCarry) block_append<kLaneWarps>(next, &a.st[a.iter + 1].list, list_out);
   }
-  reduce_iter_stats<kBandThreads>(a.st + a.iter, active, maxd, (double)energy, diverged);
+  reduce_iter_stats<kLaneThreads>(a.st + a.iter, active, maxd, (double)energy, diverged);
 }
 
 // In-place update after the last iteration: psi(list[k]) = entry k of the
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kThreads) k_trust_fix(FusedArgs a, const int *
 // depend on scheduling.  Statistics: record 0 voxels (list, from the band
 // pass), last step, last monitored energy, divergence; record 1 voxels that
 // hit the cap (active) and the most steps of one voxel (list).
-__global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_pervoxel(FusedArgs a, const int *__restrict__ list,
+__global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_pervoxel(FusedArgs a, const int *__restrict__ list,
                                                             int max_iters, int color) {
   const DevParams &dp = a.dp;
   const int nq = (int)a.st[0].list;
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_pervoxel(Fus
   float maxd = 0.f, energy = 0.f;
   unsigned capped = 0, most = 0;
   bool diverged = false;
-  for (int k = blockIdx.x * kBandThreads + threadIdx.x; k < nq; k += gridDim.x * kBandThreads) {
+  for (int k = blockIdx.x * kLaneThreads + threadIdx.x; k < nq; k += gridDim.x * kLaneThreads) {
     const int i = list[k];
     int x, y, z;
     voxel_xyz(dp, i, x, y, z);
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kBandThreads, kBandBlocksPerSM) k_pervoxel(Fus
     diverged |= div;
   }
   // voxels processed are counted by the band pass (record 0's list)
-  reduce_iter_stats<kBandThreads>(a.st, 0u, maxd, (double)energy, diverged);
+  reduce_iter_stats<kLaneThreads>(a.st, 0u, maxd, (double)energy, diverged);
   if (capped) atomicAdd(&a.st[1].active, capped);
   if (most) atomicMax(&a.st[1].list, most);
 }
@@ -232,7 +232,7 @@ void kf_fused_graph_destroy(FusedGraph *g) {
 static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
                               int iterations, IterStats *st, int *lists, int2 *runs, int *rows,
                               bool band_only, cudaStream_t s) {
-  const unsigned band_blocks = (unsigned)kf_num_sms() * kBandBlocksPerSM;  // one resident wave
+  const unsigned band_blocks = (unsigned)kf_num_sms() * kLaneBlocksPerSM;  // one resident wave
   const unsigned grid = (unsigned)std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) /
                                                         (kThreads * kFlatGroups), 1);
   const unsigned block = kThreads;
@@ -258,10 +258,10 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
       // lists alternate so that a run can still read the previous iteration's
       k_fused_stream<false><<<grid, block, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1], runs);
       if (dp.trust) {
-        k_fused_band<false, true, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], nullptr);
+        k_fused_band<false, true, true><<<band_blocks, kLaneThreads, 0, s>>>(a, lst[it & 1], nullptr);
         k_trust_fix<<<band_blocks, kThreads, 0, s>>>(a, lst[it & 1], true, next_rows);
       } else {
-        k_fused_band<false, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], nullptr);
+        k_fused_band<false, true><<<band_blocks, kLaneThreads, 0, s>>>(a, lst[it & 1], nullptr);
       }
       if (it == iterations - 1)
         k_fused_scatter<<<band_blocks, kThreads, 0, s>>>(a, lst[it & 1], (float *)in[0], (float *)in[1],
@@ -269,10 +269,10 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
     } else {
       if (it == 0) k_fused_stream<true><<<grid, block, 0, s>>>(a, lst[0], nullptr, nullptr);
       if (dp.trust) {
-        k_fused_band<true, false, true><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
+        k_fused_band<true, false, true><<<band_blocks, kLaneThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
         k_trust_fix<<<band_blocks, kThreads, 0, s>>>(a, lst[it & 1], false, next_rows);
       } else {
-        k_fused_band<true, false><<<band_blocks, kBandThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
+        k_fused_band<true, false><<<band_blocks, kLaneThreads, 0, s>>>(a, lst[it & 1], lst[(it + 1) & 1]);
       }
     }
   }
@@ -354,7 +354,7 @@ int kf_solve_pervoxel(kf_grid live, kf_grid can, kf_field psi, const DevParams &
                                                         (kThreads * kFlatGroups), 1);
   k_fused_stream<false><<<grid, kThreads, 0, s>>>(a, psi->band, nullptr, nullptr);
   for (int color = 0; color < 8; ++color)
-    k_pervoxel<<<(unsigned)kf_num_sms() * kBandBlocksPerSM, kBandThreads, 0, s>>>(a, psi->band, max_iters, color);
+    k_pervoxel<<<(unsigned)kf_num_sms() * kLaneBlocksPerSM, kLaneThreads, 0, s>>>(a, psi->band, max_iters, color);
   KF_CHECK_LAUNCH("per-voxel solve");
   return KF_OK;
 }

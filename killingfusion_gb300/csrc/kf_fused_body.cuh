@@ -21,9 +21,16 @@ using namespace kfref;
 constexpr int kTX = 32, kTY = 8, kThreads = kTX * kTY;
 constexpr int kZSlab = 8;
 constexpr int kTile = kThreads * kZSlab;
+// CTAs of the batch's band pass: 256 threads (chunks of 256 voxels per problem)
 constexpr int kBandWarps = 8;
 constexpr int kBandThreads = 32 * kBandWarps;
-constexpr int kBandBlocksPerSM = 2;  // resident band-pass CTAs (launch bounds and grid)
+// CTAs of the single-grid band pass and the per-voxel schedule: 64 threads,
+// 8 resident per SM (the register file at 128 registers), so that a small
+// band -- a few thousand voxels taken in list order -- spreads over all the
+// SMs instead of filling a few
+constexpr int kLaneWarps = 2;
+constexpr int kLaneThreads = 32 * kLaneWarps;
+constexpr int kLaneBlocksPerSM = 8;
 
 struct FusedArgs {
   const float *__restrict__ live;
@@ -465,8 +472,9 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
 // Appends the voxels `next` (>= 0 on the threads that carry one) of the
 // whole block to list_out with one atomic on *count, in thread order; every
 // thread of the block calls it.
+template <int kWarps>
 __device__ __forceinline__ void block_append(int next, unsigned *count, int *__restrict__ list_out) {
-  __shared__ unsigned s_wcnt[kBandWarps], s_wbase[kBandWarps];
+  __shared__ unsigned s_wcnt[kWarps], s_wbase[kWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool has = next >= 0;
   const unsigned ball = __ballot_sync(0xffffffffu, has);
@@ -474,12 +482,12 @@ __device__ __forceinline__ void block_append(int next, unsigned *count, int *__r
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned t = 0;
-    for (int w = 0; w < kBandWarps; ++w) {
+    for (int w = 0; w < kWarps; ++w) {
       s_wbase[w] = t;
       t += s_wcnt[w];
     }
     const unsigned b = t ? atomicAdd(count, t) : 0u;
-    for (int w = 0; w < kBandWarps; ++w) s_wbase[w] += b;
+    for (int w = 0; w < kWarps; ++w) s_wbase[w] += b;
   }
   __syncthreads();
   if (has) list_out[s_wbase[warp] + (unsigned)__popc(ball & ((1u << lane) - 1u))] = next;
