@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kThreads) k_trust_fix(FusedArgs a, const int *
 // KillingFusion::computeDisplacementField, default per-voxel schedule
 // (KillingFusion.cpp:353-396), for the listed voxels (inside the symmetric
 // band) of one colour (x&1) | (y&1)<<1 | (z&1)<<2: each is taken by one
-// group, which steps its psi in place -- a.ix and a.ox are the same planes --
+// thread, which steps its psi in place -- a.ix and a.ox are the same planes --
 // until the step or the gradient is at most the threshold or max_iters steps
 // were taken.  A voxel's gradient reads psi only in its 3x3x3 neighbourhood,
 // where no other voxel has its colour, so its neighbours stay fixed while it

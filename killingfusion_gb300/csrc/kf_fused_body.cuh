@@ -1,8 +1,8 @@
 // Device-side pieces of the fused float32 psi iteration, shared by the
 // single-grid solver (kf_fused.cu) and the batched solver (kf_batch.cu): the
-// argument block, the gradient of one band voxel (8-lane group form for the
-// interior, reference-order form for the outer shell), the dense tile pass
-// and the band-voxel update.  Included once per translation unit (internal
+// argument block, the gradient of one band voxel (one thread with closed-form
+// stencils for the interior, reference-order form for the outer shell), the
+// dense passes and the band-voxel update.  Included once per translation unit (internal
 // linkage).
 #pragma once
 
