@@ -18,7 +18,10 @@
  *    int32; psi is three float32 (or float64, see kf_precision) planes in
  *    voxel units, stored at integer positions (DisplacementField.cpp:40-58).
  *  - `stream` is a cudaStream_t (NULL = legacy default stream).  All work is
- *    stream-ordered; functions that return host values synchronise `stream`.
+ *    stream-ordered; functions that return host values synchronise `stream`
+ *    (the *_async forms do not).  A grid or field keeps its scratch (meshing,
+ *    integration, solver lists and statistics) with it, so calls on the same
+ *    handle must not run concurrently on different streams.
  *  - Buffers documented as "host or device" may be either (the copy uses
  *    cudaMemcpyDefault); all others are device pointers.
  */
