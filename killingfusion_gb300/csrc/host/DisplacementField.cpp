@@ -191,3 +191,53 @@ DisplacementField DisplacementField::loadFromBinFile(const std::string &path, kf
   }
   return f;
 }
+
+// DisplacementField::testJacobian (DisplacementField.cpp:142-169)
+void DisplacementField::testJacobian() {
+  DisplacementField t(Vec3i(8, 8, 8), 0.5);
+  for (int x = 0; x < 5; ++x)
+    for (int y = 0; y < 5; ++y)
+      for (int z = 0; z < 5; ++z) t.update(Vec3i(x, y, z), Vec3d(x + y + z, x + z, y + z));
+  const kf::Mat3d J = t.computeJacobian(2, 2, 2);
+  std::cout << "numericalJacobian at 2,2,2 is \n";
+  for (int r = 0; r < 3; ++r) std::cout << J(r, 0) << " " << J(r, 1) << " " << J(r, 2) << "\n";
+  std::cout << "analyticalJacobian at 2,2,2 is \n"
+            << "1, 1, 1\n"
+            << "1, 0, 1\n"
+            << "0, 1, 1" << std::endl;
+}
+
+// DisplacementField::testKillingEnergy (DisplacementField.cpp:214-272)
+void DisplacementField::testKillingEnergy() {
+  const double eps = kf::config().epsilon, gamma = kf::config().gammaKilling;
+  DisplacementField t(Vec3i(8, 8, 8), 0.5);
+  for (int x = 0; x < 8; ++x)
+    for (int y = 0; y < 8; ++y)
+      for (int z = 0; z < 8; ++z) t.update(Vec3i(x, y, z), Vec3d(x + y + z, x + z, y));
+  for (int x = 0; x < 7; ++x)
+    for (int y = 1; y < 7; ++y)
+      for (int z = 1; z < 7; ++z) {
+        const kf::Mat3d J = t.computeJacobian(x, y, z);
+        double avkf = 0.0;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) avkf += J(i, j) * J(i, j) + gamma * J(i, j) * J(j, i);
+        if (!(std::fabs(avkf - t.computeKillingEnergy(x, y, z)) < eps))
+          throw std::runtime_error("Whoops! Check DisplacementField::testKillingEnergy");
+      }
+  t.initializeAllVoxels(Vec3d(0, 0, 0));
+  for (int x = 0; x < 8; ++x)
+    for (int y = 0; y < 8; ++y)
+      for (int z = 0; z < 8; ++z) t.update(Vec3i(x, y, z), Vec3d((double)x * x, 0, 0));
+  int mismatches = 0, checked = 0;
+  for (int x = 1; x < 7; ++x)
+    for (int y = 1; y < 7; ++y)
+      for (int z = 1; z < 7; ++z) {
+        const Vec3d g1 = t.computeKillingEnergyGradient(Vec3i(x, y, z));
+        const Vec3d g2 = t.computeKillingEnergyGradient2(Vec3i(x, y, z));
+        ++checked;
+        if (!(std::fabs(g1(0) - g2(0)) < eps && std::fabs(g1(1) - g2(1)) < eps && std::fabs(g1(2) - g2(2)) < eps))
+          ++mismatches;
+      }
+  std::cout << "Killing energy gradient forms differ at " << mismatches << " of " << checked
+            << " voxels (finite differences against the clamped form, as in the reference)" << std::endl;
+}

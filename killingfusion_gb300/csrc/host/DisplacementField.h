@@ -50,6 +50,17 @@ class DisplacementField {
   // Reads a file written by dumpToBinFile (no counterpart in the reference).
   static DisplacementField loadFromBinFile(const std::string &path, kf_precision precision = KF_F32);
 
+  // The reference's self-tests (DisplacementField.cpp:142-169, 195-272).
+  // testJacobian prints the numerical and the analytical Jacobian at (2,2,2)
+  // as the reference does.  testKillingEnergy checks the Killing energy
+  // against the Jacobian (throwing where the reference asserts), then
+  // compares the two Killing-gradient forms on f = (x^2, 0, 0); the clamped
+  // form (computeKillingEnergyGradient2) does not equal the finite-difference
+  // one there, in the reference as here, so that part prints the mismatches
+  // instead of asserting.
+  static void testJacobian();
+  static void testKillingEnergy();
+
   kf::Vec3i getGridSize() const { return m_gridSize; }
   double getVoxelSize() const { return m_voxelSize; }
   kf_precision getPrecision() const { return m_precision; }

@@ -208,6 +208,96 @@ Vec3d SDF::computeDistanceGradient(const Vec3i &i, const DisplacementField *psi)
   return Vec3d((f[0] - f[1]) / den, (f[2] - f[3]) / den, (f[4] - f[5]) / den);
 }
 
+// The self-tests' grid: voxel 0.5 over [0, 8]^3 (17^3 voxels) holding
+// f = x + y - z in the SDF values (weights too when `weights`).
+static SDF linear_test_sdf(bool weights) {
+  SDF t(0.5, Vec3d(0, 0, 0), Vec3d(8, 8, 8), kf::config().UnknownClipDistance);
+  const Vec3i n = t.getGridSize();
+  std::vector<float> phi((size_t)n(0) * n(1) * n(2));
+  std::vector<int32_t> w(phi.size(), 0);
+  for (int z = 0; z < n(2); ++z)
+    for (int y = 0; y < n(1); ++y)
+      for (int x = 0; x < n(0); ++x) {
+        const size_t i = ((size_t)z * n(1) + y) * n(0) + x;
+        phi[i] = (float)(x + y - z);
+        if (weights) w[i] = x + y - z;
+      }
+  kf::check(kf_grid_upload(t.handle(), phi.data(), w.data(), nullptr), "kf_grid_upload");
+  return t;
+}
+
+static void self_check(bool ok, const char *what) {
+  if (!ok) throw std::runtime_error(what);
+}
+
+void SDF::testGetDistance() {
+  const SDF t = linear_test_sdf(false);
+  const Vec3i n = t.getGridSize();
+  const double eps = kf::config().epsilon;
+  std::vector<double> pts, want;
+  for (int z = 2; z < n(2) - 2; ++z)
+    for (int y = 2; y < n(1) - 2; ++y)
+      for (int x = 2; x < n(0) - 2; ++x)
+        for (int i = 0; i < 10; ++i) {
+          const double delta = i / 10.0;
+          want.push_back(x + delta + y - delta - z + delta);
+          pts.insert(pts.end(), {x + 0.5 + delta, y + 0.5 - delta, z + 0.5 - delta});
+        }
+  const std::vector<double> got = t.sampleDistances(pts);
+  for (size_t k = 0; k < want.size(); ++k)
+    self_check(std::fabs(want[k] - got[k]) < eps, "Whoops, check testGetDistance");
+}
+
+void SDF::testGetWeight() {
+  const SDF t = linear_test_sdf(true);
+  const Vec3i n = t.getGridSize();
+  const double eps = kf::config().epsilon;
+  std::vector<double> pts, want;
+  for (int z = 2; z < n(2) - 2; ++z)
+    for (int y = 2; y < n(1) - 2; ++y)
+      for (int x = 2; x < n(0) - 2; ++x)
+        for (int i = 0; i < 10; ++i) {
+          const double delta = i / 10.0f;  // float division, as the reference writes it
+          want.push_back(x + delta + y - delta - z + delta);
+          pts.insert(pts.end(), {x + 0.5 + delta, y + 0.5 - delta, z + 0.5 - delta});
+        }
+  std::vector<double> got(want.size());
+  kf_params pr = params_now();
+  kf::check(kf_grid_sample(t.handle(), &pr, pts.data(), (int)want.size(), nullptr, got.data(), nullptr),
+            "kf_grid_sample");
+  for (size_t k = 0; k < want.size(); ++k)
+    self_check(std::fabs(want[k] - got[k]) < eps, "Whoops, check testGetWeights");
+}
+
+void SDF::testComputeDistanceGradient() {
+  const SDF t = linear_test_sdf(false);
+  const Vec3i n = t.getGridSize();
+  const double eps = kf::config().epsilon;
+  for (int z = 2; z < n(2) - 2; ++z)
+    for (int y = 2; y < n(1) - 2; ++y)
+      for (int x = 2; x < n(0) - 2; ++x)
+        for (int i = 0; i < 10; ++i) {
+          const double delta = i / 10.0f;
+          const Vec3d g = t.computeDistanceGradient(Vec3d(x + 0.5 + delta, y + 0.5 - delta, z + 0.5 - delta));
+          self_check(std::fabs(g(0) - 1) < eps && std::fabs(g(1) - 1) < eps && std::fabs(g(2) + 1) < eps,
+                     "Whoops, check SDF::testComputeDistanceGradient");
+        }
+}
+
+void SDF::testComputeDistanceHessian() {
+  const SDF t = linear_test_sdf(false);
+  const Vec3i n = t.getGridSize();
+  const double voxel = 0.5;
+  for (int z = 2; z < n(2) - 2; ++z)
+    for (int y = 2; y < n(1) - 2; ++y)
+      for (int x = 2; x < n(0) - 2; ++x)
+        for (int i = 0; i < 10; ++i) {
+          const double delta = i * voxel / 10.0f;
+          const Mat3d H = t.computeDistanceHessian(Vec3d(x + 0.5 + delta, y + 0.5 - delta, z + 0.5 - delta));
+          self_check(H.isZero(1e-4), "Whoops, check SDF::testComputeDistanceGradient");
+        }
+}
+
 static const int kHess[19][3] = {{0, 0, 0},  {2, 0, 0},  {-2, 0, 0}, {0, 2, 0},   {0, -2, 0},
                                  {0, 0, 2},  {0, 0, -2}, {1, 0, 1},  {-1, 0, 1},  {0, 1, 1},
                                  {0, -1, 1}, {1, 1, 0},  {-1, 1, 0}, {-1, 0, -1}, {1, 0, -1},

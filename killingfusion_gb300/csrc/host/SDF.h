@@ -40,6 +40,15 @@ class SDF {
   // The two-sphere fixture of KillingFusion::processTest (SDF.cpp:64-115).
   static std::vector<SDF> getDataEnergyTestSample(double voxelSize, double unknownClipDistance);
 
+  // The reference's self-tests (SDF.cpp:526-568, 606-648, 681-724, 797-840)
+  // on a 17^3 grid of voxel 0.5 holding f = x + y - z, through this class's
+  // queries.  Where the reference asserts, these throw std::runtime_error
+  // with the reference's message.
+  static void testGetDistance();
+  static void testGetWeight();
+  static void testComputeDistanceGradient();
+  static void testComputeDistanceHessian();
+
   void integrateDepthFrame(const kf::DepthImage &depthFrame, const kf::Mat4d &depthFrameC2WPose,
                            const kf::Mat3d &depthIntrinsicMatrix, double minDepth, double maxDepth);
 

@@ -217,6 +217,18 @@ static int run_points(int argc, char **argv) {
   return 0;
 }
 
+// The reference's public self-tests, run on the drop-in classes.
+static int run_selftests() {
+  SDF::testGetDistance();
+  SDF::testGetWeight();
+  SDF::testComputeDistanceGradient();
+  SDF::testComputeDistanceHessian();
+  DisplacementField::testJacobian();
+  DisplacementField::testKillingEnergy();
+  std::cout << "selftests ok" << std::endl;
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) return 2;
   try {
@@ -225,6 +237,7 @@ int main(int argc, char **argv) {
     if (!std::strcmp(argv[1], "refdataset")) return run_refdataset(argc, argv);
     if (!std::strcmp(argv[1], "process")) return run_process(argc, argv);
     if (!std::strcmp(argv[1], "points")) return run_points(argc, argv);
+    if (!std::strcmp(argv[1], "selftests")) return run_selftests();
   } catch (const std::exception &e) {
     std::cerr << "error: " << e.what() << std::endl;
     return 1;

@@ -146,6 +146,21 @@ def test_process_test_spheres_trust_region(driver, oracle, tmp_path):
     assert np.any(f32(pphi) != merged)
 
 
+def test_reference_selftests_on_the_classes(driver):
+    """SDF::testGetDistance/testGetWeight/testComputeDistanceGradient/
+    testComputeDistanceHessian and DisplacementField::testJacobian/
+    testKillingEnergy (public static methods of the reference's classes,
+    SDF.cpp:526-840, DisplacementField.cpp:142-272) pass on the drop-in
+    classes; the Jacobian at (2,2,2) is the analytical one."""
+    out = driver("selftests")
+    assert "selftests ok" in out
+    lines = out.splitlines()
+    k = lines.index("numericalJacobian at 2,2,2 is ")
+    J = np.array([[float(v) for v in lines[k + 1 + r].split()] for r in range(3)])
+    np.testing.assert_allclose(J, [[1, 1, 1], [1, 0, 1], [0, 1, 1]], atol=1e-9)
+    assert "Killing energy gradient forms differ at" in out
+
+
 def small_camera_frames(n_frames=3, seed=4):
     """A 64x48 camera (f = 52.5 px) looking at a sphere that moves and
     stretches along x, float32 metres."""
