@@ -970,12 +970,15 @@ extern "C" int kf_field_add_voxels(kf_field f, const int32_t *xyz, int n, const 
     KF_REQUIRE(j >= 0 && j < f->count, "voxel index outside the displacement field");
   }
   if (n == 0) return KF_OK;
-  std::vector<char> in((size_t)n * (12 + 24));
+  // The deltas (doubles) follow the coordinates at a 16-byte boundary: n * 12 bytes alone is not
+  // 8-byte aligned when n is odd.
+  const size_t delta_off = ((size_t)n * 12 + 15) & ~(size_t)15;
+  std::vector<char> in(delta_off + (size_t)n * 24);
   memcpy(in.data(), xyz, (size_t)n * 12);
-  memcpy(in.data() + (size_t)n * 12, delta, (size_t)n * 24);
+  memcpy(in.data() + delta_off, delta, (size_t)n * 24);
   return small_query(in.data(), in.size(), nullptr, 0, kf_stream(stream), [&](char *din, char *) {
     const int32_t *dx = (const int32_t *)din;
-    const double *dd = (const double *)(din + (size_t)n * 12);
+    const double *dd = (const double *)(din + delta_off);
     if (f->prec == KF_F32)
       k_field_add_voxels<float><<<1, 1, 0, kf_stream(stream)>>>((float *)f->p[0], (float *)f->p[1],
                                                                 (float *)f->p[2], f->n[0], f->n[1], dx, n, dd);
