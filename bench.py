@@ -153,6 +153,15 @@ def mesh_once(capi, L, g, P, buf, cap):
     return n.value
 
 
+def fused_solve_launches(n3, iters):
+    """Kernel launches of one dense fused solve: a stream pass and a band pass
+    per iteration and one final write-back; on grids of at least 512 runs of
+    2048 voxels the split schedule adds the run split once and a cold pass
+    per iteration after the first."""
+    runs = max((n3 // 4 + 511) // 512, 1)
+    return 3 * iters + 1 if runs >= 512 else 2 * iters + 1
+
+
 def run_ours(args, rank, world, local):
     import numpy as np
     import torch
@@ -184,7 +193,7 @@ def run_ours(args, rank, world, local):
     # reset, integrate (3 kernels), the solve (fused: stream + band per
     # iteration and one write-back; plain: 7 kernels), warp+fuse (2), 3
     # meshes of 3 kernels each
-    launches_per_frame = 1 + 3 + 2 * args.iters + 1 + 2 + 3 * 3 if args.solver == "fused" else \
+    launches_per_frame = 1 + 3 + fused_solve_launches(N3, args.iters) + 2 + 3 * 3 if args.solver == "fused" else \
         1 + 3 + 7 * args.iters + 2 + 3 * 3
 
     counts = torch.zeros(3, dtype=torch.int64).pin_memory()  # triangle counts, written by the device

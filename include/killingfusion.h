@@ -45,7 +45,8 @@ typedef enum kf_status {
   KF_ERR_DIVERGED = 4, /* psi non-finite at a voxel in the band; the
                           reference throws -1 (KillingFusion.cpp:328-332)   */
   KF_ERR_TIMEOUT = 5,  /* a bounded device-side wait gave up                */
-  KF_ERR_CAPACITY = 6  /* caller buffer too small (count is still returned) */
+  KF_ERR_CAPACITY = 6, /* caller buffer too small (count is still returned) */
+  KF_ERR_INTERNAL = 7  /* a consistency check of the library failed         */
 } kf_status;
 
 /* Arithmetic of the psi solve. */

@@ -19,7 +19,8 @@ from . import _build
 
 LIB_PATH = _build.LIB
 
-KF_OK, KF_ERR_INVALID, KF_ERR_OOM, KF_ERR_CUDA, KF_ERR_DIVERGED, KF_ERR_TIMEOUT, KF_ERR_CAPACITY = range(7)
+(KF_OK, KF_ERR_INVALID, KF_ERR_OOM, KF_ERR_CUDA, KF_ERR_DIVERGED, KF_ERR_TIMEOUT, KF_ERR_CAPACITY,
+ KF_ERR_INTERNAL) = range(8)
 KF_F32, KF_F64 = 0, 1
 KF_SOLVER_FUSED, KF_SOLVER_PLAIN, KF_SOLVER_EXACT, KF_SOLVER_BAND, KF_SOLVER_PERVOXEL = 0, 1, 2, 3, 4
 SOLVERS = {"fused": KF_SOLVER_FUSED, "plain": KF_SOLVER_PLAIN, "exact": KF_SOLVER_EXACT,

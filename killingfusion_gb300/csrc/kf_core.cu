@@ -734,6 +734,10 @@ static int solve_finish(kf_field psi, kf_solve_stats *stats, bool presumed_swapp
       return kf_fail(KF_ERR_DIVERGED, "deformation field diverged (non-finite psi inside the band)");
     return KF_OK;
   }
+  for (int k = 0; k < iterations; ++k)
+    if (host[k].cold)
+      return kf_fail(KF_ERR_INTERNAL, "the split dense schedule found a band voxel in a run without band "
+                                      "voxels at the first iteration");
   int executed = 0;
   int diverged = 0;
   for (int k = 0; k < iterations; ++k) {

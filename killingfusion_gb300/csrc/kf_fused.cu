@@ -69,6 +69,110 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
   stream_flat<kPassThrough>(a, blockIdx.x, list, &a.st[a.iter].list, runs ? runs + blockIdx.x : nullptr);
 }
 
+// Split dense schedule (grids of at least kSplitMinRuns runs).  After the
+// first iteration's dense pass, k_split_runs sorts the runs into those that
+// listed band voxels ("hot") and the others ("cold"), each in run order.  A
+// voxel outside the band keeps its psi and phi_live does not change, so the
+// band tests of a cold run give the first iteration's result again: a cold
+// run has no psi to write back and no band voxel, and no band pass reads
+// anything a cold pass writes.  Every later iteration streams its hot runs
+// (write-back, test, list) on the solve's stream, before its band pass, and
+// its cold runs (test only) on a second stream, beside the band pass of the
+// iteration before.  A band voxel found in a cold run is counted in
+// IterStats::cold and fails the solve.
+constexpr int kSplitMinRuns = 512;
+constexpr int kSplitThreads = 1024;
+constexpr int kHotBlocksPerSM = 5;  // resident CTAs of k_fused_stream (48 registers)
+
+__global__ void __launch_bounds__(kSplitThreads) k_split_runs(const int2 *__restrict__ runs, int nruns,
+                                                             int *__restrict__ hot, int *__restrict__ cold,
+                                                             unsigned *__restrict__ counts) {
+  __shared__ int s_warp[kSplitThreads / 32];
+  __shared__ int s_total;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // thread t takes the runs [r0, r1)
+  const int per = (nruns + kSplitThreads - 1) / kSplitThreads;
+  const int r0 = min(tid * per, nruns), r1 = min(r0 + per, nruns);
+  int mine = 0;
+  for (int r = r0; r < r1; ++r) mine += runs[r].y > 0;
+  int incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const int w = s_warp[lane];
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += v;
+    }
+    s_warp[lane] = wi - w;
+    if (lane == 31) s_total = wi;
+  }
+  __syncthreads();
+  int h = s_warp[warp] + incl - mine;  // hot runs before r0
+  int c = r0 - h;                       // cold runs before r0
+  for (int r = r0; r < r1; ++r) {
+    if (runs[r].y > 0)
+      hot[h++] = r;
+    else
+      cold[c++] = r;
+  }
+  if (tid == 0) {
+    counts[0] = (unsigned)s_total;
+    counts[1] = (unsigned)(nruns - s_total);
+  }
+}
+
+// Dense pass of iteration a.iter >= 1 over the listed runs (counts[0] hot
+// runs, counts[1] cold runs), a run per loop step.  Hot: each run writes
+// back its band voxels' new psi from the iteration before (as
+// k_fused_stream), then streams and lists.  Cold (kCold): the runs are
+// tested only; their band voxels, never expected, are counted in
+// st[iter].cold.  A cold pass stops once the iteration before it was
+// skipped (the statistics of that iteration's band pass may still be in
+// flight when it runs, so it may run once after convergence, to no effect).
+template <bool kCold>
+__global__ void __launch_bounds__(kThreads) k_fused_stream_runs(FusedArgs a, const int *__restrict__ run_list,
+                                                               const unsigned *__restrict__ counts,
+                                                               int *__restrict__ list,
+                                                               const int *__restrict__ prev_list,
+                                                               int2 *__restrict__ runs) {
+  const unsigned n = counts[kCold ? 1 : 0];
+  if (kCold) {
+    if (a.st[a.iter - 1].skipped) return;
+    for (unsigned idx = blockIdx.x; idx < n; idx += gridDim.x) {
+      stream_flat<false, true>(a, run_list[idx], nullptr, &a.st[a.iter].cold);
+      __syncthreads();
+    }
+    return;
+  }
+  const bool write_back = !a.st[a.iter - 1].skipped;
+  const bool gated = iteration_gated(a.st, a.iter, a.dp);
+  if (gated && blockIdx.x == 0 && threadIdx.x == 0) a.st[a.iter].skipped = 1;
+  float *px = const_cast<float *>(a.ix), *py = const_cast<float *>(a.iy), *pz = const_cast<float *>(a.iz);
+  for (unsigned idx = blockIdx.x; idx < n; idx += gridDim.x) {
+    const int r = run_list[idx];
+    if (write_back) {
+      const int2 rr = runs[r];
+      for (int j = threadIdx.x; j < rr.y; j += kThreads) {
+        const int slot = rr.x + j, v = prev_list[slot];
+        px[v] = a.ox[slot];
+        py[v] = a.oy[slot];
+        pz[v] = a.oz[slot];
+      }
+      __syncthreads();
+    }
+    if (!gated) stream_flat<false>(a, r, list, &a.st[a.iter].list, runs + r);
+    __syncthreads();
+  }
+}
+
 // Band pass: one thread per listed voxel, launched as one resident
 // wave that loops over the list.  kCarry (band-only solver): the voxels
 // updated here form the next iteration's list (list_out, counted in
@@ -216,6 +320,8 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_pervoxel(Fus
 struct FusedGraph {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t capture = nullptr;
+  cudaStream_t cold = nullptr;                     // cold passes of the split schedule
+  cudaEvent_t fork = nullptr, join = nullptr;
   const void *key_ptr[12] = {};
   int iterations = 0;
   bool band_only = false;
@@ -226,7 +332,87 @@ void kf_fused_graph_destroy(FusedGraph *g) {
   if (!g) return;
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->capture) cudaStreamDestroy(g->capture);
+  if (g->cold) cudaStreamDestroy(g->cold);
+  if (g->fork) cudaEventDestroy(g->fork);
+  if (g->join) cudaEventDestroy(g->join);
   delete g;
+}
+
+static int64_t num_runs(const DevParams &dp) {
+  return std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) / (kThreads * kFlatGroups), 1);
+}
+
+static bool split_schedule(const DevParams &dp, bool band_only) {
+  return !band_only && !dp.trust && num_runs(dp) >= kSplitMinRuns;
+}
+
+// A launch whose graph node carries a priority: the hot chain of the split
+// schedule (hot pass, band pass) goes ahead of the cold passes' CTAs.
+template <typename... KArgs, typename... Args>
+static void launch_prio(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, int prio,
+                        Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = prio;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// The split schedule's lists after the run table: hot runs, cold runs (one
+// int per run each) and their two counts.
+static size_t runs_table_bytes(int64_t nruns) {
+  return (size_t)nruns * sizeof(int2) + ((size_t)2 * nruns + 4) * sizeof(int);
+}
+
+// The dense fused iterations on the split schedule (see k_split_runs).
+static void launch_split_iterations(FusedArgs a, kf_field psi, const DevParams &dp, int iterations,
+                                    int *lists, int2 *runs, cudaStream_t s, cudaStream_t cold_s,
+                                    cudaEvent_t fork, cudaEvent_t join) {
+  int lo = 0, hi = 0;
+  cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  const unsigned band_blocks = (unsigned)kf_num_sms() * kLaneBlocksPerSM;
+  const int64_t nruns = num_runs(dp);
+  const unsigned grid = (unsigned)nruns;
+  const unsigned hot_grid = (unsigned)std::min<int64_t>(nruns, (int64_t)kf_num_sms() * kHotBlocksPerSM);
+  int *hot = reinterpret_cast<int *>(runs + nruns), *cold = hot + nruns;
+  unsigned *counts = reinterpret_cast<unsigned *>(cold + nruns);
+  int *lst[2] = {lists, lists + dp.count};
+  a.ix = (const float *)psi->p[0];
+  a.iy = (const float *)psi->p[1];
+  a.iz = (const float *)psi->p[2];
+  a.ox = (float *)psi->q[0];
+  a.oy = (float *)psi->q[1];
+  a.oz = (float *)psi->q[2];
+  for (int it = 0; it < iterations; ++it) {
+    a.iter = it;
+    if (it == 0) {
+      launch_prio(k_fused_stream<false>, grid, kThreads, s, hi, a, lst[0], lst[1], runs);
+      launch_prio(k_split_runs, 1, kSplitThreads, s, hi, (const int2 *)runs, (int)nruns, hot, cold, counts);
+    } else {
+      // cold runs beside the band pass of the iteration before
+      cudaStreamWaitEvent(cold_s, fork, 0);
+      launch_prio(k_fused_stream_runs<true>, grid, kThreads, cold_s, lo, a, (const int *)cold,
+                  (const unsigned *)counts, (int *)nullptr, (const int *)nullptr, (int2 *)nullptr);
+      launch_prio(k_fused_stream_runs<false>, hot_grid, kThreads, s, hi, a, (const int *)hot,
+                  (const unsigned *)counts, lst[it & 1], (const int *)lst[(it + 1) & 1], runs);
+    }
+    if (it + 1 < iterations) cudaEventRecord(fork, s);
+    launch_prio(k_fused_band<false, true>, band_blocks, kLaneThreads, s, hi, a, (const int *)lst[it & 1],
+                (int *)nullptr);
+    if (it == iterations - 1)
+      launch_prio(k_fused_scatter, band_blocks, kThreads, s, hi, a, (const int *)lst[it & 1],
+                  (float *)psi->p[0], (float *)psi->p[1], (float *)psi->p[2]);
+  }
+  if (iterations > 1) {
+    cudaEventRecord(join, cold_s);
+    cudaStreamWaitEvent(s, join, 0);
+  }
 }
 
 static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
@@ -284,13 +470,12 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
   if (rc) return rc;
   rc = kf_field_band_list(psi, &psi->band);
   if (rc) return rc;
-  const int64_t nruns =
-      std::max<int64_t>((dp.count / 4 + kThreads * kFlatGroups - 1) / (kThreads * kFlatGroups), 1);
+  const int64_t nruns = num_runs(dp);
   if (psi->runs_cap < nruns) {
     cudaFree(psi->runs);
     psi->runs = nullptr;
     psi->runs_cap = 0;
-    if (cudaMalloc(&psi->runs, nruns * sizeof(int2)) != cudaSuccess) {
+    if (cudaMalloc(&psi->runs, runs_table_bytes(nruns)) != cudaSuccess) {
       cudaGetLastError();
       return kf_fail(KF_ERR_OOM, "cudaMalloc of the dense pass's run table failed");
     }
@@ -310,17 +495,27 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
     kf_fused_graph_destroy(psi->graph);
     psi->graph = g = new FusedGraph();
     KF_CHECK_CUDA(cudaStreamCreateWithFlags(&g->capture, cudaStreamNonBlocking));
+    const bool split = split_schedule(dp, band_only);
+    if (split) {
+      KF_CHECK_CUDA(cudaStreamCreateWithFlags(&g->cold, cudaStreamNonBlocking));
+      KF_CHECK_CUDA(cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming));
+      KF_CHECK_CUDA(cudaEventCreateWithFlags(&g->join, cudaEventDisableTiming));
+    }
     cudaGraph_t graph;
     KF_CHECK_CUDA(cudaStreamBeginCapture(g->capture, cudaStreamCaptureModeThreadLocal));
-    launch_iterations(live, can, psi, dp, iterations, st, psi->band, psi->runs, rows, band_only,
-                      g->capture);
+    if (split)
+      launch_split_iterations(make_args(live, can, dp, st), psi, dp, iterations, psi->band, psi->runs,
+                              g->capture, g->cold, g->fork, g->join);
+    else
+      launch_iterations(live, can, psi, dp, iterations, st, psi->band, psi->runs, rows, band_only,
+                        g->capture);
     cudaError_t le = cudaGetLastError();
     KF_CHECK_CUDA(cudaStreamEndCapture(g->capture, &graph));
     if (le != cudaSuccess) {
       cudaGraphDestroy(graph);
       return kf_cuda_fail(le, "fused kernel launch during capture");
     }
-    cudaError_t ie = cudaGraphInstantiate(&g->exec, graph, 0);
+    cudaError_t ie = cudaGraphInstantiateWithFlags(&g->exec, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) return kf_cuda_fail(ie, "cudaGraphInstantiate");
     g->iterations = iterations;

@@ -395,7 +395,10 @@ __device__ __forceinline__ void flat_test(const FusedArgs &a, int64_t i, float q
     queue[atomicAdd(qn, 1)] = (int)i;
 }
 
-template <bool kPassThrough>
+// kCheck: the run is only tested, its band voxels are counted in *count and
+// not listed (the split schedule's runs without band voxels, where a band
+// voxel would break an invariant of the solver).
+template <bool kPassThrough, bool kCheck = false>
 __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int *__restrict__ list,
                                             unsigned *count, int2 *__restrict__ range = nullptr) {
   __shared__ int queue[kFlatVoxels + 4];
@@ -461,6 +464,10 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
     if (in_band(s, a.band_hi, a.band_lo)) queue[atomicAdd(&qn, 1)] = (int)i;
   }
   __syncthreads();
+  if (kCheck) {
+    if (tid == 0 && qn) atomicAdd(count, (unsigned)qn);
+    return;
+  }
   if (tid == 0 && qn) qbase = (int)atomicAdd(count, (unsigned)qn);
   __syncthreads();
   for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];

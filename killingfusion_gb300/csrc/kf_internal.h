@@ -121,7 +121,9 @@ struct IterStats {
   int diverged;           // psi non-finite inside the band
   int skipped;            // iteration skipped after convergence
   unsigned int list;      // entries of this iteration's band-voxel list
-  unsigned int pad;
+  unsigned int cold;      // band voxels the split dense schedule found in a
+                          // run without band voxels at the first iteration
+                          // (never expected: such voxels keep psi)
 };
 
 // solver entry points implemented in the solver translation units
