@@ -263,12 +263,23 @@ def run_ours(args, rank, world, local):
     solve_ms = [a.elapsed_time(b) for a, b in solve_events]
     active = stats.active_first
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers, on a fresh canonical
+    # grid so that it replays the same frames as the timed region
     can_e2e = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
-    capi.check(L.kf_integrate_depth(can_e2e.h, pinned[0].data_ptr(), 640, 480,
-                                    capi._d(np.eye(4).ravel()), capi._d(synth.K.ravel()), 0.05, max_depth,
-                                    None))
     can, can_e2e = can_e2e, can
+
+    def canonical_from_host():
+        can.reset(P)
+        capi.check(L.kf_integrate_depth(can.h, pinned[0].data_ptr(), 640, 480,
+                                        capi._d(np.eye(4).ravel()), capi._d(synth.K.ravel()), 0.05,
+                                        max_depth, None))
+
+    # warm-up as for the timed region: one host-buffer frame captures the
+    # solve graph for the new canonical grid and sizes the depth staging
+    # buffer; the canonical grid then starts again from frame 0
+    canonical_from_host()
+    frame(pinned[1], e2e=True)
+    canonical_from_host()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -679,7 +690,10 @@ def run_main(args, rank, world, local):
                 "h2d_bytes_per_step": 640 * 480 * 4, "d2h_bytes_per_step": res["d2h_bytes_per_step"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "fused psi iteration (k_fused_stream + k_fused_band)",
+                     "kernel": ("fused psi iteration: k_fused_stream_runs over the hot and the cold runs "
+                                "+ k_fused_band, the cold runs streamed beside the band pass"
+                                if max((N3 // 4 + 511) // 512, 1) >= 512 else
+                                "fused psi iteration (k_fused_stream + k_fused_band)"),
                      "algorithmic_bytes_per_iteration": algo_bytes,
                      "algorithmic_bytes_per_voxel": ALGO_BYTES_PER_VOXEL,
                      "algorithmic_bytes_per_band_voxel": ALGO_BYTES_PER_BAND_VOXEL, "peak_source": peak_kind},

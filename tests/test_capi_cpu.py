@@ -83,6 +83,11 @@ def test_invalid_arguments_fail_cleanly(capi):
     assert L.kf_grid_create((C.c_int * 3)(0, 4, 4), 0.01, None, 0.05, C.byref(p), C.byref(h)) == capi.KF_ERR_INVALID
     assert "dims" in L.kf_last_error().decode()
     assert L.kf_field_create((C.c_int * 3)(4, 4, 4), 7, C.byref(h)) == capi.KF_ERR_INVALID
+    # voxel indices are 32-bit: grids of 2^31 voxels or more are refused
+    for dims in ((1291, 1291, 1291), (65536, 65536, 1), (2 ** 31 - 1, 2, 1)):
+        assert L.kf_grid_create((C.c_int * 3)(*dims), 0.01, None, 0.05, C.byref(p), C.byref(h)) == capi.KF_ERR_INVALID
+        assert "2^31" in L.kf_last_error().decode()
+        assert L.kf_field_create((C.c_int * 3)(*dims), capi.KF_F32, C.byref(h)) == capi.KF_ERR_INVALID
     assert L.kf_mc_case(256, None, None) == capi.KF_ERR_INVALID
     bad = capi.Params(delta_size=0.5).c()
     assert L.kf_grid_create((C.c_int * 3)(4, 4, 4), 0.01, None, 0.05, C.byref(bad), C.byref(h)) == capi.KF_ERR_INVALID
