@@ -138,8 +138,9 @@ __host__ __device__ constexpr int off25_at(int j, int c) {
 // d = -alpha * g, the warped value s at i + psi(i), the monitored energy e
 // and psi(i) in c0.  The thread loads the 20 psi neighbours of each
 // component and takes all 26 samples, whose offsets are compile-time
-// constants; the derivative stencils are the reference's (SDF.cpp:726-744,
-// 867-881).  Measured against groups of lanes per voxel that shared the
+// constants, reading the 25 cell-centre samples' corners once when they
+// share one cell; the derivative stencils are the reference's
+// (SDF.cpp:726-744, 867-881).  Measured against groups of lanes per voxel that shared the
 // neighbours by shuffles (and so replicated the Killing stencil and the
 // moments on every lane): one thread per voxel runs 112 warp instructions
 // per band voxel against 291 for 4 lanes, 1.7x the band voxels/s on
@@ -204,19 +205,39 @@ __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, 
 #pragma unroll
     for (int c = 0; c < 3; ++c) kg[c] = fm(kg[c], sc) / den;
   }
-  // the 25 cell-centre samples (SDF::getDistancef at i+0.5+h*o; the half
-  // voxel it adds is removed again by getDistance) and the warped value at
-  // i + psi(i)
+  // the 25 cell-centre samples and the warped value at i + psi(i)
   const float base[3] = {fa((float)x, 0.5f), fa((float)y, 0.5f), fa((float)z, 0.5f)};
-  float f[25];
+  // Shared corner cell.  Along axis c every sample lies within
+  // h * (2 + 2 (|m1| + |m2| + |m3|) + h (|m4| + |m5| + |m6|)) of the centre
+  // sample base + m0: the offsets are at most 2 and the products of the
+  // mixed samples' offsets are +-1.  When that interval, widened by 1e-3
+  // voxel for the roundings of the positions, has one truncated base on
+  // every axis and that cell is inside the grid, the 25 samples read the
+  // same eight corners: they are loaded once, and each sample interpolates
+  // them with its own fractions, the arithmetic phi_tri does after loading
+  // them itself.
+  int cb[3];
+  bool shared = true;
 #pragma unroll
-  for (int j = 0; j < 25; ++j) {
+  for (int c = 0; c < 3; ++c) {
+    const float m1 = fabsf(m[c][1]) + fabsf(m[c][2]) + fabsf(m[c][3]);
+    const float m2 = fabsf(m[c][4]) + fabsf(m[c][5]) + fabsf(m[c][6]);
+    const float r = h * (2.f + 2.f * m1 + h * m2) + 1e-3f;
+    const float ctr = fa(base[c], m[c][0]);
+    const float lo = ctr - r, hi = ctr + r;
+    const int b = (int)lo;
+    const int n = c == 0 ? dp.nx : (c == 1 ? dp.ny : dp.nz);
+    shared = shared && lo >= 0.f && (int)hi == b && (unsigned)b < (unsigned)(n - 1);
+    cb[c] = b;
+  }
+  // sample j's position (SDF::getDistancef at i+0.5+h*o; the half voxel it
+  // adds is removed again by getDistance): psi~ there is the cell's
+  // trilinear form in its moments, terms with a zero offset dropped at
+  // compile time
+  auto position = [&](int j, float t[3]) {
     const int o0 = off25_at(j, 0), o1 = off25_at(j, 1), o2 = off25_at(j, 2);
-    float t[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      // psi~ at the sample: the cell's trilinear form in its moments (terms
-      // with a zero offset dropped at compile time)
       float lin = 0.f, quad = 0.f;
       if (o0) lin = ff((float)o0, m[c][1], lin);
       if (o1) lin = ff((float)o1, m[c][2], lin);
@@ -227,7 +248,32 @@ __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, 
       const int oc = c == 0 ? o0 : (c == 1 ? o1 : o2);
       t[c] = fa(fa(base[c], fm(h, (float)oc)), ff(h, ff(h, quad, lin), m[c][0]));
     }
-    f[j] = phi_tri(a, t[0], t[1], t[2]);
+  };
+  float f[25];
+  if (shared) {
+    const float *p = a.live + ((int64_t)cb[2] * dp.ny + cb[1]) * dp.nx + cb[0];
+    float cell[8];
+    cell[0] = __ldg(p);
+    cell[1] = __ldg(p + 1);
+    cell[2] = __ldg(p + sy);
+    cell[3] = __ldg(p + sy + 1);
+    cell[4] = __ldg(p + sz);
+    cell[5] = __ldg(p + sz + 1);
+    cell[6] = __ldg(p + sz + sy);
+    cell[7] = __ldg(p + sz + sy + 1);
+#pragma unroll
+    for (int j = 0; j < 25; ++j) {
+      float t[3];
+      position(j, t);
+      f[j] = lerp3f(cell, fsb(t[0], (float)cb[0]), fsb(t[1], (float)cb[1]), fsb(t[2], (float)cb[2]));
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 25; ++j) {
+      float t[3];
+      position(j, t);
+      f[j] = phi_tri(a, t[0], t[1], t[2]);
+    }
   }
   const float s = phi_tri(a, fsb(fa(fa((float)x, c0[0]), 0.5f), 0.5f), fsb(fa(fa((float)y, c0[1]), 0.5f), 0.5f),
                           fsb(fa(fa((float)z, c0[2]), 0.5f), 0.5f));
