@@ -210,20 +210,21 @@ __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, 
   // Shared corner cell.  Along axis c every sample lies within
   // h * (2 + 2 (|m1| + |m2| + |m3|) + h (|m4| + |m5| + |m6|)) of the centre
   // sample base + m0: the offsets are at most 2 and the products of the
-  // mixed samples' offsets are +-1.  When that interval, widened by 1e-3
-  // voxel for the roundings of the positions, has one truncated base on
-  // every axis and that cell is inside the grid, the 25 samples read the
-  // same eight corners: they are loaded once, and each sample interpolates
-  // them with its own fractions, the arithmetic phi_tri does after loading
-  // them itself.
+  // mixed samples' offsets are +-1.  When that interval, widened for the
+  // roundings of the positions (1e-3 voxel plus 2^-20 of the coordinate,
+  // several float ulps of it), has one truncated base on every axis and
+  // that cell is inside the grid, the 25 samples read the same eight
+  // corners: they are loaded once, and each sample interpolates them with
+  // its own fractions, the arithmetic phi_tri does after loading them
+  // itself.
   int cb[3];
   bool shared = true;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const float m1 = fabsf(m[c][1]) + fabsf(m[c][2]) + fabsf(m[c][3]);
     const float m2 = fabsf(m[c][4]) + fabsf(m[c][5]) + fabsf(m[c][6]);
-    const float r = h * (2.f + 2.f * m1 + h * m2) + 1e-3f;
     const float ctr = fa(base[c], m[c][0]);
+    const float r = h * (2.f + 2.f * m1 + h * m2) + 1e-3f + fabsf(ctr) * 0x1p-20f;
     const float lo = ctr - r, hi = ctr + r;
     const int b = (int)lo;
     const int n = c == 0 ? dp.nx : (c == 1 ? dp.ny : dp.nz);
