@@ -376,6 +376,10 @@ static void launch_split_iterations(FusedArgs a, kf_field psi, const DevParams &
                                     cudaEvent_t fork, cudaEvent_t join) {
   int lo = 0, hi = 0;
   cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  // the cold passes rank between the hot chain and default-priority work
+  // that a caller runs beside the solve (the next frame's integration,
+  // meshes), where the device has more than two priority levels
+  const int mid = hi < lo - 1 ? (lo + hi) / 2 : lo;
   const unsigned band_blocks = (unsigned)kf_num_sms() * kLaneBlocksPerSM;
   const int64_t nruns = num_runs(dp);
   const unsigned grid = (unsigned)nruns;
@@ -397,7 +401,7 @@ static void launch_split_iterations(FusedArgs a, kf_field psi, const DevParams &
     } else {
       // cold runs beside the band pass of the iteration before
       cudaStreamWaitEvent(cold_s, fork, 0);
-      launch_prio(k_fused_stream_runs<true>, grid, kThreads, cold_s, lo, a, (const int *)cold,
+      launch_prio(k_fused_stream_runs<true>, grid, kThreads, cold_s, mid, a, (const int *)cold,
                   (const unsigned *)counts, (int *)nullptr, (const int *)nullptr, (int2 *)nullptr);
       launch_prio(k_fused_stream_runs<false>, hot_grid, kThreads, s, hi, a, (const int *)hot,
                   (const unsigned *)counts, lst[it & 1], (const int *)lst[(it + 1) & 1], runs);
