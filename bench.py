@@ -202,8 +202,8 @@ def run_ours(args, rank, world, local):
 
     # Two frames in flight.  Frame f uses slot f % 2: its live SDF, psi, mesh
     # buffers and triangle counts.  Four streams:
-    #   s_in   reset + integration of the frame, beside the solve of the frame before;
-    #   s_main zero psi, the solve, the live mesh, warp + fuse (the canonical SDF's chain);
+    #   s_in   reset + integration of the frame and zero psi, beside the solve of the frame before;
+    #   s_main the solve, the live mesh, warp + fuse (the canonical SDF's chain);
     #   s_out  the registered and canonical meshes, beside the next frame's solve;
     #   s_copy the host copies of a finished frame's meshes (end to end).
     # Events order what the slots and the canonical SDF share: a slot's live
@@ -228,9 +228,9 @@ def run_ours(args, rank, world, local):
         lv.reset(P, stream=s_in)
         capi.check(L.kf_integrate_depth(lv.h, depth.data_ptr(), depth.shape[1], depth.shape[0], eye, Kd,
                                         0.05, max_depth, s_in.cuda_stream))
+        ps.zero(stream=s_in)  # free too: warp + fuse of frame f - 2 came before its meshes
         ev_integ[k].record(s_in)
         s_main.wait_event(ev_integ[k])
-        ps.zero(stream=s_main)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s_main)
         capi.check(L.kf_psi_solve_async(lv.h, can.h, ps.h, C.byref(Pc), args.iters, solver, s_main.cuda_stream))
