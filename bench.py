@@ -9,9 +9,9 @@ per-frame pipeline of KillingFusion::processNextFrame
 Jacobi iterations, mesh the live SDF, warp it by psi and fuse it into the
 canonical SDF, mesh the registered and the canonical SDF.
 
-Frames run two deep on four CUDA streams: a frame's reset and integration
-beside the solve of the frame before, its registered and canonical meshes
-beside the solve of the frame after, with events ordering what they share
+Frames run two deep on four CUDA streams: a frame's reset, integration and
+live mesh beside the solve of the frame before, its registered and canonical
+meshes beside the solve of the frame after, with events ordering what they share
 (the canonical SDF, each slot's live SDF, psi and mesh buffers).
 
 value: voxel-updates/s = 256^3 * 200 * steps / time, every frame's inputs
@@ -202,8 +202,9 @@ def run_ours(args, rank, world, local):
 
     # Two frames in flight.  Frame f uses slot f % 2: its live SDF, psi, mesh
     # buffers and triangle counts.  Four streams:
-    #   s_in   reset + integration of the frame and zero psi, beside the solve of the frame before;
-    #   s_main the solve, the live mesh, warp + fuse (the canonical SDF's chain);
+    #   s_in   reset + integration of the frame, zero psi and the live mesh, beside the solve
+    #          of the frame before;
+    #   s_main the solve and warp + fuse (the canonical SDF's chain);
     #   s_out  the registered and canonical meshes, beside the next frame's solve;
     #   s_copy the host copies of a finished frame's meshes (end to end).
     # Events order what the slots and the canonical SDF share: a slot's live
@@ -229,15 +230,16 @@ def run_ours(args, rank, world, local):
         capi.check(L.kf_integrate_depth(lv.h, depth.data_ptr(), depth.shape[1], depth.shape[0], eye, Kd,
                                         0.05, max_depth, s_in.cuda_stream))
         ps.zero(stream=s_in)  # free too: warp + fuse of frame f - 2 came before its meshes
+        # the live mesh is of the SDF as integrated (the solve only reads it)
+        s_in.wait_event(ev_copied[k])
+        capi.check(L.kf_marching_cubes_async(lv.h, C.byref(Pc), ms[0].data_ptr(), MESH_CAP, cptr,
+                                             s_in.cuda_stream))
         ev_integ[k].record(s_in)
         s_main.wait_event(ev_integ[k])
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s_main)
         capi.check(L.kf_psi_solve_async(lv.h, can.h, ps.h, C.byref(Pc), args.iters, solver, s_main.cuda_stream))
         e1.record(s_main)
-        s_main.wait_event(ev_copied[k])
-        capi.check(L.kf_marching_cubes_async(lv.h, C.byref(Pc), ms[0].data_ptr(), MESH_CAP, cptr,
-                                             s_main.cuda_stream))
         s_main.wait_event(ev_meshed[1 - k])  # the canonical mesh of frame f - 1
         capi.check(L.kf_warp_fuse(can.h, lv.h, ps.h, C.byref(Pc), s_main.cuda_stream))
         ev_fused[k].record(s_main)
