@@ -171,11 +171,11 @@ def run_ours(args, rank, world, local):
     import numpy as np
     import torch
 
-    from killingfusion_gb300 import capi, synth
+    from killingfusion_gb300 import capi
+    from killingfusion_gb300.pipeline import FramePipeline
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    L = capi.load()
     seq, nseq, max_depth, _ = workload_sequence(args)
     grid = seq.grid
     P = capi.Params.paper(grid.voxel)
@@ -185,134 +185,34 @@ def run_ours(args, rank, world, local):
     dev_frames = [torch.from_numpy(f).to(dev) for f in host_frames]
     pinned = [torch.from_numpy(f).pin_memory() for f in host_frames]
 
-    can = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
-    live = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
-    psi = capi.Field(grid.dims, capi.KF_F32)
-    can.integrate(dev_frames[0], min_depth=0.05, max_depth=max_depth)
     N3 = int(np.prod(grid.dims))
-    solver = capi.SOLVERS[args.solver]
-    stats = capi.SolveStats()
     # reset, integrate (3 kernels), the solve (fused: stream + band per
     # iteration and one write-back; plain: 7 kernels), warp+fuse (2), 3
     # meshes of 3 kernels each
     launches_per_frame = 1 + 3 + fused_solve_launches(N3, args.iters) + 2 + 3 * 3 if args.solver == "fused" else \
         1 + 3 + 7 * args.iters + 2 + 3 * 3
-    Pc = P.c()
-    eye, Kd = capi._d(np.eye(4).ravel()), capi._d(synth.K.ravel())
 
-    # Two frames in flight.  Frame f uses slot f % 2: its live SDF, psi, mesh
-    # buffers and triangle counts.  Four streams:
-    #   s_in   reset + integration of the frame, zero psi and the live mesh, beside the solve
-    #          of the frame before;
-    #   s_main the solve and warp + fuse (the canonical SDF's chain);
-    #   s_out  the registered and canonical meshes, beside the next frame's solve;
-    #   s_copy the host copies of a finished frame's meshes (end to end).
-    # Events order what the slots and the canonical SDF share: a slot's live
-    # SDF is reset only after its meshes of two frames back are done, warp +
-    # fuse waits for the canonical mesh of the frame before, and the mesh
-    # buffers are rewritten only after their host copies.
-    lives = [live, capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)]
-    psis = [psi, capi.Field(grid.dims, capi.KF_F32)]
-    meshes = [[torch.empty((MESH_CAP, 9), dtype=torch.float32, device=dev) for _ in range(3)] for _ in range(2)]
-    host_mesh = [torch.empty((MESH_CAP, 9), dtype=torch.float32).pin_memory() for _ in range(3)]
-    counts = torch.zeros((2, 3), dtype=torch.int64).pin_memory()  # triangle counts, written by the device
-    s_in, s_main, s_out, s_copy = (torch.cuda.Stream(dev) for _ in range(4))
-    ev_integ, ev_fused, ev_meshed, ev_copied = ([torch.cuda.Event(), torch.cuda.Event()] for _ in range(4))
-
-    def queue(f, depth, e2e):
-        """Queue frame f (one processNextFrame, KillingFusion.cpp:123-170) on
-        the four streams without waiting; returns the solve's event pair."""
-        k = f % 2
-        lv, ps, ms = lives[k], psis[k], meshes[k]
-        cptr = counts.data_ptr() + 24 * k
-        s_in.wait_event(ev_meshed[k])
-        lv.reset(P, stream=s_in)
-        capi.check(L.kf_integrate_depth(lv.h, depth.data_ptr(), depth.shape[1], depth.shape[0], eye, Kd,
-                                        0.05, max_depth, s_in.cuda_stream))
-        ps.zero(stream=s_in)  # free too: warp + fuse of frame f - 2 came before its meshes
-        # the live mesh is of the SDF as integrated (the solve only reads it)
-        s_in.wait_event(ev_copied[k])
-        capi.check(L.kf_marching_cubes_async(lv.h, C.byref(Pc), ms[0].data_ptr(), MESH_CAP, cptr,
-                                             s_in.cuda_stream))
-        ev_integ[k].record(s_in)
-        s_main.wait_event(ev_integ[k])
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(s_main)
-        capi.check(L.kf_psi_solve_async(lv.h, can.h, ps.h, C.byref(Pc), args.iters, solver, s_main.cuda_stream))
-        e1.record(s_main)
-        s_main.wait_event(ev_meshed[1 - k])  # the canonical mesh of frame f - 1
-        capi.check(L.kf_warp_fuse(can.h, lv.h, ps.h, C.byref(Pc), s_main.cuda_stream))
-        ev_fused[k].record(s_main)
-        s_out.wait_event(ev_fused[k])
-        s_out.wait_event(ev_copied[k])
-        capi.check(L.kf_marching_cubes_async(lv.h, C.byref(Pc), ms[1].data_ptr(), MESH_CAP, cptr + 8,
-                                             s_out.cuda_stream))
-        capi.check(L.kf_marching_cubes_async(can.h, C.byref(Pc), ms[2].data_ptr(), MESH_CAP, cptr + 16,
-                                             s_out.cuda_stream))
-        ev_meshed[k].record(s_out)
-        return e0, e1
-
-    def finish(f, e2e):
-        """Wait for frame f: its solve's status, its triangle counts and (end
-        to end) the host copies of its meshes, queued on s_copy; returns the
-        counts and the bytes copied."""
-        k = f % 2
-        capi.check(L.kf_psi_solve_wait(psis[k].h, C.byref(stats)))
-        ev_meshed[k].synchronize()
-        n = [int(v) for v in counts[k].tolist()]
-        if max(n) > MESH_CAP:
-            raise RuntimeError("mesh of %d triangles above the buffers' %d" % (max(n), MESH_CAP))
-        d2h = 0
-        if e2e:
-            with torch.cuda.stream(s_copy):
-                for j in range(3):
-                    host_mesh[j][:n[j]].copy_(meshes[k][j][:n[j]], non_blocking=True)
-                    d2h += n[j] * 36
-            ev_copied[k].record(s_copy)
-        return tuple(n), d2h
-
-    def run_frames(frames, e2e, ev_start=None, ev_end=None):
-        """Frames in order, two in flight; returns the solve event pairs, the
-        triangle counts and the bytes copied to the host."""
-        if ev_start is not None:
-            ev_start.record(s_main)
-            for st_ in (s_in, s_out, s_copy):
-                st_.wait_event(ev_start)
-        solve_ev, tris, d2h = [], [], 0
-        for j, (f, depth) in enumerate(frames):
-            solve_ev.append(queue(f, depth, e2e))
-            if j > 0:
-                tc, b = finish(frames[j - 1][0], e2e)
-                tris.append(tc)
-                d2h += b
-        tc, b = finish(frames[-1][0], e2e)
-        tris.append(tc)
-        d2h += b
-        if ev_end is not None:
-            for st_ in (s_in, s_out, s_copy):
-                ev = torch.cuda.Event()
-                ev.record(st_)
-                s_main.wait_event(ev)
-            ev_end.record(s_main)
-        return solve_ev, tris, d2h
+    # two frames in flight on four streams (killingfusion_gb300.pipeline)
+    pipe = FramePipeline(grid.dims, grid.voxel, grid.origin, P, args.iters, args.solver,
+                         max_depth=max_depth, mesh_capacity=MESH_CAP, device=local)
+    stats = pipe.stats
 
     def barrier():
         torch.cuda.synchronize(dev)
         if world > 1:
             torch.distributed.barrier()
 
-    # warm-up (also captures the solve graph of each slot); the set-up above
-    # ran on the default stream
-    barrier()
-    run_frames([(f, dev_frames[f]) for f in range(1, 1 + args.warmup)], False)
+    # warm-up (also captures the solve graph of each slot)
+    pipe.start(dev_frames[0])
+    pipe.run([(f, dev_frames[f]) for f in range(1, 1 + args.warmup)])
     barrier()
 
     clocks = Clocks(local)
     clocks.start()
     t0 = time.perf_counter()
     ev_start, ev_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    solve_events, tri_counts, _ = run_frames([(f, dev_frames[f]) for f in range(1 + args.warmup, nframes)],
-                                             False, ev_start, ev_end)
+    solve_events, tri_counts, _ = pipe.run([(f, dev_frames[f]) for f in range(1 + args.warmup, nframes)],
+                                           False, ev_start, ev_end)
     barrier()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
@@ -320,31 +220,19 @@ def run_ours(args, rank, world, local):
     solve_ms = [a.elapsed_time(b) for a, b in solve_events]
     active = stats.active_first
 
-    # end to end through the C ABI with host buffers, on a fresh canonical
-    # grid so that it replays the same frames as the timed region
-    can_e2e = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
-    can, can_e2e = can_e2e, can
-
-    def canonical_from_host():
-        can.reset(P, stream=s_main)
-        capi.check(L.kf_integrate_depth(can.h, pinned[0].data_ptr(), 640, 480, eye, Kd, 0.05, max_depth,
-                                        s_main.cuda_stream))
-        s_main.synchronize()
-
-    # the same warm-up frames as the timed region, from host buffers: they
-    # capture each slot's solve graph for the new canonical grid and size the
-    # depth staging buffers, and the timed frames then meet the same
-    # canonical SDF (so their meshes must be the same)
-    barrier()
-    canonical_from_host()
-    run_frames([(f, pinned[f]) for f in range(1, 1 + args.warmup)], True)
+    # end to end through the C ABI with host buffers: the canonical SDF
+    # starts again from frame 0 and the warm-up frames are replayed, so the
+    # timed frames meet the same canonical SDF (and must give the same meshes)
+    pipe.start(pinned[0])
+    pipe.run([(f, pinned[f]) for f in range(1, 1 + args.warmup)], True)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    _, tri_e2e, d2h_total = run_frames([(f, pinned[f]) for f in range(1 + args.warmup, nframes)], True, e0, e1)
+    _, tri_e2e, d2h_total = pipe.run([(f, pinned[f]) for f in range(1 + args.warmup, nframes)], True, e0, e1)
     barrier()
     e2e_ms = e0.elapsed_time(e1)
     if tri_e2e != tri_counts:
         raise RuntimeError("end-to-end frames gave other meshes: %s vs %s" % (tri_e2e, tri_counts))
+    live, psi, can_e2e = pipe.lives[0], pipe.psis[0], pipe.can
 
     # plain per-term solver on the same frame (fewer iterations), for the ratio
     plain_it = 10
