@@ -2,12 +2,17 @@
 """Benchmark of the KillingFusion registration loop on GB300.
 
 Workload: the 256^3 / 5 mm sequence -- a union of 5 ellipsoids bending about
-a seeded hinge, 640x480 float32 depth with 1.5 mm noise -- with the paper
-weights and 200 psi iterations per frame.  One step is one frame of the
-per-frame pipeline of KillingFusion::processNextFrame
-(KillingFusion.cpp:123-170): integrate the live frame, zero psi, 200 fused
-Jacobi iterations, mesh the live SDF, warp it by psi and fuse it into the
-canonical SDF, mesh the registered and the canonical SDF.
+a seeded hinge, 640x480 float32 depth with 1.5 mm noise -- with 200 psi
+iterations per frame, at the reference's compiled-in weights (alpha 0.025,
+omega_k 0.04, gamma 0, omega_s 0.1, config.cpp:45-54; `--weights paper` for
+alpha 0.1, omega_k 0.5, gamma 0.1, omega_s 0.2).  At the paper weights the
+reference's own FP64 iteration amplifies rounding beyond a few tens of
+iterations, so psi can be compared with the oracle at 200 iterations only at
+the reference's weights.  One step is one frame of the per-frame pipeline of
+KillingFusion::processNextFrame (KillingFusion.cpp:123-170): integrate the
+live frame, zero psi, 200 fused Jacobi iterations, mesh the live SDF, warp it
+by psi and fuse it into the canonical SDF, mesh the registered and the
+canonical SDF.
 
 Frames run two deep on four CUDA streams: a frame's reset, integration and
 live mesh beside the solve of the frame before, its registered and canonical
@@ -17,9 +22,13 @@ meshes beside the solve of the frame after, with events ordering what they share
 value: voxel-updates/s = 256^3 * 200 * steps / time, every frame's inputs
 resident in HBM.  e2e: the same through the C ABI with the depth frame copied
 from pinned host memory and the three meshes copied back each step.
+psi_err_vs_oracle: one frame's float32 psi against the FP64 oracle's on the
+same SDFs, measured in the CPU-baseline leg, which runs that frame in full.
 
 `--impl reference` times the FP64 CPU restatement of the reference (the
-oracle) on the host cores on a bounded sample of the same frame.
+oracle) on the host cores: every timed step is one full frame (integrate,
+200 Jacobi iterations, update + fuse, three meshes); the untimed warm-up
+steps run the frame with 2 iterations.
 """
 import argparse
 import ctypes as C
@@ -54,8 +63,11 @@ def parse():
     ap.add_argument("--iters", type=int, default=None,
                     help="psi iterations per frame (default: 200 ellipsoid, 100 sphere, 300 large)")
     ap.add_argument("--solver", default="fused", choices=["fused", "plain"])
+    ap.add_argument("--weights", default="reference", choices=["reference", "paper"],
+                    help="reference: the compiled-in alpha/omega_k/gamma/omega_s (config.cpp:45-54); "
+                         "paper: the values in the comment at config.cpp:32-41")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-iters", type=int, default=2, help="Jacobi iterations in the CPU sample")
+    ap.add_argument("--no-band-frame", action="store_true", help="skip the band-only frame measurement")
     ap.add_argument("--workload", default="ellipsoid", choices=["ellipsoid", "sphere", "batch", "large"],
                     help="ellipsoid: 256^3 sequence (the bench line); sphere: the 64^3 two-frame sphere "
                          "pair, 100 iterations; batch: 64 registration problems of 32-160^3, 150 "
@@ -167,6 +179,36 @@ def fused_solve_launches(n3, iters):
     return 3 * iters + 1 if runs >= 512 else 2 * iters + 1
 
 
+WEIGHTS_TEXT = {
+    "reference": "reference (config.cpp:45-54): alpha 0.025, omega_k 0.04, gamma 0, omega_s 0.1",
+    "paper": "paper (config.cpp:32-41): alpha 0.1, omega_k 0.5, gamma 0.1, omega_s 0.2",
+}
+
+
+def bench_params(args, voxel):
+    """Solver parameters of the workloads: 5-voxel truncation band, the
+    weights chosen by --weights."""
+    from killingfusion_gb300 import capi
+    if args.weights == "paper":
+        return capi.Params.paper(voxel, 5.0)
+    return capi.Params.reference(voxel, 5.0)
+
+
+def bench_config(args):
+    """The workload's description, the same on both arms."""
+    seq, _, _, name = workload_sequence(args)
+    n = seq.grid.dims
+    sphere = args.workload == "sphere"
+    return {
+        "workload": name, "grid": "%dx%dx%d" % tuple(n), "voxel_mm": seq.grid.voxel * 1e3,
+        "iterations_per_frame": args.iters, "weights": WEIGHTS_TEXT[args.weights],
+        "frames": "frame 0 canonical, then live frames 1..%d in turn" % (seq.frames - 1),
+        "step": "one processNextFrame: integrate, zero psi, %d psi iterations, 3 meshes, warp+fuse" % args.iters,
+        "l2": ("inputs fit in L2 (16 B x 64^3 = 4.2 MB per iteration)" if sphere else
+               "inputs larger than L2 (psi 201 MB + phi_live 67 MB read per iteration)"),
+    }
+
+
 def run_ours(args, rank, world, local):
     import numpy as np
     import torch
@@ -178,7 +220,7 @@ def run_ours(args, rank, world, local):
     dev = torch.device("cuda", local)
     seq, nseq, max_depth, _ = workload_sequence(args)
     grid = seq.grid
-    P = capi.Params.paper(grid.voxel)
+    P = bench_params(args, grid.voxel)
     nframes = 1 + args.warmup + args.steps
     # frame 0 is the canonical frame; the live frames cycle through the rest
     host_frames = [seq.frame(0 if f == 0 else 1 + (f - 1) % (nseq - 1)) for f in range(nframes)]
@@ -248,12 +290,46 @@ def run_ours(args, rank, world, local):
         psi.zero()
         stb = capi.psi_solve(live, can_e2e, psi, P, args.iters, "band")
         band_ms.append(stb["device_ms"])
+    pipe.close()
+
+    # whole frames with the band-only solver in the same pipeline: the same
+    # psi, so the same meshes
+    band_frame = None
+    if not args.no_band_frame and args.solver == "fused":
+        pb = FramePipeline(grid.dims, grid.voxel, grid.origin, P, args.iters, "band",
+                           max_depth=max_depth, mesh_capacity=MESH_CAP, device=local)
+        pb.start(dev_frames[0])
+        pb.run([(f, dev_frames[f]) for f in range(1, 1 + args.warmup)])
+        barrier()
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        bsolve, tri_band, _ = pb.run([(f, dev_frames[f]) for f in range(1 + args.warmup, nframes)], False, b0, b1)
+        barrier()
+        if tri_band != tri_counts:
+            raise RuntimeError("band-only frames gave other meshes: %s vs %s" % (tri_band, tri_counts))
+        band_frame = {"ms_per_frame": b0.elapsed_time(b1) / args.steps,
+                      "solve_ms": statistics.mean(a.elapsed_time(b) for a, b in bsolve)}
+        pb.close()
+
+    # one frame for the psi comparison with the oracle (CPU-baseline leg):
+    # frame 1 registered onto frame 0 by the dense fused solver
+    parity = None
+    if world == 1 and not args.no_cpu_baseline:
+        gc = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
+        gl = capi.Grid(grid.dims, grid.voxel, grid.origin, P.unknown_clip, P)
+        gc.integrate(dev_frames[0], min_depth=0.05, max_depth=max_depth)
+        gl.integrate(torch.from_numpy(seq.frame(1)).to(dev), min_depth=0.05, max_depth=max_depth)
+        fp = capi.Field(grid.dims, capi.KF_F32)
+        stp = capi.psi_solve(gl, gc, fp, P, args.iters, args.solver)
+        parity = {"live": gl.download()[0], "can": gc.download()[0], "psi": fp.download(), "stats": stp}
+        for h in (gc, gl, fp):
+            h.close()
 
     res = {
         "elapsed_ms": elapsed_ms, "wall_s": wall, "solve_ms": solve_ms, "e2e_ms": e2e_ms,
         "d2h_bytes_per_step": d2h_total / args.steps, "tris": tri_counts, "active": active,
         "clocks": clk, "N3": N3, "other_vups": other_vups, "launches": launches_per_frame * args.steps,
         "band_ms": statistics.median(band_ms[1:]), "band_active_last": stb["active_last"],
+        "band_frame": band_frame, "parity": parity,
     }
     return res, seq, P
 
@@ -280,7 +356,7 @@ def run_batch(args, local):
     probs = []
     for k, n in enumerate(sizes):
         can, live, voxel = synth.shape_problem(1000 + k, n)
-        P = capi.Params.paper(voxel)
+        P = bench_params(args, voxel)
         gl = capi.Grid((n, n, n), voxel, (0, 0, 0), P.unknown_clip, P)
         gc = capi.Grid((n, n, n), voxel, (0, 0, 0), P.unknown_clip, P)
         gl.upload(live, (live <= P.max_surface).astype(np.int32))
@@ -326,14 +402,15 @@ def run_batch(args, local):
             torch.cuda.synchronize()
             seq_ms[solver] = a.elapsed_time(b)
     batch.close()
-    small = small_batch(capi, synth, torch, iters)
+    small = small_batch(capi, synth, torch, iters, lambda v: bench_params(args, v))
     value = voxels * iters / (ms / 1e3)
     return {
         "metric": METRIC, "value": value, "unit": "voxel-updates/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "batch-64", "problems": len(sizes), "edges": [min(sizes), max(sizes)],
-                   "voxels": voxels, "iterations": iters, "weights": "paper", "solver": "batched band-only",
+                   "voxels": voxels, "iterations": iters, "weights": WEIGHTS_TEXT[args.weights],
+                   "solver": "batched band-only",
                    "band_blocks_per_sm": blocks, "band_registers": regs,
                    "step": "zero psi of all 64 problems, one kf_batch_run (150 iterations each)"},
         "band_voxels_first_iteration": band_total,
@@ -344,7 +421,7 @@ def run_batch(args, local):
     }
 
 
-def small_batch(capi, synth, torch, iters, count=192):
+def small_batch(capi, synth, torch, iters, params, count=192):
     """Many small problems (edges 16-40), where one launch per problem and
     iteration is latency-bound: batched vs one after another."""
     import numpy as np
@@ -353,7 +430,7 @@ def small_batch(capi, synth, torch, iters, count=192):
     probs = []
     for k, n in enumerate(sizes):
         can, live, voxel = synth.shape_problem(5000 + k, n)
-        P = capi.Params.paper(voxel)
+        P = params(voxel)
         gl = capi.Grid((n, n, n), voxel, (0, 0, 0), P.unknown_clip, P)
         gc = capi.Grid((n, n, n), voxel, (0, 0, 0), P.unknown_clip, P)
         gl.upload(live, (live <= P.max_surface).astype(np.int32))
@@ -404,7 +481,7 @@ def run_large(args, local):
     iters = 300
     seq = synth.CapsuleSequence(seed=5, frames=100, n=512)
     grid = seq.grid
-    P = capi.Params.paper(grid.voxel)
+    P = bench_params(args, grid.voxel)
     steps = max(args.steps, 10)
     nframes = 1 + args.warmup + steps
     dev_frames = [torch.from_numpy(seq.frame(f)).to(dev) for f in range(nframes)]
@@ -451,7 +528,7 @@ def run_large(args, local):
         "steps": steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "capsule-sequence-512", "grid": [512] * 3, "voxel_mm": 2.0,
-                   "iterations_per_frame": iters, "weights": "paper", "solver": "fused",
+                   "iterations_per_frame": iters, "weights": WEIGHTS_TEXT[args.weights], "solver": "fused",
                    "step": "one frame: integrate, zero psi, 300 iterations; warp+fuse and 3 meshes "
                            "every 10th frame"},
         "solve_ms_last_frame": solve_ms, "band_voxels": stats.active_first,
@@ -461,56 +538,57 @@ def run_large(args, local):
     }
 
 
-def cpu_sample(seq, P, iters, max_depth=1.6, nthreads=0):
-    """Bounded FP64 sample of one frame on the host cores: integrate, `iters`
-    Jacobi iterations, update + fuse, three meshes; extrapolated to the
-    frame's full iteration count by the caller."""
-    import numpy as np
+class CpuFrame:
+    """One frame of the reference's pipeline on the host cores through the
+    FP64 oracle (the reference's arithmetic restated in C, OpenMP over all
+    host threads): integrate the live frame, `iters` Jacobi iterations
+    (a fresh delta field each iteration, as KillingFusion.cpp:256 allocates),
+    mesh the live SDF, warp it by psi, fuse it into the canonical SDF, mesh
+    the registered and the canonical SDF.  The canonical SDF is frame 0,
+    integrated once when the object is made (untimed)."""
 
-    from oracle.oracle import Oracle, Params as OParams
-    from killingfusion_gb300 import synth
+    def __init__(self, seq, P, max_depth):
+        import numpy as np
 
-    O = Oracle()
-    OP = OParams(**{k: getattr(P, k) for k in OParams.__dataclass_fields__})
-    g = seq.grid
-    n = g.dims[::-1]
-    f0 = seq.frame(0).astype(np.float64)
-    f1 = seq.frame(1).astype(np.float64)
-    base = np.full(n, OP.max_surface + OP.epsilon)
-    w0 = np.zeros(n, np.int64)
-    can, wc = O.integrate(base, w0, g.voxel, g.origin, OP.unknown_clip, f0, np.eye(4), synth.K, 0.05,
-                          max_depth)
-    t = {}
-    a = time.perf_counter()
-    live, wl = O.integrate(base, w0, g.voxel, g.origin, OP.unknown_clip, f1, np.eye(4), synth.K, 0.05,
-                           max_depth)
-    t["integrate"] = time.perf_counter() - a
-    a = time.perf_counter()
-    st, psi = O.solve(live, can, np.zeros(n + (3,)), iters, OP, nthreads=nthreads)
-    t["solve"] = time.perf_counter() - a
-    a = time.perf_counter()
-    m0 = O.mesh(live, OP)
-    uphi, uw = O.update(live, wl, psi, OP)
-    fphi, fw = O.fuse(can, wc, uphi, uw)
-    m1 = O.mesh(uphi, OP)
-    m2 = O.mesh(fphi, OP)
-    t["fuse_mesh"] = time.perf_counter() - a
-    return t
+        from oracle.oracle import Oracle, Params as OParams
+        from killingfusion_gb300 import synth
 
+        self.np, self.synth = np, synth
+        self.O = Oracle()
+        self.OP = OParams(**{k: getattr(P, k) for k in OParams.__dataclass_fields__})
+        self.seq, self.max_depth = seq, max_depth
+        shape = seq.grid.dims[::-1]
+        self.base = np.full(shape, self.OP.max_surface + self.OP.epsilon)
+        self.w0 = np.zeros(shape, np.int64)
+        self.can, self.wc = self._integrate(0)
 
-def cpu_sample_iters(args):
-    """Jacobi iterations the CPU sample times: all of them on the small
-    sphere pair, --cpu-iters of the 256^3 frame's 200 (then extrapolated)."""
-    return args.iters if args.workload == "sphere" else args.cpu_iters
+    def _integrate(self, f):
+        g = self.seq.grid
+        return self.O.integrate(self.base, self.w0, g.voxel, g.origin, self.OP.unknown_clip,
+                                self.seq.frame(f).astype(self.np.float64), self.np.eye(4), self.synth.K,
+                                0.05, self.max_depth)
 
-
-def cpu_sample_text(args, name, cpu_iters, cores):
-    if cpu_iters == args.iters:
-        return ("one frame of the %s workload: integrate, %d Jacobi iterations, update+fuse, 3 meshes; "
-                "FP64 oracle port on %d threads" % (name, args.iters, cores))
-    return ("one frame of the %s workload: integrate, %d of %d Jacobi iterations, update+fuse, 3 meshes; "
-            "FP64 oracle port on %d threads; frame time extrapolated to %d iterations"
-            % (name, cpu_iters, args.iters, cores, args.iters))
+    def run(self, f, iters, solve_inputs=None):
+        """Frame f; returns (seconds per stage, psi).  solve_inputs: (live,
+        canonical) SDFs to solve on instead of the oracle's own (the GPU's
+        float32 SDFs, for the psi comparison); the work is the same."""
+        np = self.np
+        t = {}
+        a = time.perf_counter()
+        live, wl = self._integrate(f)
+        t["integrate"] = time.perf_counter() - a
+        sl, sc = solve_inputs if solve_inputs is not None else (live, self.can)
+        a = time.perf_counter()
+        st, psi = self.O.solve(sl, sc, np.zeros(sl.shape + (3,)), iters, self.OP)
+        t["solve"] = time.perf_counter() - a
+        a = time.perf_counter()
+        self.O.mesh(live, self.OP)
+        uphi, uw = self.O.update(live, wl, psi, self.OP)
+        fphi, _ = self.O.fuse(self.can, self.wc, uphi, uw)
+        self.O.mesh(uphi, self.OP)
+        self.O.mesh(fphi, self.OP)
+        t["fuse_mesh"] = time.perf_counter() - a
+        return t, psi
 
 
 def cpu_threads():
@@ -532,8 +610,8 @@ def main():
     if args.workload not in ("ellipsoid", "sphere"):
         if args.impl == "reference":
             if rank == 0:
-                print(json.dumps({"impl": "reference", "unavailable": "the CPU port is timed on the 256^3 "
-                                  "ellipsoid workload only"}))
+                print(json.dumps({"impl": "reference", "unavailable": "the CPU port is timed on the "
+                                  "per-frame workloads (ellipsoid, sphere) only"}))
             return
         line = run_batch(args, local) if args.workload == "batch" else run_large(args, local)
         if rank == 0:
@@ -551,43 +629,49 @@ def max_over_ranks(values, device="cuda"):
     return [float(v) for v in t.tolist()]
 
 
+def run_reference(args):
+    """The reference arm: the FP64 CPU restatement of the reference on all
+    host threads, every timed step one full frame of the workload."""
+    import numpy as np
+
+    seq, nseq, max_depth, name = workload_sequence(args)
+    P = bench_params(args, seq.grid.voxel)
+    N3 = int(np.prod(seq.grid.dims))
+    cores = cpu_threads()
+    cf = CpuFrame(seq, P, max_depth)
+    live_frame = lambda k: 1 + k % (nseq - 1)  # noqa: E731
+    warm_iters = min(2, args.iters)
+    for k in range(args.warmup):
+        cf.run(live_frame(k), warm_iters)
+    per = []
+    for k in range(args.warmup, args.warmup + args.steps):
+        t, _ = cf.run(live_frame(k), args.iters)
+        per.append(sum(t.values()))
+    total_s = sum(per)
+    value = N3 * args.iters * args.steps / total_s
+    sample = ("%d full frames of the %s workload (integrate, %d Jacobi iterations, update+fuse, 3 meshes), "
+              "each timed in full; FP64 oracle port on %d threads; the %d untimed warm-up frames ran %d "
+              "iterations" % (args.steps, name, args.iters, cores, args.warmup, warm_iters))
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "voxel-updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": bench_config(args),
+        "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "frame_seconds": [round(v, 3) for v in per],
+    }
+
+
 def run_main(args, rank, world, local):
     import numpy as np
 
     if args.impl == "reference":
-        from killingfusion_gb300 import synth
-        seq, _, max_depth, name = workload_sequence(args)
-        from killingfusion_gb300.capi import Params
-        P = Params.paper(seq.grid.voxel)
-        N3 = int(np.prod(seq.grid.dims))
-        cores = cpu_threads()
-        cpu_iters = cpu_sample_iters(args)
-        per = []
-        for s in range(args.warmup + args.steps):
-            t = cpu_sample(seq, P, cpu_iters, max_depth)
-            frame_s = t["integrate"] + t["solve"] / cpu_iters * args.iters + t["fuse_mesh"]
-            if s >= args.warmup:
-                per.append(frame_s)
-        frame_s = statistics.mean(per)
-        value = N3 * args.iters / frame_s
-        sample = cpu_sample_text(args, name, cpu_iters, cores)
-        line = {
-            "impl": "reference", "metric": METRIC, "value": value, "unit": "voxel-updates/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": frame_s * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": name, "grid": list(seq.grid.dims), "voxel_mm": seq.grid.voxel * 1e3,
-                       "iterations_per_frame": args.iters, "weights": "paper"},
-            "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": cores, "kind": "port",
-                             "sample": sample},
-            "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0},
-        }
-        print(json.dumps(line))
+        print(json.dumps(run_reference(args)))
         return
 
     res, seq, P = run_ours(args, rank, world, local)
-    import torch
     el = res["elapsed_ms"]
     e2e_ms = res["e2e_ms"]
     if world > 1:
@@ -620,15 +704,9 @@ def run_main(args, rank, world, local):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {
-            "workload": workload_sequence(args)[3], "grid": list(seq.grid.dims),
-            "voxel_mm": seq.grid.voxel * 1e3, "iterations_per_frame": args.iters,
-            "weights": "paper", "solver": args.solver, "frames": "1 canonical + warmup + steps",
-            "step": "one processNextFrame: integrate, zero psi, %d psi iterations, 3 meshes, warp+fuse"
-                    % args.iters,
-            "l2": "inputs larger than L2 (psi 201 MB + phi_live 67 MB read per iteration)",
-            "parallelism": "replicas" if world > 1 else "1 GPU",
-        },
+        "config": bench_config(args),
+        "solver": args.solver,
+        "parallelism": "replicas" if world > 1 else "1 GPU",
         "e2e": {"value": e2e_value, "unit": "voxel-updates/s",
                 "h2d_bytes_per_step": 640 * 480 * 4, "d2h_bytes_per_step": res["d2h_bytes_per_step"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -650,28 +728,44 @@ def run_main(args, rank, world, local):
     }
     if args.workload == "sphere":
         # 64^3: 4.2 MB of psi and phi per iteration stay in the 129 MB L2
-        line["config"]["l2"] = "inputs fit in L2 (16 B x 64^3 = 4.2 MB per iteration)"
         line["roofline"] = None
         line["roofline_note"] = "L2-resident workload: the HBM roofline applies to the 256^3 bench line"
     if args.solver == "fused":
         line["fused_over_plain"] = line["solve_voxel_updates_per_s"] / res["other_vups"]
-    frame_other_ms = el / args.steps - solve_ms
-    line["band_solver"] = {
-        "solve_ms_per_frame": res["band_ms"],
-        "ms_per_frame_est": frame_other_ms + res["band_ms"],
+    band = {
+        "solve_ms": res["band_ms"],
         "dense_equivalent_voxel_updates_per_s": N3 * args.iters / (res["band_ms"] / 1e3),
         "band_voxels_last_iteration": res["band_active_last"],
         "note": "KF_SOLVER_BAND: identical psi; after the first dense pass it visits only the band, "
                 "which can only shrink (a voxel outside the band keeps psi)",
     }
+    if res["band_frame"]:
+        band["ms_per_frame"] = res["band_frame"]["ms_per_frame"]
+        band["solve_ms_in_frame"] = res["band_frame"]["solve_ms"]
+        band["frame_note"] = ("whole frames measured in the same two-frame pipeline with the band-only "
+                              "solver (same meshes as the dense frames)")
+    line["band_solver"] = band
     if world == 1 and not args.no_cpu_baseline:
-        cpu_iters = cpu_sample_iters(args)
-        t = cpu_sample(seq, P, cpu_iters, workload_sequence(args)[2])
-        frame_s = t["integrate"] + t["solve"] / cpu_iters * args.iters + t["fuse_mesh"]
+        import numpy as np
+        par = res["parity"]
+        cf = CpuFrame(seq, P, workload_sequence(args)[2])
+        t, opsi = cf.run(1, args.iters, (par["live"].astype(np.float64), par["can"].astype(np.float64)))
+        frame_s = sum(t.values())
+        err = np.abs(par["psi"].astype(np.float64) - opsi)
         line["cpu_baseline"] = {
             "value": N3 * args.iters / frame_s, "unit": "voxel-updates/s", "cores": cpu_threads(),
             "kind": "port", "ms_per_frame": frame_s * 1e3,
-            "sample": cpu_sample_text(args, workload_sequence(args)[3], cpu_iters, cpu_threads()),
+            "stage_s": {k: round(v, 3) for k, v in t.items()},
+            "sample": ("one full frame of the %s workload (frame 1 onto frame 0: integrate, %d Jacobi "
+                       "iterations, update+fuse, 3 meshes); FP64 oracle port on %d threads"
+                       % (workload_sequence(args)[3], args.iters, cpu_threads())),
+        }
+        line["psi_err_vs_oracle"] = {
+            "max_voxel": float(err.max()), "rms_voxel": float(np.sqrt((err ** 2).mean())),
+            "voxels_above_1e-4": int((err > 1e-4).sum()), "max_abs_psi_voxel": float(np.abs(opsi).max()),
+            "iterations": args.iters, "weights": args.weights, "solver": args.solver,
+            "frame": "frame 1 registered onto frame 0, float32 psi of the GPU against the FP64 oracle "
+                     "on the same float32 SDFs, every voxel",
         }
     print(json.dumps(line))
 

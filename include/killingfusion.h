@@ -391,13 +391,18 @@ int kf_fusion_state(kf_fusion f, kf_grid *canonical, kf_grid *live, kf_field *ps
  * start-up).  Same output as kf_marching_cubes, but it takes the SDF as a
  * plain device array (phi, float32, dims[0]*dims[1]*dims[2] values, x
  * fastest) and keeps its scratch in a fixed device array inside the library
- * (about 1.5 MB, held on every GPU that loads the library until the process
- * exits); it calls no cudaMalloc, cudaFree or allocating library routine.
- * Grids above KF_MC_NOALLOC_MAX_CELLS cells are rejected with
- * KF_ERR_INVALID.  The first call on a device looks up the array's address
- * on that device (make that first call outside any CUDA stream capture).
- * All calls share the one array: calls that overlap on the GPU (from two
- * streams or two host threads at once) race and must be serialised. */
+ * (786,440 bytes: a triangle count per block of 2048 cells and the blocks'
+ * 64-bit offsets for up to KF_MC_NOALLOC_MAX_CELLS cells; held on every GPU
+ * that loads the library until the process exits); it calls no cudaMalloc,
+ * cudaFree or allocating library routine.  Grids above
+ * KF_MC_NOALLOC_MAX_CELLS cells are rejected with KF_ERR_INVALID.  The
+ * first call on a device looks up the array's address on that device (make
+ * that first call outside any CUDA stream capture).  The call returns the
+ * triangle count, so it waits on `stream` until the count is known (copied
+ * into a host variable of the call); the emit pass runs over every block of
+ * cells, not only those with triangles.  All calls share the one array:
+ * calls that overlap on the GPU (from two streams or two host threads at
+ * once) race and must be serialised. */
 #define KF_MC_NOALLOC_MAX_CELLS (512LL * 512LL * 512LL)
 int kf_marching_cubes_noalloc(const float *phi, const int dims[3], const kf_params *p,
                               float *verts, int64_t capacity, int64_t *ntri, void *stream);

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
   const int lane = threadIdx.x & 31;
   // statistics of the staged problem, per thread until the problem changes
   float maxd = 0.f;
-  float energy = 0.f;
+  double energy = 0.0;  // float64 from the per-voxel terms up
   unsigned active = 0;
   bool diverged = false;
   // warp sums into the problem's shared totals (c, hence p, is the same in
@@ -164,12 +164,12 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
       if (active) {
         atomicAdd(&s_active[q], active);
         atomicMax(&s_maxd[q], __float_as_uint(maxd));
-        atomicAdd(&s_energy[q], (double)energy);
+        atomicAdd(&s_energy[q], energy);
       }
       if (any_div) s_div[q] = 1;
     }
     maxd = 0.f;
-    energy = 0.f;
+    energy = 0.0;
     active = 0;
     diverged = false;
   };

@@ -861,14 +861,28 @@ int small_query(const void *in, size_t bytes_in, void *out, size_t bytes_out, cu
   char *d = nullptr;
   KF_CHECK_CUDA(cudaMallocAsync((void **)&d, bytes_in + bytes_out + 256, s));
   char *dout = d + ((bytes_in + 255) & ~(size_t)255);
-  if (bytes_in) KF_CHECK_CUDA(cudaMemcpyAsync(d, in, bytes_in, cudaMemcpyDefault, s));
-  launch(d, dout);
-  cudaError_t le = cudaGetLastError();
-  if (bytes_out && le == cudaSuccess)
-    KF_CHECK_CUDA(cudaMemcpyAsync(out, dout, bytes_out, cudaMemcpyDefault, s));
-  KF_CHECK_CUDA(cudaFreeAsync(d, s));
-  KF_CHECK_CUDA(cudaStreamSynchronize(s));
-  if (le != cudaSuccess) return kf_cuda_fail(le, "query kernel");
+  // the buffer is released whatever fails after its allocation; the first
+  // error is the one reported
+  cudaError_t err = cudaSuccess;
+  const char *what = nullptr;
+  if (bytes_in) {
+    err = cudaMemcpyAsync(d, in, bytes_in, cudaMemcpyDefault, s);
+    what = "query input copy";
+  }
+  if (err == cudaSuccess) {
+    launch(d, dout);
+    err = cudaGetLastError();
+    what = "query kernel";
+  }
+  if (err == cudaSuccess && bytes_out) {
+    err = cudaMemcpyAsync(out, dout, bytes_out, cudaMemcpyDefault, s);
+    what = "query output copy";
+  }
+  const cudaError_t fe = cudaFreeAsync(d, s);
+  const cudaError_t se = cudaStreamSynchronize(s);
+  if (err != cudaSuccess) return kf_cuda_fail(err, what);
+  if (fe != cudaSuccess) return kf_cuda_fail(fe, "cudaFreeAsync of the query buffer");
+  if (se != cudaSuccess) return kf_cuda_fail(se, "query");
   return KF_OK;
 }
 

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
   const int total_threads = gridDim.x * kLaneThreads;
   const int rounds = (nq + total_threads - 1) / total_threads;
   float maxd = 0.f;
-  float energy = 0.f;  // this thread's voxels; the block and grid sums are float64
+  double energy = 0.0;  // this thread's voxels, summed in float64 as the block and grid sums
   unsigned active = 0;
   bool diverged = false;
   for (int r = 0; r < rounds; ++r) {
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
     }
     if (kCarry) block_append<kLaneWarps>(next, &a.st[a.iter + 1].list, list_out);
   }
-  reduce_iter_stats<kLaneThreads>(a.st + a.iter, active, maxd, (double)energy, diverged);
+  reduce_iter_stats<kLaneThreads>(a.st + a.iter, active, maxd, energy, diverged);
 }
 
 // In-place update after the last iteration: psi(list[k]) = entry k of the
@@ -262,7 +262,8 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_pervoxel(Fus
   const DevParams &dp = a.dp;
   const int nq = (int)a.st[0].list;
   const float thr = (float)dp.threshold;
-  float maxd = 0.f, energy = 0.f;
+  float maxd = 0.f;
+  double energy = 0.0;  // float64 from the per-voxel terms up
   unsigned capped = 0, most = 0;
   bool diverged = false;
   for (int k = blockIdx.x * kLaneThreads + threadIdx.x; k < nq; k += gridDim.x * kLaneThreads) {
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_pervoxel(Fus
     diverged |= div;
   }
   // voxels processed are counted by the band pass (record 0's list)
-  reduce_iter_stats<kLaneThreads>(a.st, 0u, maxd, (double)energy, diverged);
+  reduce_iter_stats<kLaneThreads>(a.st, 0u, maxd, energy, diverged);
   if (capped) atomicAdd(&a.st[1].active, capped);
   if (most) atomicMax(&a.st[1].list, most);
 }

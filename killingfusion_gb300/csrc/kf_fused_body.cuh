@@ -584,7 +584,7 @@ __device__ __noinline__ bool trust_step_f(const FusedArgs &a, int x, int y, int 
 // that the plain band pass carries no call to it.
 template <bool kTrust = false>
 __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int slot, float &maxd,
-                                                 float &energy, unsigned &active, bool &diverged) {
+                                                 double &energy, unsigned &active, bool &diverged) {
   const DevParams &dp = a.dp;
   int x, y, z;
   voxel_xyz(dp, i, x, y, z);

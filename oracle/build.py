@@ -16,6 +16,9 @@ Two products:
 Both use ``-ffp-contract=off`` so that no multiply-add is fused and the two
 agree bit for bit on the same inputs, on x86-64 and on aarch64 alike.
 
+The reference checkout is found at ``--ref REF_ROOT``, else at the path in the
+environment variable ``KF_REFERENCE_ROOT``, else at ``/root/reference``.
+
 Usage: ``python oracle/build.py [--ref REF_ROOT]``.
 """
 from __future__ import annotations
@@ -31,7 +34,13 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "libkf_oracle.so")
 REF_SO = os.path.join(REF_DIR, "libkf_ref.so")
-DEFAULT_REF_ROOT = "/root/reference"
+FALLBACK_REF_ROOT = "/root/reference"
+
+
+def default_ref_root() -> str:
+    """The reference checkout: $KF_REFERENCE_ROOT, else the fallback path."""
+    return os.environ.get("KF_REFERENCE_ROOT") or FALLBACK_REF_ROOT
+
 
 COMMON = ["-O2", "-fPIC", "-fopenmp", "-ffp-contract=off"]
 
@@ -58,15 +67,17 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def reference_available(ref_root: str = DEFAULT_REF_ROOT) -> bool:
+def reference_available(ref_root: str | None = None) -> bool:
+    ref_root = ref_root or default_ref_root()
     return os.path.isfile(os.path.join(ref_root, "KillingFusion", "src", "SDF.cpp"))
 
 
-def build_ref(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> str | None:
+def build_ref(ref_root: str | None = None, force: bool = False) -> str | None:
     """Compile the reference's hot-path sources into oracle/_ref/libkf_ref.so.
 
     Returns the library path, or None when the reference checkout is absent.
     """
+    ref_root = ref_root or default_ref_root()
     if not reference_available(ref_root):
         return None
     kf = os.path.join(ref_root, "KillingFusion")
@@ -98,7 +109,8 @@ def build_ref(ref_root: str = DEFAULT_REF_ROOT, force: bool = False) -> str | No
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("--ref", default=DEFAULT_REF_ROOT, help="reference checkout root")
+    ap.add_argument("--ref", default=None, help="reference checkout root (default: $KF_REFERENCE_ROOT, "
+                    "else %s)" % FALLBACK_REF_ROOT)
     ap.add_argument("--force", action="store_true")
     a = ap.parse_args(argv)
     print(build_oracle(a.force))

@@ -184,7 +184,7 @@ def test_mc_tables_match_reference_header(oracle):
     triTable (MarchingCubes.h:26-318), read from the reference checkout."""
     import re
     from oracle import build as obuild
-    path = os.path.join(obuild.DEFAULT_REF_ROOT, "KillingFusion", "include", "MarchingCubes.h")
+    path = os.path.join(obuild.default_ref_root(), "KillingFusion", "include", "MarchingCubes.h")
     if not os.path.exists(path):
         pytest.skip("reference checkout absent")
     src = open(path).read()

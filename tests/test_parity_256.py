@@ -1,0 +1,82 @@
+"""Float32 psi against the FP64 oracle on the benchmark's own 256^3 frame.
+
+The bench line measures the 256^3 / 5 mm ellipsoid sequence at 200 Jacobi
+iterations per frame (KillingFusion::computeDisplacementField,
+KillingFusion.cpp:248-352).  Here one of its frames (frame 3 registered onto
+frame 0) is solved by the float32 dense fused solver and the band-only
+solver (the two give the same bits) and by the FP64 oracle on the same
+float32 SDFs, and psi is compared at every voxel:
+
+* the reference's compiled-in weights (config.cpp:45-54), 200 iterations:
+  within 1e-4 voxel;
+* the paper weights, 20 iterations: within 1e-4 voxel.  Beyond a few tens of
+  iterations the paper weights amplify rounding in FP64 itself
+  (tests/test_chaos.py), so no float32 solver can track the oracle there.
+
+The band of every iteration must agree too: the oracle's count of band
+voxels at the first and the last iteration equals the GPU's.
+"""
+import numpy as np
+import pytest
+
+from killingfusion_gb300 import synth
+from oracle.oracle import Params as OParams
+
+pytestmark = pytest.mark.gpu
+
+PSI_TOL = 1e-4  # voxel
+
+
+def oparams(p):
+    return OParams(**{k: getattr(p, k) for k in OParams.__dataclass_fields__})
+
+
+@pytest.fixture(scope="module")
+def seq256(gpu):
+    """The bench's 256^3 ellipsoid sequence (its frames are seeded)."""
+    return synth.EllipsoidSequence(seed=2, frames=30, n=256)
+
+
+def solve_and_compare(capi, oracle, seq, P, iterations):
+    g = seq.grid
+    grids = []
+    for f in (0, 3):
+        grid = capi.Grid(g.dims, g.voxel, g.origin, P.unknown_clip, P)
+        grid.integrate(seq.frame(f), min_depth=0.05, max_depth=1.6)
+        grids.append(grid)
+    can, live = grids
+    psi, st = {}, {}
+    for solver in ("fused", "band"):
+        f = capi.Field(live.dims, capi.KF_F32)
+        st[solver] = capi.psi_solve(live, can, f, P, iterations, solver)
+        psi[solver] = f.download()
+        f.close()
+    np.testing.assert_array_equal(psi["fused"], psi["band"])
+    lphi, _ = live.download()
+    cphi, _ = can.download()
+    shape = g.dims[::-1]
+    ost, opsi, counts = oracle.solve(lphi.astype(np.float64), cphi.astype(np.float64),
+                                     np.zeros(shape + (3,)), iterations, oparams(P), active_counts=True)
+    assert ost == 0
+    err = np.abs(psi["fused"].astype(np.float64) - opsi)
+    s = st["fused"]
+    assert s["iterations_run"] == iterations
+    assert s["active_first"] == counts[0] > 10000
+    assert s["active_last"] == counts[-1] > 0
+    for grid in grids:
+        grid.close()
+    return err, opsi
+
+
+def test_reference_weights_200_iterations(gpu, oracle, seq256):
+    P = gpu.Params.reference(seq256.grid.voxel, 5.0)
+    err, opsi = solve_and_compare(gpu, oracle, seq256, P, 200)
+    assert np.abs(opsi).max() > 0.05  # psi moved far beyond the tolerance
+    assert err.max() <= PSI_TOL, (err.max(), int((err > PSI_TOL).sum()))
+
+
+def test_paper_weights_20_iterations(gpu, oracle, seq256):
+    P = gpu.Params.paper(seq256.grid.voxel)
+    err, opsi = solve_and_compare(gpu, oracle, seq256, P, 20)
+    assert np.abs(opsi).max() > 0.05
+    assert err.max() <= PSI_TOL, (err.max(), int((err > PSI_TOL).sum()))

@@ -78,3 +78,38 @@ def test_noalloc_capacity_and_size_limits(gpu):
                                      C.byref(m), None)
     assert st == capi.KF_ERR_INVALID
     assert "at most" in L.kf_last_error().decode()
+
+
+def test_noalloc_calls_allocate_no_device_memory(gpu):
+    """The point of the entry point: once the library is loaded and the
+    first call has looked up the scratch array's address, further calls
+    leave the device's free memory as it was.  Inputs and outputs are the
+    caller's, allocated here before the measurement."""
+    import torch
+    capi = gpu
+    L = capi.load()
+    P = capi.Params.paper(0.004)
+    grids = []
+    for k, n in enumerate((24, 40, 33)):
+        c, _ = small_pair(n, 0.004, 5.0, seed=50 + k)
+        grids.append((torch.from_numpy(c).cuda(), (n, n, n)))
+    verts = torch.empty((200_000, 9), dtype=torch.float32, device="cuda")
+    counts = []
+
+    def call(phi_dev, dims):
+        n = C.c_int64(-1)
+        st = L.kf_marching_cubes_noalloc(phi_dev.data_ptr(), capi._i3(dims), C.byref(P.c()),
+                                         verts.data_ptr(), verts.shape[0], C.byref(n), None)
+        assert st == capi.KF_OK, L.kf_last_error()
+        return n.value
+
+    for phi_dev, dims in grids:  # first calls: module load, symbol lookup
+        counts.append(call(phi_dev, dims))
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(4):
+        for k, (phi_dev, dims) in enumerate(grids):
+            assert call(phi_dev, dims) == counts[k]
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
