@@ -44,7 +44,8 @@ typedef enum kf_status {
   KF_ERR_CUDA = 3,     /* CUDA runtime error                                */
   KF_ERR_DIVERGED = 4, /* psi non-finite at a voxel in the band; the
                           reference throws -1 (KillingFusion.cpp:328-332)   */
-  KF_ERR_TIMEOUT = 5,  /* a bounded device-side wait gave up                */
+  KF_ERR_TIMEOUT = 5,  /* a bounded device-side wait gave up (the grid-wide
+                          barrier of a persistent kernel, kf_set_wait_limit) */
   KF_ERR_CAPACITY = 6, /* caller buffer too small (count is still returned) */
   KF_ERR_INTERNAL = 7  /* a consistency check of the library failed         */
 } kf_status;
@@ -135,6 +136,15 @@ void kf_params_reference(kf_params *p);
 /* Paper weights (alpha 0.1, omega_k 0.5, gamma 0.1, omega_s 0.2) with the
  * truncation band set to trunc_voxels voxels (config.cpp:32-41 comment). */
 void kf_params_paper(kf_params *p, double voxel_size, double trunc_voxels);
+/* Limit, in seconds, of one device-side wait: the grid-wide barrier between
+ * the iterations of the persistent kernels (KF_SOLVER_BAND and the batched
+ * solver run every iteration in one cooperative launch).  A wait that lasts
+ * longer gives up, the kernel ends and the call returns KF_ERR_TIMEOUT, with
+ * psi undefined.  No counterpart in the reference, which runs on the CPU.
+ * Default 1 s, process-wide; 0 makes every wait give up at once (for testing
+ * the error path).  Returns the previous limit, or -1 for a value outside
+ * [0, 60] (ignored). */
+double kf_set_wait_limit(double seconds);
 /* Introspection of the marching-cubes table (MarchingCubes.h:26-318): edge
  * mask of a cube configuration and its triangle list (edge ids, -1 padded). */
 int kf_mc_case(int cubeindex, int *edge_mask, int tri_edges[16]);

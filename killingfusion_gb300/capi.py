@@ -157,6 +157,7 @@ SIGNATURES = {
     "kf_fusion_destroy": (C.c_int, [_vp]),
     "kf_fusion_process_frame": (C.c_int, [_vp, _vp, _dp, C.c_int, C.c_void_p, _vp]),
     "kf_fusion_state": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
+    "kf_set_wait_limit": (C.c_double, [C.c_double]),
 }
 
 _lib = None
@@ -176,6 +177,15 @@ def load() -> C.CDLL:
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def set_wait_limit(seconds: float) -> float:
+    """Limit of one device-side wait of the persistent kernels (default 1 s);
+    returns the previous limit."""
+    prev = load().kf_set_wait_limit(float(seconds))
+    if prev < 0:
+        raise ValueError("wait limit outside [0, 60] s")
+    return prev
 
 
 def check(status: int):

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
 
 #include "kf_internal.h"
@@ -27,6 +28,17 @@ int kf_cuda_fail(cudaError_t e, const char *what) {
 }
 
 extern "C" int kf_version(void) { return KF_ABI_VERSION; }
+
+// Limit of a device-side wait (the grid-wide barrier of the persistent
+// kernels); one second unless kf_set_wait_limit changes it.
+static std::atomic<double> g_wait_limit_s{1.0};
+
+extern "C" double kf_set_wait_limit(double seconds) {
+  if (!(seconds >= 0.0) || seconds > 60.0) return -1.0;
+  return g_wait_limit_s.exchange(seconds);
+}
+
+unsigned long long kf_wait_limit_ns() { return (unsigned long long)(g_wait_limit_s.load() * 1e9); }
 
 extern "C" const char *kf_last_error(void) { return g_last_error.c_str(); }
 
@@ -343,7 +355,19 @@ int kf_field_trust_rows(kf_field f, int **out) {
   return KF_OK;
 }
 
+int kf_field_sync(kf_field f, void **out) {
+  if (!f->sync && cudaMalloc(&f->sync, 256) != cudaSuccess) {
+    cudaGetLastError();
+    f->sync = nullptr;
+    return kf_fail(KF_ERR_OOM, "cudaMalloc of the persistent pass's barrier failed");
+  }
+  *out = f->sync;
+  return KF_OK;
+}
+
 void kf_field_release_solver(kf_field f) {
+  cudaFree(f->sync);
+  f->sync = nullptr;
   cudaFree(f->band);
   cudaFree(f->runs);
   f->runs = nullptr;
@@ -733,6 +757,11 @@ static int solve_finish(kf_field psi, kf_solve_stats *stats, bool presumed_swapp
     if (diverged)
       return kf_fail(KF_ERR_DIVERGED, "deformation field diverged (non-finite psi inside the band)");
     return KF_OK;
+  }
+  if (host[0].timeout) {
+    if (stats) stats->device_ms = ms;
+    return kf_fail(KF_ERR_TIMEOUT, "a grid-wide wait of the persistent band pass gave up (limit " +
+                                       std::to_string(kf_wait_limit_ns() / 1e9) + " s); psi is undefined");
   }
   for (int k = 0; k < iterations; ++k)
     if (host[k].cold)

@@ -38,6 +38,7 @@
 #include <algorithm>
 
 #include "kf_fused_body.cuh"
+#include "kf_grid_sync.cuh"
 
 namespace {
 
@@ -205,6 +206,64 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
   reduce_iter_stats<kLaneThreads>(a.st + a.iter, active, maxd, energy, diverged);
 }
 
+// Band-only solver, every iteration in one cooperative launch.  One band pass
+// per iteration as k_fused_band<kCarry> (ping-pong buffers, the updated
+// voxels carried to the next iteration's list), then a grid-wide barrier
+// (kf_grid_sync.cuh) instead of a kernel boundary.  Band voxel k goes to
+// block k % G (thread k / G of it, G blocks), so a small band spreads over all
+// the SMs whatever the block size.  psi is read through L2 (the blocks write
+// it between iterations); the SDFs through the read-only path.  A gated
+// iteration (converged, diverged) ends the kernel in every block alike: each
+// reads the same statistics after the barrier.
+constexpr int kPersistThreads = 256;
+constexpr int kPersistBlocksPerSM = 2;
+
+__device__ __forceinline__ bool persistent_band_iteration(const FusedArgs &a, int it, bool last,
+                                                          const int *__restrict__ list_in,
+                                                          int *__restrict__ list_out, GridSync *sync,
+                                                          unsigned long long limit_ns) {
+  if (iteration_gated(a.st, it, a.dp)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st[it].skipped = 1;
+    return false;
+  }
+  const unsigned nq = __ldcg(&a.st[it].list);
+  const unsigned nb = gridDim.x;
+  const unsigned per_round = nb * kPersistThreads;
+  const unsigned rounds = (nq + per_round - 1) / per_round;
+  float maxd = 0.f;
+  double energy = 0.0;
+  unsigned active = 0;
+  bool diverged = false;
+  for (unsigned r = 0; r < rounds; ++r) {
+    const unsigned k = blockIdx.x + nb * (threadIdx.x + kPersistThreads * r);
+    int next = -1;
+    if (k < nq) {
+      const int v = __ldcg(list_in + k);
+      next = update_band_voxel<false, true>(a, v, v, maxd, energy, active, diverged);
+    }
+    block_append<kPersistThreads / 32>(next, &a.st[it + 1].list, list_out);
+  }
+  reduce_iter_stats<kPersistThreads>(a.st + it, active, maxd, energy, diverged);
+  if (last) return false;
+  if (!grid_sync(sync, nb, limit_ns, it)) {
+    if (threadIdx.x == 0) a.st[0].timeout = 1;
+    return false;
+  }
+  return true;
+}
+
+// even: psi in the primary planes, out to the second; odd: the reverse.
+__global__ void __launch_bounds__(kPersistThreads, kPersistBlocksPerSM)
+    k_band_persistent(FusedArgs even, FusedArgs odd, int *lst0, int *lst1, int iterations, GridSync *sync,
+                      unsigned long long limit_ns) {
+  for (int it = 0; it < iterations; it += 2) {
+    if (!persistent_band_iteration(even, it, it + 1 == iterations, lst0, lst1, sync, limit_ns)) return;
+    if (it + 1 < iterations &&
+        !persistent_band_iteration(odd, it + 1, it + 2 == iterations, lst1, lst0, sync, limit_ns))
+      return;
+  }
+}
+
 // In-place update after the last iteration: psi(list[k]) = entry k of the
 // band pass's output planes (the dense passes write back the others).
 __global__ void __launch_bounds__(kThreads) k_fused_scatter(FusedArgs a, const int *__restrict__ list,
@@ -281,7 +340,7 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_pervoxel(Fus
       if (interior) {
         gradient_lane<true>(a, x, y, z, i, d, sv, e, c0);
       } else {
-        gradient_generic(a, x, y, z, d, sv, e);
+        gradient_generic<true>(a, x, y, z, d, sv, e);
         c0[0] = __ldcg(a.ix + i);
         c0[1] = __ldcg(a.iy + i);
         c0[2] = __ldcg(a.iz + i);
@@ -469,6 +528,60 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
   }
 }
 
+// Resident blocks per SM of k_band_persistent on the current device (at most
+// kPersistBlocksPerSM): the cooperative launch must fit on the GPU at once.
+static int persistent_blocks_per_sm() {
+  static int cached[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (!cached[dev]) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_band_persistent, kPersistThreads, 0) !=
+        cudaSuccess)
+      return 0;
+    cached[dev] = std::min(n, kPersistBlocksPerSM);
+  }
+  return cached[dev];
+}
+
+// KF_SOLVER_BAND without the trust-region step: the dense first pass, then
+// every band pass in one cooperative launch (k_band_persistent).  Iteration
+// k reads buffer k % 2 and writes (k + 1) % 2, as the per-iteration form.
+static int launch_band_persistent(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
+                                  int iterations, IterStats *st, cudaStream_t s) {
+  void *sync = nullptr;
+  int rc = kf_field_sync(psi, &sync);
+  if (rc) return rc;
+  const int bps = persistent_blocks_per_sm();
+  if (bps < 1) return kf_fail(KF_ERR_CUDA, "the persistent band pass does not fit on an SM");
+  KF_CHECK_CUDA(cudaMemsetAsync(sync, 0, sizeof(GridSync), s));
+  FusedArgs even = make_args(live, can, dp, st);
+  even.ix = (const float *)psi->p[0];
+  even.iy = (const float *)psi->p[1];
+  even.iz = (const float *)psi->p[2];
+  even.ox = (float *)psi->q[0];
+  even.oy = (float *)psi->q[1];
+  even.oz = (float *)psi->q[2];
+  FusedArgs odd = even;
+  odd.ix = (const float *)psi->q[0];
+  odd.iy = (const float *)psi->q[1];
+  odd.iz = (const float *)psi->q[2];
+  odd.ox = (float *)psi->p[0];
+  odd.oy = (float *)psi->p[1];
+  odd.oz = (float *)psi->p[2];
+  int *lst0 = psi->band, *lst1 = psi->band + dp.count;
+  k_fused_stream<true><<<(unsigned)num_runs(dp), kThreads, 0, s>>>(even, lst0, nullptr, nullptr);
+  KF_CHECK_LAUNCH("dense first pass of the band-only solver");
+  GridSync *gs = static_cast<GridSync *>(sync);
+  unsigned long long limit = kf_wait_limit_ns();
+  int iters = iterations;
+  void *args[] = {&even, &odd, &lst0, &lst1, &iters, &gs, &limit};
+  KF_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)k_band_persistent,
+                                            dim3((unsigned)(kf_num_sms() * bps)), dim3(kPersistThreads), args, 0,
+                                            s));
+  return KF_OK;
+}
+
 int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp, int iterations,
                    IterStats *st, bool band_only, cudaStream_t s) {
   int rc = kf_field_ensure_pair(psi);
@@ -486,6 +599,7 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
     }
     psi->runs_cap = nruns;
   }
+  if (band_only && !dp.trust) return launch_band_persistent(live, can, psi, dp, iterations, st, s);
   int *rows = nullptr;
   if (dp.trust) {
     rc = kf_field_trust_rows(psi, &rows);

@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include <cstring>
+#include <type_traits>
 
 #include "kf_internal.h"
 #include "kf_ref_math.cuh"
@@ -330,13 +331,26 @@ __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, 
   e_out = e;
 }
 
+// A psi value read through L2 (ld.global.cg), never through the read-only
+// path: the element type of psi views in kernels that also write psi between
+// their reads (the persistent passes).  Same layout as float.
+struct CgFloat {
+  float v;
+  __device__ __forceinline__ operator float() const { return __ldcg(&v); }
+};
+
 // Generic reference-order gradient for the outer shell (one thread).
+// kCoherent: psi read through L2 (CgFloat).
+template <bool kCoherent = false>
 __device__ __noinline__ void gradient_generic(const FusedArgs &a, int x, int y, int z, float d[3],
                                               float &s_out, float &e_out) {
+  using P = typename std::conditional<kCoherent, CgFloat, float>::type;
   const DevParams &dp = a.dp;
+  const P *px = reinterpret_cast<const P *>(a.ix), *py = reinterpret_cast<const P *>(a.iy),
+          *pz = reinterpret_cast<const P *>(a.iz);
   PhiView<float> lv{a.live, dp.nx, dp.ny, dp.nz, a.oob};
   PhiView<float> cv{a.can, dp.nx, dp.ny, dp.nz, a.oob};
-  PsiView<float, float> f{a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz};
+  PsiView<float, P> f{px, py, pz, dp.nx, dp.ny, dp.nz};
   TParams<float> tp(dp);
   float g[3], gd[3];
   energy_gradient(lv, cv, f, tp, x, y, z, g);
@@ -344,8 +358,7 @@ __device__ __noinline__ void gradient_generic(const FusedArgs &a, int x, int y, 
   for (int k = 0; k < 3; ++k) d[k] = -tp.alpha * g[k];
   s_out = warped_distance(lv, f, x, y, z);
   distance_gradient(lv, f, tp.delta_size, x, y, z, gd);
-  e_out = monitor_energy(a.ix, a.iy, a.iz, dp.nx, dp.ny, dp.nz, x, y, z, s_out, cv.at(x, y, z), gd,
-                         dp);
+  e_out = monitor_energy(px, py, pz, dp.nx, dp.ny, dp.nz, x, y, z, s_out, cv.at(x, y, z), gd, dp);
 }
 
 __device__ __forceinline__ void voxel_xyz(const DevParams &dp, int i, int &x, int &y, int &z) {
@@ -582,7 +595,10 @@ __device__ __noinline__ bool trust_step_f(const FusedArgs &a, int x, int y, int 
 // if it left the band) and accumulates the statistics.
 // kTrust: the trust-region step (dp.trust set), a separate instantiation so
 // that the plain band pass carries no call to it.
-template <bool kTrust = false>
+// kCoherent: psi is read through L2 (ld.global.cg) rather than the read-only
+// path, for kernels that write psi themselves between iterations (the
+// persistent passes), where the read-only path's cache may hold old values.
+template <bool kTrust = false, bool kCoherent = false>
 __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int slot, float &maxd,
                                                  double &energy, unsigned &active, bool &diverged) {
   const DevParams &dp = a.dp;
@@ -592,12 +608,12 @@ __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int 
   const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 &&
                         z <= dp.nz - 2;
   if (interior) {
-    gradient_lane(a, x, y, z, i, d, s, en, c0);
+    gradient_lane<kCoherent>(a, x, y, z, i, d, s, en, c0);
   } else {
-    gradient_generic(a, x, y, z, d, s, en);
-    c0[0] = a.ix[i];
-    c0[1] = a.iy[i];
-    c0[2] = a.iz[i];
+    gradient_generic<kCoherent>(a, x, y, z, d, s, en);
+    c0[0] = kCoherent ? __ldcg(a.ix + i) : a.ix[i];
+    c0[1] = kCoherent ? __ldcg(a.iy + i) : a.iy[i];
+    c0[2] = kCoherent ? __ldcg(a.iz + i) : a.iz[i];
   }
   int next = -1;
   if (in_band(s, a.band_hi, a.band_lo)) {

@@ -51,6 +51,8 @@ struct kf_field_s {
   int64_t runs_cap;
   int *rows;              // trust-region step: the first x of each row (y, z)
                           // whose step failed, two arrays of ny*nz
+  void *sync;             // barrier state of the persistent band pass
+                          // (GridSync, kf_grid_sync.cuh)
   // the last solve launched on this field: its events (start, end, end of
   // the statistics copy), iteration count, solver and whether its statistics
   // are still to be read (kf_psi_solve_wait)
@@ -124,7 +126,16 @@ struct IterStats {
   unsigned int cold;      // band voxels the split dense schedule found in a
                           // run without band voxels at the first iteration
                           // (never expected: such voxels keep psi)
+  int timeout;            // record 0: a grid-wide wait of a persistent kernel
+                          // gave up (KF_ERR_TIMEOUT)
+  int pad_;
 };
+
+// Limit of one device-side wait (kf_set_wait_limit), in nanoseconds.
+unsigned long long kf_wait_limit_ns();
+// Barrier state of the persistent kernels (GridSync, 16 bytes) of a field,
+// lazily allocated.
+int kf_field_sync(kf_field f, void **out);
 
 // solver entry points implemented in the solver translation units
 int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,

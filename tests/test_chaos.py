@@ -14,7 +14,8 @@ and the two results are compared.
   of DisplacementField.cpp:342, so differences in the last bit grow until
   they are as large as the clamp allows.  No float32 (or differently ordered
   FP64) implementation can stay within 1e-4 voxel of the reference there
-  beyond a few tens of iterations.
+  beyond a few tens of iterations on this pair, and beyond a few iterations on
+  the 256^3 bench frame, where the growth is faster (tests/test_parity_256.py).
 * The reference's compiled-in weights (alpha 0.025, omega_k 0.04, gamma 0,
   omega_s 0.1, config.cpp:45-54): the perturbation does not grow over 200
   iterations, which is why the float32 parity tests and the bench line use

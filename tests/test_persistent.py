@@ -1,0 +1,82 @@
+"""The band-only solver's persistent launch (KF_SOLVER_BAND).
+
+Every band pass of a solve runs in one cooperative launch, the iterations
+separated by a grid-wide barrier whose wait is bounded (kf_set_wait_limit).
+* psi and the statistics equal the dense fused solver's, over solves long
+  enough to cross many barriers, including one that converges early;
+* a wait limit of zero makes every block but the last to arrive give up at
+  the first barrier: the solve returns KF_ERR_TIMEOUT, the GPU context stays
+  usable, and the next solve with the default limit is correct again.  No
+  kernel is made to fault or hang: the barrier's own bound ends the wait.
+"""
+import numpy as np
+import pytest
+
+from helpers import small_pair
+
+pytestmark = pytest.mark.gpu
+
+
+def grids(capi, P, n=40, seed=60):
+    can, live = small_pair(n, P.voxel_size, 5.0, seed=seed)
+    dims = (n, n, n)
+    gl = capi.Grid(dims, P.voxel_size, (0, 0, 0), P.unknown_clip, P)
+    gc = capi.Grid(dims, P.voxel_size, (0, 0, 0), P.unknown_clip, P)
+    gl.upload(live, (live <= P.max_surface).astype(np.int32))
+    gc.upload(can, (can <= P.max_surface).astype(np.int32))
+    return gl, gc, dims
+
+
+def solve(capi, gl, gc, dims, P, iters, solver):
+    f = capi.Field(dims, capi.KF_F32)
+    st = capi.psi_solve(gl, gc, f, P, iters, solver)
+    out = f.download()
+    f.close()
+    return out, st
+
+
+@pytest.mark.parametrize("iters", [1, 2, 7, 150])
+def test_persistent_band_equals_dense(gpu, iters):
+    capi = gpu
+    P = capi.Params.paper(0.004)
+    gl, gc, dims = grids(capi, P)
+    a, sa = solve(capi, gl, gc, dims, P, iters, "band")
+    b, sb = solve(capi, gl, gc, dims, P, iters, "fused")
+    np.testing.assert_array_equal(a, b)
+    for k in ("iterations_run", "active_first", "active_last", "max_delta_last", "converged", "diverged"):
+        assert sa[k] == sb[k], k
+    assert abs(sa["energy_last"] - sb["energy_last"]) <= 1e-9 * max(abs(sb["energy_last"]), 1.0)
+
+
+def test_persistent_band_early_exit(gpu):
+    capi = gpu
+    P = capi.Params.reference(0.004, 5.0).with_(early_exit=True, threshold=2e-4)
+    gl, gc, dims = grids(capi, P, seed=61)
+    a, sa = solve(capi, gl, gc, dims, P, 300, "band")
+    b, sb = solve(capi, gl, gc, dims, P, 300, "fused")
+    assert sa["converged"] == 1 and 1 < sa["iterations_run"] < 300
+    assert sa["iterations_run"] == sb["iterations_run"]
+    np.testing.assert_array_equal(a, b)
+
+
+def test_wait_limit_gives_timeout_status(gpu):
+    capi = gpu
+    L = capi.load()
+    P = capi.Params.paper(0.004)
+    gl, gc, dims = grids(capi, P, seed=62)
+    expect, _ = solve(capi, gl, gc, dims, P, 20, "fused")
+    prev = capi.set_wait_limit(0.0)
+    try:
+        f = capi.Field(dims, capi.KF_F32)
+        st = L.kf_psi_solve(gl.h, gc.h, f.h, capi.C.byref(P.c()), 20, capi.KF_SOLVER_BAND, None, None)
+        assert st == capi.KF_ERR_TIMEOUT, (st, L.kf_last_error())
+        assert b"gave up" in L.kf_last_error()
+        f.close()
+    finally:
+        assert capi.set_wait_limit(prev) == 0.0
+    # the context is usable and the next solve is right
+    got, st = solve(capi, gl, gc, dims, P, 20, "band")
+    np.testing.assert_array_equal(got, expect)
+    assert st["iterations_run"] == 20
+    with pytest.raises(ValueError):
+        capi.set_wait_limit(-1.0)
