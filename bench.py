@@ -364,7 +364,7 @@ def run_batch(args, local):
         probs.append((gl, gc, capi.Field((n, n, n), capi.KF_F32), P))
     voxels = sum(n ** 3 for n in sizes)
     batch = capi.Batch(probs, iters)
-    blocks, regs = batch.autotune()
+    shape = batch.autotune()
 
     def zero_all():
         for _, _, f, _ in probs:
@@ -411,13 +411,18 @@ def run_batch(args, local):
         "config": {"workload": "batch-64", "problems": len(sizes), "edges": [min(sizes), max(sizes)],
                    "voxels": voxels, "iterations": iters, "weights": WEIGHTS_TEXT[args.weights],
                    "solver": "batched band-only",
-                   "band_blocks_per_sm": blocks, "band_registers": regs,
-                   "step": "zero psi of all 64 problems, one kf_batch_run (150 iterations each)"},
+                   "autotuned_shape": "band CTA %d threads, chunks of %d voxels, %d CTAs/SM, %d registers; "
+                                      "dense slab %d planes" % (shape["band_threads"], shape["band_chunk"],
+                                                                 shape["band_blocks_per_sm"],
+                                                                 shape["band_registers"], shape["slab"]),
+                   "step": "zero psi of all 64 problems, one kf_batch_run (150 iterations each: a dense "
+                           "first pass, then every band pass in one persistent launch)"},
         "band_voxels_first_iteration": band_total,
         "sequential_band_ms": seq_ms["band"], "sequential_fused_ms": seq_ms["fused"],
         "batched_over_sequential_band": seq_ms["band"] / ms,
         "small_problems": small,
-        "clocks": clk, "gpu_launches": (1 + iters) * args.steps,
+        "shape": shape,
+        "clocks": clk, "gpu_launches": 2 * args.steps,
     }
 
 
@@ -463,7 +468,7 @@ def small_batch(capi, synth, torch, iters, params, count=192):
     vox = sum(n ** 3 for n in sizes)
     return {"problems": count, "edges": [min(sizes), max(sizes)], "voxels": vox, "iterations": iters,
             "batched_ms": tb, "sequential_band_ms": ts, "batched_over_sequential_band": ts / tb,
-            "batched_voxel_updates_per_s": vox * iters / (tb / 1e3), "shape": list(shape)}
+            "batched_voxel_updates_per_s": vox * iters / (tb / 1e3), "shape": shape}
 
 
 def run_large(args, local):

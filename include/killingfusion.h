@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define KF_ABI_VERSION 1
+#define KF_ABI_VERSION 2
 
 typedef enum kf_status {
   KF_OK = 0,
@@ -321,14 +321,17 @@ int kf_mesh_host(kf_grid g, const kf_params *p, float *verts, int64_t capacity, 
 
 /* ---- batched solves ---------------------------------------------------- */
 /* Many independent registration problems -- each a live SDF, a canonical SDF
- * and psi of its own size and parameters -- advanced together by one launch
- * per iteration (no counterpart in the reference, which registers one frame
- * at a time).  Each problem gets the Jacobi schedule of kf_psi_solve with
- * KF_SOLVER_BAND and the same psi bit for bit; with params.early_exit a
- * problem stops on its own once an iteration moved psi by at most
- * params.threshold (the criterion of KillingFusion.cpp:381, 392), while the
- * others go on.  Fields must be KF_F32 and distinct; at most 256 problems.
- * The batch keeps the handles: keep them alive until kf_batch_destroy. */
+ * and psi of its own size and parameters -- advanced together (no
+ * counterpart in the reference, which registers one frame at a time): one
+ * dense first pass over every problem, then every band pass of every
+ * iteration in one persistent cooperative launch, the iterations separated
+ * by a grid-wide barrier with a bounded wait (kf_set_wait_limit).  Each
+ * problem gets the Jacobi schedule of kf_psi_solve with KF_SOLVER_BAND and
+ * the same psi bit for bit; with params.early_exit a problem stops on its
+ * own once an iteration moved psi by at most params.threshold (the criterion
+ * of KillingFusion.cpp:381, 392), while the others go on.  Fields must be
+ * KF_F32 and distinct; at most 256 problems.  The batch keeps the handles:
+ * keep them alive until kf_batch_destroy. */
 typedef struct kf_batch_s *kf_batch;
 typedef struct kf_batch_item {
   kf_grid live;
@@ -337,16 +340,39 @@ typedef struct kf_batch_item {
   kf_params params;
 } kf_batch_item;
 
+/* Launch shape of a batch.  The band work of an iteration is cut into chunks
+ * of band_chunk voxels that never cross a problem; a CTA of band_threads
+ * threads takes one chunk at a time (band_chunk / band_threads voxels per
+ * thread), band_blocks_per_sm CTAs per SM with at most band_registers
+ * registers per thread.  The dense first pass takes tiles of 32 x 8 columns
+ * and `slab` z-planes.  The times are those the autotuner measured for the
+ * chosen shape (0 when the shape was set by kf_batch_set_shape). */
+typedef struct kf_batch_shape {
+  int band_threads;       /* 256 or 512                                       */
+  int band_chunk;         /* band_threads or 2 * band_threads                 */
+  int band_blocks_per_sm; /* 1, 2 or 3 (as the register budget allows)        */
+  int band_registers;     /* 128, or 80 for 3 CTAs of 256 threads per SM      */
+  int slab;               /* 4, 8 or 16                                       */
+  int reserved;
+  double band_ms;         /* one band pass (the first iteration)              */
+  double stream_ms;       /* the dense first pass                             */
+} kf_batch_shape;
+
 int kf_batch_create(const kf_batch_item *items, int count, int iterations, kf_batch *out);
 int kf_batch_destroy(kf_batch b);
-/* Times the band pass of the first iteration on this batch's data for each
- * launch shape -- a register budget of 80 (1, 2 or 3 resident CTAs per SM)
- * or 128 (1 or 2) -- and keeps the fastest for kf_batch_run (psi is not
- * changed).  blocks_per_sm and registers (may be NULL) receive the choice. */
-int kf_batch_autotune(kf_batch b, int *blocks_per_sm, int *registers, void *stream);
+/* Times, on this batch's data, the dense first pass at each slab depth and
+ * the band pass of the first iteration at each band shape (CTA size x chunk
+ * size x resident CTAs), and keeps the fastest of each for kf_batch_run
+ * (psi is not changed).  shape (may be NULL) receives the choice. */
+int kf_batch_autotune(kf_batch b, kf_batch_shape *shape, void *stream);
+/* Sets the launch shape (one of the shapes the autotuner tries); the
+ * default before any autotuning is 256 threads, chunks of 256, 2 CTAs per SM,
+ * slabs of 8.  KF_ERR_INVALID for a shape outside that set. */
+int kf_batch_set_shape(kf_batch b, const kf_batch_shape *shape);
 /* Runs the batch's iterations on every problem from its current psi.  stats:
  * one record per problem (may be NULL).  KF_ERR_DIVERGED when any problem
- * diverged (its record says which); the others are still solved. */
+ * diverged (its record says which); the others are still solved.
+ * KF_ERR_TIMEOUT when a barrier wait gave up (psi undefined). */
 int kf_batch_run(kf_batch b, kf_solve_stats *stats, void *stream);
 
 /* ---- per-frame pipeline (KillingFusion::processNextFrame) -------------- */

@@ -135,7 +135,8 @@ SIGNATURES = {
     "kf_energy_fd": (C.c_int, [_vp, _vp, _vp, _PP, _vp, _vp, C.c_int, C.c_double, _vp, _vp]),
     "kf_batch_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
     "kf_batch_destroy": (C.c_int, [_vp]),
-    "kf_batch_autotune": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), _vp]),
+    "kf_batch_autotune": (C.c_int, [_vp, C.c_void_p, _vp]),
+    "kf_batch_set_shape": (C.c_int, [_vp, C.c_void_p]),
     "kf_batch_run": (C.c_int, [_vp, _vp, _vp]),
     "kf_warp": (C.c_int, [_vp, _vp, _PP, _vp]),
     "kf_fuse": (C.c_int, [_vp, _vp, _vp]),
@@ -495,6 +496,23 @@ class BatchItem(C.Structure):
     _fields_ = [("live", _vp), ("canonical", _vp), ("psi", _vp), ("params", _Params)]
 
 
+class BatchShape(C.Structure):
+    """kf_batch_shape: launch shape of a batch (band pass and dense pass)."""
+    _fields_ = [("band_threads", C.c_int), ("band_chunk", C.c_int), ("band_blocks_per_sm", C.c_int),
+                ("band_registers", C.c_int), ("slab", C.c_int), ("reserved", C.c_int),
+                ("band_ms", C.c_double), ("stream_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+# (band threads, chunk voxels, CTAs per SM, registers) of every band-pass
+# shape the autotuner tries, and its slab depths
+BATCH_BAND_SHAPES = [(256, 256, 2, 128), (256, 256, 3, 80), (256, 512, 2, 128), (256, 512, 3, 80),
+                     (512, 512, 1, 128), (512, 1024, 1, 128)]
+BATCH_SLABS = [4, 8, 16]
+
+
 class Batch:
     """Independent registration problems solved together (kf_batch_*):
     problems is a list of (live Grid, canonical Grid, psi Field, Params)."""
@@ -517,11 +535,17 @@ class Batch:
 
     __del__ = close
 
-    def autotune(self, stream=None) -> tuple:
-        """(blocks per SM, register budget) of the fastest band-pass shape."""
-        k, r = C.c_int(0), C.c_int(0)
-        check(load().kf_batch_autotune(self.h, C.byref(k), C.byref(r), _stream(stream)))
-        return k.value, r.value
+    def autotune(self, stream=None) -> dict:
+        """The fastest launch shape on this batch's data (kf_batch_shape)."""
+        sh = BatchShape()
+        check(load().kf_batch_autotune(self.h, C.byref(sh), _stream(stream)))
+        return sh.as_dict()
+
+    def set_shape(self, band, slab=8):
+        """band: (threads, chunk, CTAs per SM, registers), one of
+        BATCH_BAND_SHAPES; slab: one of BATCH_SLABS."""
+        sh = BatchShape(*band, slab, 0, 0.0, 0.0)
+        check(load().kf_batch_set_shape(self.h, C.byref(sh)))
 
     def run(self, stream=None, raise_on_divergence=True) -> list:
         st = (SolveStats * self.n)()

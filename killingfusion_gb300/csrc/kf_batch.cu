@@ -1,37 +1,45 @@
 // Batched psi solves: many independent registration problems (each a live
 // SDF, a canonical SDF and psi, of its own size and parameters) advanced
-// together, one launch per iteration for all of them.
+// together, every iteration of all of them in one persistent launch.
 //
 // The reference registers one frame at a time (KillingFusion::processNextFrame,
 // KillingFusion.cpp:109-175); a batch runs its Jacobi schedule
 // (KillingFusion.cpp:248-352) on every problem of the set with the band-only
 // fused iteration of kf_fused.cu, so each problem's psi equals what
 // kf_psi_solve(KF_SOLVER_BAND) gives it alone, bit for bit:
-//   k_batch_stream  the dense first pass over every tile of every problem
-//                   (one flat grid; a block finds its problem by binary
-//                   search over the tile prefix) building each problem's
-//                   band list;
-//   k_batch_band    per iteration, the band voxels of all problems as one
-//                   work list cut into chunks that never cross a problem: a
-//                   block scans the per-problem chunk counts into a prefix,
-//                   finds each chunk's problem and hands each thread one
-//                   voxel; statistics stay in registers while the
-//                   block works on one problem, are warp-reduced into that
-//                   problem's shared totals when it moves on, and are
-//                   flushed once per block.
+//   k_batch_stream      the dense first pass over every tile of every problem
+//                       (one flat grid; a block finds its problem by binary
+//                       search over the tile prefix) building each problem's
+//                       band list;
+//   k_batch_persistent  every band pass of every iteration, one cooperative
+//                       launch: per iteration the band voxels of all problems
+//                       are one work list cut into chunks that never cross a
+//                       problem; a block scans the per-problem chunk counts
+//                       into a prefix, finds each chunk's problem and hands
+//                       each thread its voxels; statistics stay in registers
+//                       while the block works on one problem, are
+//                       warp-reduced into that problem's shared totals when
+//                       it moves on, and are flushed once per block and
+//                       iteration.  The iterations are separated by a
+//                       grid-wide barrier with a bounded wait
+//                       (kf_grid_sync.cuh).
 // Each problem converges on its own (params.early_exit): once its previous
 // iteration moved psi by at most params.threshold it is skipped, and its
-// voxels are no longer listed.  The whole loop is captured in one CUDA graph
-// per batch; the argument table it reads is refreshed before every launch, so
-// the graph survives the ping-pong buffer swaps of the fields.
+// voxels are no longer listed; the launch ends when every problem is.
+//
+// Launch shapes (kf_batch_autotune): the band pass's CTA size (256 or 512
+// threads), chunk size (one or two voxels per thread) and resident CTAs per
+// SM (the register budget), and the dense pass's slab depth (4, 8 or 16
+// z-planes per tile).
 #include <algorithm>
 #include <vector>
 
 #include "kf_fused_body.cuh"
+#include "kf_grid_sync.cuh"
 
 namespace {
 
-constexpr int kMaxBatch = kBandThreads;  // one problem per thread in the count scan
+constexpr int kMaxBatch = 256;  // one problem per thread in the count scan (CTAs of >= 256)
 
 // One problem of the batch on the device: the argument blocks of the two
 // ping-pong parities, its band lists and its dense-pass tiling.
@@ -54,6 +62,8 @@ __device__ __forceinline__ int find_problem(const int64_t *pre, int n, int64_t k
   return lo;
 }
 
+// tile_pre: the tiles of kSlab z-planes before each problem.
+template <int kSlab>
 __global__ void __launch_bounds__(kThreads) k_batch_stream(const BatchEntry *__restrict__ tab,
                                                           const int64_t *__restrict__ tile_pre, int nprob) {
   const int64_t b = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
@@ -64,13 +74,13 @@ __global__ void __launch_bounds__(kThreads) k_batch_stream(const BatchEntry *__r
   const int bx = (int)(local % e.gx);
   const int by = (int)((local / e.gx) % e.gy);
   const int bz = (int)(local / ((int64_t)e.gx * e.gy));
-  stream_tile<true>(e.a[0], bx, by, bz, e.band, &e.a[0].st[0].list);
+  stream_tile<true, kSlab>(e.a[0], bx, by, bz, e.band, &e.a[0].st[0].list);
 }
 
-template <int kMaxB>
-__device__ void scan_counts(unsigned *cnt, unsigned *pre, int n) {
-  // exclusive prefix of cnt[0..n) into pre[0..n], n <= blockDim.x == kMaxB
-  __shared__ unsigned s_warp[kMaxB / 32];
+// exclusive prefix of cnt[0..n) into pre[0..n], n <= kMaxBatch <= blockDim.x
+template <int kT>
+__device__ void scan_counts(const unsigned *cnt, unsigned *pre, int n) {
+  __shared__ unsigned s_warp[kT / 32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   unsigned v = t < n ? cnt[t] : 0u;
   unsigned x = v;
@@ -82,13 +92,13 @@ __device__ void scan_counts(unsigned *cnt, unsigned *pre, int n) {
   if (lane == 31) s_warp[w] = x;
   __syncthreads();
   if (w == 0) {
-    unsigned s = lane < kMaxB / 32 ? s_warp[lane] : 0u;
+    unsigned s = lane < kT / 32 ? s_warp[lane] : 0u;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       unsigned y = __shfl_up_sync(0xffffffffu, s, o);
       if (lane >= o) s += y;
     }
-    if (lane < kMaxB / 32) s_warp[lane] = s;  // inclusive warp totals
+    if (lane < kT / 32) s_warp[lane] = s;  // inclusive warp totals
   }
   __syncthreads();
   const unsigned off = w > 0 ? s_warp[w - 1] : 0u;
@@ -109,40 +119,46 @@ __device__ __forceinline__ int find_work(const unsigned *pre, int n, unsigned k)
   return lo;
 }
 
-// Band pass of iteration `it` over all problems.  The work is cut into
-// chunks of kBandThreads voxels that never cross a problem, so a CTA works
-// on one problem at a time: it stages that problem's argument block in shared
-// memory (the gradient reads it as often as the single-grid kernel reads its
-// constant parameters) and appends the chunk's carried voxels with one atomic.
-template <int kMinBlocks>
-__global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const BatchEntry *__restrict__ tab,
-                                                                        int nprob, int it) {
+// Band pass of iteration `it` over all problems, by every block of the grid.
+// The work is cut into chunks of kT * kVpt voxels that never cross a
+// problem, so a CTA works on one problem at a time: it stages that problem's
+// argument block in shared memory (the gradient reads it as often as the
+// single-grid kernel reads its constant parameters) and appends each round's
+// carried voxels with one atomic.  Returns false when every problem was
+// skipped (converged or diverged): nothing is left to run.
+template <int kT, int kVpt>
+__device__ __forceinline__ bool batch_band_pass(const BatchEntry *__restrict__ tab, int nprob, int it) {
   __shared__ unsigned s_cnt[kMaxBatch];
   __shared__ unsigned s_pre[kMaxBatch + 1];
   __shared__ unsigned s_active[kMaxBatch];
   __shared__ unsigned s_maxd[kMaxBatch];
   __shared__ double s_energy[kMaxBatch];
   __shared__ int s_div[kMaxBatch];
+  __shared__ unsigned s_chunks[kMaxBatch];
   __shared__ FusedArgs s_a;
   __shared__ int *s_list_in, *s_list_out;
+  __shared__ int s_live;  // problems not skipped this iteration
+  constexpr int kChunk = kT * kVpt;
   const int par = it & 1;
+  if (threadIdx.x == 0) s_live = 0;
+  __syncthreads();
   for (int q = threadIdx.x; q < nprob; q += blockDim.x) {
     const FusedArgs &a = tab[q].a[par];
     const bool gated = iteration_gated(a.st, it, a.dp);
     if (gated && blockIdx.x == 0) a.st[it].skipped = 1;
-    s_cnt[q] = gated ? 0u : a.st[it].list;
+    if (!gated) atomicAdd(&s_live, 1);
+    s_cnt[q] = gated ? 0u : __ldcg(&a.st[it].list);
     s_active[q] = 0u;
     s_maxd[q] = 0u;
     s_energy[q] = 0.0;
     s_div[q] = 0;
   }
   __syncthreads();
-  // chunks per problem, scanned in place of the counts' copy
-  unsigned chunks = threadIdx.x < nprob ? (s_cnt[threadIdx.x] + kBandThreads - 1) / kBandThreads : 0u;
-  __shared__ unsigned s_chunks[kMaxBatch];
-  if (threadIdx.x < nprob) s_chunks[threadIdx.x] = chunks;
+  if (s_live == 0) return false;
+  // chunks per problem, scanned
+  if (threadIdx.x < nprob) s_chunks[threadIdx.x] = (s_cnt[threadIdx.x] + kChunk - 1) / kChunk;
   __syncthreads();
-  scan_counts<kMaxBatch>(s_chunks, s_pre, nprob);
+  scan_counts<kT>(s_chunks, s_pre, nprob);
   const unsigned total = s_pre[nprob];
   const int lane = threadIdx.x & 31;
   // statistics of the staged problem, per thread until the problem changes
@@ -189,14 +205,17 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
       cur = p;
       __syncthreads();
     }
-    const unsigned k = (c - s_pre[p]) * kBandThreads + threadIdx.x;
-    int next = -1;
-    if (k < s_cnt[p]) {
-      const int v = s_list_in[k];
-      next = update_band_voxel(s_a, v, v, maxd, energy, active, diverged);
+#pragma unroll 1
+    for (int v = 0; v < kVpt; ++v) {
+      const unsigned k = (c - s_pre[p]) * kChunk + v * kT + threadIdx.x;
+      int next = -1;
+      if (k < s_cnt[p]) {
+        const int i = __ldcg(s_list_in + k);
+        next = update_band_voxel<false, kPsiL1>(s_a, i, i, maxd, energy, active, diverged);
+      }
+      // hand the round's updated voxels to the next iteration
+      block_append<kT / 32>(next, &s_a.st[it + 1].list, s_list_out);
     }
-    // hand the chunk's updated voxels to the next iteration
-    block_append<kBandWarps>(next, &s_a.st[it + 1].list, s_list_out);
   }
   if (cur >= 0) flush(cur);
   __syncthreads();
@@ -209,36 +228,71 @@ __global__ void __launch_bounds__(kBandThreads, kMinBlocks) k_batch_band(const B
     }
     if (s_div[q]) st->diverged = 1;
   }
+  return true;
 }
+
+// Every band pass of the batch: `iterations` passes separated by grid-wide
+// barriers.  A wait that gives up marks problem 0's first record
+// (IterStats::timeout) and ends the kernel.
+template <int kT, int kVpt, int kMinBlocks>
+__global__ void __launch_bounds__(kT, kMinBlocks)
+    k_batch_persistent(const BatchEntry *__restrict__ tab, int nprob, int iterations, GridSync *sync,
+                       unsigned long long limit_ns) {
+  for (int it = 0; it < iterations; ++it) {
+    if (!batch_band_pass<kT, kVpt>(tab, nprob, it) || it + 1 == iterations) return;
+    if (!grid_sync(sync, gridDim.x, limit_ns, it)) {
+      if (threadIdx.x == 0) tab[0].a[0].st[0].timeout = 1;
+      return;
+    }
+  }
+}
+
+// The band-pass shapes the autotuner tries: CTA threads, voxels per thread
+// of a chunk, resident CTAs per SM (sets the register budget), registers.
+struct BandShape {
+  int threads, vpt, min_blocks, regs;
+  const void *kernel;
+};
+
+const BandShape kBandShapes[] = {
+    {256, 1, 2, 128, (const void *)k_batch_persistent<256, 1, 2>},
+    {256, 1, 3, 80, (const void *)k_batch_persistent<256, 1, 3>},
+    {256, 2, 2, 128, (const void *)k_batch_persistent<256, 2, 2>},
+    {256, 2, 3, 80, (const void *)k_batch_persistent<256, 2, 3>},
+    {512, 1, 1, 128, (const void *)k_batch_persistent<512, 1, 1>},
+    {512, 2, 1, 128, (const void *)k_batch_persistent<512, 2, 1>},
+};
+constexpr int kNumBandShapes = sizeof(kBandShapes) / sizeof(kBandShapes[0]);
+// dense-pass slab depths (z-planes per tile of 32 x 8 columns)
+const int kSlabs[] = {4, 8, 16};
+constexpr int kNumSlabs = 3;
 
 }  // namespace
 
 struct kf_batch_s {
   std::vector<kf_batch_item> items;
   int iterations = 0;
-  int band_blocks_per_sm = 3;
-  int band_regs = 80;  // 80: variant for 3 CTAs per SM; 128: for 2
-  int64_t tiles = 0;
-  BatchEntry *tab = nullptr;        // device
-  BatchEntry *tab_host = nullptr;   // pinned
-  int64_t *tile_pre = nullptr;      // device, nprob + 1
+  int band_shape = 0;                     // index into kBandShapes
+  int slab_index = 1;                     // index into kSlabs
+  double band_ms = 0.0, stream_ms = 0.0;  // autotuned times of the choice
+  int resident[kNumBandShapes] = {};      // CTAs per SM each shape can keep resident
+  BatchEntry *tab = nullptr;              // device
+  BatchEntry *tab_host = nullptr;         // pinned
+  int64_t *tile_pre = nullptr;            // device, kNumSlabs x (nprob + 1)
+  int64_t tiles[kNumSlabs] = {};
   IterStats *stats = nullptr;       // device, nprob * (iterations + 1)
   IterStats *stats_host = nullptr;  // pinned
-  cudaGraphExec_t exec = nullptr;
-  int exec_blocks = 0;
-  int exec_regs = 0;
-  cudaStream_t capture = nullptr;
+  GridSync *sync = nullptr;         // device
 };
 
 static void batch_free(kf_batch b) {
   if (!b) return;
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->capture) cudaStreamDestroy(b->capture);
   cudaFree(b->tab);
   cudaFreeHost(b->tab_host);
   cudaFree(b->tile_pre);
   cudaFree(b->stats);
   cudaFreeHost(b->stats_host);
+  cudaFree(b->sync);
   delete b;
 }
 
@@ -272,45 +326,36 @@ static int batch_upload_table(kf_batch b, cudaStream_t s) {
   return KF_OK;
 }
 
-// One band pass with `blocks_per_sm` CTAs per SM of the 80- or 128-register
-// variant.
-static void band_launch(kf_batch b, int regs, int blocks_per_sm, int it, cudaStream_t s) {
-  const unsigned blocks = (unsigned)(kf_num_sms() * blocks_per_sm);
+// The dense first pass with slab depth kSlabs[si].
+static int stream_launch(kf_batch b, int si, cudaStream_t s) {
   const int n = (int)b->items.size();
-  if (regs > 80)
-    k_batch_band<2><<<blocks, kBandThreads, 0, s>>>(b->tab, n, it);
+  const int64_t tiles = b->tiles[si];
+  const int64_t *pre = b->tile_pre + (int64_t)si * (n + 1);
+  const dim3 grid((unsigned)std::min<int64_t>(tiles, 65535), (unsigned)((tiles + 65534) / 65535));
+  const dim3 block(kTX, kTY);
+  if (kSlabs[si] == 4)
+    k_batch_stream<4><<<grid, block, 0, s>>>(b->tab, pre, n);
+  else if (kSlabs[si] == 8)
+    k_batch_stream<8><<<grid, block, 0, s>>>(b->tab, pre, n);
   else
-    k_batch_band<3><<<blocks, kBandThreads, 0, s>>>(b->tab, n, it);
+    k_batch_stream<16><<<grid, block, 0, s>>>(b->tab, pre, n);
+  KF_CHECK_LAUNCH("k_batch_stream");
+  return KF_OK;
 }
 
-static void batch_launch(kf_batch b, int iterations, int regs, int blocks_per_sm, cudaStream_t s) {
-  const int n = (int)b->items.size();
-  const int64_t tiles = b->tiles;
-  dim3 sgrid((unsigned)std::min<int64_t>(tiles, 65535), (unsigned)((tiles + 65534) / 65535));
-  k_batch_stream<<<sgrid, dim3(kTX, kTY), 0, s>>>(b->tab, b->tile_pre, n);
-  for (int it = 0; it < iterations; ++it) band_launch(b, regs, blocks_per_sm, it, s);
-}
-
-static int batch_capture(kf_batch b, int regs, int blocks_per_sm) {
-  if (b->exec && b->exec_blocks == blocks_per_sm && b->exec_regs == regs) return KF_OK;
-  if (b->exec) {
-    cudaGraphExecDestroy(b->exec);
-    b->exec = nullptr;
-  }
-  cudaGraph_t graph;
-  KF_CHECK_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal));
-  batch_launch(b, b->iterations, regs, blocks_per_sm, b->capture);
-  cudaError_t le = cudaGetLastError();
-  KF_CHECK_CUDA(cudaStreamEndCapture(b->capture, &graph));
-  if (le != cudaSuccess) {
-    cudaGraphDestroy(graph);
-    return kf_cuda_fail(le, "batched kernel launch during capture");
-  }
-  cudaError_t ie = cudaGraphInstantiate(&b->exec, graph, 0);
-  cudaGraphDestroy(graph);
-  if (ie != cudaSuccess) return kf_cuda_fail(ie, "cudaGraphInstantiate");
-  b->exec_blocks = blocks_per_sm;
-  b->exec_regs = regs;
+// `iterations` band passes in one cooperative launch of shape kBandShapes[sh].
+static int band_launch(kf_batch b, int sh, int iterations, cudaStream_t s) {
+  const BandShape &bs = kBandShapes[sh];
+  const int resident = std::min(b->resident[sh], bs.min_blocks);
+  if (resident < 1) return kf_fail(KF_ERR_CUDA, "a batch band-pass shape does not fit on an SM");
+  KF_CHECK_CUDA(cudaMemsetAsync(b->sync, 0, sizeof(GridSync), s));
+  const BatchEntry *tab = b->tab;
+  int nprob = (int)b->items.size();
+  GridSync *sync = b->sync;
+  unsigned long long limit = kf_wait_limit_ns();
+  void *args[] = {&tab, &nprob, &iterations, &sync, &limit};
+  KF_CHECK_CUDA(cudaLaunchCooperativeKernel(bs.kernel, dim3((unsigned)(kf_num_sms() * resident)),
+                                            dim3((unsigned)bs.threads), args, 0, s));
   return KF_OK;
 }
 
@@ -338,20 +383,28 @@ extern "C" int kf_batch_create(const kf_batch_item *items, int count, int iterat
   kf_batch b = new kf_batch_s();
   b->items.assign(items, items + count);
   b->iterations = iterations;
-  std::vector<int64_t> pre(count + 1, 0);
-  for (int p = 0; p < count; ++p) {
-    const int *n = items[p].live->n;
-    pre[p + 1] = pre[p] + (int64_t)((n[0] + kTX - 1) / kTX) * ((n[1] + kTY - 1) / kTY) * ((n[2] + kZSlab - 1) / kZSlab);
+  std::vector<int64_t> pre((size_t)kNumSlabs * (count + 1), 0);
+  for (int si = 0; si < kNumSlabs; ++si) {
+    int64_t *pr = pre.data() + (size_t)si * (count + 1);
+    for (int p = 0; p < count; ++p) {
+      const int *n = items[p].live->n;
+      pr[p + 1] = pr[p] + (int64_t)((n[0] + kTX - 1) / kTX) * ((n[1] + kTY - 1) / kTY) *
+                              ((n[2] + kSlabs[si] - 1) / kSlabs[si]);
+    }
+    b->tiles[si] = pr[count];
   }
-  b->tiles = pre[count];
   const size_t nst = (size_t)count * stats_stride(b);
   cudaError_t e = cudaMalloc(&b->tab, sizeof(BatchEntry) * count);
   if (e == cudaSuccess) e = cudaMallocHost(&b->tab_host, sizeof(BatchEntry) * count);
-  if (e == cudaSuccess) e = cudaMalloc(&b->tile_pre, sizeof(int64_t) * (count + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b->tile_pre, sizeof(int64_t) * pre.size());
   if (e == cudaSuccess) e = cudaMalloc(&b->stats, sizeof(IterStats) * nst);
   if (e == cudaSuccess) e = cudaMallocHost(&b->stats_host, sizeof(IterStats) * nst);
-  if (e == cudaSuccess) e = cudaMemcpy(b->tile_pre, pre.data(), sizeof(int64_t) * (count + 1), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&b->sync, sizeof(GridSync));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->tile_pre, pre.data(), sizeof(int64_t) * pre.size(), cudaMemcpyHostToDevice);
+  for (int sh = 0; sh < kNumBandShapes && e == cudaSuccess; ++sh)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b->resident[sh], kBandShapes[sh].kernel,
+                                                      kBandShapes[sh].threads, 0);
   if (e != cudaSuccess) {
     batch_free(b);
     cudaGetLastError();
@@ -370,31 +423,65 @@ extern "C" int kf_batch_create(const kf_batch_item *items, int count, int iterat
 }
 
 extern "C" int kf_batch_destroy(kf_batch b) {
-  if (b) cudaStreamSynchronize(b->capture);
+  if (b) cudaDeviceSynchronize();
   batch_free(b);
   return KF_OK;
 }
 
-// Launches the captured loop (band pass at blocks_per_sm) into the ping-pong
-// buffers and the statistics; which buffer holds each field's psi is settled
-// by the caller from the statistics.
-static int batch_execute(kf_batch b, int regs, int blocks_per_sm, cudaStream_t s) {
+// The dense pass and the band passes into the ping-pong buffers and the
+// statistics; which buffer holds each field's psi is settled by the caller
+// from the statistics.
+static int batch_execute(kf_batch b, int iterations, cudaStream_t s) {
   const int n = (int)b->items.size();
   int rc = batch_upload_table(b, s);
   if (rc) return rc;
   KF_CHECK_CUDA(cudaMemsetAsync(b->stats, 0, sizeof(IterStats) * (size_t)n * stats_stride(b), s));
-  rc = batch_capture(b, regs, blocks_per_sm);
+  rc = stream_launch(b, b->slab_index, s);
   if (rc) return rc;
-  KF_CHECK_CUDA(cudaGraphLaunch(b->exec, s));
+  return band_launch(b, b->band_shape, iterations, s);
+}
+
+static bool shape_index(const kf_batch_shape *sh, int *band, int *slab) {
+  *band = *slab = -1;
+  for (int k = 0; k < kNumBandShapes; ++k)
+    if (kBandShapes[k].threads == sh->band_threads &&
+        kBandShapes[k].threads * kBandShapes[k].vpt == sh->band_chunk &&
+        kBandShapes[k].min_blocks == sh->band_blocks_per_sm && kBandShapes[k].regs == sh->band_registers)
+      *band = k;
+  for (int k = 0; k < kNumSlabs; ++k)
+    if (kSlabs[k] == sh->slab) *slab = k;
+  return *band >= 0 && *slab >= 0;
+}
+
+static void shape_of(kf_batch b, kf_batch_shape *out) {
+  const BandShape &bs = kBandShapes[b->band_shape];
+  memset(out, 0, sizeof(*out));
+  out->band_threads = bs.threads;
+  out->band_chunk = bs.threads * bs.vpt;
+  out->band_blocks_per_sm = bs.min_blocks;
+  out->band_registers = bs.regs;
+  out->slab = kSlabs[b->slab_index];
+  out->band_ms = b->band_ms;
+  out->stream_ms = b->stream_ms;
+}
+
+extern "C" int kf_batch_set_shape(kf_batch b, const kf_batch_shape *shape) {
+  KF_REQUIRE(b && shape, "NULL argument");
+  int band, slab;
+  KF_REQUIRE(shape_index(shape, &band, &slab), "not a batch launch shape (see kf_batch_shape)");
+  KF_REQUIRE(b->resident[band] >= kBandShapes[band].min_blocks, "that band-pass shape does not fit on this GPU");
+  b->band_shape = band;
+  b->slab_index = slab;
+  b->band_ms = b->stream_ms = 0.0;
   return KF_OK;
 }
 
-// Times the band pass of the first iteration (the longest band list) for
-// each launch shape -- the 80-register variant at 1, 2 and 3 CTAs per SM,
-// the 128-register variant at 1 and 2 -- and keeps the fastest.  Each trial
-// reruns the dense first pass, which reads psi and writes only the second
-// ping-pong buffer, so the fields keep their psi.
-extern "C" int kf_batch_autotune(kf_batch b, int *blocks_per_sm, int *registers, void *stream) {
+// Times the dense first pass at each slab depth, then the band pass of the
+// first iteration (the longest band lists) at each band shape, and keeps the
+// fastest of each.  Every trial reruns the dense first pass, which reads psi
+// and writes only the second ping-pong buffer, and at most one band pass,
+// which writes only the second buffer too, so the fields keep their psi.
+extern "C" int kf_batch_autotune(kf_batch b, kf_batch_shape *shape, void *stream) {
   KF_REQUIRE(b, "NULL batch");
   cudaStream_t s = kf_stream(stream);
   const int n = (int)b->items.size();
@@ -403,38 +490,58 @@ extern "C" int kf_batch_autotune(kf_batch b, int *blocks_per_sm, int *registers,
   cudaEvent_t e0, e1;
   KF_CHECK_CUDA(cudaEventCreate(&e0));
   KF_CHECK_CUDA(cudaEventCreate(&e1));
-  const int64_t tiles = b->tiles;
-  dim3 sgrid((unsigned)std::min<int64_t>(tiles, 65535), (unsigned)((tiles + 65534) / 65535));
-  const int shapes[5][2] = {{80, 1}, {80, 2}, {80, 3}, {128, 1}, {128, 2}};
-  float best = 0.f;
-  int best_s = -1;
-  cudaError_t err = cudaSuccess;
-  for (int sh = 0; sh < 5 && err == cudaSuccess; ++sh) {
-    float kbest = 0.f;
-    for (int rep = 0; rep < 3 && err == cudaSuccess; ++rep) {
-      cudaMemsetAsync(b->stats, 0, sizeof(IterStats) * (size_t)n * stats_stride(b), s);
-      k_batch_stream<<<sgrid, dim3(kTX, kTY), 0, s>>>(b->tab, b->tile_pre, n);
-      cudaEventRecord(e0, s);
-      band_launch(b, shapes[sh][0], shapes[sh][1], 0, s);
-      cudaEventRecord(e1, s);
-      err = cudaEventSynchronize(e1);
-      if (err == cudaSuccess) err = cudaGetLastError();
+  const size_t stats_bytes = sizeof(IterStats) * (size_t)n * stats_stride(b);
+  // one trial: the dense pass at slab si, then (sh >= 0) one band pass of
+  // shape sh; the time of the dense pass (sh < 0) or of the band pass, the
+  // best of repetitions 1..3 (repetition 0 warms up)
+  auto trial = [&](int si, int sh, float *best) -> int {
+    *best = 0.f;
+    for (int rep = 0; rep < 4; ++rep) {
+      KF_CHECK_CUDA(cudaMemsetAsync(b->stats, 0, stats_bytes, s));
+      if (sh < 0) KF_CHECK_CUDA(cudaEventRecord(e0, s));
+      int r = stream_launch(b, si, s);
+      if (r) return r;
+      if (sh >= 0) {
+        KF_CHECK_CUDA(cudaEventRecord(e0, s));
+        r = band_launch(b, sh, 1, s);
+        if (r) return r;
+      }
+      KF_CHECK_CUDA(cudaEventRecord(e1, s));
+      KF_CHECK_CUDA(cudaEventSynchronize(e1));
       float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (rep == 1 || (rep > 1 && ms < kbest)) kbest = ms;  // rep 0 warms up
+      KF_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep == 1 || (rep > 1 && ms < *best)) *best = ms;
     }
-    if (err == cudaSuccess && (best_s < 0 || kbest < best)) {
-      best = kbest;
-      best_s = sh;
+    return KF_OK;
+  };
+  float best_stream = 0.f, best_band = 0.f;
+  int si_best = -1, sh_best = -1;
+  for (int si = 0; si < kNumSlabs && rc == KF_OK; ++si) {
+    float t = 0.f;
+    rc = trial(si, -1, &t);
+    if (rc == KF_OK && (si_best < 0 || t < best_stream)) {
+      best_stream = t;
+      si_best = si;
+    }
+  }
+  for (int sh = 0; sh < kNumBandShapes && rc == KF_OK; ++sh) {
+    if (b->resident[sh] < kBandShapes[sh].min_blocks) continue;
+    float t = 0.f;
+    rc = trial(si_best, sh, &t);
+    if (rc == KF_OK && (sh_best < 0 || t < best_band)) {
+      best_band = t;
+      sh_best = sh;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (err != cudaSuccess) return kf_cuda_fail(err, "kf_batch_autotune");
-  b->band_regs = shapes[best_s][0];
-  b->band_blocks_per_sm = shapes[best_s][1];
-  if (blocks_per_sm) *blocks_per_sm = b->band_blocks_per_sm;
-  if (registers) *registers = b->band_regs;
+  if (rc) return rc;
+  if (sh_best < 0) return kf_fail(KF_ERR_CUDA, "no batch band-pass shape fits on this GPU");
+  b->band_shape = sh_best;
+  b->slab_index = si_best;
+  b->band_ms = best_band;
+  b->stream_ms = best_stream;
+  if (shape) shape_of(b, shape);
   return KF_OK;
 }
 
@@ -447,7 +554,7 @@ extern "C" int kf_batch_run(kf_batch b, kf_solve_stats *stats, void *stream) {
   KF_CHECK_CUDA(cudaEventCreate(&e0));
   KF_CHECK_CUDA(cudaEventCreate(&e1));
   cudaEventRecord(e0, s);
-  int rc = batch_execute(b, b->band_regs, b->band_blocks_per_sm, s);
+  int rc = batch_execute(b, iters, s);
   if (rc) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -462,6 +569,8 @@ extern "C" int kf_batch_run(kf_batch b, kf_solve_stats *stats, void *stream) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (e != cudaSuccess) return kf_cuda_fail(e, "kf_batch_run");
+  if (b->stats_host[0].timeout)
+    return kf_fail(KF_ERR_TIMEOUT, "a grid-wide wait of the batched band pass gave up; psi is undefined");
   int any_diverged = 0;
   for (int p = 0; p < n; ++p) {
     const IterStats *h = b->stats_host + (size_t)p * stats_stride(b);

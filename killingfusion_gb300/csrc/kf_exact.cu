@@ -17,6 +17,7 @@
 #include <cstring>
 #include <vector>
 
+#include "kf_ffloat.cuh"
 #include "kf_internal.h"
 #include "kf_ref_math.cuh"
 
@@ -59,6 +60,9 @@ struct IntegrateArgs {
   double voxel, min0, min1, min2, unknown_clip, min_depth, max_depth;
   float min_depth_up, max_depth_down;  // float neighbours of the depth range
   double depth_scale;                  // metres per unit of 16-bit depth
+  float w11h, w11l;                    // W[11] as a float pair
+  float cliph, clipl;                  // unknown_clip as a float pair
+  float tol;                           // bound on |float-float distance - reference's|
   int width, height;
 };
 
@@ -139,20 +143,46 @@ __device__ void integrate_exact_voxel(float *__restrict__ phi, int32_t *__restri
 
 // Per-axis products of the camera-depth row, W[8]*X(x), W[9]*Y(y) and
 // W[10]*Z(z), with X = voxel*(x+0.5)+min as SDF.cpp:151-157 computes it:
-// zc = ((tx + ty) + tz) + W[11] is then the reference's float64 value.
+// zc = ((tx + ty) + tz) + W[11] is then the reference's float64 value.  The
+// same products as float pairs (tf, nx + ny + nz of them) for the
+// float-float path.
 __global__ void k_integrate_tables(double *__restrict__ tx, double *__restrict__ ty, double *__restrict__ tz,
-                                   int nx, int ny, int nz, IntegrateArgs a) {
+                                   float2 *__restrict__ tf, int nx, int ny, int nz, IntegrateArgs a) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx + ny + nz; k += gridDim.x * blockDim.x) {
+    double t;
     if (k < nx) {
-      tx[k] = a.W[8] * (a.voxel * ((double)k + 0.5) + a.min0);
+      t = tx[k] = a.W[8] * (a.voxel * ((double)k + 0.5) + a.min0);
     } else if (k < nx + ny) {
       const int j = k - nx;
-      ty[j] = a.W[9] * (a.voxel * ((double)j + 0.5) + a.min1);
+      t = ty[j] = a.W[9] * (a.voxel * ((double)j + 0.5) + a.min1);
     } else {
       const int j = k - nx - ny;
-      tz[j] = a.W[10] * (a.voxel * ((double)j + 0.5) + a.min2);
+      t = tz[j] = a.W[10] * (a.voxel * ((double)j + 0.5) + a.min2);
     }
+    const FF p = ff_from_double(t);
+    tf[k] = make_float2(p.hi, p.lo);
   }
+}
+
+// A fresh voxel (w == 0, phi finite) on float depth df, in float-float: the
+// distance df - zc with zc = ((tx + ty) + tz) + W[11] from the pair tables,
+// the unknown-clip test and the float rounding, all decided when they lie
+// farther than a.tol from the reference's float64 boundaries.  Returns false
+// (nothing written) when one of them is too close to call.
+__device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
+                                                   float df, float2 tx, float2 ty, float2 tz,
+                                                   const IntegrateArgs &a) {
+  const FF zc = ff_add(ff_add(ff_add(FF{tx.x, tx.y}, FF{ty.x, ty.y}), FF{tz.x, tz.y}), FF{a.w11h, a.w11l});
+  const FF dist = ff_add(FF{df, 0.f}, ff_neg(zc));
+  const FF m = ff_add(dist, FF{a.cliph, a.clipl});  // dist + unknown_clip < 0: not integrated
+  if (!(fabsf(m.hi) > a.tol)) return false;
+  if (m.hi < 0.f) return true;
+  bool ambiguous;
+  const float r = ff_round_checked(dist, a.tol, ambiguous);
+  if (ambiguous) return false;
+  phi[i] = r;
+  w[i] = 1;
+  return true;
 }
 
 // SDF::integrateDepthFrame for one voxel per thread.  The pixel a voxel reads
@@ -169,7 +199,8 @@ __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, i
                                                       const D *__restrict__ depth,
                                                       const double *__restrict__ tx,
                                                       const double *__restrict__ ty,
-                                                      const double *__restrict__ tz, int *__restrict__ list,
+                                                      const double *__restrict__ tz,
+                                                      const float2 *__restrict__ tf, int *__restrict__ list,
                                                       unsigned *__restrict__ list_n, unsigned list_cap,
                                                       IntegrateArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -211,8 +242,17 @@ __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, i
   if (vf < -1.0f) row = -1;
   if (col < 0 || col >= a.width) return;
   if (row < 0 || row >= a.height) return;
+  const int64_t k = (int64_t)row * a.width + col;
+  if constexpr (sizeof(D) == 4) {
+    // float depth into a fresh voxel: float-float, float64 only when too close to call
+    const float df = depth[k];
+    if (df < a.min_depth_up || df > a.max_depth_down) return;  // (a NaN passes, as in the reference)
+    if (w[i] == 0 && isfinite(phi[i]) && isfinite(df) &&
+        integrate_fresh_ff(phi, w, i, df, __ldg(tf + x), __ldg(tf + nx + y), __ldg(tf + nx + ny + z), a))
+      return;
+  }
   double dd;
-  if (!depth_at(depth, (int64_t)row * a.width + col, a, dd)) return;
+  if (!depth_at(depth, k, a, dd)) return;
   const double zc = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
   integrate_update(phi, w, i, dd, zc, a);
 }
@@ -264,10 +304,22 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   a.width = width;
   a.height = height;
   a.depth_scale = depth_scale;
+  ff_split_host(w2c[11], a.w11h, a.w11l);
+  ff_split_host(g->unknown_clip, a.cliph, a.clipl);
+  {
+    // the float-float distance is within a few 2^-46 of the magnitudes it
+    // sums (and the reference's within a few 2^-53): 2^-38 of their bound
+    double mag = fabs(w2c[11]) + fabs(max_depth);
+    for (int c = 0; c < 3; ++c) {
+      const double lo_c = g->min3d[c], hi_c = g->min3d[c] + g->voxel * (double)g->n[c];
+      mag += fabs(w2c[8 + c]) * std::max(fabs(lo_c), fabs(hi_c));
+    }
+    a.tol = (float)(ldexp(mag, -38));
+  }
   // scratch: list counter, the three coordinate tables, the list
   const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
   const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(g->count / 8, 65536), 0x7fffffff);
-  const size_t tab_off = 256, list_off = tab_off + (((size_t)(nx + ny + nz) * 8 + 255) & ~(size_t)255);
+  const size_t tab_off = 256, list_off = tab_off + (((size_t)(nx + ny + nz) * 16 + 255) & ~(size_t)255);
   const size_t bytes = list_off + (size_t)cap * sizeof(int);
   if (g->integ_bytes < bytes) {
     cudaFree(g->integ);
@@ -283,12 +335,14 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   char *base = (char *)g->integ;
   unsigned *list_n = (unsigned *)base;
   double *tx = (double *)(base + tab_off), *ty = tx + nx, *tz = ty + ny;
+  float2 *tf = (float2 *)(tz + nz);
   int *list = (int *)(base + list_off);
   KF_CHECK_CUDA(cudaMemsetAsync(list_n, 0, sizeof(unsigned), s));
-  k_integrate_tables<<<blocks_for(nx + ny + nz), kBlock, 0, s>>>(tx, ty, tz, nx, ny, nz, a);
+  k_integrate_tables<<<blocks_for(nx + ny + nz), kBlock, 0, s>>>(tx, ty, tz, tf, nx, ny, nz, a);
   dim3 block(32, kBlock / 32);
   dim3 grid((nx + 31) / 32, (ny + block.y - 1) / block.y, nz);
-  k_integrate<D><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, list, list_n, cap, a);
+  k_integrate<D><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tf, list, list_n, cap,
+                                        a);
   k_integrate_exact<D><<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list,
                                                                      list_n, cap, a);
   KF_CHECK_LAUNCH("k_integrate");
@@ -350,7 +404,9 @@ __device__ __forceinline__ void warp_sample(const float *__restrict__ phi, const
   out_phi = lerp3(vp, f0, f1, f2);
 }
 
-// FUSE_BY_MERGE of (nphi, nw) into canonical voxel i (SDF.cpp:212-236).
+// FUSE_BY_MERGE of (nphi, nw) into canonical voxel i (SDF.cpp:212-236).  The
+// running mean is decided in float-float (ff_merge_mean); the rare voxel it
+// cannot decide takes the reference's float64 expression.
 __device__ __forceinline__ void fuse_voxel(float *__restrict__ cphi, int32_t *__restrict__ cw, int64_t i,
                                            float nphi, int32_t nw) {
   if (nw == 0) return;
@@ -359,8 +415,11 @@ __device__ __forceinline__ void fuse_voxel(float *__restrict__ cphi, int32_t *__
     cphi[i] = nphi;
     cw[i] = nw;
   } else {
-    const double d1 = (double)cphi[i];
-    cphi[i] = (float)(((double)w1 * d1 + (double)nw * (double)nphi) / (double)(w1 + nw));
+    const float f1 = cphi[i];
+    float r;
+    if (!ff_merge_mean(w1, f1, nw, nphi, r))
+      r = (float)(((double)w1 * (double)f1 + (double)nw * (double)nphi) / (double)(w1 + nw));
+    cphi[i] = r;
     cw[i] = w1 + nw;
   }
 }
@@ -474,16 +533,7 @@ __global__ void __launch_bounds__(kBlock) k_fuse(float *__restrict__ phi1, int32
   if (i >= n) return;
   int32_t b = w2[i];
   if (b == 0) return;
-  int32_t a = w1[i];
-  float d2 = phi2[i];
-  if (a == 0) {
-    phi1[i] = d2;
-    w1[i] = b;
-  } else {
-    double d1 = (double)phi1[i];
-    phi1[i] = (float)(((double)a * d1 + (double)b * (double)d2) / (double)(a + b));
-    w1[i] = a + b;
-  }
+  fuse_voxel(phi1, w1, i, phi2[i], b);
 }
 
 // SDF::fuse(other, psi) (SDF.cpp:244-297): the other SDF's weight stays an

@@ -209,12 +209,13 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
 // Band-only solver, every iteration in one cooperative launch.  One band pass
 // per iteration as k_fused_band<kCarry> (ping-pong buffers, the updated
 // voxels carried to the next iteration's list), then a grid-wide barrier
-// (kf_grid_sync.cuh) instead of a kernel boundary.  Band voxel k goes to
-// block k % G (thread k / G of it, G blocks), so a small band spreads over all
-// the SMs whatever the block size.  psi is read through L2 (the blocks write
-// it between iterations); the SDFs through the read-only path.  A gated
-// iteration (converged, diverged) ends the kernel in every block alike: each
-// reads the same statistics after the barrier.
+// (kf_grid_sync.cuh) instead of a kernel boundary.  Each block takes an equal
+// contiguous slice of the band list, so a small band spreads over all the
+// SMs and neighbouring band voxels (which share psi neighbours) stay in one
+// SM's L1.  psi is read through L1 and L2 (kPsiL1: the blocks write it
+// between iterations, ordered by the barrier's fences), the SDFs through the
+// read-only path.  A gated iteration (converged, diverged) ends the kernel
+// in every block alike: each reads the same statistics after the barrier.
 constexpr int kPersistThreads = 256;
 constexpr int kPersistBlocksPerSM = 2;
 
@@ -228,18 +229,19 @@ __device__ __forceinline__ bool persistent_band_iteration(const FusedArgs &a, in
   }
   const unsigned nq = __ldcg(&a.st[it].list);
   const unsigned nb = gridDim.x;
-  const unsigned per_round = nb * kPersistThreads;
-  const unsigned rounds = (nq + per_round - 1) / per_round;
+  const unsigned per = (nq + nb - 1) / nb;  // this block: list entries [k0, k1)
+  const unsigned k0 = min(blockIdx.x * per, nq), k1 = min(k0 + per, nq);
+  const unsigned rounds = (per + kPersistThreads - 1) / kPersistThreads;  // the same in every block
   float maxd = 0.f;
   double energy = 0.0;
   unsigned active = 0;
   bool diverged = false;
   for (unsigned r = 0; r < rounds; ++r) {
-    const unsigned k = blockIdx.x + nb * (threadIdx.x + kPersistThreads * r);
+    const unsigned k = k0 + r * kPersistThreads + threadIdx.x;
     int next = -1;
-    if (k < nq) {
+    if (k < k1) {
       const int v = __ldcg(list_in + k);
-      next = update_band_voxel<false, true>(a, v, v, maxd, energy, active, diverged);
+      next = update_band_voxel<false, kPsiL1>(a, v, v, maxd, energy, active, diverged);
     }
     block_append<kPersistThreads / 32>(next, &a.st[it + 1].list, list_out);
   }
@@ -338,9 +340,9 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_pervoxel(Fus
     while (true) {
       float d[3] = {0.f, 0.f, 0.f}, sv = 0.f, e = 0.f, c0[3] = {0.f, 0.f, 0.f};
       if (interior) {
-        gradient_lane<true>(a, x, y, z, i, d, sv, e, c0);
+        gradient_lane<kPsiL2>(a, x, y, z, i, d, sv, e, c0);
       } else {
-        gradient_generic<true>(a, x, y, z, d, sv, e);
+        gradient_generic<kPsiL2>(a, x, y, z, d, sv, e);
         c0[0] = __ldcg(a.ix + i);
         c0[1] = __ldcg(a.iy + i);
         c0[2] = __ldcg(a.iz + i);

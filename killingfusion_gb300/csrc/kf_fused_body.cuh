@@ -21,7 +21,6 @@ using namespace kfref;
 
 constexpr int kTX = 32, kTY = 8, kThreads = kTX * kTY;
 constexpr int kZSlab = 8;
-constexpr int kTile = kThreads * kZSlab;
 // CTAs of the batch's band pass: 256 threads (chunks of 256 voxels per problem)
 constexpr int kBandWarps = 8;
 constexpr int kBandThreads = 32 * kBandWarps;
@@ -147,7 +146,25 @@ __host__ __device__ constexpr int off25_at(int j, int c) {
 // per band voxel against 291 for 4 lanes, 1.7x the band voxels/s on
 // band-heavy grids, 2.3x on a 64-problem batch, 3 % faster on the dense
 // 256^3 iteration; 4 lanes had been 1.32x 8 lanes and 2x 16.
-template <bool kCoherent = false>
+// How a kernel reads psi: through the read-only path (psi not written during
+// the kernel), through L2 only (ld.global.cg; the per-voxel schedule, which
+// writes psi in place), or through L1 and L2 (ld.global.ca; the persistent
+// passes, which write psi between iterations and order those writes with
+// the fences of their grid-wide barrier -- the read-only path is outside
+// that ordering, L1 is not).
+enum PsiLoad { kPsiReadOnly = 0, kPsiL2 = 1, kPsiL1 = 2 };
+
+template <int kLoad>
+__device__ __forceinline__ float load_psi(const float *p) {
+  if constexpr (kLoad == kPsiL2)
+    return __ldcg(p);
+  else if constexpr (kLoad == kPsiL1)
+    return __ldca(p);
+  else
+    return __ldg(p);
+}
+
+template <int kLoad = kPsiReadOnly>
 __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, int z, int64_t idx, float d[3],
                                               float &s_out, float &e_out, float c0[3]) {
   const DevParams &dp = a.dp;
@@ -163,7 +180,7 @@ __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, 
 #pragma unroll
     for (int n = 0; n < 20; ++n) {
       const float *q = p + nb20_off(n, 0) + nb20_off(n, 1) * sy + nb20_off(n, 2) * sz;
-      v[n] = kCoherent ? __ldcg(q) : __ldg(q);
+      v[n] = load_psi<kLoad>(q);
     }
     const float v000 = v[N000];
     c0[c] = v000;
@@ -331,20 +348,20 @@ __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, 
   e_out = e;
 }
 
-// A psi value read through L2 (ld.global.cg), never through the read-only
-// path: the element type of psi views in kernels that also write psi between
-// their reads (the persistent passes).  Same layout as float.
-struct CgFloat {
+// A psi value read as load_psi<kLoad> reads it: the element type of psi
+// views in kernels that write psi themselves.  Same layout as float.
+template <int kLoad>
+struct PsiElem {
   float v;
-  __device__ __forceinline__ operator float() const { return __ldcg(&v); }
+  __device__ __forceinline__ operator float() const { return load_psi<kLoad>(&v); }
 };
 
-// Generic reference-order gradient for the outer shell (one thread).
-// kCoherent: psi read through L2 (CgFloat).
-template <bool kCoherent = false>
+// Generic reference-order gradient for the outer shell (one thread), psi
+// read as kLoad says (plain loads for kPsiReadOnly).
+template <int kLoad = kPsiReadOnly>
 __device__ __noinline__ void gradient_generic(const FusedArgs &a, int x, int y, int z, float d[3],
                                               float &s_out, float &e_out) {
-  using P = typename std::conditional<kCoherent, CgFloat, float>::type;
+  using P = typename std::conditional<kLoad == kPsiReadOnly, float, PsiElem<kLoad>>::type;
   const DevParams &dp = a.dp;
   const P *px = reinterpret_cast<const P *>(a.ix), *py = reinterpret_cast<const P *>(a.iy),
           *pz = reinterpret_cast<const P *>(a.iz);
@@ -369,29 +386,29 @@ __device__ __forceinline__ void voxel_xyz(const DevParams &dp, int i, int &x, in
   x = (int)(r - (unsigned)y * (unsigned)dp.nx);
 }
 
-// Dense pass over one tile (kTX x kTY columns, kZSlab planes) of block
+// Dense pass over one tile (kTX x kTY columns, kSlab planes) of block
 // coordinates (bx, by, bz): stream the slab, apply the band test, append the
 // band voxels to list (*count counts them).  kPassThrough (ping-pong
 // buffers): copy psi of the voxels outside the band to the output buffer;
 // without it (psi updated in place) they are only read.
-template <bool kPassThrough>
+template <bool kPassThrough, int kSlab = kZSlab>
 __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, int bz,
                                             int *__restrict__ list, unsigned *count) {
-  __shared__ int queue[kTile];
+  __shared__ int queue[kThreads * kSlab];
   __shared__ int qn, qbase;
   const DevParams &dp = a.dp;
   const int tid = threadIdx.y * kTX + threadIdx.x;
   const int x = bx * kTX + threadIdx.x;
   const int y = by * kTY + threadIdx.y;
-  const int z0 = bz * kZSlab;
+  const int z0 = bz * kSlab;
   if (tid == 0) qn = 0;
   __syncthreads();
   const bool col = x < dp.nx && y < dp.ny;
   const int64_t sz = (int64_t)dp.nx * dp.ny;
   const int64_t base = ((int64_t)z0 * dp.ny + y) * dp.nx + x;
-  float px[kZSlab], py[kZSlab], pz[kZSlab], ph[kZSlab];
+  float px[kSlab], py[kSlab], pz[kSlab], ph[kSlab];
 #pragma unroll
-  for (int j = 0; j < kZSlab; ++j) {
+  for (int j = 0; j < kSlab; ++j) {
     bool ok = col && (z0 + j) < dp.nz;
     int64_t i = base + j * sz;
     px[j] = ok ? __ldcs(a.ix + i) : 0.f;
@@ -404,7 +421,7 @@ __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, 
   // streamed values are dead (their trilinear gather is the rare, long path).
   unsigned moved = 0;
 #pragma unroll
-  for (int j = 0; j < kZSlab; ++j) {
+  for (int j = 0; j < kSlab; ++j) {
     int z = z0 + j;
     if (!col || z >= dp.nz) continue;
     int64_t i = base + j * sz;
@@ -595,10 +612,9 @@ __device__ __noinline__ bool trust_step_f(const FusedArgs &a, int x, int y, int 
 // if it left the band) and accumulates the statistics.
 // kTrust: the trust-region step (dp.trust set), a separate instantiation so
 // that the plain band pass carries no call to it.
-// kCoherent: psi is read through L2 (ld.global.cg) rather than the read-only
-// path, for kernels that write psi themselves between iterations (the
-// persistent passes), where the read-only path's cache may hold old values.
-template <bool kTrust = false, bool kCoherent = false>
+// kLoad: how psi is read (PsiLoad); the persistent passes, which write psi
+// between iterations, read it with kPsiL1.
+template <bool kTrust = false, int kLoad = kPsiReadOnly>
 __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int slot, float &maxd,
                                                  double &energy, unsigned &active, bool &diverged) {
   const DevParams &dp = a.dp;
@@ -608,12 +624,12 @@ __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int 
   const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 &&
                         z <= dp.nz - 2;
   if (interior) {
-    gradient_lane<kCoherent>(a, x, y, z, i, d, s, en, c0);
+    gradient_lane<kLoad>(a, x, y, z, i, d, s, en, c0);
   } else {
-    gradient_generic<kCoherent>(a, x, y, z, d, s, en);
-    c0[0] = kCoherent ? __ldcg(a.ix + i) : a.ix[i];
-    c0[1] = kCoherent ? __ldcg(a.iy + i) : a.iy[i];
-    c0[2] = kCoherent ? __ldcg(a.iz + i) : a.iz[i];
+    gradient_generic<kLoad>(a, x, y, z, d, s, en);
+    c0[0] = kLoad == kPsiReadOnly ? a.ix[i] : load_psi<kLoad>(a.ix + i);
+    c0[1] = kLoad == kPsiReadOnly ? a.iy[i] : load_psi<kLoad>(a.iy + i);
+    c0[2] = kLoad == kPsiReadOnly ? a.iz[i] : load_psi<kLoad>(a.iz + i);
   }
   int next = -1;
   if (in_band(s, a.band_hi, a.band_lo)) {

@@ -84,8 +84,10 @@ def test_autotune_keeps_psi(gpu):
         f.upload(p)
         psi0.append(p)
     b = gpu.Batch(probs, 20)
-    k, regs = b.autotune()
-    assert (regs, k) in ((80, 1), (80, 2), (80, 3), (128, 1), (128, 2))
+    sh = b.autotune()
+    band = (sh["band_threads"], sh["band_chunk"], sh["band_blocks_per_sm"], sh["band_registers"])
+    assert band in gpu.BATCH_BAND_SHAPES and sh["slab"] in gpu.BATCH_SLABS
+    assert sh["band_ms"] > 0 and sh["stream_ms"] > 0
     for (gl, gc, f, P), p in zip(probs, psi0):
         np.testing.assert_array_equal(f.download(), p)
     b.run()
@@ -125,3 +127,47 @@ def test_batch_argument_checks(gpu):
         gpu.Batch([(gl, gc, f64, P)], 5)
     with pytest.raises(gpu.KFError):
         gpu.Batch([(gl, gc, f, P)], 0)
+
+
+def test_every_launch_shape_gives_the_same_psi(gpu):
+    """Each band-pass shape (CTA size, chunk size, resident CTAs) and slab
+    depth the autotuner may choose gives every problem the bits of its own
+    band-only solve."""
+    probs = [make_problem(gpu, 500 + k, n) for k, n in enumerate([37, 52, 30, 61])]
+    iters = 9
+    want = [single(gpu, gl, gc, P, iters) for gl, gc, _, P in probs]
+    b = gpu.Batch(probs, iters)
+    for k, band in enumerate(gpu.BATCH_BAND_SHAPES):
+        for slab in gpu.BATCH_SLABS if k == 0 else (gpu.BATCH_SLABS[k % 3],):
+            for _, _, f, _ in probs:
+                f.zero()
+            b.set_shape(band, slab)
+            st = b.run()
+            for (_, _, f, _), (w, ws), s in zip(probs, want, st):
+                np.testing.assert_array_equal(f.download(), w)
+                for key in STAT_KEYS:
+                    assert s[key] == ws[key], (band, slab, key)
+    with pytest.raises(gpu.KFError):
+        b.set_shape((256, 768, 2, 128), 8)
+    b.close()
+
+
+def test_batch_timeout_status(gpu):
+    """A zero wait limit makes the persistent batch launch give up at its first
+    barrier: KF_ERR_TIMEOUT, and the next run with the default limit is right."""
+    probs = [make_problem(gpu, 600 + k, n) for k, n in enumerate([40, 33])]
+    want = [single(gpu, gl, gc, P, 12) for gl, gc, _, P in probs]
+    b = gpu.Batch(probs, 12)
+    prev = gpu.set_wait_limit(0.0)
+    try:
+        with pytest.raises(gpu.KFError) as e:
+            b.run()
+        assert e.value.status == gpu.KF_ERR_TIMEOUT
+    finally:
+        gpu.set_wait_limit(prev)
+    for _, _, f, _ in probs:
+        f.zero()
+    b.run()
+    for (_, _, f, _), (w, _) in zip(probs, want):
+        np.testing.assert_array_equal(f.download(), w)
+    b.close()
