@@ -41,7 +41,7 @@ def test_library_exports_every_declared_symbol(capi):
 
 def test_version_and_params_presets(capi):
     L = capi.load()
-    assert L.kf_version() == 1
+    assert L.kf_version() == 2  # KF_ABI_VERSION: kf_batch_autotune reports a kf_batch_shape
     p = capi._Params()
     L.kf_params_reference(C.byref(p))
     assert (p.voxel_size, p.alpha, p.omega_k, p.gamma_k, p.omega_s) == (0.012, 0.025, 0.04, 0.0, 0.1)
@@ -127,3 +127,23 @@ def test_dataset_writer_and_bounds(tmp_path):
     np.testing.assert_allclose(lo, [-0.3, -23.5 / 52.5 * 0.5, 0.3], rtol=1e-15)
     np.testing.assert_allclose(hi, [0.3, 23.5 / 52.5 * 0.5, 0.5], rtol=1e-15)
     assert synth.grid_from_bounds(lo, hi, 0.008) == (76, 56, 26)
+
+
+def test_batch_shape_struct_matches_header(capi):
+    """The ctypes mirror of kf_batch_shape has the header's fields in order."""
+    src = open(os.path.join(ROOT, "include", "killingfusion.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"typedef struct kf_batch_shape \{(.*?)\} kf_batch_shape;", src, flags=re.S).group(1)
+    fields = re.findall(r"(int|double)\s+(\w+);", body)
+    ctypes_of = {"int": C.c_int, "double": C.c_double}
+    assert [(n, ctypes_of[t]) for t, n in fields] == list(capi.BatchShape._fields_)
+
+
+def test_wait_limit_setting(capi):
+    """kf_set_wait_limit keeps values in [0, 60] s and returns the previous one
+    (host-side only: no kernel runs)."""
+    prev = capi.set_wait_limit(0.25)
+    assert capi.set_wait_limit(prev) == 0.25
+    assert capi.load().kf_set_wait_limit(-1.0) == -1.0
+    assert capi.load().kf_set_wait_limit(61.0) == -1.0
+    assert capi.set_wait_limit(prev) == prev
