@@ -418,6 +418,37 @@ int kf_fusion_process_frame(kf_fusion f, const float *depth, const double c2w[16
                             kf_frame_result *res, void *stream);
 /* Handles of the pipeline's state (owned by the pipeline). */
 int kf_fusion_state(kf_fusion f, kf_grid *canonical, kf_grid *live, kf_field *psi);
+/* Checkpoint and resume of the pipeline: its canonical SDF, psi and frame
+ * count go to a state file (kf_state_save); a pipeline created with the same
+ * configuration and loaded from that file continues the sequence with the
+ * same results, bit for bit, as the pipeline that wrote it.  No counterpart
+ * in the reference, whose dumps (SDF.cpp:432-446, DisplacementField.cpp:
+ * 349-366) keep no weights and have no reader. */
+int kf_fusion_save(kf_fusion f, const char *path, void *stream);
+int kf_fusion_load(kf_fusion f, const char *path, void *stream);
+
+/* ---- files ------------------------------------------------------------ */
+/* State file (version 2) of a registration sequence: the canonical SDF's
+ * float32 values and int32 weights, psi if given (float32 or float64 planes)
+ * and a frame counter, with the grid's dims, placement, voxel size and
+ * unknown-clip distance in the header.  No counterpart in the reference. */
+int kf_state_save(const char *path, kf_grid canonical, kf_field psi, int32_t frame, void *stream);
+/* Header of a state file; psi_precision receives KF_F32, KF_F64 or -1 (no
+ * psi).  Any output may be NULL. */
+int kf_state_info(const char *path, int dims[3], double *voxel, double min3d[3], double *unknown_clip,
+                  int32_t *frame, int *psi_precision);
+/* Reads a state file into existing handles of the file's size, placement
+ * and psi precision (psi may be NULL to skip it); KF_ERR_INVALID when they
+ * differ or the file is not a state file. */
+int kf_state_load(const char *path, kf_grid canonical, kf_field psi, int32_t *frame, void *stream);
+/* A grid from the reference's SDF dump (SDF::dumpToBinFile, SDF.cpp:432-446:
+ * int32 dims[3], double min[3], double voxel, double truncation, double
+ * phi[N]).  Values are stored as float32.  The file keeps no weights: a
+ * voxel whose value is not the initial MaxSurfaceVoxelDistance + epsilon of
+ * params gets weight 1, the others 0.  truncation (may be NULL) receives the
+ * file's truncation distance in voxels. */
+int kf_grid_load_ref_bin(const char *path, const kf_params *params, double unknown_clip, kf_grid *out,
+                         double *truncation, void *stream);
 
 /* Marching cubes that allocates nothing.  No counterpart in the reference:
  * it exists for callers that cannot allocate device memory on their own --

@@ -40,6 +40,7 @@ CUDA_UNITS = [
     ("kf_energy.cu", ["-fmad=false"]),
     ("kf_batch.cu", []),
     ("kf_fusion.cu", []),
+    ("kf_state.cu", []),
 ]
 HOST_UNITS = ["SDF.cpp", "DisplacementField.cpp", "DatasetReader.cpp", "KillingFusion.cpp", "png.cpp"]
 

@@ -159,6 +159,12 @@ SIGNATURES = {
     "kf_fusion_process_frame": (C.c_int, [_vp, _vp, _dp, C.c_int, C.c_void_p, _vp]),
     "kf_fusion_state": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
     "kf_set_wait_limit": (C.c_double, [C.c_double]),
+    "kf_fusion_save": (C.c_int, [_vp, C.c_char_p, _vp]),
+    "kf_fusion_load": (C.c_int, [_vp, C.c_char_p, _vp]),
+    "kf_state_save": (C.c_int, [C.c_char_p, _vp, _vp, C.c_int32, _vp]),
+    "kf_state_info": (C.c_int, [C.c_char_p, _ip3, _vp, _vp, _vp, _vp, _vp]),
+    "kf_state_load": (C.c_int, [C.c_char_p, _vp, _vp, _vp, _vp]),
+    "kf_grid_load_ref_bin": (C.c_int, [C.c_char_p, _PP, C.c_double, C.POINTER(_vp), _vp, _vp]),
 }
 
 _lib = None
@@ -628,3 +634,11 @@ class Fusion:
         c, l, f = _vp(), _vp(), _vp()
         check(load().kf_fusion_state(self.h, C.byref(c), C.byref(l), C.byref(f)))
         return c.value, l.value, f.value
+
+    def save(self, path):
+        """Checkpoint: canonical SDF, psi and frame count to a state file."""
+        check(load().kf_fusion_save(self.h, os.fsencode(path), None))
+
+    def load(self, path):
+        """Resume from a state file written by a pipeline of this configuration."""
+        check(load().kf_fusion_load(self.h, os.fsencode(path), None))

@@ -52,6 +52,33 @@ KillingFusion::~KillingFusion() {
   delete m_prev2CanDisplacementField;
 }
 
+void KillingFusion::saveState(const std::string &path) const {
+  kf::check(kf_state_save(path.c_str(), m_canonicalSdf->handle(),
+                          m_prev2CanDisplacementField ? m_prev2CanDisplacementField->handle() : nullptr,
+                          m_currFrameIndex, nullptr),
+            "kf_state_save");
+}
+
+void KillingFusion::loadState(const std::string &path) {
+  int dims[3];
+  int prec = -1;
+  int32_t frame = 0;
+  kf::check(kf_state_info(path.c_str(), dims, nullptr, nullptr, nullptr, &frame, &prec), "kf_state_info");
+  const kf::Vec3i n = m_canonicalSdf->getGridSize();
+  if (dims[0] != n(0) || dims[1] != n(1) || dims[2] != n(2))
+    throw std::runtime_error("KillingFusion::loadState: the state file's grid differs from this sequence's");
+  DisplacementField *psi = nullptr;
+  if (prec >= 0) psi = new DisplacementField(n, kf::config().VoxelSize, (kf_precision)prec);
+  int rc = kf_state_load(path.c_str(), m_canonicalSdf->handle(), psi ? psi->handle() : nullptr, &frame, nullptr);
+  if (rc) {
+    delete psi;
+    kf::check(rc, "kf_state_load");
+  }
+  delete m_prev2CanDisplacementField;
+  m_prev2CanDisplacementField = psi;
+  m_currFrameIndex = frame;
+}
+
 void KillingFusion::setFrameRange(int start, int end, int stride) {
   if (stride < 1 || end < start) throw std::invalid_argument("KillingFusion::setFrameRange");
   m_startFrame = start;

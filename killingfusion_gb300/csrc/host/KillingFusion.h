@@ -4,6 +4,7 @@
 // and warp + fuse is one kf_warp_fuse pass.
 #pragma once
 
+#include <string>
 #include <utility>
 #include <vector>
 
@@ -44,6 +45,15 @@ class KillingFusion {
   const SDF *getCanonicalSdf() const { return m_canonicalSdf; }
   // Statistics of the last computeDisplacementField.
   const kf_solve_stats &lastSolveStats() const { return m_lastStats; }
+
+  // Checkpoint (no counterpart in the reference, whose dumps keep no weights
+  // and have no reader): the canonical SDF with its weights, psi and the
+  // current frame index go to a state file (kf_state_save).
+  void saveState(const std::string &path) const;
+  // Resume from a state file of saveState, written by a KillingFusion over a
+  // dataset of the same geometry: the next processNextFrame continues the
+  // sequence where the saved object stood, with the same results.
+  void loadState(const std::string &path);
 
   // The frustum bounds of a w x h camera between minDepth and maxDepth in
   // world space with pose = identity (KillingFusion.cpp:478-519).

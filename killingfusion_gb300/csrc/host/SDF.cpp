@@ -61,6 +61,25 @@ SDF::SDF(SDF &&o) noexcept
 
 SDF::~SDF() { kf_grid_destroy(m_grid); }
 
+SDF::SDF(kf_grid grid, double unknownClipDistance) : m_grid(grid), m_unknownClipDistance(unknownClipDistance) {
+  int dims[3];
+  double mn[3];
+  kf::check(kf_grid_info(grid, dims, &m_voxelSize, mn, nullptr), "kf_grid_info");
+  for (int k = 0; k < 3; ++k) {
+    m_gridSize(k) = dims[k];
+    m_min3dLoc(k) = mn[k];
+    m_max3dLoc(k) = mn[k] + ((double)dims[k] - 0.5) * m_voxelSize;
+  }
+}
+
+SDF *SDF::loadFromBinFile(const std::string &path, double unknownClipDistance) {
+  kf_params p = params_now();
+  kf_grid g = nullptr;
+  kf::check(kf_grid_load_ref_bin(path.c_str(), &p, unknownClipDistance, &g, nullptr, nullptr),
+            "kf_grid_load_ref_bin");
+  return new SDF(g, unknownClipDistance);
+}
+
 std::vector<SDF> SDF::getDataEnergyTestSample(double voxelSize, double unknownClipDistance) {
   Vec3d mn(0, 0, 0), mx(voxelSize * 9, voxelSize * 9, voxelSize * 9);
   SDF can(voxelSize, mn, mx, unknownClipDistance), next(voxelSize, mn, mx, unknownClipDistance);

@@ -85,6 +85,13 @@ class SDF {
   // phi (SDF.cpp:432-460).
   void dumpToBinFile(std::string outputFilePath, double truncationDistanceInVoxelSizeUnit,
                      double minimumWeightThreshold) const;
+  // Reads a file in dumpToBinFile's layout (no counterpart in the reference,
+  // which only writes it): the grid's dims, placement and voxel size come
+  // from the file, values are stored as float32.  The file keeps no
+  // weights: a voxel whose value is not the initial MaxSurfaceVoxelDistance
+  // + epsilon gets weight 1, the others 0.  getMax3dLoc() is the min corner
+  // plus (dims - 1/2) voxels, a bound that gives the file's dims back.
+  static SDF *loadFromBinFile(const std::string &path, double unknownClipDistance);
 
   kf::Vec3d getMin3dLoc() const { return m_min3dLoc; }
   kf::Vec3d getMax3dLoc() const { return m_max3dLoc; }
@@ -97,6 +104,7 @@ class SDF {
 
  private:
   void allocate();
+  SDF(kf_grid grid, double unknownClipDistance);  // adopts a grid made by the C ABI
   std::vector<double> sampleDistances(const std::vector<double> &pts) const;
   std::vector<double> warpedPoints(const std::vector<double> &pts, const DisplacementField *psi) const;
   kf_grid m_grid = nullptr;

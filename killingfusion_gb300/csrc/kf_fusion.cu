@@ -173,3 +173,18 @@ extern "C" int kf_fusion_process_frame(kf_fusion f, const float *depth, const do
   if (res) *res = r;
   return KF_OK;
 }
+
+extern "C" int kf_fusion_save(kf_fusion f, const char *path, void *stream) {
+  KF_REQUIRE(f && path, "NULL argument");
+  return kf_state_save(path, f->can, f->psi, f->frames, stream);
+}
+
+extern "C" int kf_fusion_load(kf_fusion f, const char *path, void *stream) {
+  KF_REQUIRE(f && path, "NULL argument");
+  int32_t frames = 0;
+  int rc = kf_state_load(path, f->can, f->psi, &frames, stream);
+  if (rc) return rc;
+  KF_REQUIRE(frames >= 0, "negative frame count in the state file");
+  f->frames = frames;
+  return KF_OK;
+}
