@@ -229,10 +229,10 @@ def run_ours(args, rank, world, local):
 
     N3 = int(np.prod(grid.dims))
     # reset, integrate (3 kernels), the solve (fused: stream + band per
-    # iteration and one write-back; plain: 7 kernels), warp+fuse (2), 3
+    # iteration and one write-back; plain: 7 kernels), warp+fuse (3), 3
     # meshes of 3 kernels each
-    launches_per_frame = 1 + 3 + fused_solve_launches(N3, args.iters) + 2 + 3 * 3 if args.solver == "fused" else \
-        1 + 3 + 7 * args.iters + 2 + 3 * 3
+    launches_per_frame = 1 + 3 + fused_solve_launches(N3, args.iters) + 3 + 3 * 3 if args.solver == "fused" else \
+        1 + 3 + 7 * args.iters + 3 + 3 * 3
 
     # two frames in flight on four streams (killingfusion_gb300.pipeline)
     pipe = FramePipeline(grid.dims, grid.voxel, grid.origin, P, args.iters, args.solver,

@@ -427,11 +427,13 @@ __device__ __forceinline__ void fuse_voxel(float *__restrict__ cphi, int32_t *__
 // SDF::update followed by canonical->fuse(live) (KillingFusion.cpp:158-159,
 // SDF.cpp:199-241, 300-328), in place.  A voxel with psi == 0 keeps its
 // values (zero interpolation weights), so only the moved voxels -- the band
-// the solver updated -- change: their resampled values go to a side list
-// (warp-aggregated slots) and k_warp_scatter writes them back once every
-// moved voxel has read its neighbours' old values.  Each thread takes four
-// consecutive voxels with 16-byte loads.  When `cphi` is null only the warp
-// is done.
+// the solver updated -- change.  This pass fuses the others and lists the
+// moved ones (warp-aggregated slots); k_warp_moved resamples and fuses those
+// in float64, spread over every SM (in the blocks of this pass, which hold
+// the surface, their float64 arithmetic was the kernel's tail), and
+// k_warp_scatter writes their values back once every moved voxel has read
+// its neighbours' old values.  Each thread takes four consecutive voxels
+// with 16-byte loads.  When `cphi` is null only the warp is done.
 template <typename P>
 __global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ lphi,
                                                       const int32_t *__restrict__ lw,
@@ -492,21 +494,37 @@ __global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ 
   for (int e = 0; e < 4; ++e) {
     if (e >= valid) break;
     const int64_t i = i0 + e;
-    float nphi = ph[e];
-    int32_t nw = wv[e];
-    if (moved & (1u << e)) {
-      int x, y, z;
-      voxel_xyz(i, nx, ny, x, y, z);
-      double dphi, dw;
-      bool m;
-      warp_sample(lphi, lw, nx, ny, nz, oob, f, i, x, y, z, dphi, dw, m);
-      nphi = (float)dphi;
-      nw = (int32_t)(int64_t)dw;
-      side_phi[slot] = nphi;
-      side_w[slot] = nw;
-      side_i[slot] = (int32_t)i;
-      ++slot;
-    }
+    if (moved & (1u << e))
+      side_i[slot++] = (int32_t)i;
+    else if (cphi)
+      fuse_voxel(cphi, cw, i, ph[e], wv[e]);
+  }
+}
+
+// The moved voxels listed by k_warp_fuse: resample (phi, w) at i+0.5+psi(i)
+// in float64 (SDF::update, SDF.cpp:309-321), fuse into the canonical SDF,
+// keep the new values in the side list for k_warp_scatter.
+template <typename P>
+__global__ void __launch_bounds__(kBlock) k_warp_moved(const float *__restrict__ lphi,
+                                                       const int32_t *__restrict__ lw,
+                                                       float *__restrict__ cphi, int32_t *__restrict__ cw,
+                                                       PsiPlanes<P> f, int nx, int ny, int nz, double oob,
+                                                       float *__restrict__ side_phi,
+                                                       int32_t *__restrict__ side_w,
+                                                       const int32_t *__restrict__ side_i,
+                                                       const unsigned *__restrict__ ctr) {
+  const unsigned n = *ctr;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t i = side_i[k];
+    int x, y, z;
+    voxel_xyz(i, nx, ny, x, y, z);
+    double dphi, dw;
+    bool m;
+    warp_sample(lphi, lw, nx, ny, nz, oob, f, i, x, y, z, dphi, dw, m);
+    const float nphi = (float)dphi;
+    const int32_t nw = (int32_t)(int64_t)dw;
+    side_phi[k] = nphi;
+    side_w[k] = nw;
     if (cphi) fuse_voxel(cphi, cw, i, nphi, nw);
   }
 }
@@ -716,8 +734,16 @@ static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevPara
     k_warp_fuse<double><<<blocks, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<double>(psi), live->n[0],
                                                   live->n[1], live->n[2], dp.oob_phi, side_phi, side_w, side_i,
                                                   live->ctr);
-  k_warp_scatter<<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(live->phi, live->w, side_phi, side_w, side_i,
-                                                               live->ctr);
+  const unsigned spread = (unsigned)kf_num_sms() * 4;
+  if (psi->prec == KF_F32)
+    k_warp_moved<float><<<spread, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<float>(psi), live->n[0],
+                                                  live->n[1], live->n[2], dp.oob_phi, side_phi, side_w, side_i,
+                                                  live->ctr);
+  else
+    k_warp_moved<double><<<spread, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<double>(psi),
+                                                   live->n[0], live->n[1], live->n[2], dp.oob_phi, side_phi,
+                                                   side_w, side_i, live->ctr);
+  k_warp_scatter<<<spread, kBlock, 0, s>>>(live->phi, live->w, side_phi, side_w, side_i, live->ctr);
   KF_CHECK_LAUNCH("k_warp_fuse");
   return KF_OK;
 }

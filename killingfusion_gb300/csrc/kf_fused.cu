@@ -216,8 +216,11 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
 // between iterations, ordered by the barrier's fences), the SDFs through the
 // read-only path.  A gated iteration (converged, diverged) ends the kernel
 // in every block alike: each reads the same statistics after the barrier.
-constexpr int kPersistThreads = 256;
-constexpr int kPersistBlocksPerSM = 2;
+// 64-thread blocks, 4 per SM: a 255-register budget (the band update does not
+// spill) and, for a small band, one working warp on each of an SM's four
+// schedulers
+constexpr int kPersistThreads = 64;
+constexpr int kPersistBlocksPerSM = 4;
 
 __device__ __forceinline__ bool persistent_band_iteration(const FusedArgs &a, int it, bool last,
                                                           const int *__restrict__ list_in,

@@ -48,6 +48,6 @@ def test_batch_problems_match_oracle(gpu, oracle):
         assert st["active_first"] == counts[0] > 100, KINDS[seed]
         assert st["active_last"] == counts[-1], KINDS[seed]
         err = np.abs(f.download().astype(np.float64) - opsi)
-        assert np.abs(opsi).max() > 0.05, KINDS[seed]
         assert err.max() <= PSI_TOL, (KINDS[seed], err.max(), int((err > PSI_TOL).sum()))
+        assert np.abs(opsi).max() > 50 * PSI_TOL, KINDS[seed]  # psi moved well beyond the tolerance
     b.close()
