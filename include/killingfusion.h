@@ -145,6 +145,21 @@ void kf_params_paper(kf_params *p, double voxel_size, double trunc_voxels);
  * the error path).  Returns the previous limit, or -1 for a value outside
  * [0, 60] (ignored). */
 double kf_set_wait_limit(double seconds);
+/* Bounds-check build (the library compiled with -DKF_BOUNDS_CHECK,
+ * libkillingfusion_bc.so): the kernels of the hot path check every index
+ * they take from data (band lists and their append positions, the dense
+ * passes' queues and run tables, the in-place write-back, side lists, the
+ * marching-cubes block list) and skip an access outside its bound instead
+ * of making it.  kf_bounds_status reports whether this build checks
+ * (enabled), how many checks failed since the last kf_bounds_reset, and the
+ * first failure's site (KfBoundsSite in kf_bounds.cuh), index and bound; the
+ * normal build reports enabled = 0 and no failures.  kf_bounds_reset clears
+ * the records; a positive limit also lowers every bound to `limit` (the
+ * checked build only), so that a test can make the checks fire on a small
+ * grid while every access stays inside its buffer.  No counterpart in the
+ * reference, which has no sanitizer mode. */
+int kf_bounds_status(int *enabled, int64_t *violations, int *site, int64_t *index, int64_t *bound);
+int kf_bounds_reset(int64_t limit);
 /* Introspection of the marching-cubes table (MarchingCubes.h:26-318): edge
  * mask of a cube configuration and its triangle list (edge ids, -1 padded). */
 int kf_mc_case(int cubeindex, int *edge_mask, int tri_edges[16]);

@@ -5,7 +5,10 @@ Produces, in-tree:
 * ``killingfusion_gb300/_lib/libkillingfusion.so`` -- the C ABI of
   ``include/killingfusion.h`` (CUDA kernels + host entry points);
 * ``killingfusion_gb300/_lib/libkf_host.so`` -- the C++ classes with the
-  reference's names and call shapes (``csrc/host``), linked against the former.
+  reference's names and call shapes (``csrc/host``), linked against the former;
+* ``killingfusion_gb300/_lib/libkillingfusion_bc.so`` -- the same C ABI built
+  with ``-DKF_BOUNDS_CHECK`` (every data-derived index of the hot-path
+  kernels checked, see ``csrc/kf_bounds.cuh``), for tests.
 
 One ``-gencode arch=compute_103a,code=sm_103a``; translation units are
 compiled in parallel.  ``kf_exact.cu`` is compiled with ``-fmad=false``: its
@@ -28,6 +31,7 @@ LIB_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(LIB_DIR, "libkillingfusion.so")
 HOST_LIB = os.path.join(LIB_DIR, "libkf_host.so")
+LIB_BC = os.path.join(LIB_DIR, "libkillingfusion_bc.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, extra flags)
@@ -82,22 +86,28 @@ def build(force: bool = False, verbose: bool = False) -> str:
     common = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC] + ARCH
     hdrs = _headers()
-    jobs, objs = [], []
-    for src, extra in CUDA_UNITS:
-        s = os.path.join(CSRC, src)
-        if not os.path.exists(s):
-            continue
-        o = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
-        objs.append(o)
-        if force or _stale(o, [s] + hdrs):
-            jobs.append([nv] + common + extra + ["-Xptxas", "-v"] * verbose + ["-c", s, "-o", o])
+    jobs = []
+    objs = {LIB: [], LIB_BC: []}
+    for lib, obj_dir, defs in ((LIB, OBJ_DIR, []), (LIB_BC, os.path.join(OBJ_DIR, "bc"), ["-DKF_BOUNDS_CHECK"])):
+        os.makedirs(obj_dir, exist_ok=True)
+        for src, extra in CUDA_UNITS:
+            s = os.path.join(CSRC, src)
+            if not os.path.exists(s):
+                continue
+            o = os.path.join(obj_dir, src.replace(".cu", ".o"))
+            objs[lib].append(o)
+            if force or _stale(o, [s] + hdrs):
+                jobs.append([nv] + common + defs + extra + ["-Xptxas", "-v"] * verbose + ["-c", s, "-o", o])
+    # the longest units first, so that they do not start last
+    jobs.sort(key=lambda j: 0 if any(u in j[-3] for u in ("kf_batch", "kf_fused", "kf_exact")) else 1)
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
         for o in outs:
             sys.stdout.write(o)
-    if force or _stale(LIB, objs):
-        _run([nv, "-shared"] + ARCH + ["-o", LIB] + objs + ["-lcudart_static", "-ldl", "-lrt", "-lpthread"])
+    for lib, o in objs.items():
+        if force or _stale(lib, o):
+            _run([nv, "-shared"] + ARCH + ["-o", lib] + o + ["-lcudart_static", "-ldl", "-lrt", "-lpthread"])
     _build_host(force)
     return LIB
 

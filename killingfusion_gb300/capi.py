@@ -17,7 +17,9 @@ import numpy as np
 
 from . import _build
 
-LIB_PATH = _build.LIB
+# KF_LIBRARY=bounds_check selects the build with checked indices
+# (_build.LIB_BC); tests run it in a process of its own
+LIB_PATH = _build.LIB_BC if os.environ.get("KF_LIBRARY") == "bounds_check" else _build.LIB
 
 (KF_OK, KF_ERR_INVALID, KF_ERR_OOM, KF_ERR_CUDA, KF_ERR_DIVERGED, KF_ERR_TIMEOUT, KF_ERR_CAPACITY,
  KF_ERR_INTERNAL) = range(8)
@@ -159,6 +161,9 @@ SIGNATURES = {
     "kf_fusion_process_frame": (C.c_int, [_vp, _vp, _dp, C.c_int, C.c_void_p, _vp]),
     "kf_fusion_state": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
     "kf_set_wait_limit": (C.c_double, [C.c_double]),
+    "kf_bounds_status": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "kf_bounds_reset": (C.c_int, [C.c_int64]),
     "kf_fusion_save": (C.c_int, [_vp, C.c_char_p, _vp]),
     "kf_fusion_load": (C.c_int, [_vp, C.c_char_p, _vp]),
     "kf_state_save": (C.c_int, [C.c_char_p, _vp, _vp, C.c_int32, _vp]),
@@ -184,6 +189,18 @@ def load() -> C.CDLL:
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def bounds_status() -> dict:
+    """The bounds-check build's record (enabled = 0 in the normal build)."""
+    en, n, site, idx, bound = C.c_int(), C.c_int64(), C.c_int(), C.c_int64(), C.c_int64()
+    check(load().kf_bounds_status(C.byref(en), C.byref(n), C.byref(site), C.byref(idx), C.byref(bound)))
+    return {"enabled": en.value, "violations": n.value, "site": site.value, "index": idx.value,
+            "bound": bound.value}
+
+
+def bounds_reset(limit: int = 0):
+    check(load().kf_bounds_reset(int(limit)))
 
 
 def set_wait_limit(seconds: float) -> float:

@@ -214,7 +214,7 @@ __device__ __forceinline__ bool batch_band_pass(const BatchEntry *__restrict__ t
         next = update_band_voxel<false, kPsiL1>(s_a, i, i, maxd, energy, active, diverged);
       }
       // hand the round's updated voxels to the next iteration
-      block_append<kT / 32>(next, &s_a.st[it + 1].list, s_list_out);
+      block_append<kT / 32>(next, &s_a.st[it + 1].list, s_list_out, s_a.dp.count);
     }
   }
   if (cur >= 0) flush(cur);
@@ -609,3 +609,5 @@ extern "C" int kf_batch_run(kf_batch b, kf_solve_stats *stats, void *stream) {
   if (any_diverged) return kf_fail(KF_ERR_DIVERGED, "a problem of the batch diverged (see its statistics)");
   return KF_OK;
 }
+
+KF_BOUNDS_TU_API(batch)

@@ -40,6 +40,40 @@ extern "C" double kf_set_wait_limit(double seconds) {
 
 unsigned long long kf_wait_limit_ns() { return (unsigned long long)(g_wait_limit_s.load() * 1e9); }
 
+// Bounds-check build mode: the records of the translation units with
+// checked kernels, summed; the first failed check of the first unit that
+// has one.
+extern "C" int kf_bounds_status(int *enabled, int64_t *violations, int *site, int64_t *index, int64_t *bound) {
+#ifdef KF_BOUNDS_CHECK
+  if (enabled) *enabled = 1;
+#else
+  if (enabled) *enabled = 0;
+#endif
+  int (*readers[])(KfBoundsRecord *) = {kf_bounds_tu_read_fused, kf_bounds_tu_read_batch, kf_bounds_tu_read_exact,
+                                        kf_bounds_tu_read_mc};
+  int64_t total = 0;
+  KfBoundsRecord first = {0u, 0, 0, 0};
+  for (auto rd : readers) {
+    KfBoundsRecord r;
+    KF_CHECK_CUDA((cudaError_t)rd(&r));
+    if (r.count && !first.count) first = r;
+    total += r.count;
+  }
+  if (violations) *violations = total;
+  if (site) *site = first.site;
+  if (index) *index = first.index;
+  if (bound) *bound = first.bound;
+  return KF_OK;
+}
+
+extern "C" int kf_bounds_reset(int64_t limit) {
+  const long long l = limit > 0 ? (long long)limit : 0x7fffffffffffffffLL;
+  int (*resets[])(long long) = {kf_bounds_tu_reset_fused, kf_bounds_tu_reset_batch, kf_bounds_tu_reset_exact,
+                                kf_bounds_tu_reset_mc};
+  for (auto rs : resets) KF_CHECK_CUDA((cudaError_t)rs(l));
+  return KF_OK;
+}
+
 extern "C" const char *kf_last_error(void) { return g_last_error.c_str(); }
 
 // ---------------------------------------------------------------------------

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <vector>
 
+#include "kf_bounds.cuh"
 #include "kf_ffloat.cuh"
 #include "kf_internal.h"
 #include "kf_ref_math.cuh"
@@ -64,6 +65,7 @@ struct IntegrateArgs {
   float cliph, clipl;                  // unknown_clip as a float pair
   float tol;                           // bound on |float-float distance - reference's|
   int width, height;
+  int64_t count;                       // voxels of the grid
 };
 
 // Pixel coordinates exactly as SDF::integrateDepthFrame computes them, in
@@ -267,6 +269,7 @@ __global__ void __launch_bounds__(kBlock) k_integrate_exact(float *__restrict__ 
   const unsigned n = min(*list_n, list_cap);
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int64_t i = list[k];
+    if (!KF_IN_BOUNDS(i, a.count, KF_SITE_INTEGRATE_LIST)) continue;
     int x, y, z;
     voxel_xyz(i, nx, ny, x, y, z);
     integrate_exact_voxel(phi, w, x, y, z, i, depth, a);
@@ -303,6 +306,7 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   a.max_depth_down = hi;
   a.width = width;
   a.height = height;
+  a.count = g->count;
   a.depth_scale = depth_scale;
   ff_split_host(w2c[11], a.w11h, a.w11l);
   ff_split_host(g->unknown_clip, a.cliph, a.clipl);
@@ -494,8 +498,10 @@ __global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ 
   for (int e = 0; e < 4; ++e) {
     if (e >= valid) break;
     const int64_t i = i0 + e;
-    if (moved & (1u << e))
-      side_i[slot++] = (int32_t)i;
+    if (moved & (1u << e)) {
+      if (KF_IN_BOUNDS(slot, N, KF_SITE_SIDE_LIST)) side_i[slot] = (int32_t)i;
+      ++slot;
+    }
     else if (cphi)
       fuse_voxel(cphi, cw, i, ph[e], wv[e]);
   }
@@ -516,6 +522,9 @@ __global__ void __launch_bounds__(kBlock) k_warp_moved(const float *__restrict__
   const unsigned n = *ctr;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int64_t i = side_i[k];
+    if (!KF_IN_BOUNDS(k, (int64_t)nx * ny * nz, KF_SITE_SIDE_LIST) ||
+        !KF_IN_BOUNDS(i, (int64_t)nx * ny * nz, KF_SITE_SIDE_LIST))
+      continue;
     int x, y, z;
     voxel_xyz(i, nx, ny, x, y, z);
     double dphi, dw;
@@ -534,10 +543,11 @@ __global__ void __launch_bounds__(kBlock) k_warp_scatter(float *__restrict__ lph
                                                          const float *__restrict__ side_phi,
                                                          const int32_t *__restrict__ side_w,
                                                          const int32_t *__restrict__ side_i,
-                                                         const unsigned *__restrict__ ctr) {
+                                                         const unsigned *__restrict__ ctr, int64_t count) {
   const unsigned n = *ctr;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int32_t i = side_i[k];
+    if (!KF_IN_BOUNDS(k, count, KF_SITE_SIDE_LIST) || !KF_IN_BOUNDS(i, count, KF_SITE_SIDE_LIST)) continue;
     lphi[i] = side_phi[k];
     lw[i] = side_w[k];
   }
@@ -743,7 +753,7 @@ static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevPara
     k_warp_moved<double><<<spread, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<double>(psi),
                                                    live->n[0], live->n[1], live->n[2], dp.oob_phi, side_phi,
                                                    side_w, side_i, live->ctr);
-  k_warp_scatter<<<spread, kBlock, 0, s>>>(live->phi, live->w, side_phi, side_w, side_i, live->ctr);
+  k_warp_scatter<<<spread, kBlock, 0, s>>>(live->phi, live->w, side_phi, side_w, side_i, live->ctr, live->count);
   KF_CHECK_LAUNCH("k_warp_fuse");
   return KF_OK;
 }
@@ -1110,3 +1120,5 @@ extern "C" int kf_field_fill(kf_field f, const double v[3], void *stream) {
   KF_CHECK_LAUNCH("k_field_fill");
   return KF_OK;
 }
+
+KF_BOUNDS_TU_API(exact)

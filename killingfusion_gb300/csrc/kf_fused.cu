@@ -56,7 +56,10 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
     const int2 r = runs[blockIdx.x];
     float *px = const_cast<float *>(a.ix), *py = const_cast<float *>(a.iy), *pz = const_cast<float *>(a.iz);
     for (int j = threadIdx.x; j < r.y; j += kThreads) {
-      const int slot = r.x + j, v = prev_list[slot];
+      const int slot = r.x + j;
+      if (!KF_IN_BOUNDS(slot, a.dp.count, KF_SITE_WRITE_BACK)) continue;
+      const int v = prev_list[slot];
+      if (!KF_IN_BOUNDS(v, a.dp.count, KF_SITE_WRITE_BACK)) continue;
       px[v] = a.ox[slot];
       py[v] = a.oy[slot];
       pz[v] = a.oz[slot];
@@ -119,10 +122,13 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_runs(const int2 *__rest
   int h = s_warp[warp] + incl - mine;  // hot runs before r0
   int c = r0 - h;                       // cold runs before r0
   for (int r = r0; r < r1; ++r) {
-    if (runs[r].y > 0)
-      hot[h++] = r;
-    else
-      cold[c++] = r;
+    if (runs[r].y > 0) {
+      if (KF_IN_BOUNDS(h, nruns, KF_SITE_RUNS)) hot[h] = r;
+      ++h;
+    } else {
+      if (KF_IN_BOUNDS(c, nruns, KF_SITE_RUNS)) cold[c] = r;
+      ++c;
+    }
   }
   if (tid == 0) {
     counts[0] = (unsigned)s_total;
@@ -148,7 +154,10 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream_runs(FusedArgs a, con
   if (kCold) {
     if (a.st[a.iter - 1].skipped) return;
     for (unsigned idx = blockIdx.x; idx < n; idx += gridDim.x) {
-      stream_flat<false, true>(a, run_list[idx], nullptr, &a.st[a.iter].cold);
+      const int r = run_list[idx];
+      if (KF_IN_BOUNDS(r, max((a.dp.count / 4 + kThreads * kFlatGroups - 1) / (kThreads * kFlatGroups), (int64_t)1),
+                       KF_SITE_RUNS))
+        stream_flat<false, true>(a, r, nullptr, &a.st[a.iter].cold);
       __syncthreads();
     }
     return;
@@ -159,10 +168,16 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream_runs(FusedArgs a, con
   float *px = const_cast<float *>(a.ix), *py = const_cast<float *>(a.iy), *pz = const_cast<float *>(a.iz);
   for (unsigned idx = blockIdx.x; idx < n; idx += gridDim.x) {
     const int r = run_list[idx];
+    if (!KF_IN_BOUNDS(r, max((a.dp.count / 4 + kThreads * kFlatGroups - 1) / (kThreads * kFlatGroups), (int64_t)1),
+                      KF_SITE_RUNS))
+      continue;
     if (write_back) {
       const int2 rr = runs[r];
       for (int j = threadIdx.x; j < rr.y; j += kThreads) {
-        const int slot = rr.x + j, v = prev_list[slot];
+        const int slot = rr.x + j;
+        if (!KF_IN_BOUNDS(slot, a.dp.count, KF_SITE_WRITE_BACK)) continue;
+        const int v = prev_list[slot];
+        if (!KF_IN_BOUNDS(v, a.dp.count, KF_SITE_WRITE_BACK)) continue;
         px[v] = a.ox[slot];
         py[v] = a.oy[slot];
         pz[v] = a.oz[slot];
@@ -201,7 +216,7 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
       const int v = list_in[k];
       next = update_band_voxel<kTrust>(a, v, kInPlace ? k : v, maxd, energy, active, diverged);
     }
-    if (kCarry) block_append<kLaneWarps>(next, &a.st[a.iter + 1].list, list_out);
+    if (kCarry) block_append<kLaneWarps>(next, &a.st[a.iter + 1].list, list_out, a.dp.count);
   }
   reduce_iter_stats<kLaneThreads>(a.st + a.iter, active, maxd, energy, diverged);
 }
@@ -209,48 +224,81 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
 // Band-only solver, every iteration in one cooperative launch.  One band pass
 // per iteration as k_fused_band<kCarry> (ping-pong buffers, the updated
 // voxels carried to the next iteration's list), then a grid-wide barrier
-// (kf_grid_sync.cuh) instead of a kernel boundary.  Each block takes an equal
-// contiguous slice of the band list, so a small band spreads over all the
-// SMs and neighbouring band voxels (which share psi neighbours) stay in one
-// SM's L1.  psi is read through L1 and L2 (kPsiL1: the blocks write it
-// between iterations, ordered by the barrier's fences), the SDFs through the
-// read-only path.  A gated iteration (converged, diverged) ends the kernel
-// in every block alike: each reads the same statistics after the barrier.
+// (kf_grid_sync.cuh) instead of a kernel boundary.
+// - Each block takes an equal contiguous slice of the first band list and
+//   keeps its own voxels from then on: the band can only shrink, so a
+//   block's carried voxels are compacted into its own slice of the other
+//   list, with no global atomic on the iteration's critical path.
+// - A block's voxels alternate between its warps, so that a small band (a
+//   few dozen voxels per block at 256^3) keeps every scheduler of the SM
+//   busy; neighbouring band voxels (which share psi neighbours) stay in one
+//   SM's L1.
+// - psi is read through L1 and L2 (kPsiL1: the blocks write it between
+//   iterations, ordered by the barrier's fences), the SDFs through the
+//   read-only path.  A gated iteration (converged, diverged) ends the kernel
+//   in every block alike: each reads the same statistics after the barrier.
 // 64-thread blocks, 4 per SM: a 255-register budget (the band update does not
-// spill) and, for a small band, one working warp on each of an SM's four
-// schedulers
+// spill), two warps a block.
 constexpr int kPersistThreads = 64;
+constexpr int kPersistWarps = kPersistThreads / 32;
 constexpr int kPersistBlocksPerSM = 4;
 
+// Compacts the voxels `next` (>= 0 on the threads that carry one) of the
+// block into out[base...] (capacity entries), with no atomic; returns how
+// many there were.  Every thread of the block calls it.
+__device__ __forceinline__ unsigned block_compact(int next, int *__restrict__ out, unsigned base,
+                                                  unsigned capacity) {
+  __shared__ unsigned s_w[kPersistWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool has = next >= 0;
+  const unsigned ball = __ballot_sync(0xffffffffu, has);
+  if (lane == 0) s_w[warp] = (unsigned)__popc(ball);
+  __syncthreads();
+  unsigned before = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < kPersistWarps; ++w) {
+    const unsigned c = s_w[w];
+    before += w < warp ? c : 0u;
+    total += c;
+  }
+  if (has) {
+    const unsigned pos = base + before + (unsigned)__popc(ball & ((1u << lane) - 1u));
+    if (KF_IN_BOUNDS(pos, capacity, KF_SITE_BAND_APPEND)) out[pos] = next;
+  }
+  __syncthreads();  // s_w is written again by the next call
+  return total;
+}
+
+// Iteration `it` of the block's n voxels in[0..n) (carried ones to out,
+// n updated); false when the kernel must end (the iteration was gated, was
+// the last, or a barrier wait gave up).
 __device__ __forceinline__ bool persistent_band_iteration(const FusedArgs &a, int it, bool last,
-                                                          const int *__restrict__ list_in,
-                                                          int *__restrict__ list_out, GridSync *sync,
+                                                          const int *__restrict__ in, int *__restrict__ out,
+                                                          unsigned &n, unsigned capacity, GridSync *sync,
                                                           unsigned long long limit_ns) {
   if (iteration_gated(a.st, it, a.dp)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[it].skipped = 1;
     return false;
   }
-  const unsigned nq = __ldcg(&a.st[it].list);
-  const unsigned nb = gridDim.x;
-  const unsigned per = (nq + nb - 1) / nb;  // this block: list entries [k0, k1)
-  const unsigned k0 = min(blockIdx.x * per, nq), k1 = min(k0 + per, nq);
-  const unsigned rounds = (per + kPersistThreads - 1) / kPersistThreads;  // the same in every block
+  const unsigned rounds = (n + kPersistThreads - 1) / kPersistThreads;
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float maxd = 0.f;
   double energy = 0.0;
-  unsigned active = 0;
+  unsigned active = 0, carried = 0;
   bool diverged = false;
   for (unsigned r = 0; r < rounds; ++r) {
-    const unsigned k = k0 + r * kPersistThreads + threadIdx.x;
+    const unsigned k = r * kPersistThreads + lane * kPersistWarps + warp;
     int next = -1;
-    if (k < k1) {
-      const int v = __ldcg(list_in + k);
+    if (k < n) {
+      const int v = __ldcg(in + k);
       next = update_band_voxel<false, kPsiL1>(a, v, v, maxd, energy, active, diverged);
     }
-    block_append<kPersistThreads / 32>(next, &a.st[it + 1].list, list_out);
+    carried += block_compact(next, out, carried, capacity);
   }
+  n = carried;
   reduce_iter_stats<kPersistThreads>(a.st + it, active, maxd, energy, diverged);
   if (last) return false;
-  if (!grid_sync(sync, nb, limit_ns, it)) {
+  if (!grid_sync(sync, gridDim.x, limit_ns, it)) {
     if (threadIdx.x == 0) a.st[0].timeout = 1;
     return false;
   }
@@ -258,13 +306,19 @@ __device__ __forceinline__ bool persistent_band_iteration(const FusedArgs &a, in
 }
 
 // even: psi in the primary planes, out to the second; odd: the reverse.
+// The band list of the dense first pass is lst0[0, st[0].list).
 __global__ void __launch_bounds__(kPersistThreads, kPersistBlocksPerSM)
     k_band_persistent(FusedArgs even, FusedArgs odd, int *lst0, int *lst1, int iterations, GridSync *sync,
                       unsigned long long limit_ns) {
+  const unsigned nq = __ldcg(&even.st[0].list);
+  const unsigned per = (nq + gridDim.x - 1) / gridDim.x;  // this block's slice [k0, k0 + per)
+  const unsigned k0 = min(blockIdx.x * per, nq);
+  unsigned n = min(k0 + per, nq) - k0;
   for (int it = 0; it < iterations; it += 2) {
-    if (!persistent_band_iteration(even, it, it + 1 == iterations, lst0, lst1, sync, limit_ns)) return;
-    if (it + 1 < iterations &&
-        !persistent_band_iteration(odd, it + 1, it + 2 == iterations, lst1, lst0, sync, limit_ns))
+    if (!persistent_band_iteration(even, it, it + 1 == iterations, lst0 + k0, lst1 + k0, n, per, sync, limit_ns))
+      return;
+    if (it + 1 < iterations && !persistent_band_iteration(odd, it + 1, it + 2 == iterations, lst1 + k0, lst0 + k0,
+                                                          n, per, sync, limit_ns))
       return;
   }
 }
@@ -278,6 +332,8 @@ __global__ void __launch_bounds__(kThreads) k_fused_scatter(FusedArgs a, const i
   const int nq = (int)a.st[a.iter].list;
   for (int k = blockIdx.x * kThreads + threadIdx.x; k < nq; k += gridDim.x * kThreads) {
     const int v = list[k];
+    if (!KF_IN_BOUNDS(k, a.dp.count, KF_SITE_WRITE_BACK) || !KF_IN_BOUNDS(v, a.dp.count, KF_SITE_WRITE_BACK))
+      continue;
     px[v] = a.ox[k];
     py[v] = a.oy[k];
     pz[v] = a.oz[k];
@@ -299,6 +355,7 @@ __global__ void __launch_bounds__(kThreads) k_trust_fix(FusedArgs a, const int *
   const int nq = (int)a.st[a.iter].list;
   for (int k = t0; k < nq; k += stride) {
     const int v = list[k];
+    if (!KF_IN_BOUNDS(v, a.dp.count, KF_SITE_BAND_LIST)) continue;
     int x, y, z;
     voxel_xyz(a.dp, v, x, y, z);
     if (x >= a.rows[z * a.dp.ny + y]) {
@@ -332,6 +389,7 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_pervoxel(Fus
   bool diverged = false;
   for (int k = blockIdx.x * kLaneThreads + threadIdx.x; k < nq; k += gridDim.x * kLaneThreads) {
     const int i = list[k];
+    if (!KF_IN_BOUNDS(i, dp.count, KF_SITE_BAND_LIST)) continue;
     int x, y, z;
     voxel_xyz(dp, i, x, y, z);
     if (((x & 1) | (y & 1) << 1 | (z & 1) << 2) != color) continue;
@@ -678,3 +736,5 @@ int kf_solve_pervoxel(kf_grid live, kf_grid can, kf_field psi, const DevParams &
   return KF_OK;
 }
 
+
+KF_BOUNDS_TU_API(fused)

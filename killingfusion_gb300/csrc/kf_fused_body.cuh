@@ -12,6 +12,7 @@
 #include <cstring>
 #include <type_traits>
 
+#include "kf_bounds.cuh"
 #include "kf_internal.h"
 #include "kf_ref_math.cuh"
 
@@ -428,7 +429,8 @@ __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, 
     if (px[j] != 0.f || py[j] != 0.f || pz[j] != 0.f) {
       moved |= 1u << j;
     } else if (in_band(ph[j], a.band_hi, a.band_lo)) {
-      queue[atomicAdd(&qn, 1)] = (int)i;
+      const int q = atomicAdd(&qn, 1);
+      if (KF_IN_BOUNDS(q, kThreads * kSlab, KF_SITE_STREAM_QUEUE)) queue[q] = (int)i;
     } else if (kPassThrough) {
       __stcs(a.ox + i, 0.f);
       __stcs(a.oy + i, 0.f);
@@ -442,7 +444,8 @@ __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, 
     const float qx = a.ix[i], qy = a.iy[i], qz = a.iz[i];
     const float s = warped_value(a, x, y, z0 + j, qx, qy, qz);
     if (in_band(s, a.band_hi, a.band_lo)) {
-      queue[atomicAdd(&qn, 1)] = (int)i;
+      const int q = atomicAdd(&qn, 1);
+      if (KF_IN_BOUNDS(q, kThreads * kSlab, KF_SITE_STREAM_QUEUE)) queue[q] = (int)i;
     } else if (kPassThrough) {
       __stcs(a.ox + i, qx);
       __stcs(a.oy + i, qy);
@@ -452,7 +455,8 @@ __device__ __forceinline__ void stream_tile(const FusedArgs &a, int bx, int by, 
   __syncthreads();
   if (tid == 0 && qn) qbase = (int)atomicAdd(count, (unsigned)qn);
   __syncthreads();
-  for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
+  for (int k = tid; k < min(qn, kThreads * kSlab); k += kThreads)
+    if (KF_IN_BOUNDS(qbase + k, dp.count, KF_SITE_STREAM_LIST)) list[qbase + k] = queue[k];
 }
 
 // Dense pass over one run of kFlatVoxels consecutive voxels (flat index
@@ -468,8 +472,10 @@ __device__ __forceinline__ void flat_test(const FusedArgs &a, int64_t i, float q
                                           int *queue, int *qn, unsigned &moved, int bit) {
   if (qx != 0.f || qy != 0.f || qz != 0.f)
     moved |= 1u << bit;
-  else if (in_band(ph, a.band_hi, a.band_lo))
-    queue[atomicAdd(qn, 1)] = (int)i;
+  else if (in_band(ph, a.band_hi, a.band_lo)) {
+    const int q = atomicAdd(qn, 1);
+    if (KF_IN_BOUNDS(q, kFlatVoxels + 4, KF_SITE_STREAM_QUEUE)) queue[q] = (int)i;
+  }
 }
 
 // kCheck: the run is only tested, its band voxels are counted in *count and
@@ -538,7 +544,10 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
     const int y = (int)(r / (unsigned)dp.nx);
     const int x = (int)(r - (unsigned)y * (unsigned)dp.nx);
     const float s = warped_value(a, x, y, z, a.ix[i], a.iy[i], a.iz[i]);
-    if (in_band(s, a.band_hi, a.band_lo)) queue[atomicAdd(&qn, 1)] = (int)i;
+    if (in_band(s, a.band_hi, a.band_lo)) {
+      const int q = atomicAdd(&qn, 1);
+      if (KF_IN_BOUNDS(q, kFlatVoxels + 4, KF_SITE_STREAM_QUEUE)) queue[q] = (int)i;
+    }
   }
   __syncthreads();
   if (kCheck) {
@@ -547,17 +556,19 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
   }
   if (tid == 0 && qn) qbase = (int)atomicAdd(count, (unsigned)qn);
   __syncthreads();
-  for (int k = tid; k < qn; k += kThreads) list[qbase + k] = queue[k];
+  for (int k = tid; k < min(qn, kFlatVoxels + 4); k += kThreads)
+    if (KF_IN_BOUNDS(qbase + k, dp.count, KF_SITE_STREAM_LIST)) list[qbase + k] = queue[k];
   // where this run's band voxels sit in the list (for the next iteration's
   // write-back of their new psi)
   if (range && tid == 0) *range = make_int2(qn ? qbase : 0, qn);
 }
 
 // Appends the voxels `next` (>= 0 on the threads that carry one) of the
-// whole block to list_out with one atomic on *count, in thread order; every
-// thread of the block calls it.
+// whole block to list_out (of `capacity` entries) with one atomic on
+// *count, in thread order; every thread of the block calls it.
 template <int kWarps>
-__device__ __forceinline__ void block_append(int next, unsigned *count, int *__restrict__ list_out) {
+__device__ __forceinline__ void block_append(int next, unsigned *count, int *__restrict__ list_out,
+                                             int64_t capacity) {
   __shared__ unsigned s_wcnt[kWarps], s_wbase[kWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool has = next >= 0;
@@ -574,7 +585,10 @@ __device__ __forceinline__ void block_append(int next, unsigned *count, int *__r
     for (int w = 0; w < kWarps; ++w) s_wbase[w] += b;
   }
   __syncthreads();
-  if (has) list_out[s_wbase[warp] + (unsigned)__popc(ball & ((1u << lane) - 1u))] = next;
+  if (has) {
+    const unsigned pos = s_wbase[warp] + (unsigned)__popc(ball & ((1u << lane) - 1u));
+    if (KF_IN_BOUNDS(pos, capacity, KF_SITE_BAND_APPEND)) list_out[pos] = next;
+  }
 }
 
 // The trust-region step (KillingFusion.cpp:288-314) for the float solvers:
@@ -618,6 +632,7 @@ template <bool kTrust = false, int kLoad = kPsiReadOnly>
 __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int slot, float &maxd,
                                                  double &energy, unsigned &active, bool &diverged) {
   const DevParams &dp = a.dp;
+  if (!KF_IN_BOUNDS(i, dp.count, KF_SITE_BAND_LIST) || !KF_IN_BOUNDS(slot, dp.count, KF_SITE_BAND_LIST)) return -1;
   int x, y, z;
   voxel_xyz(dp, i, x, y, z);
   float d[3] = {0.f, 0.f, 0.f}, s = 0.f, en = 0.f, c0[3] = {0.f, 0.f, 0.f};

@@ -131,6 +131,22 @@ struct IterStats {
   int pad_;
 };
 
+// The bounds-check build's record of one translation unit (kf_bounds.cuh).
+struct KfBoundsRecord {
+  unsigned count;  // checks that failed
+  int site;        // the first one's site, index and bound
+  long long index;
+  long long bound;
+};
+int kf_bounds_tu_read_fused(KfBoundsRecord *r);
+int kf_bounds_tu_reset_fused(long long limit);
+int kf_bounds_tu_read_batch(KfBoundsRecord *r);
+int kf_bounds_tu_reset_batch(long long limit);
+int kf_bounds_tu_read_exact(KfBoundsRecord *r);
+int kf_bounds_tu_reset_exact(long long limit);
+int kf_bounds_tu_read_mc(KfBoundsRecord *r);
+int kf_bounds_tu_reset_mc(long long limit);
+
 // Limit of one device-side wait (kf_set_wait_limit), in nanoseconds.
 unsigned long long kf_wait_limit_ns();
 // Barrier state of the persistent kernels (GridSync, 16 bytes) of a field,

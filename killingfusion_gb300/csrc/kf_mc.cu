@@ -21,6 +21,7 @@
 #include <mutex>
 #include <string>
 
+#include "kf_bounds.cuh"
 #include "kf_internal.h"
 #include "kf_mc_tables.h"
 
@@ -204,7 +205,8 @@ __global__ void __launch_bounds__(kThreads) k_mc_scan(const uint32_t *block_tris
       const uint32_t v = s_v[i + (i >> 5)];
       if (i < n) {
         block_off[c0 + i] = (int64_t)(excl >> 24);
-        if (nonempty && v) nonempty[excl & 0xffffffu] = (int)(c0 + i);
+        if (nonempty && v && KF_IN_BOUNDS(excl & 0xffffffu, nblocks, KF_SITE_MC_BLOCK))
+          nonempty[excl & 0xffffffu] = (int)(c0 + i);
       }
       excl += ((uint64_t)v << 24) | (uint64_t)(v != 0);
     }
@@ -353,6 +355,7 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit_listed(McGrid g, const int
   const int n = *n_nonempty;
   for (int e = blockIdx.x; e < n; e += gridDim.x) {
     const int64_t b = nonempty[e];
+    if (!KF_IN_BOUNDS(b, (g.count + kCellsPerBlock - 1) / kCellsPerBlock, KF_SITE_MC_BLOCK)) continue;
     const int64_t base = b * kCellsPerBlock + threadIdx.x;
     bool has[kRounds];
     float d[kRounds];
@@ -547,3 +550,5 @@ extern "C" int kf_marching_cubes_noalloc(const float *phi, const int dims[3], co
     return kf_fail(KF_ERR_CAPACITY, "vertex buffer holds fewer triangles than the mesh has");
   return KF_OK;
 }
+
+KF_BOUNDS_TU_API(mc)
