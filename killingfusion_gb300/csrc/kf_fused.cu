@@ -323,80 +323,6 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistBlocksPerSM)
   }
 }
 
-// The same solver with each band voxel taken by a group of four lanes
-// (gradient_quad: the same bits, about a third of the dependent instructions
-// per lane), for bands that leave the GPU latency-bound.  64-thread CTAs of 16
-// groups, kQuadBlocksPerSM per SM; a CTA's slice of the band list, its
-// compaction and its barrier as in k_band_persistent.  Lane 0 of a group
-// does the voxel's bookkeeping; a voxel on the grid's outer shell takes the
-// generic path on lane 0 alone.
-constexpr int kQuadGroups = kPersistThreads / 4;
-constexpr int kQuadBlocksPerSM = 8;
-
-__device__ __forceinline__ bool persistent_quad_iteration(const FusedArgs &a, int it, bool last,
-                                                          const int *__restrict__ in, int *__restrict__ out,
-                                                          unsigned &n, unsigned capacity, GridSync *sync,
-                                                          unsigned long long limit_ns) {
-  if (iteration_gated(a.st, it, a.dp)) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.st[it].skipped = 1;
-    return false;
-  }
-  const DevParams &dp = a.dp;
-  const int q = threadIdx.x & 3, grp = threadIdx.x >> 2;
-  const unsigned rounds = (n + kQuadGroups - 1) / kQuadGroups;
-  float maxd = 0.f;
-  double energy = 0.0;
-  unsigned active = 0, carried = 0;
-  bool diverged = false;
-  for (unsigned r = 0; r < rounds; ++r) {
-    // the round's voxels alternate between the CTA's two warps
-    const unsigned k = r * kQuadGroups + (grp & 7) * 2 + (grp >> 3);
-    const int i = k < n ? __ldcg(in + k) : -1;
-    const bool ok = i >= 0 && KF_IN_BOUNDS(i, dp.count, KF_SITE_BAND_LIST);
-    int x = 0, y = 0, z = 0;
-    if (ok) voxel_xyz(dp, i, x, y, z);
-    const bool interior =
-        ok && x >= 1 && y >= 1 && z >= 1 && x <= dp.nx - 2 && y <= dp.ny - 2 && z <= dp.nz - 2;
-    const unsigned qmask = __ballot_sync(0xffffffffu, interior);
-    float d[3] = {0.f, 0.f, 0.f}, s = 0.f, en = 0.f, c0[3] = {0.f, 0.f, 0.f};
-    if (interior) {
-      gradient_quad<kPsiL1>(a, x, y, z, i, qmask, q, d, s, en, c0);
-    } else if (ok && q == 0) {
-      gradient_generic<kPsiL1>(a, x, y, z, d, s, en);
-      c0[0] = load_psi<kPsiL1>(a.ix + i);
-      c0[1] = load_psi<kPsiL1>(a.iy + i);
-      c0[2] = load_psi<kPsiL1>(a.iz + i);
-    }
-    int next = -1;
-    if (ok && q == 0) next = finish_band_voxel(a, i, i, x, y, z, d, s, en, c0, maxd, energy, active, diverged);
-    carried += block_compact(next, out, carried, capacity);
-  }
-  n = carried;
-  reduce_iter_stats<kPersistThreads>(a.st + it, active, maxd, energy, diverged);
-  if (last) return false;
-  if (!grid_sync(sync, gridDim.x, limit_ns, it)) {
-    if (threadIdx.x == 0) a.st[0].timeout = 1;
-    return false;
-  }
-  return true;
-}
-
-__global__ void __launch_bounds__(kPersistThreads, kQuadBlocksPerSM)
-    k_band_persistent_quad(FusedArgs even, FusedArgs odd, int *lst0, int *lst1, int iterations, GridSync *sync,
-                           unsigned long long limit_ns) {
-  const unsigned nq = __ldcg(&even.st[0].list);
-  const unsigned per = (nq + gridDim.x - 1) / gridDim.x;
-  const unsigned k0 = min(blockIdx.x * per, nq);
-  unsigned n = min(k0 + per, nq) - k0;
-  for (int it = 0; it < iterations; it += 2) {
-    if (!persistent_quad_iteration(even, it, it + 1 == iterations, lst0 + k0, lst1 + k0, n, per, sync, limit_ns))
-      return;
-    if (it + 1 < iterations && !persistent_quad_iteration(odd, it + 1, it + 2 == iterations, lst1 + k0, lst0 + k0,
-                                                          n, per, sync, limit_ns))
-      return;
-  }
-}
-
 // In-place update after the last iteration: psi(list[k]) = entry k of the
 // band pass's output planes (the dense passes write back the others).
 __global__ void __launch_bounds__(kThreads) k_fused_scatter(FusedArgs a, const int *__restrict__ list,
@@ -665,18 +591,18 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
   }
 }
 
-// Resident blocks per SM of k_band_persistent_quad on the current device (at
-// most kQuadBlocksPerSM): the cooperative launch must fit on the GPU at once.
+// Resident blocks per SM of k_band_persistent on the current device (at most
+// kPersistBlocksPerSM): the cooperative launch must fit on the GPU at once.
 static int persistent_blocks_per_sm() {
   static int cached[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
   if (!cached[dev]) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_band_persistent_quad, kPersistThreads, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_band_persistent, kPersistThreads, 0) !=
         cudaSuccess)
       return 0;
-    cached[dev] = std::min(n, kQuadBlocksPerSM);
+    cached[dev] = std::min(n, kPersistBlocksPerSM);
   }
   return cached[dev];
 }
@@ -713,7 +639,7 @@ static int launch_band_persistent(kf_grid live, kf_grid can, kf_field psi, const
   unsigned long long limit = kf_wait_limit_ns();
   int iters = iterations;
   void *args[] = {&even, &odd, &lst0, &lst1, &iters, &gs, &limit};
-  KF_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)k_band_persistent_quad,
+  KF_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)k_band_persistent,
                                             dim3((unsigned)(kf_num_sms() * bps)), dim3(kPersistThreads), args, 0,
                                             s));
   return KF_OK;

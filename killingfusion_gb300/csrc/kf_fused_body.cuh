@@ -349,208 +349,6 @@ __device__ __forceinline__ void gradient_lane(const FusedArgs &a, int x, int y, 
   e_out = e;
 }
 
-// gradient_lane's result for one interior voxel, computed by a group of four
-// lanes (lanes 4g..4g+3 of the warp, q = lane & 3; `mask`: the lanes of every
-// group in the warp that calls it, whole groups).  The float operations are
-// gradient_lane's, value for value, so the result is the same bits:
-// - lane q < 3 loads psi component q's 20 neighbours and forms its Killing
-//   differences, Jacobian row and cell moments; lane 3 loads phi_can;
-// - shuffles give every lane the divergence sums, the Killing vector, the
-//   21 moments, psi(i) and the Jacobian;
-// - lane q takes the cell-centre samples j = q, q + 4, ... (the sample
-//   offsets become per-lane data: a zero offset adds an exact zero where
-//   gradient_lane skipped the term at compile time); lane 1 also takes the
-//   warped value at i + psi(i);
-// - the samples are gathered and every lane evaluates the same tail, so all
-//   four return d, s, e and psi(i).
-// For a small band (latency-bound), the voxel's ~1.5 k dependent
-// instructions become about a third as many per lane.
-template <int kLoad>
-__device__ __forceinline__ void gradient_quad(const FusedArgs &a, int x, int y, int z, int64_t idx, unsigned mask,
-                                              int q, float d[3], float &s_out, float &e_out, float c0[3]) {
-  const DevParams &dp = a.dp;
-  const int64_t sy = dp.nx, sz = (int64_t)dp.nx * dp.ny;
-  const float h = a.h;
-  const float two_h = fm(2.f, h), hh = fm(h, h);
-  // per component (lane q = component q)
-  float dv[3] = {0.f, 0.f, 0.f};  // contributions to div[0], div[1], div[2]
-  float kgq = 0.f, Jq[3] = {0.f, 0.f, 0.f}, mq[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, v000 = 0.f, cv = 0.f;
-  if (q < 3) {
-    const float *p = (q == 0 ? a.ix : (q == 1 ? a.iy : a.iz)) + idx;
-    float v[20];
-#pragma unroll
-    for (int n = 0; n < 20; ++n) v[n] = load_psi<kLoad>(p + nb20_off(n, 0) + nb20_off(n, 1) * sy + nb20_off(n, 2) * sz);
-    v000 = v[N000];
-    // Killing second differences (DisplacementField.cpp:326-331)
-    const float xx = fm(two_h, fa(fsb(v[NXP], v000), fsb(v[NXM], v000)));
-    const float yy = fm(two_h, fa(fsb(v[NYP], v000), fsb(v[NYM], v000)));
-    const float zz = fm(two_h, fa(fsb(v[NZP], v000), fsb(v[NZM], v000)));
-    const float xy = fm(hh, fsb(fsb(v[NXPYP], v[NXPYM]), fsb(v[NXMYP], v[NXMYM])));
-    const float xz = fm(hh, fsb(fsb(v[NXPZP], v[NXPZM]), fsb(v[NXMZP], v[NXMZM])));
-    const float yz = fm(hh, fsb(fsb(v[NYPZP], v[NYPZM]), fsb(v[NYMZP], v[NYMZM])));
-    kgq = fm(-2.f, fa(fa(xx, yy), zz));
-    dv[0] = q == 0 ? xx : (q == 1 ? xy : xz);
-    dv[1] = q == 0 ? xy : (q == 1 ? yy : yz);
-    dv[2] = q == 0 ? xz : (q == 1 ? yz : zz);
-    Jq[0] = fm(0.5f, fsb(v[NXP], v[NXM]));
-    Jq[1] = fm(0.5f, fsb(v[NYP], v[NYM]));
-    Jq[2] = fm(0.5f, fsb(v[NZP], v[NZM]));
-    const float k000 = v000, k100 = v[NXP], k010 = v[NYP], k110 = v[NXPYP];
-    const float k001 = v[NZP], k101 = v[NXPZP], k011 = v[NYPZP], k111 = v[N111];
-    const float sx0 = fa(fa(k000, k010), fa(k001, k011)), sx1 = fa(fa(k100, k110), fa(k101, k111));
-    const float sy0 = fa(fa(k000, k100), fa(k001, k101)), sy1 = fa(fa(k010, k110), fa(k011, k111));
-    const float sz0 = fa(fa(k000, k100), fa(k010, k110)), sz1 = fa(fa(k001, k101), fa(k011, k111));
-    mq[0] = fm(0.125f, fa(sx0, sx1));
-    mq[1] = fm(0.25f, fsb(sx1, sx0));
-    mq[2] = fm(0.25f, fsb(sy1, sy0));
-    mq[3] = fm(0.25f, fsb(sz1, sz0));
-    mq[4] = fm(0.5f, fsb(fa(fsb(fsb(k110, k010), fsb(k100, k000)), fsb(k111, k011)), fsb(k101, k001)));
-    mq[5] = fm(0.5f, fsb(fa(fsb(fsb(k101, k001), fsb(k100, k000)), fsb(k111, k011)), fsb(k110, k010)));
-    mq[6] = fm(0.5f, fsb(fa(fsb(fsb(k011, k001), fsb(k010, k000)), fsb(k111, k101)), fsb(k110, k100)));
-  } else {
-    cv = __ldg(a.can + idx);
-  }
-  // the divergence sums in gradient_lane's order (from 0, then components 0, 1, 2)
-  float div[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-    div[k] = fa(fa(fa(0.f, __shfl_sync(mask, dv[k], 0, 4)), __shfl_sync(mask, dv[k], 1, 4)),
-                __shfl_sync(mask, dv[k], 2, 4));
-  const float m2g = fm(-2.f, a.gamma_k);
-  if (q < 3) kgq = ff(m2g, div[q], kgq);
-  float kg[3], m[3][7], J[3][3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    kg[c] = __shfl_sync(mask, kgq, c, 4);
-    c0[c] = __shfl_sync(mask, v000, c, 4);
-#pragma unroll
-    for (int k = 0; k < 7; ++k) m[c][k] = __shfl_sync(mask, mq[k], c, 4);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) J[c][k] = __shfl_sync(mask, Jq[k], c, 4);
-  }
-  cv = __shfl_sync(mask, cv, 3, 4);
-  {
-    const float nrm = sqrtf(ff(kg[2], kg[2], ff(kg[1], kg[1], fm(kg[0], kg[0]))));
-    const float sc = nrm > a.clamp ? a.clamp / nrm : 1.f;
-    const float den = fm(fm(4.f, h), h);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) kg[c] = fm(kg[c], sc) / den;
-  }
-  const float base[3] = {fa((float)x, 0.5f), fa((float)y, 0.5f), fa((float)z, 0.5f)};
-  // shared corner cell (as gradient_lane)
-  int cb[3];
-  bool shared = true;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const float m1 = fabsf(m[c][1]) + fabsf(m[c][2]) + fabsf(m[c][3]);
-    const float m2 = fabsf(m[c][4]) + fabsf(m[c][5]) + fabsf(m[c][6]);
-    const float ctr = fa(base[c], m[c][0]);
-    const float r = h * (2.f + 2.f * m1 + h * m2) + 1e-3f + fabsf(ctr) * 0x1p-20f;
-    const float lo = ctr - r, hi = ctr + r;
-    const int b = (int)lo;
-    const int n = c == 0 ? dp.nx : (c == 1 ? dp.ny : dp.nz);
-    shared = shared && lo >= 0.f && (int)hi == b && (unsigned)b < (unsigned)(n - 1);
-    cb[c] = b;
-  }
-  float cell[8];
-  if (shared) {
-    const float *p = a.live + ((int64_t)cb[2] * dp.ny + cb[1]) * dp.nx + cb[0];
-    cell[0] = __ldg(p);
-    cell[1] = __ldg(p + 1);
-    cell[2] = __ldg(p + sy);
-    cell[3] = __ldg(p + sy + 1);
-    cell[4] = __ldg(p + sz);
-    cell[5] = __ldg(p + sz + 1);
-    cell[6] = __ldg(p + sz + sy);
-    cell[7] = __ldg(p + sz + sy + 1);
-  }
-  // this lane's samples j = q + 4i, offsets as data
-  float fl[7];
-#pragma unroll
-  for (int i = 0; i < 7; ++i) {
-    const int j = q + 4 * i;
-    fl[i] = 0.f;
-    if (j < 25) {
-      // off25_at(4i + q, c): i is unrolled, so each candidate is a constant
-      int o[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const int a0 = off25_at(min(4 * i, 24), c), a1 = off25_at(min(4 * i + 1, 24), c);
-        const int a2 = off25_at(min(4 * i + 2, 24), c), a3 = off25_at(min(4 * i + 3, 24), c);
-        o[c] = q == 0 ? a0 : (q == 1 ? a1 : (q == 2 ? a2 : a3));
-      }
-      float t[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float lin = 0.f, quad = 0.f;
-        lin = ff((float)o[0], m[c][1], lin);
-        lin = ff((float)o[1], m[c][2], lin);
-        lin = ff((float)o[2], m[c][3], lin);
-        quad = ff((float)(o[0] * o[1]), m[c][4], quad);
-        quad = ff((float)(o[0] * o[2]), m[c][5], quad);
-        quad = ff((float)(o[1] * o[2]), m[c][6], quad);
-        t[c] = fa(fa(base[c], fm(h, (float)o[c])), ff(h, ff(h, quad, lin), m[c][0]));
-      }
-      fl[i] = shared ? lerp3f(cell, fsb(t[0], (float)cb[0]), fsb(t[1], (float)cb[1]), fsb(t[2], (float)cb[2]))
-                     : phi_tri(a, t[0], t[1], t[2]);
-    }
-  }
-  float sw = 0.f;
-  if (q == 1)
-    sw = phi_tri(a, fsb(fa(fa((float)x, c0[0]), 0.5f), 0.5f), fsb(fa(fa((float)y, c0[1]), 0.5f), 0.5f),
-                 fsb(fa(fa((float)z, c0[2]), 0.5f), 0.5f));
-  const float s = __shfl_sync(mask, sw, 1, 4);
-  float f[25];
-#pragma unroll
-  for (int j = 0; j < 25; ++j) f[j] = __shfl_sync(mask, fl[j >> 2], j & 3, 4);
-  const float inv2h = 1.f / fm(2.f, h), inv4hh = 1.f / fm(fm(4.f, h), h);
-  const float g[3] = {fm(fsb(f[1], f[2]), inv2h), fm(fsb(f[3], f[4]), inv2h), fm(fsb(f[5], f[6]), inv2h)};
-  const float f02 = fm(2.f, f[0]);
-  const float hxx = fm(fa(fsb(f[7], f02), f[8]), inv4hh);
-  const float hyy = fm(fa(fsb(f[9], f02), f[10]), inv4hh);
-  const float hzz = fm(fa(fsb(f[11], f02), f[12]), inv4hh);
-  const float hxz = fm(fsb(fsb(fa(f[13], f[19]), f[20]), f[14]), inv4hh);
-  const float hyz = fm(fsb(fsb(fa(f[15], f[21]), f[22]), f[16]), inv4hh);
-  const float hxy = fm(fsb(fsb(fa(f[17], f[23]), f[24]), f[18]), inv4hh);
-  float grad[3] = {0.f, 0.f, 0.f};
-  float e = 0.f;
-  if (dp.use_data) {
-    const float r = fsb(s, cv) / a.voxel;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) grad[k] = ff(r, g[k], grad[k]);
-    e = ff(fm(0.5f, r), r, e);
-  }
-  if (dp.use_killing) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) grad[k] = ff(kg[k], a.omega_k, grad[k]);
-    float fr = 0.f, tr = 0.f;
-#pragma unroll
-    for (int p = 0; p < 3; ++p)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        fr = ff(J[p][k], J[p][k], fr);
-        tr = ff(J[p][k], J[k][p], tr);
-      }
-    e = ff(a.omega_k, ff(a.gamma_k, tr, fr), e);
-  }
-  if (dp.use_levelset) {
-    const float gn = sqrtf(ff(g[2], g[2], ff(g[1], g[1], fm(g[0], g[0]))));
-    const float hg0 = ff(hxz, g[2], ff(hxy, g[1], fm(hxx, g[0])));
-    const float hg1 = ff(hyz, g[2], ff(hyy, g[1], fm(hxy, g[0])));
-    const float hg2 = ff(hzz, g[2], ff(hyz, g[1], fm(hxz, g[0])));
-    const float sc = fm(fsb(gn, 1.f) / fa(gn, a.eps), a.omega_s);
-    grad[0] = ff(hg0, sc, grad[0]);
-    grad[1] = ff(hg1, sc, grad[1]);
-    grad[2] = ff(hg2, sc, grad[2]);
-    const float r = fsb(gn / a.voxel, 1.f);
-    e = ff(fm(fm(a.omega_s, 0.5f), r), r, e);
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) d[k] = fm(-a.alpha, grad[k]);
-  s_out = s;
-  e_out = e;
-}
-
 // A psi value read as load_psi<kLoad> reads it: the element type of psi
 // views in kernels that write psi themselves.  Same layout as float.
 template <int kLoad>
@@ -828,37 +626,6 @@ __device__ __noinline__ bool trust_step_f(const FusedArgs &a, int x, int y, int 
 // if it left the band) and accumulates the statistics.
 // kTrust: the trust-region step (dp.trust set), a separate instantiation so
 // that the plain band pass carries no call to it.
-// The second half of a band voxel's update, once its step d, warped value s,
-// energy en and psi c0 are known: the band re-test, the new psi to entry
-// `slot` of the output planes, the statistics.  Returns the voxel for the
-// next iteration's list, -1 if it left the band.
-template <bool kTrust = false>
-__device__ __forceinline__ int finish_band_voxel(const FusedArgs &a, int i, int slot, int x, int y, int z,
-                                                 float d[3], float s, float en, const float c0[3], float &maxd,
-                                                 double &energy, unsigned &active, bool &diverged) {
-  int next = -1;
-  if (in_band(s, a.band_hi, a.band_lo)) {
-    if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
-    if (kTrust && !trust_step_f(a, x, y, z, i, c0, d)) {
-      // this voxel and the rest of its row keep psi (k_trust_fix)
-      atomicMin(a.rows + (z * a.dp.ny + y), x);
-      d[0] = d[1] = d[2] = 0.f;
-    }
-    a.ox[slot] = c0[0] + d[0];
-    a.oy[slot] = c0[1] + d[1];
-    a.oz[slot] = c0[2] + d[2];
-    maxd = fmaxf(maxd, sqrtf(ff(d[2], d[2], ff(d[1], d[1], fm(d[0], d[0])))));
-    energy += en;
-    ++active;
-    next = i;
-  } else {  // left the band: its psi is final, settle the output buffer
-    a.ox[slot] = c0[0];
-    a.oy[slot] = c0[1];
-    a.oz[slot] = c0[2];
-  }
-  return next;
-}
-
 // kLoad: how psi is read (PsiLoad); the persistent passes, which write psi
 // between iterations, read it with kPsiL1.
 template <bool kTrust = false, int kLoad = kPsiReadOnly>
@@ -879,7 +646,27 @@ __device__ __forceinline__ int update_band_voxel(const FusedArgs &a, int i, int 
     c0[1] = kLoad == kPsiReadOnly ? a.iy[i] : load_psi<kLoad>(a.iy + i);
     c0[2] = kLoad == kPsiReadOnly ? a.iz[i] : load_psi<kLoad>(a.iz + i);
   }
-  return finish_band_voxel<kTrust>(a, i, slot, x, y, z, d, s, en, c0, maxd, energy, active, diverged);
+  int next = -1;
+  if (in_band(s, a.band_hi, a.band_lo)) {
+    if (!isfinite(c0[0]) || !isfinite(c0[1]) || !isfinite(c0[2])) diverged = true;
+    if (kTrust && !trust_step_f(a, x, y, z, i, c0, d)) {
+      // this voxel and the rest of its row keep psi (k_trust_fix)
+      atomicMin(a.rows + (z * dp.ny + y), x);
+      d[0] = d[1] = d[2] = 0.f;
+    }
+    a.ox[slot] = c0[0] + d[0];
+    a.oy[slot] = c0[1] + d[1];
+    a.oz[slot] = c0[2] + d[2];
+    maxd = fmaxf(maxd, sqrtf(ff(d[2], d[2], ff(d[1], d[1], fm(d[0], d[0])))));
+    energy += en;
+    ++active;
+    next = i;
+  } else {  // left the band: its psi is final, settle the output buffer
+    a.ox[slot] = c0[0];
+    a.oy[slot] = c0[1];
+    a.oz[slot] = c0[2];
+  }
+  return next;
 }
 
 FusedArgs make_args(kf_grid live, kf_grid can, const DevParams &dp, IterStats *st) {
