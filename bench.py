@@ -68,6 +68,9 @@ def parse():
                          "paper: the values in the comment at config.cpp:32-41")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-band-frame", action="store_true", help="skip the band-only frame measurement")
+    ap.add_argument("--log", default=None,
+                    help="JSONL log: the configuration, each timed frame's solve time, the per-iteration "
+                         "energy, max |dpsi| and band count of the parity frame's solve, the result line")
     ap.add_argument("--workload", default="ellipsoid", choices=["ellipsoid", "sphere", "batch", "large"],
                     help="ellipsoid: 256^3 sequence (the bench line); sphere: the 64^3 two-frame sphere "
                          "pair, 100 iterations; batch: 64 registration problems of 32-160^3, 150 "
@@ -320,7 +323,8 @@ def run_ours(args, rank, world, local):
         gl.integrate(torch.from_numpy(seq.frame(1)).to(dev), min_depth=0.05, max_depth=max_depth)
         fp = capi.Field(grid.dims, capi.KF_F32)
         stp = capi.psi_solve(gl, gc, fp, P, args.iters, args.solver)
-        parity = {"live": gl.download()[0], "can": gc.download()[0], "psi": fp.download(), "stats": stp}
+        parity = {"live": gl.download()[0], "can": gc.download()[0], "psi": fp.download(), "stats": stp,
+                  "history": capi.solve_history(fp) if args.solver != "plain" else None}
         for h in (gc, gl, fp):
             h.close()
 
@@ -772,7 +776,26 @@ def run_main(args, rank, world, local):
             "frame": "frame 1 registered onto frame 0, float32 psi of the GPU against the FP64 oracle "
                      "on the same float32 SDFs, every voxel",
         }
+    if args.log:
+        write_log(args.log, line, res)
     print(json.dumps(line))
+
+
+def write_log(path, line, res):
+    """JSONL: one record per line (kind = config, frame, iteration, result)."""
+    with open(path, "w") as f:
+        f.write(json.dumps({"kind": "config", "config": line["config"], "solver": line.get("solver"),
+                            "metric": line["metric"]}) + "\n")
+        for k, ms in enumerate(res["solve_ms"]):
+            f.write(json.dumps({"kind": "frame", "frame": k, "solve_ms": ms}) + "\n")
+        par = res.get("parity")
+        if par and par.get("history"):
+            h = par["history"]
+            for k in range(len(h["energy"])):
+                f.write(json.dumps({"kind": "iteration", "frame": "parity", "iteration": k,
+                                    "energy": float(h["energy"][k]), "max_delta": float(h["max_delta"][k]),
+                                    "band_voxels": int(h["active"][k])}) + "\n")
+        f.write(json.dumps({"kind": "result", **line}) + "\n")
 
 
 if __name__ == "__main__":

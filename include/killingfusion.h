@@ -261,6 +261,15 @@ int kf_psi_solve_async(kf_grid live, kf_grid canonical, kf_field psi, const kf_p
                        int iterations, kf_solver solver, void *stream);
 int kf_psi_solve_wait(kf_field psi, kf_solve_stats *stats);
 
+/* Per-iteration statistics of the last solve on psi, once it has been waited
+ * for (no counterpart in the reference, which prints only timings): for
+ * each executed iteration k < max_iterations, the monitored energy (FP64
+ * sum), max |dpsi| and the number of band voxels, into the arrays given
+ * (any may be NULL); *count receives the number of iterations written.
+ * KF_ERR_INVALID for the per-voxel schedule, which keeps none. */
+int kf_psi_solve_history(kf_field psi, int32_t max_iterations, double *energy, double *max_delta,
+                         int64_t *active, int32_t *count);
+
 /* KillingFusion::computeEnergyGradient (KillingFusion.cpp:399-442) at
  * `count` voxels (device int32 xyz triples), in the field's precision;
  * out: device double[count][3].  Also the band test (KillingFusion.cpp:272)

@@ -161,6 +161,7 @@ SIGNATURES = {
     "kf_fusion_process_frame": (C.c_int, [_vp, _vp, _dp, C.c_int, C.c_void_p, _vp]),
     "kf_fusion_state": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
     "kf_set_wait_limit": (C.c_double, [C.c_double]),
+    "kf_psi_solve_history": (C.c_int, [_vp, C.c_int32, _vp, _vp, _vp, C.POINTER(C.c_int32)]),
     "kf_bounds_status": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_int),
                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "kf_bounds_reset": (C.c_int, [C.c_int64]),
@@ -189,6 +190,19 @@ def load() -> C.CDLL:
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def solve_history(field, max_iterations: int = 100000) -> dict:
+    """Per-iteration energy, max |dpsi| and band count of the last solve on
+    field (kf_psi_solve_history)."""
+    e = np.zeros(max_iterations)
+    d = np.zeros(max_iterations)
+    a = np.zeros(max_iterations, np.int64)
+    n = C.c_int32(0)
+    check(load().kf_psi_solve_history(field.h, max_iterations, e.ctypes.data, d.ctypes.data, a.ctypes.data,
+                                      C.byref(n)))
+    k = n.value
+    return {"energy": e[:k], "max_delta": d[:k], "active": a[:k]}
 
 
 def bounds_status() -> dict:

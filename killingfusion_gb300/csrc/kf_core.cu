@@ -871,6 +871,31 @@ extern "C" int kf_psi_solve_async(kf_grid live, kf_grid canonical, kf_field psi,
   return KF_OK;
 }
 
+extern "C" int kf_psi_solve_history(kf_field psi, int32_t max_iterations, double *energy, double *max_delta,
+                                    int64_t *active, int32_t *count) {
+  KF_REQUIRE(psi && count, "NULL argument");
+  KF_REQUIRE(max_iterations >= 0, "max_iterations must be >= 0");
+  *count = 0;
+  KF_REQUIRE(psi->stats_host && psi->last_iterations > 0, "no solve has run on this field");
+  KF_REQUIRE(psi->pending == 0, "the last solve on this field has not been waited for (kf_psi_solve_wait)");
+  KF_REQUIRE(psi->last_solver != KF_SOLVER_PERVOXEL,
+             "the per-voxel schedule keeps no per-iteration statistics");
+  int n = 0;
+  for (int k = 0; k < psi->last_iterations && n < max_iterations; ++k) {
+    const IterStats &h = psi->stats_host[k];
+    if (h.skipped) break;
+    float md;
+    memcpy(&md, &h.max_delta, sizeof(md));
+    if (energy) energy[n] = h.energy;
+    if (max_delta) max_delta[n] = md;
+    if (active) active[n] = h.active;
+    ++n;
+    if (h.diverged) break;
+  }
+  *count = n;
+  return KF_OK;
+}
+
 extern "C" int kf_psi_solve_wait(kf_field psi, kf_solve_stats *stats) {
   KF_REQUIRE(psi, "NULL argument");
   if (stats) memset(stats, 0, sizeof(*stats));
