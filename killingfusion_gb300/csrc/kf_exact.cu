@@ -187,6 +187,20 @@ __device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int3
   return true;
 }
 
+// The float64 distance and running mean of one voxel whose pixel is known
+// (depth[k]), as the reference computes them.  Not inlined: in the z loop of
+// k_integrate the compiler would otherwise evaluate this rare path's float64
+// sums for every voxel.
+template <typename D>
+__device__ __noinline__ void integrate_double(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
+                                              const D *__restrict__ depth, int64_t k, const double *tx,
+                                              const double *ty, const double *tz, const IntegrateArgs &a) {
+  double dd;
+  if (!depth_at(depth, k, a, dd)) return;
+  const double zc = ((__ldg(tx) + __ldg(ty)) + __ldg(tz)) + a.W[11] * 1.0;
+  integrate_update(phi, w, i, dd, zc, a);
+}
+
 // SDF::integrateDepthFrame, one thread per (x, y) column over kIntegrateZ
 // consecutive z (the x and y parts of the projection and of the camera depth
 // are the column's).  The pixel a voxel reads flips only where u or v
@@ -268,10 +282,7 @@ __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, i
           integrate_fresh_ff(phi, w, i, df, zxy, __ldg(tf + nx + ny + z), a))
         continue;
     }
-    double dd;
-    if (!depth_at(depth, k, a, dd)) continue;
-    const double zc = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
-    integrate_update(phi, w, i, dd, zc, a);
+    integrate_double(phi, w, i, depth, k, tx + x, ty + y, tz + z, a);
   }
 }
 
