@@ -167,14 +167,14 @@ __global__ void k_integrate_tables(double *__restrict__ tx, double *__restrict__
 }
 
 // A fresh voxel (w == 0, phi finite) on float depth df, in float-float: the
-// distance df - zc with zc = ((tx + ty) + W[11]) + tz from the pair tables
-// (zxy: the column's x and y part), the unknown-clip test and the float
-// rounding, all decided when they lie farther than a.tol from the
-// reference's float64 boundaries.  Returns false (nothing written) when one
-// of them is too close to call.
+// distance df - zc with zc = ((tx + ty) + tz) + W[11] from the pair tables,
+// the unknown-clip test and the float rounding, all decided when they lie
+// farther than a.tol from the reference's float64 boundaries.  Returns false
+// (nothing written) when one of them is too close to call.
 __device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
-                                                   float df, FF zxy, float2 tz, const IntegrateArgs &a) {
-  const FF zc = ff_add(zxy, FF{tz.x, tz.y});
+                                                   float df, float2 tx, float2 ty, float2 tz,
+                                                   const IntegrateArgs &a) {
+  const FF zc = ff_add(ff_add(ff_add(FF{tx.x, tx.y}, FF{ty.x, ty.y}), FF{tz.x, tz.y}), FF{a.w11h, a.w11l});
   const FF dist = ff_add(FF{df, 0.f}, ff_neg(zc));
   const FF m = ff_add(dist, FF{a.cliph, a.clipl});  // dist + unknown_clip < 0: not integrated
   if (!(fabsf(m.hi) > a.tol)) return false;
@@ -187,33 +187,14 @@ __device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int3
   return true;
 }
 
-// The float64 distance and running mean of one voxel whose pixel is known
-// (depth[k]), as the reference computes them.  Not inlined: in the z loop of
-// k_integrate the compiler would otherwise evaluate this rare path's float64
-// sums for every voxel.
-template <typename D>
-__device__ __noinline__ void integrate_double(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
-                                              const D *__restrict__ depth, int64_t k, const double *tx,
-                                              const double *ty, const double *tz, const IntegrateArgs &a) {
-  double dd;
-  if (!depth_at(depth, k, a, dd)) return;
-  const double zc = ((__ldg(tx) + __ldg(ty)) + __ldg(tz)) + a.W[11] * 1.0;
-  integrate_update(phi, w, i, dd, zc, a);
-}
-
-// SDF::integrateDepthFrame, one thread per (x, y) column over kIntegrateZ
-// consecutive z (the x and y parts of the projection and of the camera depth
-// are the column's).  The pixel a voxel reads flips only where u or v
-// crosses an integer, so the projection runs in float and is left to the
-// float64 path when either coordinate lies within 1/128 pixel of an integer
-// (the float error is below 1e-3 pixel) or is not finite.  Those voxels are
-// listed (warp-aggregated) for k_integrate_exact, so the slow float64
-// projection runs on full warps instead of stalling the warps they fall in;
-// past the list's capacity a voxel takes the path in place.  Float depth into
-// a fresh voxel is integrated in float-float (integrate_fresh_ff); the rest,
-// and what that cannot decide, in float64 as in the reference.
-constexpr int kIntegrateZ = 8;
-
+// SDF::integrateDepthFrame for one voxel per thread.  The pixel a voxel reads
+// flips only where u or v crosses an integer, so the projection runs in float
+// and is left to the float64 path when either coordinate lies within 1/128
+// pixel of an integer (the float error is below 1e-3 pixel) or is not finite.
+// Those voxels are listed (warp-aggregated) for k_integrate_exact, so the
+// slow float64 projection runs on full warps instead of stalling the warps
+// they fall in; past the list's capacity a voxel takes the path in place.
+// The distance and the running mean are float64 as in the reference.
 template <typename D>
 __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, int32_t *__restrict__ w,
                                                       int nx, int ny, int nz,
@@ -226,64 +207,56 @@ __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, i
                                                       IntegrateArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
   if (x >= nx || y >= ny) return;
+  const int64_t i = ((int64_t)z * ny + y) * nx + x;
   // voxel centre in float (its error, < 1e-6 m, is covered by the margin)
   const float Xf = a.vf * ((float)x + 0.5f) + a.min0f;
   const float Yf = a.vf * ((float)y + 0.5f) + a.min1f;
-  const float cxy0 = (a.Wf[0] * Xf + a.Wf[1] * Yf) + a.Wf[3];
-  const float cxy1 = (a.Wf[4] * Xf + a.Wf[5] * Yf) + a.Wf[7];
-  const float cxy2 = (a.Wf[8] * Xf + a.Wf[9] * Yf) + a.Wf[11];
-  FF zxy = {0.f, 0.f};
+  const float Zf = a.vf * ((float)z + 0.5f) + a.min2f;
+  const float c0 = a.Wf[0] * Xf + a.Wf[1] * Yf + a.Wf[2] * Zf + a.Wf[3];
+  const float c1 = a.Wf[4] * Xf + a.Wf[5] * Yf + a.Wf[6] * Zf + a.Wf[7];
+  const float c2 = a.Wf[8] * Xf + a.Wf[9] * Yf + a.Wf[10] * Zf + a.Wf[11];
+  const float pa = c0 / c2, pb = c1 / c2;
+  const float uf = a.Kf[0] * pa + a.Kf[1] * pb + a.Kf[2];
+  const float vf = a.Kf[3] * pa + a.Kf[4] * pb + a.Kf[5];
+  constexpr float kMargin = 1.0f / 128.0f;
+  const bool sure = isfinite(uf) && isfinite(vf) && fabsf(uf - rintf(uf)) > kMargin &&
+                    fabsf(vf - rintf(vf)) > kMargin && fabsf(uf) < 1e7f && fabsf(vf) < 1e7f;
+  const unsigned act = __activemask();
+  const unsigned need = __ballot_sync(act, !sure);
+  if (!sure) {
+    const int lane = threadIdx.x & 31;  // blockDim.x == 32
+    const int leader = __ffs(need) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(list_n, (unsigned)__popc(need));
+    base = __shfl_sync(need, base, leader);
+    const unsigned slot = base + (unsigned)__popc(need & ((1u << lane) - 1u));
+    if (slot < list_cap)
+      list[slot] = (int)i;
+    else
+      integrate_exact_voxel(phi, w, x, y, z, i, depth, a);
+    return;
+  }
+  int col = (int)floorf(uf + 1.0f);  // == roundf(u + 0.5) away from the flips
+  int row = (int)floorf(vf + 1.0f);
+  if (uf < -1.0f) col = -1;  // roundf(u + 0.5) < 0: outside
+  if (vf < -1.0f) row = -1;
+  if (col < 0 || col >= a.width) return;
+  if (row < 0 || row >= a.height) return;
+  const int64_t k = (int64_t)row * a.width + col;
   if constexpr (sizeof(D) == 4) {
-    const float2 px = __ldg(tf + x), py = __ldg(tf + nx + y);
-    zxy = ff_add(ff_add(FF{px.x, px.y}, FF{py.x, py.y}), FF{a.w11h, a.w11l});
+    // float depth into a fresh voxel: float-float, float64 only when too close to call
+    const float df = depth[k];
+    if (df < a.min_depth_up || df > a.max_depth_down) return;  // (a NaN passes, as in the reference)
+    if (w[i] == 0 && isfinite(phi[i]) && isfinite(df) &&
+        integrate_fresh_ff(phi, w, i, df, __ldg(tf + x), __ldg(tf + nx + y), __ldg(tf + nx + ny + z), a))
+      return;
   }
-  const int z1 = min((int)blockIdx.z * kIntegrateZ + kIntegrateZ, nz);
-  for (int z = blockIdx.z * kIntegrateZ; z < z1; ++z) {
-    const int64_t i = ((int64_t)z * ny + y) * nx + x;
-    const float Zf = a.vf * ((float)z + 0.5f) + a.min2f;
-    const float c0 = cxy0 + a.Wf[2] * Zf;
-    const float c1 = cxy1 + a.Wf[6] * Zf;
-    const float c2 = cxy2 + a.Wf[10] * Zf;
-    const float rc = 1.0f / c2;
-    const float pa = c0 * rc, pb = c1 * rc;
-    const float uf = a.Kf[0] * pa + a.Kf[1] * pb + a.Kf[2];
-    const float vf = a.Kf[3] * pa + a.Kf[4] * pb + a.Kf[5];
-    constexpr float kMargin = 1.0f / 128.0f;
-    const bool sure = isfinite(uf) && isfinite(vf) && fabsf(uf - rintf(uf)) > kMargin &&
-                      fabsf(vf - rintf(vf)) > kMargin && fabsf(uf) < 1e7f && fabsf(vf) < 1e7f;
-    const unsigned act = __activemask();
-    const unsigned need = __ballot_sync(act, !sure);
-    if (!sure) {
-      const int lane = threadIdx.x & 31;  // blockDim.x == 32
-      const int leader = __ffs(need) - 1;
-      unsigned base = 0;
-      if (lane == leader) base = atomicAdd(list_n, (unsigned)__popc(need));
-      base = __shfl_sync(need, base, leader);
-      const unsigned slot = base + (unsigned)__popc(need & ((1u << lane) - 1u));
-      if (slot < list_cap)
-        list[slot] = (int)i;
-      else
-        integrate_exact_voxel(phi, w, x, y, z, i, depth, a);
-      continue;
-    }
-    int col = (int)floorf(uf + 1.0f);  // == roundf(u + 0.5) away from the flips
-    int row = (int)floorf(vf + 1.0f);
-    if (uf < -1.0f) col = -1;  // roundf(u + 0.5) < 0: outside
-    if (vf < -1.0f) row = -1;
-    if (col < 0 || col >= a.width) continue;
-    if (row < 0 || row >= a.height) continue;
-    const int64_t k = (int64_t)row * a.width + col;
-    if constexpr (sizeof(D) == 4) {
-      // float depth into a fresh voxel: float-float, float64 only when too close to call
-      const float df = depth[k];
-      if (df < a.min_depth_up || df > a.max_depth_down) continue;  // (a NaN passes, as in the reference)
-      if (w[i] == 0 && isfinite(phi[i]) && isfinite(df) &&
-          integrate_fresh_ff(phi, w, i, df, zxy, __ldg(tf + nx + ny + z), a))
-        continue;
-    }
-    integrate_double(phi, w, i, depth, k, tx + x, ty + y, tz + z, a);
-  }
+  double dd;
+  if (!depth_at(depth, k, a, dd)) return;
+  const double zc = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
+  integrate_update(phi, w, i, dd, zc, a);
 }
 
 // The listed voxels of k_integrate, each on the float64 path.
@@ -371,7 +344,7 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   KF_CHECK_CUDA(cudaMemsetAsync(list_n, 0, sizeof(unsigned), s));
   k_integrate_tables<<<blocks_for(nx + ny + nz), kBlock, 0, s>>>(tx, ty, tz, tf, nx, ny, nz, a);
   dim3 block(32, kBlock / 32);
-  dim3 grid((nx + 31) / 32, (ny + block.y - 1) / block.y, (nz + kIntegrateZ - 1) / kIntegrateZ);
+  dim3 grid((nx + 31) / 32, (ny + block.y - 1) / block.y, nz);
   k_integrate<D><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tf, list, list_n, cap,
                                         a);
   k_integrate_exact<D><<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list,
