@@ -56,14 +56,15 @@ __device__ __forceinline__ void voxel_xyz(int64_t i, int nx, int ny, int &x, int
 struct IntegrateArgs {
   double W[16];  // world -> camera, row-major
   double K[9];   // intrinsics, row-major
-  float Wf[12], Kf[6];
-  float vf, min0f, min1f, min2f;
+  float Kf[6];                          // K[0..5] rounded to float
+  float gu, gv;                        // projection error gains (launch_integrate)
+  float c2_min;                        // smallest |camera depth| the float path takes
   double voxel, min0, min1, min2, unknown_clip, min_depth, max_depth;
   float min_depth_up, max_depth_down;  // float neighbours of the depth range
   double depth_scale;                  // metres per unit of 16-bit depth
-  float w11h, w11l;                    // W[11] as a float pair
   float cliph, clipl;                  // unknown_clip as a float pair
   float tol;                           // bound on |float-float distance - reference's|
+  float clip_thr;                      // |dist.hi + cliph| above this decides the clip test
   int width, height;
   int64_t count;                       // voxels of the grid
 };
@@ -97,13 +98,12 @@ __device__ __forceinline__ int pixel_of(double u) {
 // The running-mean update of SDF.cpp:185-193 once the pixel and the camera
 // depth zc are known.  With w == 0 and a finite phi the mean
 // (phi*0 + dist)/1 is dist itself, so the float64 multiply and divide are
-// skipped.
+// skipped.  wi and ph are the voxel's weight and value, loaded by the caller.
 __device__ __forceinline__ void integrate_update(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
-                                                 double depth, double zc, const IntegrateArgs &a) {
+                                                 double depth, double zc, const IntegrateArgs &a, int32_t wi,
+                                                 float ph) {
   const double dist = depth - zc;
   if (dist < -a.unknown_clip) return;
-  const int32_t wi = w[i];
-  const float ph = phi[i];
   if (wi == 0 && isfinite(ph)) {
     phi[i] = (float)dist;
   } else {
@@ -140,45 +140,64 @@ __device__ void integrate_exact_voxel(float *__restrict__ phi, int32_t *__restri
   if (col < 0 || col >= a.width || row < 0 || row >= a.height) return;
   double dd;
   if (!depth_at(depth, (int64_t)row * a.width + col, a, dd)) return;
-  integrate_update(phi, w, i, dd, zc, a);
+  integrate_update(phi, w, i, dd, zc, a, w[i], phi[i]);
 }
 
 // Per-axis products of the camera-depth row, W[8]*X(x), W[9]*Y(y) and
 // W[10]*Z(z), with X = voxel*(x+0.5)+min as SDF.cpp:151-157 computes it:
-// zc = ((tx + ty) + tz) + W[11] is then the reference's float64 value.  The
-// same products as float pairs (tf, nx + ny + nz of them) for the
-// float-float path.
+// zc = ((tx + ty) + tz) + W[11] is then the reference's float64 value.
+// The float path's table tp (nx + ny + nz entries, x then y then z) holds
+// per axis value: the camera-x and camera-y row products rounded to float
+// and the camera-depth product as a float pair, with the rows' constant
+// terms W[3], W[7] and W[11] added to the x entries.
 __global__ void k_integrate_tables(double *__restrict__ tx, double *__restrict__ ty, double *__restrict__ tz,
-                                   float2 *__restrict__ tf, int nx, int ny, int nz, IntegrateArgs a) {
+                                   float4 *__restrict__ tp, int nx, int ny, int nz, IntegrateArgs a) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx + ny + nz; k += gridDim.x * blockDim.x) {
-    double t;
+    double c, t, r0, r1;
     if (k < nx) {
-      t = tx[k] = a.W[8] * (a.voxel * ((double)k + 0.5) + a.min0);
+      c = a.voxel * ((double)k + 0.5) + a.min0;
+      t = tx[k] = a.W[8] * c;
+      r0 = a.W[0] * c + a.W[3];
+      r1 = a.W[4] * c + a.W[7];
+      t += a.W[11];
     } else if (k < nx + ny) {
       const int j = k - nx;
-      t = ty[j] = a.W[9] * (a.voxel * ((double)j + 0.5) + a.min1);
+      c = a.voxel * ((double)j + 0.5) + a.min1;
+      t = ty[j] = a.W[9] * c;
+      r0 = a.W[1] * c;
+      r1 = a.W[5] * c;
     } else {
       const int j = k - nx - ny;
-      t = tz[j] = a.W[10] * (a.voxel * ((double)j + 0.5) + a.min2);
+      c = a.voxel * ((double)j + 0.5) + a.min2;
+      t = tz[j] = a.W[10] * c;
+      r0 = a.W[2] * c;
+      r1 = a.W[6] * c;
     }
     const FF p = ff_from_double(t);
-    tf[k] = make_float2(p.hi, p.lo);
+    tp[k] = make_float4(__double2float_rn(r0), __double2float_rn(r1), p.hi, p.lo);
   }
 }
 
 // A fresh voxel (w == 0, phi finite) on float depth df, in float-float: the
-// distance df - zc with zc = ((tx + ty) + tz) + W[11] from the pair tables,
-// the unknown-clip test and the float rounding, all decided when they lie
+// distance df - zc with the camera depth zc from the pair tables, the
+// unknown-clip test and the float rounding, all decided when they lie
 // farther than a.tol from the reference's float64 boundaries.  Returns false
 // (nothing written) when one of them is too close to call.
 __device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
-                                                   float df, float2 tx, float2 ty, float2 tz,
-                                                   const IntegrateArgs &a) {
-  const FF zc = ff_add(ff_add(ff_add(FF{tx.x, tx.y}, FF{ty.x, ty.y}), FF{tz.x, tz.y}), FF{a.w11h, a.w11l});
-  const FF dist = ff_add(FF{df, 0.f}, ff_neg(zc));
-  const FF m = ff_add(dist, FF{a.cliph, a.clipl});  // dist + unknown_clip < 0: not integrated
-  if (!(fabsf(m.hi) > a.tol)) return false;
-  if (m.hi < 0.f) return true;
+                                                   float df, FF zc, const IntegrateArgs &a) {
+  const FF dist = ff_add_short(FF{df, 0.f}, ff_neg(zc));
+  // dist + unknown_clip < 0: not integrated.  One float add decides it: its
+  // error is below 2^-23 (|mf| + |unknown_clip|) plus the distance's, which
+  // clip_thr = 2^-18 |unknown_clip| + 2 tol exceeds; the float-float sum
+  // decides the rest
+  const float mf = __fadd_rn(dist.hi, a.cliph);
+  if (!(fabsf(mf) > a.clip_thr)) {
+    const FF m = ff_add(dist, FF{a.cliph, a.clipl});
+    if (!(fabsf(m.hi) > a.tol)) return false;
+    if (m.hi < 0.f) return true;
+  } else if (mf < 0.f) {
+    return true;
+  }
   bool ambiguous;
   const float r = ff_round_checked(dist, a.tol, ambiguous);
   if (ambiguous) return false;
@@ -189,40 +208,61 @@ __device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int3
 
 // SDF::integrateDepthFrame for one voxel per thread.  The pixel a voxel reads
 // flips only where u or v crosses an integer, so the projection runs in float
-// and is left to the float64 path when either coordinate lies within 1/128
-// pixel of an integer (the float error is below 1e-3 pixel) or is not finite.
-// Those voxels are listed (warp-aggregated) for k_integrate_exact, so the
-// slow float64 projection runs on full warps instead of stalling the warps
-// they fall in; past the list's capacity a voxel takes the path in place.
-// The distance and the running mean are float64 as in the reference.
+// from the per-axis tables and is left to the float64 path when either
+// coordinate lies within its error bound (below) of an integer, or is not
+// finite.  Those voxels are listed (warp-aggregated) for k_integrate_exact,
+// so the slow float64 projection runs on full warps instead of stalling the
+// warps they fall in; past the list's capacity a voxel takes the path in
+// place.
+//
+// The bound on |u - u_ref| (u_ref the reference's float64 value):
+// * the camera-x row c0 is the sum of three table entries, each the float64
+//   product rounded to float, in two float adds: within E0 = 3 * 2^-24 * T0
+//   of the float64 row, T0 the largest sum of the entries' magnitudes over
+//   the grid (likewise E1 for c1); the camera depth c2 is the float-float
+//   sum's high part, within 2^-24 |c2|;
+// * 1/c2 by __fdividef (2 ulp) and the products pa = c0 / c2, pb = c1 / c2
+//   add 5 * 2^-24 of |pa| and |pb|, and u = K0 pa + K1 pb + K2 four more
+//   roundings of at most the sum of its terms' magnitudes S;
+// * so |u - u_ref| <= (|K0| E0 + |K1| E1) / |c2| + 10 * 2^-24 * S, to first
+//   order; the float rounding of u_ref + 0.5 in the reference's pixel_of
+//   moves the flip by half a float spacing, 2^-24 (S + 1.5) at most.
+// The margin 1.5 (|K0| E0 + |K1| E1) |1/c2| + 2^-19 (S + 2) holds all of
+// that with room for the second-order terms (a.gu carries the first part).
+// The distance and the running mean are float64 as in the reference, decided
+// in float-float for a fresh voxel (integrate_fresh_ff).
 template <typename D>
-__global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, int32_t *__restrict__ w,
-                                                      int nx, int ny, int nz,
-                                                      const D *__restrict__ depth,
-                                                      const double *__restrict__ tx,
-                                                      const double *__restrict__ ty,
-                                                      const double *__restrict__ tz,
-                                                      const float2 *__restrict__ tf, int *__restrict__ list,
-                                                      unsigned *__restrict__ list_n, unsigned list_cap,
-                                                      IntegrateArgs a) {
+__global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a full SM
+    k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
+                const D *__restrict__ depth, const double *__restrict__ tx, const double *__restrict__ ty,
+                const double *__restrict__ tz, const float4 *__restrict__ tp, int *__restrict__ list,
+                unsigned *__restrict__ list_n, unsigned list_cap, IntegrateArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   if (x >= nx || y >= ny) return;
   const int64_t i = ((int64_t)z * ny + y) * nx + x;
-  // voxel centre in float (its error, < 1e-6 m, is covered by the margin)
-  const float Xf = a.vf * ((float)x + 0.5f) + a.min0f;
-  const float Yf = a.vf * ((float)y + 0.5f) + a.min1f;
-  const float Zf = a.vf * ((float)z + 0.5f) + a.min2f;
-  const float c0 = a.Wf[0] * Xf + a.Wf[1] * Yf + a.Wf[2] * Zf + a.Wf[3];
-  const float c1 = a.Wf[4] * Xf + a.Wf[5] * Yf + a.Wf[6] * Zf + a.Wf[7];
-  const float c2 = a.Wf[8] * Xf + a.Wf[9] * Yf + a.Wf[10] * Zf + a.Wf[11];
-  const float pa = c0 / c2, pb = c1 / c2;
-  const float uf = a.Kf[0] * pa + a.Kf[1] * pb + a.Kf[2];
-  const float vf = a.Kf[3] * pa + a.Kf[4] * pb + a.Kf[5];
-  constexpr float kMargin = 1.0f / 128.0f;
-  const bool sure = isfinite(uf) && isfinite(vf) && fabsf(uf - rintf(uf)) > kMargin &&
-                    fabsf(vf - rintf(vf)) > kMargin && fabsf(uf) < 1e7f && fabsf(vf) < 1e7f;
+  // the voxel's weight and value, loaded first so that their latency runs
+  // under the projection's arithmetic
+  const int32_t wi = w[i];
+  const float ph = phi[i];
+  const float4 px = __ldg(tp + x), py = __ldg(tp + nx + y), pz = __ldg(tp + nx + ny + z);
+  const float c0 = __fadd_rn(__fadd_rn(px.x, py.x), pz.x);
+  const float c1 = __fadd_rn(__fadd_rn(px.y, py.y), pz.y);
+  const FF zc = ff_add_short(ff_add_short(FF{px.z, px.w}, FF{py.z, py.w}), FF{pz.z, pz.w});
+  const float c2 = zc.hi;
+  const float rc = __fdividef(1.0f, c2);
+  const float pa = __fmul_rn(c0, rc), pb = __fmul_rn(c1, rc);
+  const float ua = __fmul_rn(a.Kf[0], pa), ub = __fmul_rn(a.Kf[1], pb);
+  const float va = __fmul_rn(a.Kf[3], pa), vb = __fmul_rn(a.Kf[4], pb);
+  const float uf = __fadd_rn(__fadd_rn(ua, ub), a.Kf[2]);
+  const float vf = __fadd_rn(__fadd_rn(va, vb), a.Kf[5]);
+  const float arc = fabsf(rc);
+  const float mu = a.gu * arc + 0x1p-19f * (fabsf(ua) + fabsf(ub) + (fabsf(a.Kf[2]) + 2.0f));
+  const float mv = a.gv * arc + 0x1p-19f * (fabsf(va) + fabsf(vb) + (fabsf(a.Kf[5]) + 2.0f));
+  const bool sure = fabsf(c2) > a.c2_min && fabsf(c2) < 0x1p100f && isfinite(uf) && isfinite(vf) &&
+                    fabsf(uf) < 1e7f && fabsf(vf) < 1e7f && fabsf(uf - rintf(uf)) > mu &&
+                    fabsf(vf - rintf(vf)) > mv;
   const unsigned act = __activemask();
   const unsigned need = __ballot_sync(act, !sure);
   if (!sure) {
@@ -249,14 +289,14 @@ __global__ void __launch_bounds__(kBlock) k_integrate(float *__restrict__ phi, i
     // float depth into a fresh voxel: float-float, float64 only when too close to call
     const float df = depth[k];
     if (df < a.min_depth_up || df > a.max_depth_down) return;  // (a NaN passes, as in the reference)
-    if (w[i] == 0 && isfinite(phi[i]) && isfinite(df) &&
-        integrate_fresh_ff(phi, w, i, df, __ldg(tf + x), __ldg(tf + nx + y), __ldg(tf + nx + ny + z), a))
+    if (wi == 0 && isfinite(ph) && isfinite(df) &&
+        integrate_fresh_ff(phi, w, i, df, zc, a))
       return;
   }
   double dd;
   if (!depth_at(depth, k, a, dd)) return;
-  const double zc = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
-  integrate_update(phi, w, i, dd, zc, a);
+  const double zd = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
+  integrate_update(phi, w, i, dd, zd, a, wi, ph);
 }
 
 // The listed voxels of k_integrate, each on the float64 path.
@@ -285,16 +325,11 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   IntegrateArgs a;
   for (int k = 0; k < 16; ++k) a.W[k] = w2c[k];
   for (int k = 0; k < 9; ++k) a.K[k] = K[k];
-  for (int k = 0; k < 12; ++k) a.Wf[k] = (float)w2c[k];
   for (int k = 0; k < 6; ++k) a.Kf[k] = (float)K[k];
   a.voxel = g->voxel;
   a.min0 = g->min3d[0];
   a.min1 = g->min3d[1];
   a.min2 = g->min3d[2];
-  a.vf = (float)g->voxel;
-  a.min0f = (float)g->min3d[0];
-  a.min1f = (float)g->min3d[1];
-  a.min2f = (float)g->min3d[2];
   a.unknown_clip = g->unknown_clip;
   a.min_depth = min_depth;
   a.max_depth = max_depth;
@@ -308,7 +343,6 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   a.height = height;
   a.count = g->count;
   a.depth_scale = depth_scale;
-  ff_split_host(w2c[11], a.w11h, a.w11l);
   ff_split_host(g->unknown_clip, a.cliph, a.clipl);
   {
     // the float-float distance is within a few 2^-46 of the magnitudes it
@@ -319,11 +353,27 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
       mag += fabs(w2c[8 + c]) * std::max(fabs(lo_c), fabs(hi_c));
     }
     a.tol = (float)(ldexp(mag, -38));
+    a.clip_thr = (float)(ldexp(fabs(g->unknown_clip), -18) + 2.0 * (double)a.tol);
+  }
+  {
+    // the float projection's error gains (k_integrate): T_r is the largest
+    // sum of the table entries' magnitudes for row r (each entry is affine
+    // in its coordinate, so its extremes are at the grid's ends), E_r =
+    // 3 * 2^-24 * T_r the bound on the float row's error
+    double T[3] = {fabs(w2c[3]), fabs(w2c[7]), fabs(w2c[11])};
+    for (int c = 0; c < 3; ++c) {
+      const double lo_c = g->voxel * 0.5 + g->min3d[c], hi_c = g->voxel * ((double)g->n[c] - 0.5) + g->min3d[c];
+      for (int r = 0; r < 3; ++r) T[r] += fabs(w2c[4 * r + c]) * std::max(fabs(lo_c), fabs(hi_c));
+    }
+    const double E0 = ldexp(3.0001 * T[0], -24), E1 = ldexp(3.0001 * T[1], -24);
+    a.gu = (float)(1.5 * (fabs(K[0]) * E0 + fabs(K[1]) * E1) * (1.0 + 0x1p-20));
+    a.gv = (float)(1.5 * (fabs(K[3]) * E0 + fabs(K[4]) * E1) * (1.0 + 0x1p-20));
+    a.c2_min = (float)std::max(ldexp(T[2], -36), 0x1p-100);
   }
   // scratch: list counter, the three coordinate tables, the list
   const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
   const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(g->count / 8, 65536), 0x7fffffff);
-  const size_t tab_off = 256, list_off = tab_off + (((size_t)(nx + ny + nz) * 16 + 255) & ~(size_t)255);
+  const size_t tab_off = 256, list_off = tab_off + (((size_t)(nx + ny + nz) * 24 + 255) & ~(size_t)255);
   const size_t bytes = list_off + (size_t)cap * sizeof(int);
   if (g->integ_bytes < bytes) {
     cudaFree(g->integ);
@@ -338,14 +388,14 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   }
   char *base = (char *)g->integ;
   unsigned *list_n = (unsigned *)base;
-  double *tx = (double *)(base + tab_off), *ty = tx + nx, *tz = ty + ny;
-  float2 *tf = (float2 *)(tz + nz);
+  float4 *tp = (float4 *)(base + tab_off);
+  double *tx = (double *)(tp + (nx + ny + nz)), *ty = tx + nx, *tz = ty + ny;
   int *list = (int *)(base + list_off);
   KF_CHECK_CUDA(cudaMemsetAsync(list_n, 0, sizeof(unsigned), s));
-  k_integrate_tables<<<blocks_for(nx + ny + nz), kBlock, 0, s>>>(tx, ty, tz, tf, nx, ny, nz, a);
+  k_integrate_tables<<<blocks_for(nx + ny + nz), kBlock, 0, s>>>(tx, ty, tz, tp, nx, ny, nz, a);
   dim3 block(32, kBlock / 32);
   dim3 grid((nx + 31) / 32, (ny + block.y - 1) / block.y, nz);
-  k_integrate<D><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tf, list, list_n, cap,
+  k_integrate<D><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list, list_n, cap,
                                         a);
   k_integrate_exact<D><<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list,
                                                                      list_n, cap, a);

@@ -65,6 +65,15 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
   return ff_fast_two_sum(v.hi, __fadd_rn(t.lo, v.lo));
 }
 
+// a + b with an error of a few 2^-48 of |a| + |b| too, in fewer operations:
+// the low parts are summed in one rounding (the bound is relative to the
+// operands' magnitudes, not to the sum's, which is what the callers' bounds
+// need)
+__device__ __forceinline__ FF ff_add_short(FF a, FF b) {
+  const FF s = ff_two_sum(a.hi, b.hi);
+  return ff_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
 __device__ __forceinline__ FF ff_neg(FF a) { return {-a.hi, -a.lo}; }
 
 // Float nearest to hi + lo (round to nearest even).  ambiguous is set when a

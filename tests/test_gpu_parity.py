@@ -73,6 +73,39 @@ def test_integrate_pose_and_running_mean(gpu, oracle):
     assert np.abs(phi2[m] - ref[m]).max() <= 2e-7 * np.abs(ref[m]).max() + 1e-9
 
 
+@pytest.mark.parametrize("shift", [(0.0, 0.0, 0.0), (3.0, -2.0, 1.5), (120.0, -75.0, 300.0)])
+def test_integrate_far_from_origin(gpu, oracle, shift):
+    """Grid and camera moved together away from the world origin, the camera
+    turned by 4 degrees.  The camera coordinates are then differences of
+    world coordinates of up to hundreds of metres, whose float rounding is
+    hundreds of times that of the unshifted grid: the float projection's
+    per-voxel error bound grows with them (at the largest shift about a
+    quarter of the voxels lie within it of a pixel edge and take the float64
+    path, past the side list's capacity some in place), and every pixel,
+    weight and distance stays the reference's.  A fixed margin of 1/128
+    pixel would misplace about 1.4 k voxels at the largest shift."""
+    grid, frames = synth.sphere_pair()
+    P = gpu.Params.paper(grid.voxel)
+    t = np.asarray(shift, dtype=np.float64)
+    a = np.deg2rad(4.0)
+    c2w = np.eye(4)
+    c2w[:3, :3] = [[np.cos(a), 0.0, np.sin(a)], [0.0, 1.0, 0.0], [-np.sin(a), 0.0, np.cos(a)]]
+    c2w[:3, 3] = t
+    origin = np.asarray(grid.origin, dtype=np.float64) + t
+    w2c = oracle.invert4(c2w)
+    n = grid.dims[::-1]
+    for f in frames:
+        g = gpu.Grid(grid.dims, grid.voxel, origin, P.unknown_clip, P)
+        g.integrate(f, c2w, synth.K, 0.05, 1.2)
+        phi, w = g.download()
+        g.close()
+        ophi, ow = oracle.integrate(np.full(n, P.max_surface + P.epsilon), np.zeros(n, np.int64), grid.voxel,
+                                    origin, P.unknown_clip, f.astype(np.float64), w2c, synth.K, 0.05, 1.2)
+        np.testing.assert_array_equal(w, ow)
+        np.testing.assert_array_equal(phi, ophi.astype(np.float32))
+        assert (w > 0).sum() > 1000
+
+
 # ---------------------------------------------------------------------------
 # reference gradient at single voxels
 # ---------------------------------------------------------------------------
