@@ -57,7 +57,8 @@ struct IntegrateArgs {
   double W[16];  // world -> camera, row-major
   double K[9];   // intrinsics, row-major
   float Kf[6];                          // K[0..5] rounded to float
-  float gu, gv;                        // projection error gains (launch_integrate)
+  float e0, e1, e2;                    // error bounds of the float camera rows (launch_integrate)
+  float ku0, ku1, kv0, kv1;            // 1.5 |K[0]|, 1.5 |K[1]|, 1.5 |K[3]|, 1.5 |K[4]|
   float c2_min;                        // smallest |camera depth| the float path takes
   double voxel, min0, min1, min2, unknown_clip, min_depth, max_depth;
   float min_depth_up, max_depth_down;  // float neighbours of the depth range
@@ -216,21 +217,22 @@ __device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int3
 // place.
 //
 // The bound on |u - u_ref| (u_ref the reference's float64 value):
-// * the camera-x row c0 is the sum of three table entries, each the float64
-//   product rounded to float, in two float adds: within E0 = 3 * 2^-24 * T0
-//   of the float64 row, T0 the largest sum of the entries' magnitudes over
-//   the grid (likewise E1 for c1); the camera depth c2 is the float-float
-//   sum's high part, within 2^-24 |c2|;
-// * 1/c2 by __fdividef (2 ulp) and the products pa = c0 / c2, pb = c1 / c2
-//   add 5 * 2^-24 of |pa| and |pb|, and u = K0 pa + K1 pb + K2 four more
-//   roundings of at most the sum of its terms' magnitudes S;
-// * so |u - u_ref| <= (|K0| E0 + |K1| E1) / |c2| + 10 * 2^-24 * S, to first
-//   order; the float rounding of u_ref + 0.5 in the reference's pixel_of
-//   moves the flip by half a float spacing, 2^-24 (S + 1.5) at most.
-// The margin 1.5 (|K0| E0 + |K1| E1) |1/c2| + 2^-19 (S + 2) holds all of
-// that with room for the second-order terms (a.gu carries the first part).
+// * each camera row c_r is the sum of three table entries, each the float64
+//   product rounded to float, in two float adds: within E_r = 3 * 2^-24 *
+//   T_r of the float64 row, T_r the largest sum of the entries' magnitudes
+//   over the grid (the camera depth c2 from the high parts of its pairs);
+// * so pa = c0 / c2 is within (E0 + |pa| E2) / |c2| of the float64 quotient
+//   to first order (|c2| > 8 E2 is required), and likewise pb;
+// * 1/c2 by __fdividef (2 ulp) and the products add 5 * 2^-24 of |pa| and
+//   |pb|, and u = K0 pa + K1 pb + K2 four more roundings of at most the sum
+//   of its terms' magnitudes S; the float rounding of u_ref + 0.5 in the
+//   reference's pixel_of moves the flip by half a float spacing, 2^-24 (S +
+//   1.5) at most.
+// The margin 1.5 (|K0| (E0 + |pa| E2) + |K1| (E1 + |pb| E2)) |1/c2| + 2^-19
+// (S + 2) holds all of that with room for the second-order terms.
 // The distance and the running mean are float64 as in the reference, decided
-// in float-float for a fresh voxel (integrate_fresh_ff).
+// in float-float for a fresh voxel (integrate_fresh_ff), with the camera
+// depth summed from the tables' pairs there.
 template <typename D>
 __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a full SM
     k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
@@ -249,8 +251,7 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
   const float4 px = __ldg(tp + x), py = __ldg(tp + nx + y), pz = __ldg(tp + nx + ny + z);
   const float c0 = __fadd_rn(__fadd_rn(px.x, py.x), pz.x);
   const float c1 = __fadd_rn(__fadd_rn(px.y, py.y), pz.y);
-  const FF zc = ff_add_short(ff_add_short(FF{px.z, px.w}, FF{py.z, py.w}), FF{pz.z, pz.w});
-  const float c2 = zc.hi;
+  const float c2 = __fadd_rn(__fadd_rn(px.z, py.z), pz.z);
   const float rc = __fdividef(1.0f, c2);
   const float pa = __fmul_rn(c0, rc), pb = __fmul_rn(c1, rc);
   const float ua = __fmul_rn(a.Kf[0], pa), ub = __fmul_rn(a.Kf[1], pb);
@@ -258,8 +259,9 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
   const float uf = __fadd_rn(__fadd_rn(ua, ub), a.Kf[2]);
   const float vf = __fadd_rn(__fadd_rn(va, vb), a.Kf[5]);
   const float arc = fabsf(rc);
-  const float mu = a.gu * arc + 0x1p-19f * (fabsf(ua) + fabsf(ub) + (fabsf(a.Kf[2]) + 2.0f));
-  const float mv = a.gv * arc + 0x1p-19f * (fabsf(va) + fabsf(vb) + (fabsf(a.Kf[5]) + 2.0f));
+  const float ea = a.e0 + fabsf(pa) * a.e2, eb = a.e1 + fabsf(pb) * a.e2;
+  const float mu = (a.ku0 * ea + a.ku1 * eb) * arc + 0x1p-19f * (fabsf(ua) + fabsf(ub) + (fabsf(a.Kf[2]) + 2.0f));
+  const float mv = (a.kv0 * ea + a.kv1 * eb) * arc + 0x1p-19f * (fabsf(va) + fabsf(vb) + (fabsf(a.Kf[5]) + 2.0f));
   const bool sure = fabsf(c2) > a.c2_min && fabsf(c2) < 0x1p100f && isfinite(uf) && isfinite(vf) &&
                     fabsf(uf) < 1e7f && fabsf(vf) < 1e7f && fabsf(uf - rintf(uf)) > mu &&
                     fabsf(vf - rintf(vf)) > mv;
@@ -290,7 +292,8 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
     const float df = depth[k];
     if (df < a.min_depth_up || df > a.max_depth_down) return;  // (a NaN passes, as in the reference)
     if (wi == 0 && isfinite(ph) && isfinite(df) &&
-        integrate_fresh_ff(phi, w, i, df, zc, a))
+        integrate_fresh_ff(phi, w, i, df,
+                           ff_add_short(ff_add_short(FF{px.z, px.w}, FF{py.z, py.w}), FF{pz.z, pz.w}), a))
       return;
   }
   double dd;
@@ -356,7 +359,7 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
     a.clip_thr = (float)(ldexp(fabs(g->unknown_clip), -18) + 2.0 * (double)a.tol);
   }
   {
-    // the float projection's error gains (k_integrate): T_r is the largest
+    // the float projection's error bounds (k_integrate): T_r is the largest
     // sum of the table entries' magnitudes for row r (each entry is affine
     // in its coordinate, so its extremes are at the grid's ends), E_r =
     // 3 * 2^-24 * T_r the bound on the float row's error
@@ -365,10 +368,16 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
       const double lo_c = g->voxel * 0.5 + g->min3d[c], hi_c = g->voxel * ((double)g->n[c] - 0.5) + g->min3d[c];
       for (int r = 0; r < 3; ++r) T[r] += fabs(w2c[4 * r + c]) * std::max(fabs(lo_c), fabs(hi_c));
     }
-    const double E0 = ldexp(3.0001 * T[0], -24), E1 = ldexp(3.0001 * T[1], -24);
-    a.gu = (float)(1.5 * (fabs(K[0]) * E0 + fabs(K[1]) * E1) * (1.0 + 0x1p-20));
-    a.gv = (float)(1.5 * (fabs(K[3]) * E0 + fabs(K[4]) * E1) * (1.0 + 0x1p-20));
-    a.c2_min = (float)std::max(ldexp(T[2], -36), 0x1p-100);
+    // (rounded up a little, so that their float values stay bounds)
+    const double up = 1.0 + 0x1p-20;
+    a.e0 = (float)(ldexp(3.0001 * T[0], -24) * up);
+    a.e1 = (float)(ldexp(3.0001 * T[1], -24) * up);
+    a.e2 = (float)(ldexp(3.0001 * T[2], -24) * up);
+    a.ku0 = (float)(1.5 * fabs(K[0]) * up);
+    a.ku1 = (float)(1.5 * fabs(K[1]) * up);
+    a.kv0 = (float)(1.5 * fabs(K[3]) * up);
+    a.kv1 = (float)(1.5 * fabs(K[4]) * up);
+    a.c2_min = (float)std::max(8.0 * (double)a.e2, 0x1p-100);
   }
   // scratch: list counter, the three coordinate tables, the list
   const int nx = g->n[0], ny = g->n[1], nz = g->n[2];

@@ -1,13 +1,24 @@
 // Marching cubes in the reference's order (SDF::getMesh, SDF.cpp:396-414;
 // ProcessVolumeCell, SDF.cpp:330-378; Polygonise, MarchingCubes.h:366-422).
 //
-// Three passes keep the triangle soup in the reference's order (cells in
-// z, y, x order; triangles of a cell in table order):
-//   1. k_mc_count: each CTA classifies a contiguous run of kCellsPerBlock
-//      cells and writes its triangle total;
+// The triangle soup keeps the reference's order (cells in z, y, x order;
+// triangles of a cell in table order): every cell writes its triangles at
+// its block's offset plus the triangles of the block's earlier cells.
+//
+// kf_mc_run (grids the library owns), two passes:
+//   1. k_mc_count_list: each CTA classifies a block of kCellsPerBlock cells,
+//      thread t the kCellsPerThread cells from t * kCellsPerThread on (two
+//      16-byte loads), scans the block's triangle counts and lists every
+//      cell with triangles: its index, configuration and offset in the
+//      block.  The last CTA to finish turns the block totals into offsets.
+//   2. k_mc_emit_cells: one thread per listed cell writes its triangles.
+//      When a grid has more such cells than the list holds, it falls back
+//      to re-classifying every block with triangles (emit_block).
+// kf_marching_cubes_noalloc, three passes over caller memory:
+//   1. k_mc_count: each CTA classifies a block and writes its total;
 //   2. k_mc_scan:  one CTA turns the totals into exclusive offsets, a chunk
 //      of kScanChunk totals at a time through registers;
-//   3. k_mc_emit:  each CTA re-classifies its run round by round (thread t
+//   3. k_mc_emit:  each CTA re-classifies its block round by round (thread t
 //      takes cell r*kThreads + t of round r, so the reads coalesce), scans
 //      the round's triangle counts and writes every triangle at its final
 //      position.
@@ -30,6 +41,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kRounds = 8;
 constexpr int kCellsPerBlock = kThreads * kRounds;
+constexpr int kCellsPerThread = kCellsPerBlock / kThreads;
 constexpr int kScanPerThread = 32;
 constexpr int kScanChunk = kThreads * kScanPerThread;
 
@@ -145,12 +157,7 @@ __device__ T block_exclusive_scan(T v, T *total) {
   return prefix;
 }
 
-// Words of the per-block mask of cells with triangles: one per warp and
-// round, bit t for the warp's lane t.
-constexpr int kMaskWords = kRounds * (kThreads / 32);
-
-template <bool kMask>
-__global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block_tris, uint32_t *mask) {
+__global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block_tris) {
   const int64_t base = (int64_t)blockIdx.x * kCellsPerBlock + threadIdx.x;
   float d[kRounds];
 #pragma unroll
@@ -160,62 +167,191 @@ __global__ void __launch_bounds__(kThreads) k_mc_count(McGrid g, uint32_t *block
   for (int r = 0; r < kRounds; ++r) {
     int x, y, z;
     float val[8];
-    const int c = cube_tris(classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val));
-    n += c;
-    if (kMask) {
-      const uint32_t ball = __ballot_sync(0xffffffffu, c != 0);
-      if ((threadIdx.x & 31) == 0)
-        mask[(int64_t)blockIdx.x * kMaskWords + r * (kThreads / 32) + (threadIdx.x >> 5)] = ball;
-    }
+    n += cube_tris(classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val));
   }
   uint32_t total;
   block_exclusive_scan<uint32_t>(n, &total);
   if (threadIdx.x == 0) block_tris[blockIdx.x] = total;
 }
 
-// Exclusive scan of the per-block totals into 64-bit offsets (one CTA), a
-// chunk of kScanChunk totals at a time: the chunk is staged in shared memory
-// with coalesced loads (padded by one word per 32, so that thread t's
-// kScanPerThread consecutive totals sit in distinct banks), each thread
-// sums its totals, the block scans the sums, and each thread writes its
-// offsets.  With `nonempty` it also lists the blocks that have triangles,
-// in order: the triangle count and a has-triangles flag travel in one
-// 64-bit scan (count << 24 | flag; fewer than 2^24 blocks).
-__global__ void __launch_bounds__(kThreads) k_mc_scan(const uint32_t *block_tris, int64_t nblocks,
-                                                      int64_t *block_off, int64_t *grand_total,
-                                                      int *nonempty, int *n_nonempty) {
+// Exclusive scan of the per-block totals into 64-bit offsets and the grand
+// total, by one CTA (every thread calls it), a chunk of kScanChunk totals at
+// a time: the chunk is staged in shared memory with coalesced loads (padded
+// by one word per 32, so that thread t's kScanPerThread consecutive totals
+// sit in distinct banks), each thread sums its totals, the block scans the
+// sums, and each thread writes its offsets.  The totals are read through L2
+// (other CTAs of the same launch may have written them).
+__device__ void scan_block_totals(const uint32_t *block_tris, int64_t nblocks, int64_t *block_off,
+                                  int64_t *grand_total) {
   __shared__ uint32_t s_v[kScanChunk + kScanChunk / 32];
   uint64_t carry = 0;
   for (int64_t c0 = 0; c0 < nblocks; c0 += kScanChunk) {
     const int64_t n = nblocks - c0 < kScanChunk ? nblocks - c0 : kScanChunk;
-    for (int i = threadIdx.x; i < kScanChunk; i += kThreads) s_v[i + (i >> 5)] = i < n ? block_tris[c0 + i] : 0u;
+    for (int i = threadIdx.x; i < kScanChunk; i += kThreads)
+      s_v[i + (i >> 5)] = i < n ? __ldcg(block_tris + c0 + i) : 0u;
     __syncthreads();
     const int first = threadIdx.x * kScanPerThread;
     uint64_t sum = 0;
 #pragma unroll
-    for (int j = 0; j < kScanPerThread; ++j) {
-      const uint32_t v = s_v[first + j + ((first + j) >> 5)];
-      sum += ((uint64_t)v << 24) | (uint64_t)(v != 0);
-    }
+    for (int j = 0; j < kScanPerThread; ++j) sum += s_v[first + j + ((first + j) >> 5)];
     uint64_t total;
     uint64_t excl = carry + block_exclusive_scan<uint64_t>(sum, &total);
 #pragma unroll
     for (int j = 0; j < kScanPerThread; ++j) {
       const int i = first + j;
-      const uint32_t v = s_v[i + (i >> 5)];
-      if (i < n) {
-        block_off[c0 + i] = (int64_t)(excl >> 24);
-        if (nonempty && v && KF_IN_BOUNDS(excl & 0xffffffu, nblocks, KF_SITE_MC_BLOCK))
-          nonempty[excl & 0xffffffu] = (int)(c0 + i);
-      }
-      excl += ((uint64_t)v << 24) | (uint64_t)(v != 0);
+      if (i < n) block_off[c0 + i] = (int64_t)excl;
+      excl += s_v[i + (i >> 5)];
     }
     carry += total;
     __syncthreads();  // the chunk is read before the next one is staged
   }
+  if (threadIdx.x == 0) *grand_total = (int64_t)carry;
+}
+
+__global__ void __launch_bounds__(kThreads) k_mc_scan(const uint32_t *block_tris, int64_t nblocks,
+                                                      int64_t *block_off, int64_t *grand_total) {
+  scan_block_totals(block_tris, nblocks, block_off, grand_total);
+}
+
+// The same scan in registers (no shared staging, so that the count pass,
+// whose last CTA runs it, keeps its shared memory small): thread t sums the
+// kScanPerThread totals from c0 + t * kScanPerThread on with 16-byte loads,
+// the block scans the sums, and the thread reads its totals again to write
+// their offsets.  block_tris and block_off are 16-byte aligned.
+__device__ void scan_block_totals_regs(const uint32_t *block_tris, int64_t nblocks, int64_t *block_off,
+                                       int64_t *grand_total) {
+  uint64_t carry = 0;
+  for (int64_t c0 = 0; c0 < nblocks; c0 += kScanChunk) {
+    const int64_t first = c0 + (int64_t)threadIdx.x * kScanPerThread;
+    const bool whole = first + kScanPerThread <= nblocks;
+    uint64_t sum = 0;
+    if (whole) {
+      const uint4 *p = reinterpret_cast<const uint4 *>(block_tris + first);
+#pragma unroll
+      for (int j = 0; j < kScanPerThread / 4; ++j) {
+        const uint4 v = __ldcg(p + j);
+        sum += (uint64_t)v.x + v.y + v.z + v.w;
+      }
+    } else {
+      for (int64_t i = first; i < nblocks; ++i) sum += __ldcg(block_tris + i);
+    }
+    uint64_t total;
+    uint64_t excl = carry + block_exclusive_scan<uint64_t>(sum, &total);
+    if (whole) {
+      const uint4 *p = reinterpret_cast<const uint4 *>(block_tris + first);
+      longlong2 *o = reinterpret_cast<longlong2 *>(block_off + first);
+#pragma unroll
+      for (int j = 0; j < kScanPerThread / 4; ++j) {
+        const uint4 v = __ldcg(p + j);
+        const int64_t a = (int64_t)excl, b = a + v.x, c = b + v.y, d = c + v.z;
+        o[2 * j] = make_longlong2(a, b);
+        o[2 * j + 1] = make_longlong2(c, d);
+        excl = (uint64_t)(d + v.w);
+      }
+    } else {
+      for (int64_t i = first; i < nblocks; ++i) {
+        block_off[i] = (int64_t)excl;
+        excl += __ldcg(block_tris + i);
+      }
+    }
+    carry += total;
+  }
+  if (threadIdx.x == 0) *grand_total = (int64_t)carry;
+}
+
+// Scratch of kf_mc_run's two passes.
+struct McList {
+  uint32_t *block_tris;  // triangles per block
+  int64_t *block_off;    // exclusive offsets per block, then the grand total
+  uint2 *cells;          // per listed cell: index, (offset in its block << 8) | configuration
+  unsigned *done;        // CTAs of the count pass finished (the last one resets it)
+  unsigned *n_cells;     // cells appended by the count pass (the last CTA resets it)
+  unsigned *n_listed;    // their final number, for the emit pass
+  unsigned cap;          // entries `cells` holds (0: list nothing)
+};
+
+// Pass 1 of kf_mc_run.  Thread t of block b takes the kCellsPerThread
+// contiguous cells from b * kCellsPerBlock + t * kCellsPerThread (two
+// 16-byte loads; the grid's base is 256-byte aligned); its band cells
+// gather their corners one at a time (they are few).  The cells with
+// triangles are appended to the list with one atomic per warp; an entry
+// carries the cell's position among the block's triangles, so the list's
+// order does not matter.
+__global__ void __launch_bounds__(kThreads) k_mc_count_list(McGrid g, McList L, int64_t nblocks) {
+  const int64_t first = (int64_t)blockIdx.x * kCellsPerBlock + (int64_t)threadIdx.x * kCellsPerThread;
+  float d[kCellsPerThread];
+  if (first + kCellsPerThread <= g.count) {
+    const float4 *p = reinterpret_cast<const float4 *>(g.phi + first);
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    d[0] = a.x, d[1] = a.y, d[2] = a.z, d[3] = a.w, d[4] = b.x, d[5] = b.y, d[6] = b.z, d[7] = b.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < kCellsPerThread; ++k) d[k] = own_value(g, first + k);
+  }
+  unsigned band = 0;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; ++k)
+    if (!(d[k] > g.hi || d[k] < g.lo)) band |= 1u << k;  // SDF.cpp:407 (a NaN is not skipped)
+  uint32_t n = 0, counts = 0;  // counts: 4 bits per cell (at most 5 triangles)
+  uint64_t cubes = 0;          // 8 bits per cell
+  for (unsigned rest = band; rest; rest &= rest - 1) {
+    const int k = __ffs(rest) - 1;
+    int x, y, z;
+    float val[8];
+    const int cube = classify(g, first + k, __ldg(g.phi + first + k), x, y, z, val);
+    const uint32_t c = (uint32_t)cube_tris(cube);
+    n += c;
+    counts |= c << (4 * k);
+    cubes |= (uint64_t)(cube & 255) << (8 * k);
+  }
+  uint32_t total;
+  uint32_t run = block_exclusive_scan<uint32_t>(n, &total);
+  // one slot per cell with triangles, taken with one atomic per warp
+  unsigned m = 0;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; ++k) m += ((counts >> (4 * k)) & 15u) != 0u;
+  const int lane = threadIdx.x & 31;
+  unsigned incl = m;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const unsigned warp_total = __shfl_sync(0xffffffffu, incl, 31);
+  if (warp_total) {
+    unsigned base = 0;
+    if (lane == 31) base = atomicAdd(L.n_cells, warp_total);
+    unsigned slot = __shfl_sync(0xffffffffu, base, 31) + incl - m;
+#pragma unroll
+    for (int k = 0; k < kCellsPerThread; ++k) {
+      const uint32_t c = (counts >> (4 * k)) & 15u;
+      if (c) {
+        if (slot < L.cap)
+          L.cells[slot] = make_uint2((uint32_t)(first + k), (run << 8) | (uint32_t)((cubes >> (8 * k)) & 255u));
+        ++slot;
+        run += c;
+      }
+    }
+  }
+  // the last CTA to finish turns the totals into offsets (the classic
+  // fence-and-count pattern: no CTA waits for another); every warp's
+  // appends are done before the CTA counts itself finished
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
   if (threadIdx.x == 0) {
-    *grand_total = (int64_t)(carry >> 24);
-    if (n_nonempty) *n_nonempty = (int)(carry & 0xffffffu);
+    L.block_tris[blockIdx.x] = total;
+    __threadfence();
+    s_last = atomicAdd(L.done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    scan_block_totals_regs(L.block_tris, nblocks, L.block_off, L.block_off + nblocks);
+    if (threadIdx.x == 0) {
+      *L.n_listed = atomicExch(L.n_cells, 0u);
+      *L.done = 0u;
+    }
   }
 }
 
@@ -296,35 +432,21 @@ __device__ __noinline__ void emit_cell(const McGrid &g, int64_t i, int cube, int
 }
 
 // The triangles of cell block b (cells b*kCellsPerBlock + r*kThreads + t),
-// from position out0 on.  kMask: mask holds k_mc_count's cells with
-// triangles and only those gather their corners; otherwise every cell is
-// classified again.
-template <bool kMask>
-__device__ __forceinline__ void emit_block(const McGrid &g, int64_t b, int64_t out0,
-                                           const uint32_t *__restrict__ mask, float *__restrict__ verts,
+// from position out0 on; every cell is classified again.
+__device__ __forceinline__ void emit_block(const McGrid &g, int64_t b, int64_t out0, float *__restrict__ verts,
                                            int64_t capacity) {
   const int64_t base = b * kCellsPerBlock + threadIdx.x;
   // classify every round first (the loads in flight together), then scan
   // and emit the rounds that have triangles
   float d[kRounds];
-  bool has[kRounds];
 #pragma unroll
-  for (int r = 0; r < kRounds; ++r) {
-    if (kMask) {
-      const uint32_t w = __ldg(mask + b * kMaskWords + r * (kThreads / 32) + (threadIdx.x >> 5));
-      has[r] = (w >> (threadIdx.x & 31)) & 1u;
-      d[r] = has[r] ? __ldg(g.phi + base + (int64_t)r * kThreads) : g.hi + 1.0f;
-    } else {
-      has[r] = true;
-      d[r] = own_value(g, base + (int64_t)r * kThreads);
-    }
-  }
+  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, base + (int64_t)r * kThreads);
   int cube[kRounds];
 #pragma unroll
   for (int r = 0; r < kRounds; ++r) {
     int x, y, z;
     float val[8];
-    cube[r] = has[r] ? classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val) : -1;
+    cube[r] = classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val);
   }
 #pragma unroll
   for (int r = 0; r < kRounds; ++r) {
@@ -340,51 +462,30 @@ __device__ __forceinline__ void emit_block(const McGrid &g, int64_t b, int64_t o
 // Every cell block, one CTA each.
 __global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *block_off,
                                                       float *__restrict__ verts, int64_t capacity) {
-  emit_block<false>(g, blockIdx.x, block_off[blockIdx.x], nullptr, verts, capacity);
+  emit_block(g, blockIdx.x, block_off[blockIdx.x], verts, capacity);
 }
 
-// Only the blocks with triangles (k_mc_scan's list), a resident grid of CTAs
-// looping over them.  A block's cells with triangles (k_mc_count's mask)
-// gather their corners together, one scan orders the triangles of all its
-// rounds at once, and each cell then writes its own.
-__global__ void __launch_bounds__(kThreads) k_mc_emit_listed(McGrid g, const int64_t *block_off,
-                                                             const int *__restrict__ nonempty,
-                                                             const int *__restrict__ n_nonempty,
-                                                             const uint32_t *__restrict__ mask,
-                                                             float *__restrict__ verts, int64_t capacity) {
-  const int n = *n_nonempty;
-  for (int e = blockIdx.x; e < n; e += gridDim.x) {
-    const int64_t b = nonempty[e];
-    if (!KF_IN_BOUNDS(b, (g.count + kCellsPerBlock - 1) / kCellsPerBlock, KF_SITE_MC_BLOCK)) continue;
-    const int64_t base = b * kCellsPerBlock + threadIdx.x;
-    bool has[kRounds];
-    float d[kRounds];
-#pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      const uint32_t w = __ldg(mask + b * kMaskWords + r * (kThreads / 32) + (threadIdx.x >> 5));
-      has[r] = (w >> (threadIdx.x & 31)) & 1u;
-      d[r] = has[r] ? __ldg(g.phi + base + (int64_t)r * kThreads) : g.hi + 1.0f;
+// Pass 2 of kf_mc_run: a resident grid.  Each thread writes the triangles of
+// listed cells; when the list overflowed, each CTA instead takes blocks with
+// triangles and re-classifies them (emit_block).
+__global__ void __launch_bounds__(kThreads) k_mc_emit_cells(McGrid g, McList L, int64_t nblocks,
+                                                            float *__restrict__ verts, int64_t capacity) {
+  const unsigned n = *L.n_listed;
+  if (n <= L.cap) {
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+      const uint2 c = L.cells[e];
+      const int64_t i = c.x;
+      if (!KF_IN_BOUNDS(i, g.count, KF_SITE_MC_BLOCK)) continue;
+      emit_cell(g, i, (int)(c.y & 255u), L.block_off[i / kCellsPerBlock] + (int64_t)(c.y >> 8), verts,
+                capacity);
     }
-    int cube[kRounds];
-    uint32_t nt[kRounds], pre[kRounds], tot[kRounds];
-#pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      int x, y, z;
-      float val[8];
-      cube[r] = has[r] ? classify(g, base + (int64_t)r * kThreads, d[r], x, y, z, val) : -1;
-      nt[r] = (uint32_t)cube_tris(cube[r]);
-    }
-    block_scan_vec<kRounds>(nt, pre, tot);
-    int64_t out = block_off[b];
-#pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      if (nt[r]) emit_cell(g, base + (int64_t)r * kThreads, cube[r], out + pre[r], verts, capacity);
-      out += tot[r];
-    }
+  } else {
+    for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x)
+      if (__ldg(L.block_tris + b)) emit_block(g, b, L.block_off[b], verts, capacity);
   }
 }
 
-// Resident CTAs of the listed emit pass (at most one per cell block).
+// Resident CTAs of the emit pass.
 unsigned emit_grid(int64_t nblocks) {
   return (unsigned)std::min<int64_t>(nblocks, (int64_t)kf_num_sms() * 8);
 }
@@ -410,10 +511,18 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   mg.hy = (float)g->n[1] / 2.0f;
   mg.hz = (float)g->n[2] / 2.0f;
   int64_t nblocks = (g->count + kCellsPerBlock - 1) / kCellsPerBlock;
-  // scratch, kept with the grid (calls on one grid are stream-ordered):
-  // offsets (i64) and the grand total right after them, the per-block totals
-  // (u32) and the masks of cells with triangles (u32)
-  const size_t bytes = (nblocks + 1) * sizeof(int64_t) + nblocks * sizeof(uint32_t) * (2 + kMaskWords) + 16;
+  // scratch, kept with the grid (calls on one grid are stream-ordered): the
+  // per-block totals (u32), their offsets (i64) and the grand total right
+  // after them, three counters and the list of cells with triangles (count
+  // / 16 of them, at least 2^18; none for grids of 2^32 cells or more, whose
+  // indices the list does not hold)
+  const int64_t cap = g->count >= (int64_t)1 << 32 ? 0
+                                                   : std::min<int64_t>(g->count, std::max<int64_t>(g->count / 16, 1 << 18));
+  const size_t off_off = ((size_t)nblocks * sizeof(uint32_t) + 255) & ~(size_t)255;
+  const size_t cnt_off = off_off + (((size_t)nblocks + 1) * sizeof(int64_t) + 15) / 16 * 16;
+  const size_t list_off = cnt_off + 16;
+  const size_t bytes = list_off + (size_t)cap * sizeof(uint2);
+  bool fresh = false;
   if (g->mc_bytes < bytes) {
     cudaFree(g->mc);
     g->mc = nullptr;
@@ -424,22 +533,26 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
       return kf_fail(KF_ERR_OOM, "cudaMalloc of the marching-cubes scratch failed");
     }
     g->mc_bytes = bytes;
+    fresh = true;
   }
-  int64_t *off = (int64_t *)g->mc;
-  int64_t *total_dev = off + nblocks;
-  uint32_t *tris = (uint32_t *)(total_dev + 1);
-  uint32_t *mask = tris + nblocks;
-  int *nonempty = (int *)(mask + nblocks * kMaskWords);
-  int *n_nonempty = nonempty + nblocks;
-  k_mc_count<true><<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris, mask);
-  k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev, nonempty, n_nonempty);
-  KF_CHECK_LAUNCH("k_mc_count/k_mc_scan");
+  McList L;
+  L.block_tris = (uint32_t *)g->mc;
+  L.block_off = (int64_t *)((char *)g->mc + off_off);
+  int64_t *total_dev = L.block_off + nblocks;
+  L.done = (unsigned *)((char *)g->mc + cnt_off);
+  L.n_cells = L.done + 1;
+  L.n_listed = L.done + 2;
+  L.cells = (uint2 *)((char *)g->mc + list_off);
+  L.cap = (unsigned)cap;
+  // the counters start at zero; the count pass's last CTA leaves them so
+  if (fresh) KF_CHECK_CUDA(cudaMemsetAsync(L.done, 0, 3 * sizeof(unsigned), s));
+  k_mc_count_list<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, L, nblocks);
+  KF_CHECK_LAUNCH("k_mc_count_list");
   if (ntri_async) {
     KF_CHECK_CUDA(cudaMemcpyAsync(ntri_async, total_dev, sizeof(int64_t), cudaMemcpyDefault, s));
     if (verts && capacity > 0) {
-      k_mc_emit_listed<<<emit_grid(nblocks), kThreads, 0, s>>>(mg, off, nonempty, n_nonempty, mask, verts,
-                                                              capacity);
-      KF_CHECK_LAUNCH("k_mc_emit_listed");
+      k_mc_emit_cells<<<emit_grid(nblocks), kThreads, 0, s>>>(mg, L, nblocks, verts, capacity);
+      KF_CHECK_LAUNCH("k_mc_emit_cells");
     }
     return KF_OK;
   }
@@ -450,9 +563,8 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   KF_CHECK_CUDA(cudaStreamSynchronize(s));
   *ntri = total;
   if (verts && total > 0 && capacity > 0) {
-    k_mc_emit_listed<<<emit_grid(nblocks), kThreads, 0, s>>>(mg, off, nonempty, n_nonempty, mask, verts,
-                                                            capacity);
-    KF_CHECK_LAUNCH("k_mc_emit_listed");
+    k_mc_emit_cells<<<emit_grid(nblocks), kThreads, 0, s>>>(mg, L, nblocks, verts, capacity);
+    KF_CHECK_LAUNCH("k_mc_emit_cells");
   }
   if (verts && capacity < total)
     return kf_fail(KF_ERR_CAPACITY, "vertex buffer holds fewer triangles than the mesh has");
@@ -537,8 +649,8 @@ extern "C" int kf_marching_cubes_noalloc(const float *phi, const int dims[3], co
   // Every word read below is written earlier in this call; the grand total is
   // cleared anyway so a failed launch cannot report a previous call's count.
   KF_CHECK_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(int64_t), s));
-  k_mc_count<false><<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris, nullptr);
-  k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev, nullptr, nullptr);
+  k_mc_count<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, tris);
+  k_mc_scan<<<1, kThreads, 0, s>>>(tris, nblocks, off, total_dev);
   if (verts && capacity > 0)
     k_mc_emit<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, off, verts, capacity);
   KF_CHECK_LAUNCH("kf_marching_cubes_noalloc kernels");

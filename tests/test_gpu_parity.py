@@ -79,8 +79,8 @@ def test_integrate_far_from_origin(gpu, oracle, shift):
     turned by 4 degrees.  The camera coordinates are then differences of
     world coordinates of up to hundreds of metres, whose float rounding is
     hundreds of times that of the unshifted grid: the float projection's
-    per-voxel error bound grows with them (at the largest shift about a
-    quarter of the voxels lie within it of a pixel edge and take the float64
+    per-voxel error bound grows with them (at the largest shift more than a
+    third of the voxels lie within it of a pixel edge and take the float64
     path, past the side list's capacity some in place), and every pixel,
     weight and distance stays the reference's.  A fixed margin of 1/128
     pixel would misplace about 1.4 k voxels at the largest shift."""
@@ -375,6 +375,50 @@ def test_marching_cubes_counts_exact(gpu, oracle, which):
         n = max(g.dims)
         err_vox = np.abs(tris - otris).max() / (2.0 / n)
         assert err_vox <= 1e-4, err_vox
+
+
+def mesh_against_oracle(gpu, oracle, phi, P, min_tris):
+    nz, ny, nx = phi.shape
+    g = make_grid(gpu, phi, 0.004, P)
+    tris = gpu.marching_cubes(g, P)
+    g.close()
+    otris = oracle.mesh(phi.astype(np.float64), oparams(P))
+    assert tris.shape == otris.shape and len(tris) >= min_tris, (tris.shape, otris.shape)
+    # vertex coordinates are (index / half size - 1): one voxel is 2/n of the range
+    err_vox = (np.abs(tris - otris).reshape(-1, 3, 3) / (2.0 / np.array([nx, ny, nz]))).max()
+    assert err_vox <= 1e-4, err_vox
+
+
+def test_marching_cubes_ragged_dims(gpu, oracle):
+    """A grid whose sizes are not multiples of anything the passes use
+    (37 x 29 x 23): rows end inside a thread's run of cells and the last
+    block is partial."""
+    P = gpu.Params.paper(0.004)
+    dims = (37, 29, 23)
+    Z, Y, X = np.meshgrid(*[np.arange(n) + 0.5 for n in dims[::-1]], indexing="ij")
+    d = (np.sqrt((X - 17.3) ** 2 + ((Y - 14.1) / 0.9) ** 2 + (Z - 11.6) ** 2) - 8.2) * 0.004
+    phi = np.where(d > P.max_surface, P.max_surface + 1e-5, d).astype(np.float32)
+    mesh_against_oracle(gpu, oracle, phi, P, 200)
+
+
+def test_marching_cubes_list_overflow(gpu, oracle):
+    """More cells with triangles than the marching cubes' cell list holds
+    (count / 16 entries at 200^3): a noise box of 112 x 96 x 72 cells, all
+    in the band with random signs, inside an otherwise empty grid.  The emit
+    pass then re-classifies every block with triangles, and the mesh is
+    still the reference's, triangle for triangle."""
+    P = gpu.Params.paper(0.004)
+    n = 200
+    rng = np.random.default_rng(41)
+    phi = np.full((n, n, n), P.max_surface + 1e-5, np.float32)
+    box = rng.uniform(0.2, 0.8, (72, 96, 112)) * np.where(rng.random((72, 96, 112)) < 0.5, -P.unknown_clip,
+                                                            P.max_surface)
+    phi[60:132, 50:146, 40:152] = box.astype(np.float32)
+    # all but 1/128 of the box's cells (those with eight equal signs) have
+    # triangles, each at least one
+    min_cells = int(0.9 * box.size)
+    assert min_cells > n ** 3 // 16
+    mesh_against_oracle(gpu, oracle, phi, P, min_cells)
 
 
 def test_mesh_capacity_error(gpu):
