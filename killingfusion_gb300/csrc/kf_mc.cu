@@ -7,10 +7,10 @@
 //
 // kf_mc_run (grids the library owns), two passes:
 //   1. k_mc_count_list: each CTA classifies a block of kCellsPerBlock cells,
-//      thread t the kCellsPerThread cells from t * kCellsPerThread on (two
-//      16-byte loads), scans the block's triangle counts and lists every
-//      cell with triangles: its index, configuration and offset in the
-//      block.  The last CTA to finish turns the block totals into offsets.
+//      warp w the 256 from 256 w on (lane l the cells 32 r + l), and lists
+//      every cell with triangles: its index, configuration and offset in
+//      the block.  The last CTA to finish turns the block totals into
+//      offsets.
 //   2. k_mc_emit_cells: one thread per listed cell writes its triangles.
 //      When a grid has more such cells than the list holds, it falls back
 //      to re-classifying every block with triangles (emit_block).
@@ -41,7 +41,6 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kRounds = 8;
 constexpr int kCellsPerBlock = kThreads * kRounds;
-constexpr int kCellsPerThread = kCellsPerBlock / kThreads;
 constexpr int kScanPerThread = 32;
 constexpr int kScanChunk = kThreads * kScanPerThread;
 
@@ -77,7 +76,12 @@ constexpr McTables build_tables() {
   return t;
 }
 
+// Uniform lookups (corner offsets, edge ends) read the constant bank; the
+// per-cell ones (indexed by each thread's own configuration) read the same
+// tables from global memory through L1, which serves a warp's different
+// entries together where the constant bank would serialise them.
 __constant__ McTables c_mc = build_tables();
+__device__ const McTables g_mc = build_tables();
 
 struct McGrid {
   const float *phi;
@@ -126,7 +130,7 @@ __device__ __forceinline__ int classify(const McGrid &g, int64_t i, float d, int
 }
 
 __device__ __forceinline__ int cube_tris(int cube) {
-  return (cube < 0 || c_mc.edge[cube] == 0) ? 0 : (int)c_mc.ntri[cube];
+  return (cube < 0 || __ldg(&g_mc.edge[cube]) == 0) ? 0 : (int)__ldg(&g_mc.ntri[cube]);
 }
 
 template <typename T>
@@ -270,74 +274,89 @@ struct McList {
   unsigned cap;          // entries `cells` holds (0: list nothing)
 };
 
-// Pass 1 of kf_mc_run.  Thread t of block b takes the kCellsPerThread
-// contiguous cells from b * kCellsPerBlock + t * kCellsPerThread (two
-// 16-byte loads; the grid's base is 256-byte aligned); its band cells
-// gather their corners one at a time (they are few).  The cells with
-// triangles are appended to the list with one atomic per warp; an entry
-// carries the cell's position among the block's triangles, so the list's
-// order does not matter.
-__global__ void __launch_bounds__(kThreads) k_mc_count_list(McGrid g, McList L, int64_t nblocks) {
-  const int64_t first = (int64_t)blockIdx.x * kCellsPerBlock + (int64_t)threadIdx.x * kCellsPerThread;
-  float d[kCellsPerThread];
-  if (first + kCellsPerThread <= g.count) {
-    const float4 *p = reinterpret_cast<const float4 *>(g.phi + first);
-    const float4 a = __ldg(p), b = __ldg(p + 1);
-    d[0] = a.x, d[1] = a.y, d[2] = a.z, d[3] = a.w, d[4] = b.x, d[5] = b.y, d[6] = b.z, d[7] = b.w;
-  } else {
+// Pass 1 of kf_mc_run.  Warp w of block b takes the 256 cells from
+// b * kCellsPerBlock + 256 w on, in kRounds rounds of 32 (lane l the cell
+// 32 r + l of round r: the loads coalesce, and the band cells of a surface
+// spread over the lanes).  The band cells gather their corners; the warp's
+// triangle total and the block's warp totals give each warp its offset in
+// the block, and a warp scan per round each cell's.  The cells with
+// triangles are appended to the list, one atomic per warp; an entry carries
+// the cell's position among the block's triangles, so the list's order does
+// not matter.
+__global__ void __launch_bounds__(kThreads, 6)  // 40 registers: 6 CTAs per SM
+    k_mc_count_list(McGrid g, McList L, int64_t nblocks) {
+  constexpr int kWarpCells = kRounds * 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t wbase = (int64_t)blockIdx.x * kCellsPerBlock + (int64_t)warp * kWarpCells + lane;
+  float d[kRounds];
 #pragma unroll
-    for (int k = 0; k < kCellsPerThread; ++k) d[k] = own_value(g, first + k);
-  }
+  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, wbase + 32 * r);
   unsigned band = 0;
 #pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k)
-    if (!(d[k] > g.hi || d[k] < g.lo)) band |= 1u << k;  // SDF.cpp:407 (a NaN is not skipped)
-  uint32_t n = 0, counts = 0;  // counts: 4 bits per cell (at most 5 triangles)
-  uint64_t cubes = 0;          // 8 bits per cell
+  for (int r = 0; r < kRounds; ++r)
+    if (!(d[r] > g.hi || d[r] < g.lo)) band |= 1u << r;  // SDF.cpp:407 (a NaN is not skipped)
+  uint32_t n = 0, counts = 0;  // counts: 4 bits per round (at most 5 triangles)
+  uint64_t cubes = 0;          // 8 bits per round
   for (unsigned rest = band; rest; rest &= rest - 1) {
-    const int k = __ffs(rest) - 1;
+    const int r = __ffs(rest) - 1;
+    const int64_t i = wbase + 32 * r;
     int x, y, z;
     float val[8];
-    const int cube = classify(g, first + k, __ldg(g.phi + first + k), x, y, z, val);
+    const int cube = classify(g, i, __ldg(g.phi + i), x, y, z, val);
     const uint32_t c = (uint32_t)cube_tris(cube);
     n += c;
-    counts |= c << (4 * k);
-    cubes |= (uint64_t)(cube & 255) << (8 * k);
+    counts |= c << (4 * r);
+    cubes |= (uint64_t)(cube & 255) << (8 * r);
   }
-  uint32_t total;
-  uint32_t run = block_exclusive_scan<uint32_t>(n, &total);
-  // one slot per cell with triangles, taken with one atomic per warp
-  unsigned m = 0;
+  // the warps' totals and offsets in the block
+  __shared__ uint32_t s_warp[kThreads / 32];
+  const uint32_t warp_total = __reduce_add_sync(0xffffffffu, n);
+  if (lane == 0) s_warp[warp] = warp_total;
+  __syncthreads();
+  uint32_t run = 0, total = 0;
 #pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) m += ((counts >> (4 * k)) & 15u) != 0u;
-  const int lane = threadIdx.x & 31;
-  unsigned incl = m;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
+  for (int w = 0; w < kThreads / 32; ++w) {
+    const uint32_t t = s_warp[w];
+    run += w < warp ? t : 0u;
+    total += t;
   }
-  const unsigned warp_total = __shfl_sync(0xffffffffu, incl, 31);
   if (warp_total) {
+    // one slot per cell with triangles
+    unsigned m = 0;
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) m += ((counts >> (4 * r)) & 15u) != 0u;
+    unsigned incl = m;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
     unsigned base = 0;
-    if (lane == 31) base = atomicAdd(L.n_cells, warp_total);
+    if (lane == 31) base = atomicAdd(L.n_cells, incl);
     unsigned slot = __shfl_sync(0xffffffffu, base, 31) + incl - m;
 #pragma unroll
-    for (int k = 0; k < kCellsPerThread; ++k) {
-      const uint32_t c = (counts >> (4 * k)) & 15u;
+    for (int r = 0; r < kRounds; ++r) {
+      const uint32_t c = (counts >> (4 * r)) & 15u;
+      if (!__any_sync(0xffffffffu, c != 0u)) continue;  // a round without triangles
+      uint32_t ci = c;  // inclusive scan of the round's counts over the lanes
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, ci, o);
+        if (lane >= o) ci += t;
+      }
       if (c) {
         if (slot < L.cap)
-          L.cells[slot] = make_uint2((uint32_t)(first + k), (run << 8) | (uint32_t)((cubes >> (8 * k)) & 255u));
+          L.cells[slot] = make_uint2((uint32_t)(wbase + 32 * r),
+                                     ((run + ci - c) << 8) | (uint32_t)((cubes >> (8 * r)) & 255u));
         ++slot;
-        run += c;
       }
+      run += __shfl_sync(0xffffffffu, ci, 31);
     }
   }
   // the last CTA to finish turns the totals into offsets (the classic
   // fence-and-count pattern: no CTA waits for another); every warp's
   // appends are done before the CTA counts itself finished
   __shared__ bool s_last;
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     L.block_tris[blockIdx.x] = total;
@@ -404,7 +423,7 @@ __device__ __noinline__ void emit_cell(const McGrid &g, int64_t i, int cube, int
   int x, y, z;
   float val[8];
   classify(g, i, __ldg(g.phi + i), x, y, z, val);
-  const int em = c_mc.edge[cube];
+  const int em = __ldg(&g_mc.edge[cube]);
   float p[8][3];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
@@ -417,13 +436,13 @@ __device__ __noinline__ void emit_cell(const McGrid &g, int64_t i, int cube, int
   for (int e = 0; e < 12; ++e)
     if (em & (1 << e))
       vinterp(p[c_mc.ends[e][0]], p[c_mc.ends[e][1]], val[c_mc.ends[e][0]], val[c_mc.ends[e][1]], vl[e]);
-  const int n = c_mc.ntri[cube];
+  const int n = __ldg(&g_mc.ntri[cube]);
   for (int t = 0; t < n; ++t, ++out) {
     if (out >= capacity) break;
     float *o = verts + 9 * out;
 #pragma unroll
     for (int j2 = 0; j2 < 3; ++j2) {
-      const float *v = vl[c_mc.tri[cube][3 * t + j2]];
+      const float *v = vl[__ldg(&g_mc.tri[cube][3 * t + j2])];
       o[3 * j2 + 0] = v[0];
       o[3 * j2 + 1] = -v[1];
       o[3 * j2 + 2] = v[2];
