@@ -504,8 +504,7 @@ def run_large(args, local):
     stats = capi.SolveStats()
 
     def frame(f, fuse):
-        live.reset(P)
-        live.integrate(dev_frames[f], min_depth=0.05, max_depth=1.6)
+        live.compute_sdf(P, dev_frames[f], min_depth=0.05, max_depth=1.6)
         psi.zero()
         capi.check(L.kf_psi_solve(live.h, can.h, psi.h, C.byref(P.c()), iters, capi.KF_SOLVER_FUSED,
                                   C.byref(stats), None))

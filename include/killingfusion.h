@@ -236,6 +236,17 @@ int kf_integrate_depth(kf_grid g, const float *depth, int width, int height,
 int kf_integrate_depth_u16(kf_grid g, const uint16_t *depth, int width, int height, double scale,
                            const double c2w[16], const double K[9], double min_depth,
                            double max_depth, void *stream);
+/* KillingFusion::computeSDF (KillingFusion.cpp:209-230): a new SDF of one
+ * frame, i.e. kf_grid_reset (phi = max_surface + epsilon, w = 0) followed by
+ * kf_integrate_depth, with the same result, in one pass that writes every
+ * voxel once instead of a fill and an integration that reads the grid back. */
+int kf_compute_sdf(kf_grid g, const kf_params *p, const float *depth, int width, int height,
+                   const double c2w[16], const double K[9], double min_depth, double max_depth,
+                   void *stream);
+/* The same on 16-bit depth (kf_grid_reset + kf_integrate_depth_u16). */
+int kf_compute_sdf_u16(kf_grid g, const kf_params *p, const uint16_t *depth, int width, int height,
+                       double scale, const double c2w[16], const double K[9], double min_depth,
+                       double max_depth, void *stream);
 
 /* KillingFusion::computeDisplacementField, Jacobi schedule
  * (KillingFusion.cpp:240-352): `iterations` gradient-descent steps of psi

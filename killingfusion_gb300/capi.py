@@ -128,6 +128,9 @@ SIGNATURES = {
                                      C.c_double, _vp]),
     "kf_integrate_depth_u16": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_double,
                                          C.c_double, _vp]),
+    "kf_compute_sdf": (C.c_int, [_vp, _PP, _vp, C.c_int, C.c_int, _dp, _dp, C.c_double, C.c_double, _vp]),
+    "kf_compute_sdf_u16": (C.c_int, [_vp, _PP, _vp, C.c_int, C.c_int, C.c_double, _dp, _dp, C.c_double,
+                                     C.c_double, _vp]),
     "kf_psi_solve": (C.c_int, [_vp, _vp, _vp, _PP, C.c_int, C.c_int, C.POINTER(SolveStats), _vp]),
     "kf_psi_solve_async": (C.c_int, [_vp, _vp, _vp, _PP, C.c_int, C.c_int, _vp]),
     "kf_psi_solve_wait": (C.c_int, [_vp, C.POINTER(SolveStats)]),
@@ -304,6 +307,28 @@ class Grid:
             ptr, (hh, ww) = depth.data_ptr(), tuple(depth.shape)
         check(load().kf_integrate_depth(self.h, ptr, ww, hh, _d(c2w.ravel()), _d(K.ravel()),
                                         min_depth, max_depth, _stream(stream)))
+
+    def compute_sdf(self, params, depth, c2w=None, K=None, min_depth=0.05, max_depth=1.2, u16_scale=None,
+                    stream=None):
+        """KillingFusion::computeSDF: reset + integrate in one pass (the same
+        result as reset() then integrate() / integrate_u16()).  depth: numpy
+        float32 (or uint16 with u16_scale) [h, w], or a CUDA tensor."""
+        from . import synth
+        c2w = np.eye(4) if c2w is None else np.asarray(c2w, dtype=np.float64)
+        K = synth.K if K is None else np.asarray(K, dtype=np.float64)
+        dt = np.float32 if u16_scale is None else np.uint16
+        if isinstance(depth, np.ndarray):
+            d = np.ascontiguousarray(depth, dtype=dt)
+            ptr, (hh, ww) = d.ctypes.data, d.shape
+        else:
+            ptr, (hh, ww) = depth.data_ptr(), tuple(depth.shape)
+        if u16_scale is None:
+            check(load().kf_compute_sdf(self.h, C.byref(params.c()), ptr, ww, hh, _d(c2w.ravel()),
+                                        _d(K.ravel()), min_depth, max_depth, _stream(stream)))
+        else:
+            check(load().kf_compute_sdf_u16(self.h, C.byref(params.c()), ptr, ww, hh, float(u16_scale),
+                                            _d(c2w.ravel()), _d(K.ravel()), min_depth, max_depth,
+                                            _stream(stream)))
 
     def integrate_u16(self, depth, scale=0.001, c2w=None, K=None, min_depth=0.05, max_depth=1.2, stream=None):
         """SDF::integrateDepthFrame on 16-bit depth (numpy uint16 [h, w] or a

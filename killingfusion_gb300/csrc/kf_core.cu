@@ -574,34 +574,58 @@ static int stage_depth(kf_grid g, const void *depth, size_t bytes, cudaStream_t 
   return KF_OK;
 }
 
-extern "C" int kf_integrate_depth(kf_grid g, const float *depth, int width, int height,
-                                  const double c2w[16], const double K[9], double min_depth,
-                                  double max_depth, void *stream) {
+// Both depth formats of integration, into the grid as it is (fresh == NULL)
+// or into a fresh grid of phi = *fresh, w = 0.
+static int integrate_entry(kf_grid g, const void *depth, size_t pixel_bytes, int width, int height, double scale,
+                           const double c2w[16], const double K[9], double min_depth, double max_depth,
+                           const float *fresh, void *stream) {
   KF_REQUIRE(g && depth && c2w && K, "NULL argument");
   KF_REQUIRE(width > 0 && height > 0, "depth frame size must be positive");
+  KF_REQUIRE(pixel_bytes == sizeof(float) || scale > 0.0, "depth scale must be positive");
   cudaStream_t s = kf_stream(stream);
   double w2c[16];
   KF_REQUIRE(invert4(c2w, w2c), "camera pose is singular");
   const void *dev = nullptr;
-  int rc = stage_depth(g, depth, (size_t)width * height * sizeof(float), s, &dev);
+  int rc = stage_depth(g, depth, (size_t)width * height * pixel_bytes, s, &dev);
   if (rc) return rc;
-  return kf_launch_integrate(g, (const float *)dev, width, height, w2c, K, min_depth, max_depth, s);
+  if (pixel_bytes == sizeof(float))
+    return kf_launch_integrate(g, (const float *)dev, width, height, w2c, K, min_depth, max_depth, fresh, s);
+  return kf_launch_integrate_u16(g, (const uint16_t *)dev, scale, width, height, w2c, K, min_depth, max_depth,
+                                 fresh, s);
+}
+
+extern "C" int kf_integrate_depth(kf_grid g, const float *depth, int width, int height,
+                                  const double c2w[16], const double K[9], double min_depth,
+                                  double max_depth, void *stream) {
+  return integrate_entry(g, depth, sizeof(float), width, height, 0.0, c2w, K, min_depth, max_depth, nullptr,
+                         stream);
 }
 
 extern "C" int kf_integrate_depth_u16(kf_grid g, const uint16_t *depth, int width, int height, double scale,
                                       const double c2w[16], const double K[9], double min_depth,
                                       double max_depth, void *stream) {
-  KF_REQUIRE(g && depth && c2w && K, "NULL argument");
-  KF_REQUIRE(width > 0 && height > 0, "depth frame size must be positive");
-  KF_REQUIRE(scale > 0.0, "depth scale must be positive");
-  cudaStream_t s = kf_stream(stream);
-  double w2c[16];
-  KF_REQUIRE(invert4(c2w, w2c), "camera pose is singular");
-  const void *dev = nullptr;
-  int rc = stage_depth(g, depth, (size_t)width * height * sizeof(uint16_t), s, &dev);
+  return integrate_entry(g, depth, sizeof(uint16_t), width, height, scale, c2w, K, min_depth, max_depth, nullptr,
+                         stream);
+}
+
+extern "C" int kf_compute_sdf(kf_grid g, const kf_params *p, const float *depth, int width, int height,
+                              const double c2w[16], const double K[9], double min_depth, double max_depth,
+                              void *stream) {
+  int rc = kf_check_params(p);
   if (rc) return rc;
-  return kf_launch_integrate_u16(g, (const uint16_t *)dev, scale, width, height, w2c, K, min_depth, max_depth,
-                                 s);
+  const float fresh = (float)(p->max_surface + p->epsilon);  // kf_grid_reset's value
+  return integrate_entry(g, depth, sizeof(float), width, height, 0.0, c2w, K, min_depth, max_depth, &fresh,
+                         stream);
+}
+
+extern "C" int kf_compute_sdf_u16(kf_grid g, const kf_params *p, const uint16_t *depth, int width, int height,
+                                  double scale, const double c2w[16], const double K[9], double min_depth,
+                                  double max_depth, void *stream) {
+  int rc = kf_check_params(p);
+  if (rc) return rc;
+  const float fresh = (float)(p->max_surface + p->epsilon);
+  return integrate_entry(g, depth, sizeof(uint16_t), width, height, scale, c2w, K, min_depth, max_depth, &fresh,
+                         stream);
 }
 
 extern "C" int kf_warp(kf_grid g, kf_field psi, const kf_params *p, void *stream) {

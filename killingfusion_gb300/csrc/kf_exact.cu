@@ -60,6 +60,7 @@ struct IntegrateArgs {
   float e0, e1, e2;                    // error bounds of the float camera rows (launch_integrate)
   float ku0, ku1, kv0, kv1;            // 1.5 |K[0]|, 1.5 |K[1]|, 1.5 |K[3]|, 1.5 |K[4]|
   float c2_min;                        // smallest |camera depth| the float path takes
+  float fresh_phi;                     // a fresh grid's phi (k_integrate<D, true>)
   double voxel, min0, min1, min2, unknown_clip, min_depth, max_depth;
   float min_depth_up, max_depth_down;  // float neighbours of the depth range
   double depth_scale;                  // metres per unit of 16-bit depth
@@ -100,17 +101,19 @@ __device__ __forceinline__ int pixel_of(double u) {
 // depth zc are known.  With w == 0 and a finite phi the mean
 // (phi*0 + dist)/1 is dist itself, so the float64 multiply and divide are
 // skipped.  wi and ph are the voxel's weight and value, loaded by the caller.
-__device__ __forceinline__ void integrate_update(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
+// False when the voxel is not integrated (nothing written).
+__device__ __forceinline__ bool integrate_update(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
                                                  double depth, double zc, const IntegrateArgs &a, int32_t wi,
                                                  float ph) {
   const double dist = depth - zc;
-  if (dist < -a.unknown_clip) return;
+  if (dist < -a.unknown_clip) return false;
   if (wi == 0 && isfinite(ph)) {
     phi[i] = (float)dist;
   } else {
     phi[i] = (float)(((double)ph * (double)wi + dist) / (double)(wi + 1));
   }
   w[i] = wi + 1;
+  return true;
 }
 
 // The depth at pixel k as the reference reads it (a double) and its range
@@ -182,10 +185,14 @@ __global__ void k_integrate_tables(double *__restrict__ tx, double *__restrict__
 // A fresh voxel (w == 0, phi finite) on float depth df, in float-float: the
 // distance df - zc with the camera depth zc from the pair tables, the
 // unknown-clip test and the float rounding, all decided when they lie
-// farther than a.tol from the reference's float64 boundaries.  Returns false
-// (nothing written) when one of them is too close to call.
-__device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
-                                                   float df, FF zc, const IntegrateArgs &a) {
+// farther than a.tol from the reference's float64 boundaries.  Returns
+// kFfWritten (phi and w written), kFfClipped (not integrated, nothing
+// written) or kFfUndecided (nothing written) when one of them is too close
+// to call.
+enum FfOutcome { kFfUndecided = 0, kFfWritten = 1, kFfClipped = 2 };
+
+__device__ __forceinline__ int integrate_fresh_ff(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i,
+                                                  float df, FF zc, const IntegrateArgs &a) {
   const FF dist = ff_add_short(FF{df, 0.f}, ff_neg(zc));
   // dist + unknown_clip < 0: not integrated.  One float add decides it: its
   // error is below 2^-23 (|mf| + |unknown_clip|) plus the distance's, which
@@ -194,17 +201,17 @@ __device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int3
   const float mf = __fadd_rn(dist.hi, a.cliph);
   if (!(fabsf(mf) > a.clip_thr)) {
     const FF m = ff_add(dist, FF{a.cliph, a.clipl});
-    if (!(fabsf(m.hi) > a.tol)) return false;
-    if (m.hi < 0.f) return true;
+    if (!(fabsf(m.hi) > a.tol)) return kFfUndecided;
+    if (m.hi < 0.f) return kFfClipped;
   } else if (mf < 0.f) {
-    return true;
+    return kFfClipped;
   }
   bool ambiguous;
   const float r = ff_round_checked(dist, a.tol, ambiguous);
-  if (ambiguous) return false;
+  if (ambiguous) return kFfUndecided;
   phi[i] = r;
   w[i] = 1;
-  return true;
+  return kFfWritten;
 }
 
 // SDF::integrateDepthFrame for one voxel per thread.  The pixel a voxel reads
@@ -233,7 +240,11 @@ __device__ __forceinline__ bool integrate_fresh_ff(float *__restrict__ phi, int3
 // The distance and the running mean are float64 as in the reference, decided
 // in float-float for a fresh voxel (integrate_fresh_ff), with the camera
 // depth summed from the tables' pairs there.
-template <typename D>
+//
+// kFresh: the grid is taken as just reset (phi = a.fresh_phi, w = 0; nothing
+// read) and every voxel is written, the reset values where nothing is
+// integrated (KillingFusion::computeSDF: a new SDF, then the frame).
+template <typename D, bool kFresh>
 __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a full SM
     k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
                 const D *__restrict__ depth, const double *__restrict__ tx, const double *__restrict__ ty,
@@ -246,8 +257,14 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
   const int64_t i = ((int64_t)z * ny + y) * nx + x;
   // the voxel's weight and value, loaded first so that their latency runs
   // under the projection's arithmetic
-  const int32_t wi = w[i];
-  const float ph = phi[i];
+  const int32_t wi = kFresh ? 0 : w[i];
+  const float ph = kFresh ? a.fresh_phi : phi[i];
+  const auto leave = [&]() {  // nothing integrated here
+    if (kFresh) {
+      phi[i] = a.fresh_phi;
+      w[i] = 0;
+    }
+  };
   const float4 px = __ldg(tp + x), py = __ldg(tp + nx + y), pz = __ldg(tp + nx + ny + z);
   const float c0 = __fadd_rn(__fadd_rn(px.x, py.x), pz.x);
   const float c1 = __fadd_rn(__fadd_rn(px.y, py.y), pz.y);
@@ -268,6 +285,7 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
   const unsigned act = __activemask();
   const unsigned need = __ballot_sync(act, !sure);
   if (!sure) {
+    leave();  // (before the float64 path reads the voxel)
     const int lane = threadIdx.x & 31;  // blockDim.x == 32
     const int leader = __ffs(need) - 1;
     unsigned base = 0;
@@ -284,22 +302,28 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
   int row = (int)floorf(vf + 1.0f);
   if (uf < -1.0f) col = -1;  // roundf(u + 0.5) < 0: outside
   if (vf < -1.0f) row = -1;
-  if (col < 0 || col >= a.width) return;
-  if (row < 0 || row >= a.height) return;
+  if (col < 0 || col >= a.width || row < 0 || row >= a.height) {
+    leave();
+    return;
+  }
   const int64_t k = (int64_t)row * a.width + col;
   if constexpr (sizeof(D) == 4) {
     // float depth into a fresh voxel: float-float, float64 only when too close to call
     const float df = depth[k];
-    if (df < a.min_depth_up || df > a.max_depth_down) return;  // (a NaN passes, as in the reference)
-    if (wi == 0 && isfinite(ph) && isfinite(df) &&
-        integrate_fresh_ff(phi, w, i, df,
-                           ff_add_short(ff_add_short(FF{px.z, px.w}, FF{py.z, py.w}), FF{pz.z, pz.w}), a))
+    if (df < a.min_depth_up || df > a.max_depth_down) {  // (a NaN passes, as in the reference)
+      leave();
       return;
+    }
+    if (wi == 0 && isfinite(ph) && isfinite(df)) {
+      const int r = integrate_fresh_ff(phi, w, i, df,
+                                       ff_add_short(ff_add_short(FF{px.z, px.w}, FF{py.z, py.w}), FF{pz.z, pz.w}), a);
+      if (r == kFfClipped) leave();
+      if (r != kFfUndecided) return;
+    }
   }
   double dd;
-  if (!depth_at(depth, k, a, dd)) return;
   const double zd = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
-  integrate_update(phi, w, i, dd, zd, a, wi, ph);
+  if (!depth_at(depth, k, a, dd) || !integrate_update(phi, w, i, dd, zd, a, wi, ph)) leave();
 }
 
 // The listed voxels of k_integrate, each on the float64 path.
@@ -324,7 +348,7 @@ __global__ void __launch_bounds__(kBlock) k_integrate_exact(float *__restrict__ 
 template <typename D>
 static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, int width, int height,
                             const double w2c[16], const double K[9], double min_depth, double max_depth,
-                            cudaStream_t s) {
+                            const float *fresh_phi, cudaStream_t s) {
   IntegrateArgs a;
   for (int k = 0; k < 16; ++k) a.W[k] = w2c[k];
   for (int k = 0; k < 9; ++k) a.K[k] = K[k];
@@ -346,6 +370,7 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   a.height = height;
   a.count = g->count;
   a.depth_scale = depth_scale;
+  a.fresh_phi = fresh_phi ? *fresh_phi : 0.0f;
   ff_split_host(g->unknown_clip, a.cliph, a.clipl);
   {
     // the float-float distance is within a few 2^-46 of the magnitudes it
@@ -404,8 +429,12 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   k_integrate_tables<<<blocks_for(nx + ny + nz), kBlock, 0, s>>>(tx, ty, tz, tp, nx, ny, nz, a);
   dim3 block(32, kBlock / 32);
   dim3 grid((nx + 31) / 32, (ny + block.y - 1) / block.y, nz);
-  k_integrate<D><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list, list_n, cap,
-                                        a);
+  if (fresh_phi)
+    k_integrate<D, true><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list, list_n,
+                                                cap, a);
+  else
+    k_integrate<D, false><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list,
+                                                 list_n, cap, a);
   k_integrate_exact<D><<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list,
                                                                      list_n, cap, a);
   KF_CHECK_LAUNCH("k_integrate");
@@ -413,14 +442,15 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
 }
 
 int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height, const double w2c[16],
-                        const double K[9], double min_depth, double max_depth, cudaStream_t s) {
-  return launch_integrate(g, depth_dev, 0.0, width, height, w2c, K, min_depth, max_depth, s);
+                        const double K[9], double min_depth, double max_depth, const float *fresh_phi,
+                        cudaStream_t s) {
+  return launch_integrate(g, depth_dev, 0.0, width, height, w2c, K, min_depth, max_depth, fresh_phi, s);
 }
 
 int kf_launch_integrate_u16(kf_grid g, const uint16_t *depth_dev, double scale, int width, int height,
                             const double w2c[16], const double K[9], double min_depth, double max_depth,
-                            cudaStream_t s) {
-  return launch_integrate(g, depth_dev, scale, width, height, w2c, K, min_depth, max_depth, s);
+                            const float *fresh_phi, cudaStream_t s) {
+  return launch_integrate(g, depth_dev, scale, width, height, w2c, K, min_depth, max_depth, fresh_phi, s);
 }
 
 namespace {

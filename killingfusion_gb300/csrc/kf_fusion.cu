@@ -124,9 +124,7 @@ extern "C" int kf_fusion_process_frame(kf_fusion f, const float *depth, const do
   int rc = KF_OK;
   if (f->frames == 0) {
     // the first frame becomes the canonical SDF (KillingFusion.cpp:115-121)
-    rc = kf_grid_reset(f->can, p, s);
-    if (!rc) rc = kf_integrate_depth(f->can, depth, c.width, c.height, pose, c.K, c.min_depth,
-                                     c.max_depth, s);
+    rc = kf_compute_sdf(f->can, p, depth, c.width, c.height, pose, c.K, c.min_depth, c.max_depth, s);
     if (!rc) rc = kf_field_zero(f->psi, s);
     if (!rc && (meshes & KF_MESH_LIVE)) rc = mesh_to_host(f, f->can, 0, &r.ntri[0], s);
     if (!rc && (meshes & KF_MESH_REGISTERED)) {
@@ -139,9 +137,7 @@ extern "C" int kf_fusion_process_frame(kf_fusion f, const float *depth, const do
     }
   } else {
     // computeSDF, zero psi, register, mesh, warp + fuse (KillingFusion.cpp:130-160)
-    rc = kf_grid_reset(f->live, p, s);
-    if (!rc) rc = kf_integrate_depth(f->live, depth, c.width, c.height, pose, c.K, c.min_depth,
-                                     c.max_depth, s);
+    rc = kf_compute_sdf(f->live, p, depth, c.width, c.height, pose, c.K, c.min_depth, c.max_depth, s);
     if (!rc) rc = kf_field_zero(f->psi, s);
     // the live mesh queues behind the solve without the host waiting in
     // between; the solve's status is read before warp + fuse changes the

@@ -190,12 +190,14 @@ int kf_num_sms();
 // launches implemented in kf_exact.cu (float64 arithmetic without fused
 // multiply-add where the reference's rounding decides a discrete outcome)
 int kf_grid_ensure_alt(kf_grid g);
+// fresh_phi == NULL: integrate into the grid as it is; otherwise the grid is
+// taken as reset to (*fresh_phi, 0) and every voxel is written
 int kf_launch_integrate_u16(kf_grid g, const uint16_t *depth_dev, double scale, int width, int height,
                             const double w2c[16], const double K[9], double min_depth, double max_depth,
-                            cudaStream_t s);
+                            const float *fresh_phi, cudaStream_t s);
 int kf_launch_integrate(kf_grid g, const float *depth_dev, int width, int height,
                         const double w2c[16], const double K[9], double min_depth,
-                        double max_depth, cudaStream_t s);
+                        double max_depth, const float *fresh_phi, cudaStream_t s);
 int kf_launch_warp(kf_grid g, kf_field psi, const DevParams &dp, cudaStream_t s);
 int kf_launch_fuse(kf_grid can, kf_grid other, cudaStream_t s);
 int kf_launch_warp_fuse(kf_grid can, kf_grid live, kf_field psi, const DevParams &dp,

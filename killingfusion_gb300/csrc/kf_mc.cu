@@ -41,6 +41,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kRounds = 8;
 constexpr int kCellsPerBlock = kThreads * kRounds;
+constexpr int kCountCtasPerSm = 3;  // resident CTAs of k_mc_count_list per SM
 constexpr int kScanPerThread = 32;
 constexpr int kScanChunk = kThreads * kScanPerThread;
 
@@ -274,84 +275,97 @@ struct McList {
   unsigned cap;          // entries `cells` holds (0: list nothing)
 };
 
-// Pass 1 of kf_mc_run.  Warp w of block b takes the 256 cells from
-// b * kCellsPerBlock + 256 w on, in kRounds rounds of 32 (lane l the cell
-// 32 r + l of round r: the loads coalesce, and the band cells of a surface
-// spread over the lanes).  The band cells gather their corners; the warp's
-// triangle total and the block's warp totals give each warp its offset in
-// the block, and a warp scan per round each cell's.  The cells with
-// triangles are appended to the list, one atomic per warp; an entry carries
-// the cell's position among the block's triangles, so the list's order does
-// not matter.
-__global__ void __launch_bounds__(kThreads, 6)  // 40 registers: 6 CTAs per SM
+// Pass 1 of kf_mc_run, a resident grid: CTA c takes the blocks c, c + G,
+// c + 2G, ... (G CTAs), loading the next block's cells while it classifies
+// the current one.  Warp w of a block takes the 256 cells from 256 w on, in
+// kRounds rounds of 32 (lane l the cell 32 r + l of round r: the loads
+// coalesce, and the band cells of a surface spread over the lanes).  The
+// band cells gather their corners; the warp's triangle total and the
+// block's warp totals give each warp its offset in the block, and a warp
+// scan per round each cell's.  The cells with triangles are appended to the
+// list, one atomic per warp; an entry carries the cell's position among the
+// block's triangles, so the list's order does not matter.
+__global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     k_mc_count_list(McGrid g, McList L, int64_t nblocks) {
   constexpr int kWarpCells = kRounds * 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t wbase = (int64_t)blockIdx.x * kCellsPerBlock + (int64_t)warp * kWarpCells + lane;
+  const int64_t lane_off = (int64_t)warp * kWarpCells + lane;
+  __shared__ uint32_t s_warp[2][kThreads / 32];  // alternate blocks use alternate rows
   float d[kRounds];
+  int64_t b = blockIdx.x;
 #pragma unroll
-  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, wbase + 32 * r);
-  unsigned band = 0;
+  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, b * kCellsPerBlock + lane_off + 32 * r);
+  for (int parity = 0; b < nblocks; b += gridDim.x, parity ^= 1) {
+    const int64_t wbase = b * kCellsPerBlock + lane_off;
+    // the next block's cells, in flight while this one is classified
+    float nxt[kRounds];
+    const int64_t bn = b + gridDim.x;
 #pragma unroll
-  for (int r = 0; r < kRounds; ++r)
-    if (!(d[r] > g.hi || d[r] < g.lo)) band |= 1u << r;  // SDF.cpp:407 (a NaN is not skipped)
-  uint32_t n = 0, counts = 0;  // counts: 4 bits per round (at most 5 triangles)
-  uint64_t cubes = 0;          // 8 bits per round
-  for (unsigned rest = band; rest; rest &= rest - 1) {
-    const int r = __ffs(rest) - 1;
-    const int64_t i = wbase + 32 * r;
-    int x, y, z;
-    float val[8];
-    const int cube = classify(g, i, __ldg(g.phi + i), x, y, z, val);
-    const uint32_t c = (uint32_t)cube_tris(cube);
-    n += c;
-    counts |= c << (4 * r);
-    cubes |= (uint64_t)(cube & 255) << (8 * r);
-  }
-  // the warps' totals and offsets in the block
-  __shared__ uint32_t s_warp[kThreads / 32];
-  const uint32_t warp_total = __reduce_add_sync(0xffffffffu, n);
-  if (lane == 0) s_warp[warp] = warp_total;
-  __syncthreads();
-  uint32_t run = 0, total = 0;
+    for (int r = 0; r < kRounds; ++r) nxt[r] = own_value(g, bn * kCellsPerBlock + lane_off + 32 * r);
+    unsigned band = 0;
 #pragma unroll
-  for (int w = 0; w < kThreads / 32; ++w) {
-    const uint32_t t = s_warp[w];
-    run += w < warp ? t : 0u;
-    total += t;
-  }
-  if (warp_total) {
-    // one slot per cell with triangles
-    unsigned m = 0;
-#pragma unroll
-    for (int r = 0; r < kRounds; ++r) m += ((counts >> (4 * r)) & 15u) != 0u;
-    unsigned incl = m;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += t;
+    for (int r = 0; r < kRounds; ++r)
+      if (!(d[r] > g.hi || d[r] < g.lo)) band |= 1u << r;  // SDF.cpp:407 (a NaN is not skipped)
+    uint32_t n = 0, counts = 0;  // counts: 4 bits per round (at most 5 triangles)
+    uint64_t cubes = 0;          // 8 bits per round
+    for (unsigned rest = band; rest; rest &= rest - 1) {
+      const int r = __ffs(rest) - 1;
+      const int64_t i = wbase + 32 * r;
+      int x, y, z;
+      float val[8];
+      const int cube = classify(g, i, __ldg(g.phi + i), x, y, z, val);
+      const uint32_t c = (uint32_t)cube_tris(cube);
+      n += c;
+      counts |= c << (4 * r);
+      cubes |= (uint64_t)(cube & 255) << (8 * r);
     }
-    unsigned base = 0;
-    if (lane == 31) base = atomicAdd(L.n_cells, incl);
-    unsigned slot = __shfl_sync(0xffffffffu, base, 31) + incl - m;
+    // the warps' totals and offsets in the block
+    const uint32_t warp_total = __reduce_add_sync(0xffffffffu, n);
+    if (lane == 0) s_warp[parity][warp] = warp_total;
+    __syncthreads();
+    uint32_t run = 0, total = 0;
 #pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      const uint32_t c = (counts >> (4 * r)) & 15u;
-      if (!__any_sync(0xffffffffu, c != 0u)) continue;  // a round without triangles
-      uint32_t ci = c;  // inclusive scan of the round's counts over the lanes
+    for (int w = 0; w < kThreads / 32; ++w) {
+      const uint32_t t = s_warp[parity][w];
+      run += w < warp ? t : 0u;
+      total += t;
+    }
+    if (threadIdx.x == 0) L.block_tris[b] = total;
+    if (warp_total) {
+      // one slot per cell with triangles
+      unsigned m = 0;
+#pragma unroll
+      for (int r = 0; r < kRounds; ++r) m += ((counts >> (4 * r)) & 15u) != 0u;
+      unsigned incl = m;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, ci, o);
-        if (lane >= o) ci += t;
+        const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
       }
-      if (c) {
-        if (slot < L.cap)
-          L.cells[slot] = make_uint2((uint32_t)(wbase + 32 * r),
-                                     ((run + ci - c) << 8) | (uint32_t)((cubes >> (8 * r)) & 255u));
-        ++slot;
+      unsigned base = 0;
+      if (lane == 31) base = atomicAdd(L.n_cells, incl);
+      unsigned slot = __shfl_sync(0xffffffffu, base, 31) + incl - m;
+#pragma unroll
+      for (int r = 0; r < kRounds; ++r) {
+        const uint32_t c = (counts >> (4 * r)) & 15u;
+        if (!__any_sync(0xffffffffu, c != 0u)) continue;  // a round without triangles
+        uint32_t ci = c;  // inclusive scan of the round's counts over the lanes
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(0xffffffffu, ci, o);
+          if (lane >= o) ci += t;
+        }
+        if (c) {
+          if (slot < L.cap)
+            L.cells[slot] = make_uint2((uint32_t)(wbase + 32 * r),
+                                       ((run + ci - c) << 8) | (uint32_t)((cubes >> (8 * r)) & 255u));
+          ++slot;
+        }
+        run += __shfl_sync(0xffffffffu, ci, 31);
       }
-      run += __shfl_sync(0xffffffffu, ci, 31);
     }
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) d[r] = nxt[r];
   }
   // the last CTA to finish turns the totals into offsets (the classic
   // fence-and-count pattern: no CTA waits for another); every warp's
@@ -359,7 +373,6 @@ __global__ void __launch_bounds__(kThreads, 6)  // 40 registers: 6 CTAs per SM
   __shared__ bool s_last;
   __syncthreads();
   if (threadIdx.x == 0) {
-    L.block_tris[blockIdx.x] = total;
     __threadfence();
     s_last = atomicAdd(L.done, 1u) == gridDim.x - 1;
   }
@@ -417,32 +430,40 @@ __device__ __forceinline__ void vinterp(const float p1[3], const float p2[3], fl
 }
 
 // Writes the n triangles of cell i (configuration `cube`) from position out
-// on; re-gathers the corners (band cells only, off the common path).
+// on; re-gathers the corners (band cells only, off the common path).  Each
+// triangle vertex is interpolated on its edge as VertexInterp does
+// (MarchingCubes.h:424-436): the corners' positions take two values per axis
+// and their values stay in registers, picked by selects, so nothing is
+// indexed by a per-thread value in local memory.
 __device__ __noinline__ void emit_cell(const McGrid &g, int64_t i, int cube, int64_t out,
                                        float *__restrict__ verts, int64_t capacity) {
   int x, y, z;
   float val[8];
   classify(g, i, __ldg(g.phi + i), x, y, z, val);
-  const int em = __ldg(&g_mc.edge[cube]);
-  float p[8][3];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    p[k][0] = (float)(x + c_mc.corner[k][0]) / g.hx - 1.0f;
-    p[k][1] = (float)(y + c_mc.corner[k][1]) / g.hy - 1.0f;
-    p[k][2] = (float)(z + c_mc.corner[k][2]) / g.hz - 1.0f;
-  }
-  float vl[12][3];
-#pragma unroll
-  for (int e = 0; e < 12; ++e)
-    if (em & (1 << e))
-      vinterp(p[c_mc.ends[e][0]], p[c_mc.ends[e][1]], val[c_mc.ends[e][0]], val[c_mc.ends[e][1]], vl[e]);
+  const float q[3][2] = {{(float)x / g.hx - 1.0f, (float)(x + 1) / g.hx - 1.0f},
+                         {(float)y / g.hy - 1.0f, (float)(y + 1) / g.hy - 1.0f},
+                         {(float)z / g.hz - 1.0f, (float)(z + 1) / g.hz - 1.0f}};
   const int n = __ldg(&g_mc.ntri[cube]);
   for (int t = 0; t < n; ++t, ++out) {
     if (out >= capacity) break;
     float *o = verts + 9 * out;
 #pragma unroll
     for (int j2 = 0; j2 < 3; ++j2) {
-      const float *v = vl[__ldg(&g_mc.tri[cube][3 * t + j2])];
+      const int e = __ldg(&g_mc.tri[cube][3 * t + j2]);
+      const int a = __ldg(&g_mc.ends[e][0]), b = __ldg(&g_mc.ends[e][1]);
+      float va = val[0], vb = val[0];
+#pragma unroll
+      for (int c = 1; c < 8; ++c) {
+        va = a == c ? val[c] : va;
+        vb = b == c ? val[c] : vb;
+      }
+      float pa[3], pb[3], v[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        pa[k] = __ldg(&g_mc.corner[a][k]) ? q[k][1] : q[k][0];
+        pb[k] = __ldg(&g_mc.corner[b][k]) ? q[k][1] : q[k][0];
+      }
+      vinterp(pa, pb, va, vb, v);
       o[3 * j2 + 0] = v[0];
       o[3 * j2 + 1] = -v[1];
       o[3 * j2 + 2] = v[2];
@@ -565,7 +586,8 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   L.cap = (unsigned)cap;
   // the counters start at zero; the count pass's last CTA leaves them so
   if (fresh) KF_CHECK_CUDA(cudaMemsetAsync(L.done, 0, 3 * sizeof(unsigned), s));
-  k_mc_count_list<<<(unsigned)nblocks, kThreads, 0, s>>>(mg, L, nblocks);
+  const unsigned count_grid = (unsigned)std::min<int64_t>(nblocks, (int64_t)kf_num_sms() * kCountCtasPerSm);
+  k_mc_count_list<<<count_grid, kThreads, 0, s>>>(mg, L, nblocks);
   KF_CHECK_LAUNCH("k_mc_count_list");
   if (ntri_async) {
     KF_CHECK_CUDA(cudaMemcpyAsync(ntri_async, total_dev, sizeof(int64_t), cudaMemcpyDefault, s));

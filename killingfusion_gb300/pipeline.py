@@ -60,17 +60,18 @@ class FramePipeline:
         self.ev_integ, self.ev_fused, self.ev_meshed, self.ev_copied = ev(), ev(), ev(), ev()
         self.stats = capi.SolveStats()
 
-    def _integrate(self, grid, depth, stream):
-        capi.check(self.L.kf_integrate_depth(grid.h, depth.data_ptr(), depth.shape[1], depth.shape[0],
-                                             self.eye, self.K, self.min_depth, self.max_depth,
-                                             stream.cuda_stream))
+    def _compute_sdf(self, grid, depth, stream):
+        """KillingFusion::computeSDF: the grid reset and the frame integrated
+        in one pass."""
+        capi.check(self.L.kf_compute_sdf(grid.h, C.byref(self.Pc), depth.data_ptr(), depth.shape[1],
+                                         depth.shape[0], self.eye, self.K, self.min_depth, self.max_depth,
+                                         stream.cuda_stream))
 
     def start(self, depth):
         """The first frame becomes the canonical SDF (KillingFusion.cpp:115-121).
         depth: a float32 [h, w] CUDA tensor or pinned host tensor."""
         self.torch.cuda.synchronize(self.dev)
-        self.can.reset(self.P, stream=self.s_main)
-        self._integrate(self.can, depth, self.s_main)
+        self._compute_sdf(self.can, depth, self.s_main)
         self.s_main.synchronize()
 
     def queue(self, f: int, depth):
@@ -82,8 +83,7 @@ class FramePipeline:
         cptr = self.counts.data_ptr() + 24 * k
         s_in, s_main, s_out = self.s_in, self.s_main, self.s_out
         s_in.wait_event(self.ev_meshed[k])
-        lv.reset(self.P, stream=s_in)
-        self._integrate(lv, depth, s_in)
+        self._compute_sdf(lv, depth, s_in)
         ps.zero(stream=s_in)
         s_in.wait_event(self.ev_copied[k])
         capi.check(L.kf_marching_cubes_async(lv.h, C.byref(Pc), ms[0].data_ptr(), self.cap, cptr,

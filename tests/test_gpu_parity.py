@@ -106,6 +106,42 @@ def test_integrate_far_from_origin(gpu, oracle, shift):
         assert (w > 0).sum() > 1000
 
 
+@pytest.mark.parametrize("case", ["float", "float_far", "u16"])
+def test_compute_sdf_equals_reset_then_integrate(gpu, case):
+    """kf_compute_sdf (KillingFusion::computeSDF in one pass) leaves the grid
+    bit for bit as kf_grid_reset followed by kf_integrate_depth does, also
+    when the grid held other values before (every voxel is written)."""
+    grid, frames = synth.sphere_pair()
+    P = gpu.Params.paper(grid.voxel)
+    c2w, origin = None, grid.origin
+    if case == "float_far":
+        c2w = np.eye(4)
+        c2w[:3, 3] = (120.0, -75.0, 300.0)
+        origin = np.asarray(grid.origin) + c2w[:3, 3]
+    rng = np.random.default_rng(51)
+    for f in frames:
+        a = gpu.Grid(grid.dims, grid.voxel, origin, P.unknown_clip, P)
+        b = gpu.Grid(grid.dims, grid.voxel, origin, P.unknown_clip, P)
+        shape = grid.dims[::-1]
+        b.upload(rng.normal(0, 1, shape).astype(np.float32), rng.integers(0, 9, shape).astype(np.int32))
+        if case == "u16":
+            d16 = np.where(np.isfinite(f), np.round(f * 1000.0), 0).astype(np.uint16)
+            a.reset(P)
+            a.integrate_u16(d16, 0.001, c2w, min_depth=0.05, max_depth=1.2)
+            b.compute_sdf(P, d16, c2w, min_depth=0.05, max_depth=1.2, u16_scale=0.001)
+        else:
+            a.reset(P)
+            a.integrate(f, c2w, min_depth=0.05, max_depth=1.2)
+            b.compute_sdf(P, f, c2w, min_depth=0.05, max_depth=1.2)
+        pa, wa = a.download()
+        pb, wb = b.download()
+        a.close()
+        b.close()
+        np.testing.assert_array_equal(wb, wa)
+        np.testing.assert_array_equal(pb.view(np.int32), pa.view(np.int32))
+        assert (wa > 0).sum() > 1000
+
+
 # ---------------------------------------------------------------------------
 # reference gradient at single voxels
 # ---------------------------------------------------------------------------
