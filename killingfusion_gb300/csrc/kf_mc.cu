@@ -42,6 +42,7 @@ constexpr int kThreads = 256;
 constexpr int kRounds = 8;
 constexpr int kCellsPerBlock = kThreads * kRounds;
 constexpr int kCountCtasPerSm = 3;  // resident CTAs of k_mc_count_list per SM
+constexpr int kWarpCells = kRounds * 32;  // a warp block of k_mc_count_list
 constexpr int kScanPerThread = 32;
 constexpr int kScanChunk = kThreads * kScanPerThread;
 
@@ -222,8 +223,9 @@ __global__ void __launch_bounds__(kThreads) k_mc_scan(const uint32_t *block_tris
 // whose last CTA runs it, keeps its shared memory small): thread t sums the
 // kScanPerThread totals from c0 + t * kScanPerThread on with 16-byte loads,
 // the block scans the sums, and the thread reads its totals again to write
-// their offsets.  block_tris and block_off are 16-byte aligned.
-__device__ void scan_block_totals_regs(const uint32_t *block_tris, int64_t nblocks, int64_t *block_off,
+// their offsets and clear them (the count pass adds into zeroed totals).
+// block_tris and block_off are 16-byte aligned.
+__device__ void scan_block_totals_regs(uint32_t *block_tris, int64_t nblocks, int64_t *block_off,
                                        int64_t *grand_total) {
   uint64_t carry = 0;
   for (int64_t c0 = 0; c0 < nblocks; c0 += kScanChunk) {
@@ -243,7 +245,7 @@ __device__ void scan_block_totals_regs(const uint32_t *block_tris, int64_t nbloc
     uint64_t total;
     uint64_t excl = carry + block_exclusive_scan<uint64_t>(sum, &total);
     if (whole) {
-      const uint4 *p = reinterpret_cast<const uint4 *>(block_tris + first);
+      uint4 *p = reinterpret_cast<uint4 *>(block_tris + first);
       longlong2 *o = reinterpret_cast<longlong2 *>(block_off + first);
 #pragma unroll
       for (int j = 0; j < kScanPerThread / 4; ++j) {
@@ -251,12 +253,14 @@ __device__ void scan_block_totals_regs(const uint32_t *block_tris, int64_t nbloc
         const int64_t a = (int64_t)excl, b = a + v.x, c = b + v.y, d = c + v.z;
         o[2 * j] = make_longlong2(a, b);
         o[2 * j + 1] = make_longlong2(c, d);
+        p[j] = make_uint4(0u, 0u, 0u, 0u);
         excl = (uint64_t)(d + v.w);
       }
     } else {
       for (int64_t i = first; i < nblocks; ++i) {
         block_off[i] = (int64_t)excl;
         excl += __ldcg(block_tris + i);
+        block_tris[i] = 0u;
       }
     }
     carry += total;
@@ -266,42 +270,41 @@ __device__ void scan_block_totals_regs(const uint32_t *block_tris, int64_t nbloc
 
 // Scratch of kf_mc_run's two passes.
 struct McList {
-  uint32_t *block_tris;  // triangles per block
+  uint32_t *block_tris;  // triangles per block (zero between calls: the scan clears it)
   int64_t *block_off;    // exclusive offsets per block, then the grand total
-  uint2 *cells;          // per listed cell: index, (offset in its block << 8) | configuration
+  uint32_t *warp_tris;   // triangles per warp block (kWarpCells cells), 8 per block
+  uint2 *cells;          // per listed cell: index, (offset in its warp block << 8) | configuration
   unsigned *done;        // CTAs of the count pass finished (the last one resets it)
   unsigned *n_cells;     // cells appended by the count pass (the last CTA resets it)
   unsigned *n_listed;    // their final number, for the emit pass
   unsigned cap;          // entries `cells` holds (0: list nothing)
 };
 
-// Pass 1 of kf_mc_run, a resident grid: CTA c takes the blocks c, c + G,
-// c + 2G, ... (G CTAs), loading the next block's cells while it classifies
-// the current one.  Warp w of a block takes the 256 cells from 256 w on, in
-// kRounds rounds of 32 (lane l the cell 32 r + l of round r: the loads
-// coalesce, and the band cells of a surface spread over the lanes).  The
-// band cells gather their corners; the warp's triangle total and the
-// block's warp totals give each warp its offset in the block, and a warp
-// scan per round each cell's.  The cells with triangles are appended to the
-// list, one atomic per warp; an entry carries the cell's position among the
-// block's triangles, so the list's order does not matter.
+// Pass 1 of kf_mc_run, a resident grid of independent warps: warp v of the
+// grid takes the warp blocks (kWarpCells consecutive cells) v, v + V, v +
+// 2V, ... (V warps), loading the next one's cells while it classifies the
+// current one, and never waits for another warp.  Lane l takes the cell
+// 32 r + l of round r: the loads coalesce, and the band cells of a surface
+// spread over the lanes.  The band cells gather their corners; a warp scan
+// per round gives each cell its offset among the warp block's triangles.
+// The cells with triangles are appended to the list, one atomic per warp
+// block; an entry carries that offset, so the list's order does not matter.
+// The warp block's total is stored and added to its block's.
 __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     k_mc_count_list(McGrid g, McList L, int64_t nblocks) {
-  constexpr int kWarpCells = kRounds * 32;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t lane_off = (int64_t)warp * kWarpCells + lane;
-  __shared__ uint32_t s_warp[2][kThreads / 32];  // alternate blocks use alternate rows
+  const int lane = threadIdx.x & 31;
+  const int64_t nwb = (g.count + kWarpCells - 1) / kWarpCells;
+  const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
+  int64_t wb = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
   float d[kRounds];
-  int64_t b = blockIdx.x;
 #pragma unroll
-  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, b * kCellsPerBlock + lane_off + 32 * r);
-  for (int parity = 0; b < nblocks; b += gridDim.x, parity ^= 1) {
-    const int64_t wbase = b * kCellsPerBlock + lane_off;
-    // the next block's cells, in flight while this one is classified
+  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, wb * kWarpCells + 32 * r + lane);
+  for (; wb < nwb; wb += nwarps) {
+    const int64_t base = wb * kWarpCells + lane;
+    // the next warp block's cells, in flight while this one is classified
     float nxt[kRounds];
-    const int64_t bn = b + gridDim.x;
 #pragma unroll
-    for (int r = 0; r < kRounds; ++r) nxt[r] = own_value(g, bn * kCellsPerBlock + lane_off + 32 * r);
+    for (int r = 0; r < kRounds; ++r) nxt[r] = own_value(g, (wb + nwarps) * kWarpCells + 32 * r + lane);
     unsigned band = 0;
 #pragma unroll
     for (int r = 0; r < kRounds; ++r)
@@ -310,7 +313,7 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     uint64_t cubes = 0;          // 8 bits per round
     for (unsigned rest = band; rest; rest &= rest - 1) {
       const int r = __ffs(rest) - 1;
-      const int64_t i = wbase + 32 * r;
+      const int64_t i = base + 32 * r;
       int x, y, z;
       float val[8];
       const int cube = classify(g, i, __ldg(g.phi + i), x, y, z, val);
@@ -319,19 +322,12 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
       counts |= c << (4 * r);
       cubes |= (uint64_t)(cube & 255) << (8 * r);
     }
-    // the warps' totals and offsets in the block
-    const uint32_t warp_total = __reduce_add_sync(0xffffffffu, n);
-    if (lane == 0) s_warp[parity][warp] = warp_total;
-    __syncthreads();
-    uint32_t run = 0, total = 0;
-#pragma unroll
-    for (int w = 0; w < kThreads / 32; ++w) {
-      const uint32_t t = s_warp[parity][w];
-      run += w < warp ? t : 0u;
-      total += t;
+    const uint32_t total = __reduce_add_sync(0xffffffffu, n);
+    if (lane == 0) {
+      L.warp_tris[wb] = total;
+      if (total) atomicAdd(L.block_tris + wb / (kCellsPerBlock / kWarpCells), total);
     }
-    if (threadIdx.x == 0) L.block_tris[b] = total;
-    if (warp_total) {
+    if (total) {
       // one slot per cell with triangles
       unsigned m = 0;
 #pragma unroll
@@ -342,9 +338,10 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
         const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += t;
       }
-      unsigned base = 0;
-      if (lane == 31) base = atomicAdd(L.n_cells, incl);
-      unsigned slot = __shfl_sync(0xffffffffu, base, 31) + incl - m;
+      unsigned slot = 0;
+      if (lane == 31) slot = atomicAdd(L.n_cells, incl);
+      slot = __shfl_sync(0xffffffffu, slot, 31) + incl - m;
+      uint32_t run = 0;
 #pragma unroll
       for (int r = 0; r < kRounds; ++r) {
         const uint32_t c = (counts >> (4 * r)) & 15u;
@@ -357,7 +354,7 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
         }
         if (c) {
           if (slot < L.cap)
-            L.cells[slot] = make_uint2((uint32_t)(wbase + 32 * r),
+            L.cells[slot] = make_uint2((uint32_t)(base + 32 * r),
                                        ((run + ci - c) << 8) | (uint32_t)((cubes >> (8 * r)) & 255u));
           ++slot;
         }
@@ -367,15 +364,13 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
 #pragma unroll
     for (int r = 0; r < kRounds; ++r) d[r] = nxt[r];
   }
-  // the last CTA to finish turns the totals into offsets (the classic
+  // the last CTA to finish turns the block totals into offsets (the classic
   // fence-and-count pattern: no CTA waits for another); every warp's
-  // appends are done before the CTA counts itself finished
+  // additions and appends are done before the CTA counts itself finished
   __shared__ bool s_last;
+  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(L.done, 1u) == gridDim.x - 1;
-  }
+  if (threadIdx.x == 0) s_last = atomicAdd(L.done, 1u) == gridDim.x - 1;
   __syncthreads();
   if (s_last) {
     __threadfence();
@@ -516,12 +511,20 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit_cells(McGrid g, McList L, 
       const uint2 c = L.cells[e];
       const int64_t i = c.x;
       if (!KF_IN_BOUNDS(i, g.count, KF_SITE_MC_BLOCK)) continue;
-      emit_cell(g, i, (int)(c.y & 255u), L.block_off[i / kCellsPerBlock] + (int64_t)(c.y >> 8), verts,
-                capacity);
+      // the warp block's offset: its block's plus its block's earlier warp blocks'
+      const int64_t wb = i / kWarpCells, b = wb / (kCellsPerBlock / kWarpCells);
+      const uint4 *wt = reinterpret_cast<const uint4 *>(L.warp_tris + b * (kCellsPerBlock / kWarpCells));
+      const uint4 t0 = __ldg(wt), t1 = __ldg(wt + 1);
+      const uint32_t tw[8] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w};
+      const int k = (int)(wb - b * (kCellsPerBlock / kWarpCells));
+      int64_t off = L.block_off[b];
+#pragma unroll
+      for (int j = 0; j < 7; ++j) off += j < k ? tw[j] : 0u;
+      emit_cell(g, i, (int)(c.y & 255u), off + (int64_t)(c.y >> 8), verts, capacity);
     }
   } else {
     for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x)
-      if (__ldg(L.block_tris + b)) emit_block(g, b, L.block_off[b], verts, capacity);
+      if (L.block_off[b + 1] > L.block_off[b]) emit_block(g, b, L.block_off[b], verts, capacity);
   }
 }
 
@@ -553,14 +556,17 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   int64_t nblocks = (g->count + kCellsPerBlock - 1) / kCellsPerBlock;
   // scratch, kept with the grid (calls on one grid are stream-ordered): the
   // per-block totals (u32), their offsets (i64) and the grand total right
-  // after them, three counters and the list of cells with triangles (count
-  // / 16 of them, at least 2^18; none for grids of 2^32 cells or more, whose
-  // indices the list does not hold)
-  const int64_t cap = g->count >= (int64_t)1 << 32 ? 0
-                                                   : std::min<int64_t>(g->count, std::max<int64_t>(g->count / 16, 1 << 18));
+  // after them, three counters, the per-warp-block totals (u32, 8 per block)
+  // and the list of cells with triangles (count / 16 of them, at least 2^18;
+  // none for grids of 2^32 cells or more, whose indices the list does not
+  // hold)
+  const int64_t cap = g->count >= (int64_t)1 << 32
+                          ? 0
+                          : std::min<int64_t>(g->count, std::max<int64_t>(g->count / 16, 1 << 18));
   const size_t off_off = ((size_t)nblocks * sizeof(uint32_t) + 255) & ~(size_t)255;
   const size_t cnt_off = off_off + (((size_t)nblocks + 1) * sizeof(int64_t) + 15) / 16 * 16;
-  const size_t list_off = cnt_off + 16;
+  const size_t warp_off = cnt_off + 16;
+  const size_t list_off = warp_off + (size_t)nblocks * (kCellsPerBlock / kWarpCells) * sizeof(uint32_t);
   const size_t bytes = list_off + (size_t)cap * sizeof(uint2);
   bool fresh = false;
   if (g->mc_bytes < bytes) {
@@ -582,10 +588,15 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   L.done = (unsigned *)((char *)g->mc + cnt_off);
   L.n_cells = L.done + 1;
   L.n_listed = L.done + 2;
+  L.warp_tris = (uint32_t *)((char *)g->mc + warp_off);
   L.cells = (uint2 *)((char *)g->mc + list_off);
   L.cap = (unsigned)cap;
-  // the counters start at zero; the count pass's last CTA leaves them so
-  if (fresh) KF_CHECK_CUDA(cudaMemsetAsync(L.done, 0, 3 * sizeof(unsigned), s));
+  // the block totals and the counters start at zero; the count pass's last
+  // CTA leaves them so
+  if (fresh) {
+    KF_CHECK_CUDA(cudaMemsetAsync(L.block_tris, 0, (size_t)nblocks * sizeof(uint32_t), s));
+    KF_CHECK_CUDA(cudaMemsetAsync(L.done, 0, 3 * sizeof(unsigned), s));
+  }
   const unsigned count_grid = (unsigned)std::min<int64_t>(nblocks, (int64_t)kf_num_sms() * kCountCtasPerSm);
   k_mc_count_list<<<count_grid, kThreads, 0, s>>>(mg, L, nblocks);
   KF_CHECK_LAUNCH("k_mc_count_list");
