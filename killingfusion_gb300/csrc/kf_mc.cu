@@ -41,7 +41,8 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kRounds = 8;
 constexpr int kCellsPerBlock = kThreads * kRounds;
-constexpr int kCountCtasPerSm = 3;  // resident CTAs of k_mc_count_list per SM
+constexpr int kCountCtasPerSm = 4;  // resident CTAs of k_mc_count_list per SM
+constexpr int kCountStages = 4;     // its ring of warp-block buffers (32 KB per CTA)
 constexpr int kWarpCells = kRounds * 32;  // a warp block of k_mc_count_list
 constexpr int kScanPerThread = 32;
 constexpr int kScanChunk = kThreads * kScanPerThread;
@@ -280,31 +281,62 @@ struct McList {
   unsigned cap;          // entries `cells` holds (0: list nothing)
 };
 
+// 16-byte asynchronous copy global -> shared (cp.async, L2 only) and its
+// group bookkeeping; a thread's wait covers only its own copies.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned dst = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // Pass 1 of kf_mc_run, a resident grid of independent warps: warp v of the
 // grid takes the warp blocks (kWarpCells consecutive cells) v, v + V, v +
-// 2V, ... (V warps), loading the next one's cells while it classifies the
-// current one, and never waits for another warp.  Lane l takes the cell
-// 32 r + l of round r: the loads coalesce, and the band cells of a surface
-// spread over the lanes.  The band cells gather their corners; a warp scan
-// per round gives each cell its offset among the warp block's triangles.
-// The cells with triangles are appended to the list, one atomic per warp
-// block; an entry carries that offset, so the list's order does not matter.
-// The warp block's total is stored and added to its block's.
+// 2V, ... (V warps) and never waits for another warp.  Each warp streams
+// its warp blocks through a ring of kCountStages shared-memory buffers with
+// cp.async, kCountStages - 1 blocks ahead, so that the loads in flight cost
+// no registers.  Lane l takes the cell 32 r + l of round r (the band cells
+// of a surface spread over the lanes).  The band cells gather their
+// corners; a warp scan per round gives each cell its offset among the warp
+// block's triangles.  The cells with triangles are appended to the list,
+// one atomic per warp block; an entry carries that offset, so the list's
+// order does not matter.  The warp block's total is stored and added to its
+// block's.
 __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     k_mc_count_list(McGrid g, McList L, int64_t nblocks) {
+  __shared__ __align__(16) float s_ring[kThreads / 32][kCountStages][kWarpCells];
   const int lane = threadIdx.x & 31;
+  float(*ring)[kWarpCells] = s_ring[threadIdx.x >> 5];
   const int64_t nwb = (g.count + kWarpCells - 1) / kWarpCells;
+  const int64_t whole = g.count / kWarpCells;  // warp blocks entirely inside the grid
   const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
-  int64_t wb = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
-  float d[kRounds];
+  const int64_t wb0 = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+  // lane l copies the 16-byte chunks l and l + 32 of a warp block (kWarpCells = 256
+  // cells = 64 chunks); a warp block past the whole ones is read directly
+  const auto issue = [&](int64_t wb, int stage) {
+    if (wb < whole) {
+      const float *src = g.phi + wb * kWarpCells;
+      cp_async16(&ring[stage][4 * lane], src + 4 * lane);
+      cp_async16(&ring[stage][4 * (lane + 32)], src + 4 * (lane + 32));
+    }
+    cp_async_commit();  // (an empty group where nothing was copied)
+  };
 #pragma unroll
-  for (int r = 0; r < kRounds; ++r) d[r] = own_value(g, wb * kWarpCells + 32 * r + lane);
-  for (; wb < nwb; wb += nwarps) {
+  for (int k = 0; k < kCountStages - 1; ++k) issue(wb0 + k * nwarps, k);
+  int stage = 0;
+  for (int64_t wb = wb0; wb < nwb; wb += nwarps, stage = stage == kCountStages - 1 ? 0 : stage + 1) {
+    // the buffer read in the previous round takes the block kCountStages - 1 ahead
+    issue(wb + (kCountStages - 1) * nwarps, stage == 0 ? kCountStages - 1 : stage - 1);
+    cp_async_wait<kCountStages - 1>();  // this lane's copies of the current block
+    __syncwarp();                        // ... and every lane's
     const int64_t base = wb * kWarpCells + lane;
-    // the next warp block's cells, in flight while this one is classified
-    float nxt[kRounds];
+    float d[kRounds];
 #pragma unroll
-    for (int r = 0; r < kRounds; ++r) nxt[r] = own_value(g, (wb + nwarps) * kWarpCells + 32 * r + lane);
+    for (int r = 0; r < kRounds; ++r) d[r] = wb < whole ? ring[stage][32 * r + lane] : own_value(g, base + 32 * r);
+    __syncwarp();  // the buffer is read before it is refilled
     unsigned band = 0;
 #pragma unroll
     for (int r = 0; r < kRounds; ++r)
@@ -361,9 +393,8 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
         run += __shfl_sync(0xffffffffu, ci, 31);
       }
     }
-#pragma unroll
-    for (int r = 0; r < kRounds; ++r) d[r] = nxt[r];
   }
+  cp_async_wait<0>();  // no copy outlives the warp (those past the end are empty)
   // the last CTA to finish turns the block totals into offsets (the classic
   // fence-and-count pattern: no CTA waits for another); every warp's
   // additions and appends are done before the CTA counts itself finished
@@ -528,6 +559,23 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit_cells(McGrid g, McList L, 
   }
 }
 
+// The count pass wants shared memory for kCountCtasPerSm rings of 32 KB per
+// SM: ask for the largest shared-memory carve-out, once per device (setting
+// it twice is harmless).
+void prefer_shared_for_count() {
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return;
+  }
+  if (done[dev]) return;
+  if (cudaFuncSetAttribute(k_mc_count_list, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+    cudaGetLastError();  // a preference only
+  done[dev] = true;
+}
+
 // Resident CTAs of the emit pass.
 unsigned emit_grid(int64_t nblocks) {
   return (unsigned)std::min<int64_t>(nblocks, (int64_t)kf_num_sms() * 8);
@@ -597,6 +645,7 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
     KF_CHECK_CUDA(cudaMemsetAsync(L.block_tris, 0, (size_t)nblocks * sizeof(uint32_t), s));
     KF_CHECK_CUDA(cudaMemsetAsync(L.done, 0, 3 * sizeof(unsigned), s));
   }
+  prefer_shared_for_count();
   const unsigned count_grid = (unsigned)std::min<int64_t>(nblocks, (int64_t)kf_num_sms() * kCountCtasPerSm);
   k_mc_count_list<<<count_grid, kThreads, 0, s>>>(mg, L, nblocks);
   KF_CHECK_LAUNCH("k_mc_count_list");
