@@ -6,11 +6,12 @@
 // its block's offset plus the triangles of the block's earlier cells.
 //
 // kf_mc_run (grids the library owns), two passes:
-//   1. k_mc_count_list: each CTA classifies a block of kCellsPerBlock cells,
-//      warp w the 256 from 256 w on (lane l the cells 32 r + l), and lists
-//      every cell with triangles: its index, configuration and offset in
-//      the block.  The last CTA to finish turns the block totals into
-//      offsets.
+//   1. k_mc_count_list: independent warps stream warp blocks of kWarpCells
+//      cells through shared memory (cp.async), classify them and list every
+//      cell with triangles: its index, configuration and offset in the warp
+//      block.  Warp-block totals are stored and added into the totals of the
+//      blocks of kCellsPerBlock cells; the last CTA to finish turns those
+//      into offsets.
 //   2. k_mc_emit_cells: one thread per listed cell writes its triangles.
 //      When a grid has more such cells than the list holds, it falls back
 //      to re-classifying every block with triangles (emit_block).
@@ -277,6 +278,7 @@ struct McList {
   uint2 *cells;          // per listed cell: index, (offset in its warp block << 8) | configuration
   unsigned *done;        // CTAs of the count pass finished (the last one resets it)
   unsigned *n_cells;     // cells appended by the count pass (the last CTA resets it)
+  unsigned long long *next_wb;  // the next warp block to claim (the last CTA resets it)
   unsigned *n_listed;    // their final number, for the emit pass
   unsigned cap;          // entries `cells` holds (0: list nothing)
 };
@@ -293,12 +295,11 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Pass 1 of kf_mc_run, a resident grid of independent warps: warp v of the
-// grid takes the warp blocks (kWarpCells consecutive cells) v, v + V, v +
-// 2V, ... (V warps) and never waits for another warp.  Each warp streams
-// its warp blocks through a ring of kCountStages shared-memory buffers with
-// cp.async, kCountStages - 1 blocks ahead, so that the loads in flight cost
-// no registers.  Lane l takes the cell 32 r + l of round r (the band cells
+// Pass 1 of kf_mc_run, a resident grid of independent warps: each warp
+// claims warp blocks (kWarpCells consecutive cells) from a counter and never
+// waits for another warp.  It streams them through a ring of kCountStages
+// shared-memory buffers with cp.async, kCountStages - 1 blocks ahead, so
+// that the loads in flight cost no registers.  Lane l takes the cell 32 r + l of round r (the band cells
 // of a surface spread over the lanes).  The band cells gather their
 // corners; a warp scan per round gives each cell its offset among the warp
 // block's triangles.  The cells with triangles are appended to the list,
@@ -308,12 +309,12 @@ __device__ __forceinline__ void cp_async_wait() {
 __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     k_mc_count_list(McGrid g, McList L, int64_t nblocks) {
   __shared__ __align__(16) float s_ring[kThreads / 32][kCountStages][kWarpCells];
-  const int lane = threadIdx.x & 31;
-  float(*ring)[kWarpCells] = s_ring[threadIdx.x >> 5];
+  __shared__ long long s_claimed[kThreads / 32][kCountStages];  // the warp block in each buffer
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float(*ring)[kWarpCells] = s_ring[warp];
+  long long *claimed = s_claimed[warp];
   const int64_t nwb = (g.count + kWarpCells - 1) / kWarpCells;
   const int64_t whole = g.count / kWarpCells;  // warp blocks entirely inside the grid
-  const int64_t nwarps = (int64_t)gridDim.x * (kThreads / 32);
-  const int64_t wb0 = (int64_t)blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
   // lane l copies the 16-byte chunks l and l + 32 of a warp block (kWarpCells = 256
   // cells = 64 chunks); a warp block past the whole ones is read directly
   const auto issue = [&](int64_t wb, int stage) {
@@ -324,12 +325,33 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     }
     cp_async_commit();  // (an empty group where nothing was copied)
   };
+  // warp blocks are claimed one at a time from a shared counter (the surface
+  // makes some much slower than others), one round before their copy is
+  // issued so that the claim's latency is hidden
+  unsigned long long pending = 0;
+  if (lane == 0) pending = atomicAdd(L.next_wb, 1ull);
 #pragma unroll
-  for (int k = 0; k < kCountStages - 1; ++k) issue(wb0 + k * nwarps, k);
-  int stage = 0;
-  for (int64_t wb = wb0; wb < nwb; wb += nwarps, stage = stage == kCountStages - 1 ? 0 : stage + 1) {
-    // the buffer read in the previous round takes the block kCountStages - 1 ahead
-    issue(wb + (kCountStages - 1) * nwarps, stage == 0 ? kCountStages - 1 : stage - 1);
+  for (int k = 0; k < kCountStages - 1; ++k) {
+    const int64_t wb = (int64_t)__shfl_sync(0xffffffffu, pending, 0);
+    if (lane == 0) {
+      claimed[k] = wb;
+      pending = atomicAdd(L.next_wb, 1ull);
+    }
+    issue(wb, k);
+  }
+  __syncwarp();
+  for (int stage = 0;; stage = stage == kCountStages - 1 ? 0 : stage + 1) {
+    const int64_t wb = claimed[stage];
+    if (wb >= nwb) break;  // (claims only grow: the later ones are past the end too)
+    // the buffer read in the previous round takes the block claimed then
+    const int prev = stage == 0 ? kCountStages - 1 : stage - 1;
+    const int64_t nb = (int64_t)__shfl_sync(0xffffffffu, pending, 0);
+    __syncwarp();
+    if (lane == 0) {
+      claimed[prev] = nb;
+      pending = atomicAdd(L.next_wb, 1ull);
+    }
+    issue(nb, prev);
     cp_async_wait<kCountStages - 1>();  // this lane's copies of the current block
     __syncwarp();                        // ... and every lane's
     const int64_t base = wb * kWarpCells + lane;
@@ -408,6 +430,7 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     scan_block_totals_regs(L.block_tris, nblocks, L.block_off, L.block_off + nblocks);
     if (threadIdx.x == 0) {
       *L.n_listed = atomicExch(L.n_cells, 0u);
+      *L.next_wb = 0ull;
       *L.done = 0u;
     }
   }
@@ -613,7 +636,7 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
                           : std::min<int64_t>(g->count, std::max<int64_t>(g->count / 16, 1 << 18));
   const size_t off_off = ((size_t)nblocks * sizeof(uint32_t) + 255) & ~(size_t)255;
   const size_t cnt_off = off_off + (((size_t)nblocks + 1) * sizeof(int64_t) + 15) / 16 * 16;
-  const size_t warp_off = cnt_off + 16;
+  const size_t warp_off = cnt_off + 32;
   const size_t list_off = warp_off + (size_t)nblocks * (kCellsPerBlock / kWarpCells) * sizeof(uint32_t);
   const size_t bytes = list_off + (size_t)cap * sizeof(uint2);
   bool fresh = false;
@@ -636,6 +659,7 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   L.done = (unsigned *)((char *)g->mc + cnt_off);
   L.n_cells = L.done + 1;
   L.n_listed = L.done + 2;
+  L.next_wb = (unsigned long long *)(L.done + 4);
   L.warp_tris = (uint32_t *)((char *)g->mc + warp_off);
   L.cells = (uint2 *)((char *)g->mc + list_off);
   L.cap = (unsigned)cap;
@@ -643,7 +667,7 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   // CTA leaves them so
   if (fresh) {
     KF_CHECK_CUDA(cudaMemsetAsync(L.block_tris, 0, (size_t)nblocks * sizeof(uint32_t), s));
-    KF_CHECK_CUDA(cudaMemsetAsync(L.done, 0, 3 * sizeof(unsigned), s));
+    KF_CHECK_CUDA(cudaMemsetAsync(L.done, 0, 32, s));
   }
   prefer_shared_for_count();
   const unsigned count_grid = (unsigned)std::min<int64_t>(nblocks, (int64_t)kf_num_sms() * kCountCtasPerSm);
