@@ -278,7 +278,6 @@ struct McList {
   uint2 *cells;          // per listed cell: index, (offset in its warp block << 8) | configuration
   unsigned *done;        // CTAs of the count pass finished (the last one resets it)
   unsigned *n_cells;     // cells appended by the count pass (the last CTA resets it)
-  unsigned long long *next_wb;  // the next warp block to claim (the last CTA resets it)
   unsigned *n_listed;    // their final number, for the emit pass
   unsigned cap;          // entries `cells` holds (0: list nothing)
 };
@@ -296,8 +295,8 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 // Pass 1 of kf_mc_run, a resident grid of independent warps: each warp
-// claims warp blocks (kWarpCells consecutive cells) from a counter and never
-// waits for another warp.  It streams them through a ring of kCountStages
+// claims warp blocks (kWarpCells consecutive cells) from its CTA's counter
+// and never waits for another warp.  It streams them through a ring of kCountStages
 // shared-memory buffers with cp.async, kCountStages - 1 blocks ahead, so
 // that the loads in flight cost no registers.  Lane l takes the cell 32 r + l of round r (the band cells
 // of a surface spread over the lanes).  The band cells gather their
@@ -310,7 +309,10 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     k_mc_count_list(McGrid g, McList L, int64_t nblocks) {
   __shared__ __align__(16) float s_ring[kThreads / 32][kCountStages][kWarpCells];
   __shared__ long long s_claimed[kThreads / 32][kCountStages];  // the warp block in each buffer
+  __shared__ unsigned s_next;                                    // the CTA's next claim
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_next = 0u;
+  __syncthreads();
   float(*ring)[kWarpCells] = s_ring[warp];
   long long *claimed = s_claimed[warp];
   const int64_t nwb = (g.count + kWarpCells - 1) / kWarpCells;
@@ -325,17 +327,21 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     }
     cp_async_commit();  // (an empty group where nothing was copied)
   };
-  // warp blocks are claimed one at a time from a shared counter (the surface
-  // makes some much slower than others), one round before their copy is
-  // issued so that the claim's latency is hidden
-  unsigned long long pending = 0;
-  if (lane == 0) pending = atomicAdd(L.next_wb, 1ull);
+  // CTA c owns the warp blocks c, c + G, c + 2G, ... (G CTAs: the surface
+  // spreads evenly over the CTAs); its warps claim them one at a time from a
+  // shared-memory counter (the surface makes some much slower than others),
+  // one round before their copy is issued
+  const auto claim = [&]() -> int64_t {
+    return (int64_t)blockIdx.x + (int64_t)atomicAdd(&s_next, 1u) * gridDim.x;
+  };
+  int64_t pending = 0;
+  if (lane == 0) pending = claim();
 #pragma unroll
   for (int k = 0; k < kCountStages - 1; ++k) {
-    const int64_t wb = (int64_t)__shfl_sync(0xffffffffu, pending, 0);
+    const int64_t wb = __shfl_sync(0xffffffffu, pending, 0);
     if (lane == 0) {
       claimed[k] = wb;
-      pending = atomicAdd(L.next_wb, 1ull);
+      pending = claim();
     }
     issue(wb, k);
   }
@@ -345,11 +351,11 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     if (wb >= nwb) break;  // (claims only grow: the later ones are past the end too)
     // the buffer read in the previous round takes the block claimed then
     const int prev = stage == 0 ? kCountStages - 1 : stage - 1;
-    const int64_t nb = (int64_t)__shfl_sync(0xffffffffu, pending, 0);
+    const int64_t nb = __shfl_sync(0xffffffffu, pending, 0);
     __syncwarp();
     if (lane == 0) {
       claimed[prev] = nb;
-      pending = atomicAdd(L.next_wb, 1ull);
+      pending = claim();
     }
     issue(nb, prev);
     cp_async_wait<kCountStages - 1>();  // this lane's copies of the current block
@@ -430,7 +436,6 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     scan_block_totals_regs(L.block_tris, nblocks, L.block_off, L.block_off + nblocks);
     if (threadIdx.x == 0) {
       *L.n_listed = atomicExch(L.n_cells, 0u);
-      *L.next_wb = 0ull;
       *L.done = 0u;
     }
   }
@@ -659,7 +664,6 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   L.done = (unsigned *)((char *)g->mc + cnt_off);
   L.n_cells = L.done + 1;
   L.n_listed = L.done + 2;
-  L.next_wb = (unsigned long long *)(L.done + 4);
   L.warp_tris = (uint32_t *)((char *)g->mc + warp_off);
   L.cells = (uint2 *)((char *)g->mc + list_off);
   L.cap = (unsigned)cap;
