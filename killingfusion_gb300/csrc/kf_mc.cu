@@ -45,6 +45,7 @@ constexpr int kCellsPerBlock = kThreads * kRounds;
 constexpr int kCountCtasPerSm = 4;  // resident CTAs of k_mc_count_list per SM
 constexpr int kCountStages = 4;     // its ring of warp-block buffers (32 KB per CTA)
 constexpr int kWarpCells = kRounds * 32;  // a warp block of k_mc_count_list
+constexpr int kSuperWarpBlocks = 64;      // warp blocks per superblock (the unit of its offsets)
 constexpr int kScanPerThread = 32;
 constexpr int kScanChunk = kThreads * kScanPerThread;
 
@@ -272,9 +273,9 @@ __device__ void scan_block_totals_regs(uint32_t *block_tris, int64_t nblocks, in
 
 // Scratch of kf_mc_run's two passes.
 struct McList {
-  uint32_t *block_tris;  // triangles per block (zero between calls: the scan clears it)
-  int64_t *block_off;    // exclusive offsets per block, then the grand total
-  uint32_t *warp_tris;   // triangles per warp block (kWarpCells cells), 8 per block
+  uint32_t *super_tris;  // triangles per superblock (zero between calls: the scan clears it)
+  int64_t *super_off;    // exclusive offsets per superblock, then the grand total
+  uint32_t *warp_tris;   // triangles per warp block, kSuperWarpBlocks per superblock
   uint2 *cells;          // per listed cell: index, (offset in its warp block << 8) | configuration
   unsigned *done;        // CTAs of the count pass finished (the last one resets it)
   unsigned *n_cells;     // cells appended by the count pass (the last CTA resets it)
@@ -304,9 +305,10 @@ __device__ __forceinline__ void cp_async_wait() {
 // block's triangles.  The cells with triangles are appended to the list,
 // one atomic per warp block; an entry carries that offset, so the list's
 // order does not matter.  The warp block's total is stored and added to its
-// block's.
+// superblock's (kSuperWarpBlocks warp blocks); the last CTA to finish turns
+// the superblock totals into offsets.
 __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
-    k_mc_count_list(McGrid g, McList L, int64_t nblocks) {
+    k_mc_count_list(McGrid g, McList L, int64_t nsuper) {
   __shared__ __align__(16) float s_ring[kThreads / 32][kCountStages][kWarpCells];
   __shared__ long long s_claimed[kThreads / 32][kCountStages];  // the warp block in each buffer
   __shared__ unsigned s_next;                                    // the CTA's next claim
@@ -385,7 +387,7 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
     const uint32_t total = __reduce_add_sync(0xffffffffu, n);
     if (lane == 0) {
       L.warp_tris[wb] = total;
-      if (total) atomicAdd(L.block_tris + wb / (kCellsPerBlock / kWarpCells), total);
+      if (total) atomicAdd(L.super_tris + wb / kSuperWarpBlocks, total);
     }
     if (total) {
       // one slot per cell with triangles
@@ -433,7 +435,7 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
   __syncthreads();
   if (s_last) {
     __threadfence();
-    scan_block_totals_regs(L.block_tris, nblocks, L.block_off, L.block_off + nblocks);
+    scan_block_totals_regs(L.super_tris, nsuper, L.super_off, L.super_off + nsuper);
     if (threadIdx.x == 0) {
       *L.n_listed = atomicExch(L.n_cells, 0u);
       *L.done = 0u;
@@ -559,9 +561,27 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(McGrid g, const int64_t *b
   emit_block(g, blockIdx.x, block_off[blockIdx.x], verts, capacity);
 }
 
+// The first triangle of warp block wb: its superblock's offset plus the
+// triangles of the superblock's earlier warp blocks (all of them counted:
+// they precede wb, which lies inside the grid).  The superblock's 64 totals
+// are loaded together; those from wb on are masked out.
+__device__ __forceinline__ int64_t warp_block_offset(const McList &L, int64_t wb) {
+  const int64_t sb = wb / kSuperWarpBlocks;
+  const int k = (int)(wb - sb * kSuperWarpBlocks);
+  const uint4 *wt = reinterpret_cast<const uint4 *>(L.warp_tris + sb * kSuperWarpBlocks);
+  uint32_t sum = 0;
+#pragma unroll
+  for (int j = 0; j < kSuperWarpBlocks / 4; ++j) {
+    const uint4 t = __ldg(wt + j);
+    sum += (4 * j < k ? t.x : 0u) + (4 * j + 1 < k ? t.y : 0u) + (4 * j + 2 < k ? t.z : 0u) +
+           (4 * j + 3 < k ? t.w : 0u);
+  }
+  return L.super_off[sb] + (int64_t)sum;
+}
+
 // Pass 2 of kf_mc_run: a resident grid.  Each thread writes the triangles of
-// listed cells; when the list overflowed, each CTA instead takes blocks with
-// triangles and re-classifies them (emit_block).
+// listed cells; when the list overflowed, each CTA instead takes blocks of
+// kCellsPerBlock cells with triangles and re-classifies them (emit_block).
 __global__ void __launch_bounds__(kThreads) k_mc_emit_cells(McGrid g, McList L, int64_t nblocks,
                                                             float *__restrict__ verts, int64_t capacity) {
   const unsigned n = *L.n_listed;
@@ -570,20 +590,17 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit_cells(McGrid g, McList L, 
       const uint2 c = L.cells[e];
       const int64_t i = c.x;
       if (!KF_IN_BOUNDS(i, g.count, KF_SITE_MC_BLOCK)) continue;
-      // the warp block's offset: its block's plus its block's earlier warp blocks'
-      const int64_t wb = i / kWarpCells, b = wb / (kCellsPerBlock / kWarpCells);
-      const uint4 *wt = reinterpret_cast<const uint4 *>(L.warp_tris + b * (kCellsPerBlock / kWarpCells));
-      const uint4 t0 = __ldg(wt), t1 = __ldg(wt + 1);
-      const uint32_t tw[8] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w};
-      const int k = (int)(wb - b * (kCellsPerBlock / kWarpCells));
-      int64_t off = L.block_off[b];
-#pragma unroll
-      for (int j = 0; j < 7; ++j) off += j < k ? tw[j] : 0u;
-      emit_cell(g, i, (int)(c.y & 255u), off + (int64_t)(c.y >> 8), verts, capacity);
+      emit_cell(g, i, (int)(c.y & 255u), warp_block_offset(L, i / kWarpCells) + (int64_t)(c.y >> 8), verts,
+                capacity);
     }
   } else {
-    for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x)
-      if (L.block_off[b + 1] > L.block_off[b]) emit_block(g, b, L.block_off[b], verts, capacity);
+    constexpr int kPerBlock = kCellsPerBlock / kWarpCells;
+    const int64_t nwb = (g.count + kWarpCells - 1) / kWarpCells;
+    for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
+      uint32_t tris = 0;
+      for (int64_t wb = b * kPerBlock; wb < (b + 1) * kPerBlock && wb < nwb; ++wb) tris += __ldg(L.warp_tris + wb);
+      if (tris) emit_block(g, b, warp_block_offset(L, b * kPerBlock), verts, capacity);
+    }
   }
 }
 
@@ -629,20 +646,22 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
   mg.hx = (float)g->n[0] / 2.0f;
   mg.hy = (float)g->n[1] / 2.0f;
   mg.hz = (float)g->n[2] / 2.0f;
-  int64_t nblocks = (g->count + kCellsPerBlock - 1) / kCellsPerBlock;
+  const int64_t nblocks = (g->count + kCellsPerBlock - 1) / kCellsPerBlock;
+  const int64_t nwb = (g->count + kWarpCells - 1) / kWarpCells;
+  const int64_t nsuper = (nwb + kSuperWarpBlocks - 1) / kSuperWarpBlocks;
   // scratch, kept with the grid (calls on one grid are stream-ordered): the
-  // per-block totals (u32), their offsets (i64) and the grand total right
-  // after them, three counters, the per-warp-block totals (u32, 8 per block)
-  // and the list of cells with triangles (count / 16 of them, at least 2^18;
-  // none for grids of 2^32 cells or more, whose indices the list does not
-  // hold)
+  // per-superblock totals (u32), their offsets (i64) and the grand total
+  // right after them, three counters, the per-warp-block totals (u32,
+  // kSuperWarpBlocks per superblock) and the list of cells with triangles
+  // (count / 16 of them, at least 2^18; none for grids of 2^32 cells or
+  // more, whose indices the list does not hold)
   const int64_t cap = g->count >= (int64_t)1 << 32
                           ? 0
                           : std::min<int64_t>(g->count, std::max<int64_t>(g->count / 16, 1 << 18));
-  const size_t off_off = ((size_t)nblocks * sizeof(uint32_t) + 255) & ~(size_t)255;
-  const size_t cnt_off = off_off + (((size_t)nblocks + 1) * sizeof(int64_t) + 15) / 16 * 16;
+  const size_t off_off = ((size_t)nsuper * sizeof(uint32_t) + 255) & ~(size_t)255;
+  const size_t cnt_off = off_off + (((size_t)nsuper + 1) * sizeof(int64_t) + 15) / 16 * 16;
   const size_t warp_off = cnt_off + 32;
-  const size_t list_off = warp_off + (size_t)nblocks * (kCellsPerBlock / kWarpCells) * sizeof(uint32_t);
+  const size_t list_off = warp_off + (size_t)nsuper * kSuperWarpBlocks * sizeof(uint32_t);
   const size_t bytes = list_off + (size_t)cap * sizeof(uint2);
   bool fresh = false;
   if (g->mc_bytes < bytes) {
@@ -658,24 +677,25 @@ int kf_mc_run(kf_grid g, const DevParams &dp, float *verts, int64_t capacity, in
     fresh = true;
   }
   McList L;
-  L.block_tris = (uint32_t *)g->mc;
-  L.block_off = (int64_t *)((char *)g->mc + off_off);
-  int64_t *total_dev = L.block_off + nblocks;
+  L.super_tris = (uint32_t *)g->mc;
+  L.super_off = (int64_t *)((char *)g->mc + off_off);
+  int64_t *total_dev = L.super_off + nsuper;
   L.done = (unsigned *)((char *)g->mc + cnt_off);
   L.n_cells = L.done + 1;
   L.n_listed = L.done + 2;
   L.warp_tris = (uint32_t *)((char *)g->mc + warp_off);
   L.cells = (uint2 *)((char *)g->mc + list_off);
   L.cap = (unsigned)cap;
-  // the block totals and the counters start at zero; the count pass's last
-  // CTA leaves them so
+  // the superblock totals and the counters start at zero; the count pass's
+  // last CTA leaves them so
   if (fresh) {
-    KF_CHECK_CUDA(cudaMemsetAsync(L.block_tris, 0, (size_t)nblocks * sizeof(uint32_t), s));
+    KF_CHECK_CUDA(cudaMemsetAsync(L.super_tris, 0, (size_t)nsuper * sizeof(uint32_t), s));
     KF_CHECK_CUDA(cudaMemsetAsync(L.done, 0, 32, s));
   }
   prefer_shared_for_count();
-  const unsigned count_grid = (unsigned)std::min<int64_t>(nblocks, (int64_t)kf_num_sms() * kCountCtasPerSm);
-  k_mc_count_list<<<count_grid, kThreads, 0, s>>>(mg, L, nblocks);
+  const unsigned count_grid = (unsigned)std::min<int64_t>((nwb + kThreads / 32 - 1) / (kThreads / 32),
+                                                          (int64_t)kf_num_sms() * kCountCtasPerSm);
+  k_mc_count_list<<<count_grid, kThreads, 0, s>>>(mg, L, nsuper);
   KF_CHECK_LAUNCH("k_mc_count_list");
   if (ntri_async) {
     KF_CHECK_CUDA(cudaMemcpyAsync(ntri_async, total_dev, sizeof(int64_t), cudaMemcpyDefault, s));
