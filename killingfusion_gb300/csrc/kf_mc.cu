@@ -222,49 +222,55 @@ __global__ void __launch_bounds__(kThreads) k_mc_scan(const uint32_t *block_tris
   scan_block_totals(block_tris, nblocks, block_off, grand_total);
 }
 
-// The same scan in registers (no shared staging, so that the count pass,
-// whose last CTA runs it, keeps its shared memory small): thread t sums the
-// kScanPerThread totals from c0 + t * kScanPerThread on with 16-byte loads,
-// the block scans the sums, and the thread reads its totals again to write
-// their offsets and clear them (the count pass adds into zeroed totals).
-// block_tris and block_off are 16-byte aligned.
-__device__ void scan_block_totals_regs(uint32_t *block_tris, int64_t nblocks, int64_t *block_off,
-                                       int64_t *grand_total) {
+// The same scan for the count pass's last CTA, in registers (no shared
+// staging, so that the count pass keeps its shared memory for its rings):
+// thread t holds the kPer totals from c0 + t * kPer on (16-byte loads), the
+// block scans the sums, and the thread writes their offsets and clears them
+// (the count pass adds into zeroed totals).  A thread's chain of dependent
+// steps is what the scan costs, so kPer is kept small for small n.  tris and
+// off are 16-byte aligned.
+template <int kPer>
+__device__ void scan_totals_tail(uint32_t *tris, int64_t n, int64_t *off, int64_t *grand_total) {
+  static_assert(kPer % 4 == 0, "16-byte groups");
   uint64_t carry = 0;
-  for (int64_t c0 = 0; c0 < nblocks; c0 += kScanChunk) {
-    const int64_t first = c0 + (int64_t)threadIdx.x * kScanPerThread;
-    const bool whole = first + kScanPerThread <= nblocks;
-    uint64_t sum = 0;
+  for (int64_t c0 = 0; c0 < n; c0 += (int64_t)kThreads * kPer) {
+    const int64_t first = c0 + (int64_t)threadIdx.x * kPer;
+    const bool whole = first + kPer <= n;
+    uint32_t v[kPer];
     if (whole) {
-      const uint4 *p = reinterpret_cast<const uint4 *>(block_tris + first);
+      const uint4 *p = reinterpret_cast<const uint4 *>(tris + first);
 #pragma unroll
-      for (int j = 0; j < kScanPerThread / 4; ++j) {
-        const uint4 v = __ldcg(p + j);
-        sum += (uint64_t)v.x + v.y + v.z + v.w;
+      for (int j = 0; j < kPer / 4; ++j) {
+        const uint4 q = __ldcg(p + j);
+        v[4 * j] = q.x, v[4 * j + 1] = q.y, v[4 * j + 2] = q.z, v[4 * j + 3] = q.w;
       }
     } else {
-      for (int64_t i = first; i < nblocks; ++i) sum += __ldcg(block_tris + i);
+#pragma unroll
+      for (int j = 0; j < kPer; ++j) v[j] = first + j < n ? __ldcg(tris + first + j) : 0u;
     }
-    uint64_t total;
-    uint64_t excl = carry + block_exclusive_scan<uint64_t>(sum, &total);
-    if (whole) {
-      uint4 *p = reinterpret_cast<uint4 *>(block_tris + first);
-      longlong2 *o = reinterpret_cast<longlong2 *>(block_off + first);
+    uint64_t sum = 0;
 #pragma unroll
-      for (int j = 0; j < kScanPerThread / 4; ++j) {
-        const uint4 v = __ldcg(p + j);
-        const int64_t a = (int64_t)excl, b = a + v.x, c = b + v.y, d = c + v.z;
-        o[2 * j] = make_longlong2(a, b);
-        o[2 * j + 1] = make_longlong2(c, d);
-        p[j] = make_uint4(0u, 0u, 0u, 0u);
-        excl = (uint64_t)(d + v.w);
+    for (int j = 0; j < kPer; ++j) sum += v[j];
+    uint64_t total;
+    int64_t excl = (int64_t)(carry + block_exclusive_scan<uint64_t>(sum, &total));
+    if (whole) {
+      longlong2 *o = reinterpret_cast<longlong2 *>(off + first);
+#pragma unroll
+      for (int j = 0; j < kPer / 2; ++j) {
+        o[j] = make_longlong2(excl, excl + v[2 * j]);
+        excl += (int64_t)v[2 * j] + v[2 * j + 1];
       }
+      uint4 *p = reinterpret_cast<uint4 *>(tris + first);
+#pragma unroll
+      for (int j = 0; j < kPer / 4; ++j) p[j] = make_uint4(0u, 0u, 0u, 0u);
     } else {
-      for (int64_t i = first; i < nblocks; ++i) {
-        block_off[i] = (int64_t)excl;
-        excl += __ldcg(block_tris + i);
-        block_tris[i] = 0u;
-      }
+#pragma unroll
+      for (int j = 0; j < kPer; ++j)
+        if (first + j < n) {
+          off[first + j] = excl;
+          excl += v[j];
+          tris[first + j] = 0u;
+        }
     }
     carry += total;
   }
@@ -435,7 +441,10 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
   __syncthreads();
   if (s_last) {
     __threadfence();
-    scan_block_totals_regs(L.super_tris, nsuper, L.super_off, L.super_off + nsuper);
+    if (nsuper <= (int64_t)kThreads * 4)
+      scan_totals_tail<4>(L.super_tris, nsuper, L.super_off, L.super_off + nsuper);
+    else
+      scan_totals_tail<16>(L.super_tris, nsuper, L.super_off, L.super_off + nsuper);
     if (threadIdx.x == 0) {
       *L.n_listed = atomicExch(L.n_cells, 0u);
       *L.done = 0u;
