@@ -237,11 +237,15 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
 //   iterations, ordered by the barrier's fences), the SDFs through the
 //   read-only path.  A gated iteration (converged, diverged) ends the kernel
 //   in every block alike: each reads the same statistics after the barrier.
-// 64-thread blocks, 4 per SM: a 255-register budget (the band update does not
-// spill), two warps a block.
-constexpr int kPersistThreads = 64;
+// 128-thread blocks, 2 per SM: a 255-register budget (the band update does
+// not spill), four warps a block.  The grid barrier's cost grows with the
+// number of blocks (alone, with no work between barriers: 2.3 us for 608
+// blocks, 1.5 us for 304, 1.3 us for 152), so the blocks are made as large
+// as the register budget allows while all four schedulers of an SM keep a
+// warp.
+constexpr int kPersistThreads = 128;
 constexpr int kPersistWarps = kPersistThreads / 32;
-constexpr int kPersistBlocksPerSM = 4;
+constexpr int kPersistBlocksPerSM = 2;
 
 // Compacts the voxels `next` (>= 0 on the threads that carry one) of the
 // block into out[base...] (capacity entries), with no atomic; returns how
