@@ -237,15 +237,14 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
 //   iterations, ordered by the barrier's fences), the SDFs through the
 //   read-only path.  A gated iteration (converged, diverged) ends the kernel
 //   in every block alike: each reads the same statistics after the barrier.
-// 128-thread blocks, 2 per SM: a 255-register budget (the band update does
-// not spill), four warps a block.  The grid barrier's cost grows with the
+// 256-thread blocks, 1 per SM: a 255-register budget (the band update does
+// not spill), eight warps a block.  The grid barrier's cost grows with the
 // number of blocks (alone, with no work between barriers: 2.3 us for 608
 // blocks, 1.5 us for 304, 1.3 us for 152), so the blocks are made as large
-// as the register budget allows while all four schedulers of an SM keep a
-// warp.
-constexpr int kPersistThreads = 128;
+// as the register budget allows.
+constexpr int kPersistThreads = 256;
 constexpr int kPersistWarps = kPersistThreads / 32;
-constexpr int kPersistBlocksPerSM = 2;
+constexpr int kPersistBlocksPerSM = 1;
 
 // Compacts the voxels `next` (>= 0 on the threads that carry one) of the
 // block into out[base...] (capacity entries), with no atomic; returns how
@@ -280,21 +279,25 @@ __device__ __forceinline__ bool persistent_band_iteration(const FusedArgs &a, in
                                                           const int *__restrict__ in, int *__restrict__ out,
                                                           unsigned &n, unsigned capacity, GridSync *sync,
                                                           unsigned long long limit_ns) {
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned k0 = lane * kPersistWarps + warp;  // this thread's voxel of round 0
+  // its list entry is loaded before the gate reads the previous iteration's
+  // statistics, so that the two loads overlap
+  const int v0 = k0 < n ? __ldcg(in + k0) : -1;
   if (iteration_gated(a.st, it, a.dp)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[it].skipped = 1;
     return false;
   }
   const unsigned rounds = (n + kPersistThreads - 1) / kPersistThreads;
-  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float maxd = 0.f;
   double energy = 0.0;
   unsigned active = 0, carried = 0;
   bool diverged = false;
   for (unsigned r = 0; r < rounds; ++r) {
-    const unsigned k = r * kPersistThreads + lane * kPersistWarps + warp;
+    const unsigned k = r * kPersistThreads + k0;
     int next = -1;
     if (k < n) {
-      const int v = __ldcg(in + k);
+      const int v = r == 0 ? v0 : __ldcg(in + k);
       next = update_band_voxel<false, kPsiL1>(a, v, v, maxd, energy, active, diverged);
     }
     carried += block_compact(next, out, carried, capacity);
