@@ -452,41 +452,6 @@ __global__ void __launch_bounds__(kThreads, kCountCtasPerSm)
   }
 }
 
-// Exclusive prefix over the block of K values per thread at once, and the K
-// block totals; every thread calls it.
-template <int K>
-__device__ __forceinline__ void block_scan_vec(const uint32_t v[K], uint32_t excl[K], uint32_t tot[K]) {
-  __shared__ uint32_t s_w[kThreads / 32][K];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  uint32_t inc[K];
-#pragma unroll
-  for (int k = 0; k < K; ++k) inc[k] = v[k];
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1)
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, inc[k], o);
-      if (lane >= o) inc[k] += t;
-    }
-  if (lane == 31)
-#pragma unroll
-    for (int k = 0; k < K; ++k) s_w[wid][k] = inc[k];
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    uint32_t before = 0, all = 0;
-#pragma unroll
-    for (int w = 0; w < kThreads / 32; ++w) {
-      const uint32_t x = s_w[w][k];
-      if (w < wid) before += x;
-      all += x;
-    }
-    excl[k] = before + inc[k] - v[k];
-    tot[k] = all;
-  }
-  __syncthreads();  // s_w is free for the next call
-}
-
 __device__ __forceinline__ void vinterp(const float p1[3], const float p2[3], float v1, float v2,
                                         float out[3]) {
   float t = (0.0f - v1) / (v1 - v2);
