@@ -154,9 +154,31 @@ __device__ void integrate_exact_voxel(float *__restrict__ phi, int32_t *__restri
 // per axis value: the camera-x and camera-y row products rounded to float
 // and the camera-depth product as a float pair, with the rows' constant
 // terms W[3], W[7] and W[11] added to the x entries.
-__global__ void k_integrate_tables(double *__restrict__ tx, double *__restrict__ ty, double *__restrict__ tz,
-                                   float4 *__restrict__ tp, int nx, int ny, int nz, IntegrateArgs a) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx + ny + nz; k += gridDim.x * blockDim.x) {
+//
+// The CTAs from `tab_blocks` on mark the depth frame's 16 x 16-pixel blocks
+// that hold a pixel passing the reference's depth test (SDF.cpp:176-179; a
+// NaN passes it): flags[by * bw + bx] = 1.  k_integrate skips a tile of
+// voxels whose possible pixels lie in unmarked blocks only.
+constexpr int kPixBlock = 16;
+
+template <typename D>
+__global__ void __launch_bounds__(kBlock) k_integrate_prep(double *__restrict__ tx, double *__restrict__ ty,
+                                                           double *__restrict__ tz, float4 *__restrict__ tp,
+                                                           int nx, int ny, int nz, unsigned tab_blocks,
+                                                           const D *__restrict__ depth,
+                                                           uint8_t *__restrict__ flags, int bw,
+                                                           IntegrateArgs a) {
+  if (blockIdx.x >= tab_blocks) {
+    const int b = (int)(blockIdx.x - tab_blocks), bx = b % bw, by = b / bw;
+    const int col = bx * kPixBlock + (int)(threadIdx.x % kPixBlock);
+    const int row = by * kPixBlock + (int)(threadIdx.x / kPixBlock);
+    double d;
+    const bool ok = col < a.width && row < a.height && depth_at(depth, (int64_t)row * a.width + col, a, d);
+    const int any = __syncthreads_or(ok);
+    if (threadIdx.x == 0) flags[b] = (uint8_t)any;
+    return;
+  }
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx + ny + nz; k += tab_blocks * blockDim.x) {
     double c, t, r0, r1;
     if (k < nx) {
       c = a.voxel * ((double)k + 0.5) + a.min0;
@@ -180,6 +202,93 @@ __global__ void k_integrate_tables(double *__restrict__ tx, double *__restrict__
     const FF p = ff_from_double(t);
     tp[k] = make_float4(__double2float_rn(r0), __double2float_rn(r1), p.hi, p.lo);
   }
+}
+
+// The float projection of voxel (x, y, z) from the tables and its error
+// bounds mu, mv (k_integrate's comment derives them); c2 is the float camera
+// depth, px/py/pz the voxel's table entries.
+struct FloatProjection {
+  float4 px, py, pz;
+  float c2, uf, vf, mu, mv;
+};
+
+__device__ __forceinline__ FloatProjection project_float(const float4 *__restrict__ tp, int nx, int ny, int x, int y,
+                                                         int z, const IntegrateArgs &a) {
+  FloatProjection q;
+  q.px = __ldg(tp + x);
+  q.py = __ldg(tp + nx + y);
+  q.pz = __ldg(tp + nx + ny + z);
+  const float c0 = __fadd_rn(__fadd_rn(q.px.x, q.py.x), q.pz.x);
+  const float c1 = __fadd_rn(__fadd_rn(q.px.y, q.py.y), q.pz.y);
+  q.c2 = __fadd_rn(__fadd_rn(q.px.z, q.py.z), q.pz.z);
+  const float rc = __fdividef(1.0f, q.c2);
+  const float pa = __fmul_rn(c0, rc), pb = __fmul_rn(c1, rc);
+  const float ua = __fmul_rn(a.Kf[0], pa), ub = __fmul_rn(a.Kf[1], pb);
+  const float va = __fmul_rn(a.Kf[3], pa), vb = __fmul_rn(a.Kf[4], pb);
+  q.uf = __fadd_rn(__fadd_rn(ua, ub), a.Kf[2]);
+  q.vf = __fadd_rn(__fadd_rn(va, vb), a.Kf[5]);
+  const float arc = fabsf(rc);
+  const float ea = a.e0 + fabsf(pa) * a.e2, eb = a.e1 + fabsf(pb) * a.e2;
+  q.mu = (a.ku0 * ea + a.ku1 * eb) * arc + 0x1p-19f * (fabsf(ua) + fabsf(ub) + (fabsf(a.Kf[2]) + 2.0f));
+  q.mv = (a.kv0 * ea + a.kv1 * eb) * arc + 0x1p-19f * (fabsf(va) + fabsf(vb) + (fabsf(a.Kf[5]) + 2.0f));
+  return q;
+}
+
+// Whether no voxel of the kernel's tile (32 x blockDim.y voxels of plane z)
+// can integrate anything, decided by warp 0.  The camera depth is affine
+// over the tile and positive at its four corners, so it is positive on the
+// whole tile, where u and v are linear-fractional and take their extremes
+// at the corners: each corner's float projection, widened by its error
+// bound, bounds them.  The tile is skipped when that range of u or v lies
+// off the image (every voxel's pixel is rejected by SDF.cpp:167-172), or
+// when every 16 x 16-pixel block its pixels can fall in holds no pixel that
+// passes the depth test (every voxel is rejected by SDF.cpp:176-179).
+__device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, int nx, int ny, int z,
+                                               const uint8_t *__restrict__ flags, int bw,
+                                               const IntegrateArgs &a) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x;  // warp 0: threadIdx.y == 0, blockDim.x == 32
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * blockDim.y;
+  const int x1 = min(x0 + 31, nx - 1), y1 = min(y0 + (int)blockDim.y - 1, ny - 1);
+  bool ok = true;
+  float ulo = INFINITY, uhi = -INFINITY, vlo = INFINITY, vhi = -INFINITY;
+  if (lane < 4) {
+    const FloatProjection q = project_float(tp, nx, ny, lane & 1 ? x1 : x0, lane & 2 ? y1 : y0, z, a);
+    ok = q.c2 > a.c2_min && isfinite(q.uf) && isfinite(q.vf) && fabsf(q.uf) < 1e7f && fabsf(q.vf) < 1e7f &&
+         isfinite(q.mu) && isfinite(q.mv) && q.mu < 1e6f && q.mv < 1e6f;
+    ulo = q.uf - q.mu;
+    uhi = q.uf + q.mu;
+    vlo = q.vf - q.mv;
+    vhi = q.vf + q.mv;
+  }
+  if (!__all_sync(full, ok)) return false;
+#pragma unroll
+  for (int o = 1; o < 4; o <<= 1) {
+    ulo = fminf(ulo, __shfl_xor_sync(full, ulo, o));
+    uhi = fmaxf(uhi, __shfl_xor_sync(full, uhi, o));
+    vlo = fminf(vlo, __shfl_xor_sync(full, vlo, o));
+    vhi = fmaxf(vhi, __shfl_xor_sync(full, vhi, o));
+  }
+  ulo = __shfl_sync(full, ulo, 0);
+  uhi = __shfl_sync(full, uhi, 0);
+  vlo = __shfl_sync(full, vlo, 0);
+  vhi = __shfl_sync(full, vhi, 0);
+  // col = roundf(u + 0.5) is below 0 for u < -1 and at least width for
+  // u > width - 1 (the float rounding of u + 0.5 moves that by 2^-24 of it)
+  if (uhi < -1.001f || ulo > (float)a.width - 0.999f || vhi < -1.001f || vlo > (float)a.height - 0.999f)
+    return true;
+  // the pixels the tile's voxels can read, one more on every side
+  const int c_lo = max(0, (int)floorf(ulo + 1.0f) - 1), c_hi = min(a.width - 1, (int)floorf(uhi + 1.0f) + 1);
+  const int r_lo = max(0, (int)floorf(vlo + 1.0f) - 1), r_hi = min(a.height - 1, (int)floorf(vhi + 1.0f) + 1);
+  if (c_lo > c_hi || r_lo > r_hi) return true;
+  const int bx0 = c_lo / kPixBlock, nbx = c_hi / kPixBlock - bx0 + 1;
+  const int by0 = r_lo / kPixBlock, nb = nbx * (r_hi / kPixBlock - by0 + 1);
+  for (int k0 = 0; k0 < nb; k0 += 32) {
+    const int k = k0 + lane;
+    const bool v = k < nb && __ldg(flags + (by0 + k / nbx) * bw + bx0 + k % nbx) != 0;
+    if (__any_sync(full, v)) return false;
+  }
+  return true;
 }
 
 // A fresh voxel (w == 0, phi finite) on float depth df, in float-float: the
@@ -249,12 +358,26 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
     k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
                 const D *__restrict__ depth, const double *__restrict__ tx, const double *__restrict__ ty,
                 const double *__restrict__ tz, const float4 *__restrict__ tp, int *__restrict__ list,
-                unsigned *__restrict__ list_n, unsigned list_cap, IntegrateArgs a) {
+                unsigned *__restrict__ list_n, unsigned list_cap, const uint8_t *__restrict__ flags, int bw,
+                IntegrateArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
+  __shared__ int s_skip;
+  if (threadIdx.y == 0) {
+    const bool skip = tile_skippable(tp, nx, ny, z, flags, bw, a);
+    if (threadIdx.x == 0) s_skip = skip;
+  }
+  __syncthreads();
   if (x >= nx || y >= ny) return;
   const int64_t i = ((int64_t)z * ny + y) * nx + x;
+  if (s_skip) {  // nothing of the tile is integrated
+    if (kFresh) {
+      phi[i] = a.fresh_phi;
+      w[i] = 0;
+    }
+    return;
+  }
   // the voxel's weight and value, loaded first so that their latency runs
   // under the projection's arithmetic
   const int32_t wi = kFresh ? 0 : w[i];
@@ -265,23 +388,12 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
       w[i] = 0;
     }
   };
-  const float4 px = __ldg(tp + x), py = __ldg(tp + nx + y), pz = __ldg(tp + nx + ny + z);
-  const float c0 = __fadd_rn(__fadd_rn(px.x, py.x), pz.x);
-  const float c1 = __fadd_rn(__fadd_rn(px.y, py.y), pz.y);
-  const float c2 = __fadd_rn(__fadd_rn(px.z, py.z), pz.z);
-  const float rc = __fdividef(1.0f, c2);
-  const float pa = __fmul_rn(c0, rc), pb = __fmul_rn(c1, rc);
-  const float ua = __fmul_rn(a.Kf[0], pa), ub = __fmul_rn(a.Kf[1], pb);
-  const float va = __fmul_rn(a.Kf[3], pa), vb = __fmul_rn(a.Kf[4], pb);
-  const float uf = __fadd_rn(__fadd_rn(ua, ub), a.Kf[2]);
-  const float vf = __fadd_rn(__fadd_rn(va, vb), a.Kf[5]);
-  const float arc = fabsf(rc);
-  const float ea = a.e0 + fabsf(pa) * a.e2, eb = a.e1 + fabsf(pb) * a.e2;
-  const float mu = (a.ku0 * ea + a.ku1 * eb) * arc + 0x1p-19f * (fabsf(ua) + fabsf(ub) + (fabsf(a.Kf[2]) + 2.0f));
-  const float mv = (a.kv0 * ea + a.kv1 * eb) * arc + 0x1p-19f * (fabsf(va) + fabsf(vb) + (fabsf(a.Kf[5]) + 2.0f));
+  const FloatProjection q = project_float(tp, nx, ny, x, y, z, a);
+  const float4 px = q.px, py = q.py, pz = q.pz;
+  const float c2 = q.c2, uf = q.uf, vf = q.vf;
   const bool sure = fabsf(c2) > a.c2_min && fabsf(c2) < 0x1p100f && isfinite(uf) && isfinite(vf) &&
-                    fabsf(uf) < 1e7f && fabsf(vf) < 1e7f && fabsf(uf - rintf(uf)) > mu &&
-                    fabsf(vf - rintf(vf)) > mv;
+                    fabsf(uf) < 1e7f && fabsf(vf) < 1e7f && fabsf(uf - rintf(uf)) > q.mu &&
+                    fabsf(vf - rintf(vf)) > q.mv;
   const unsigned act = __activemask();
   const unsigned need = __ballot_sync(act, !sure);
   if (!sure) {
@@ -404,10 +516,13 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
     a.kv1 = (float)(1.5 * fabs(K[4]) * up);
     a.c2_min = (float)std::max(8.0 * (double)a.e2, 0x1p-100);
   }
-  // scratch: list counter, the three coordinate tables, the list
+  // scratch: list counter, the three coordinate tables, the pixel-block
+  // flags, the list
   const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
   const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(g->count / 8, 65536), 0x7fffffff);
-  const size_t tab_off = 256, list_off = tab_off + (((size_t)(nx + ny + nz) * 24 + 255) & ~(size_t)255);
+  const int bw = (width + kPixBlock - 1) / kPixBlock, bh = (height + kPixBlock - 1) / kPixBlock;
+  const size_t tab_off = 256, flag_off = tab_off + (((size_t)(nx + ny + nz) * 24 + 255) & ~(size_t)255);
+  const size_t list_off = flag_off + (((size_t)bw * bh + 255) & ~(size_t)255);
   const size_t bytes = list_off + (size_t)cap * sizeof(int);
   if (g->integ_bytes < bytes) {
     cudaFree(g->integ);
@@ -424,17 +539,20 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   unsigned *list_n = (unsigned *)base;
   float4 *tp = (float4 *)(base + tab_off);
   double *tx = (double *)(tp + (nx + ny + nz)), *ty = tx + nx, *tz = ty + ny;
+  uint8_t *flags = (uint8_t *)(base + flag_off);
   int *list = (int *)(base + list_off);
   KF_CHECK_CUDA(cudaMemsetAsync(list_n, 0, sizeof(unsigned), s));
-  k_integrate_tables<<<blocks_for(nx + ny + nz), kBlock, 0, s>>>(tx, ty, tz, tp, nx, ny, nz, a);
+  const unsigned tab_blocks = blocks_for(nx + ny + nz);
+  k_integrate_prep<D><<<tab_blocks + (unsigned)(bw * bh), kBlock, 0, s>>>(tx, ty, tz, tp, nx, ny, nz, tab_blocks,
+                                                                          depth_dev, flags, bw, a);
   dim3 block(32, kBlock / 32);
   dim3 grid((nx + 31) / 32, (ny + block.y - 1) / block.y, nz);
   if (fresh_phi)
     k_integrate<D, true><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list, list_n,
-                                                cap, a);
+                                                cap, flags, bw, a);
   else
     k_integrate<D, false><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list,
-                                                 list_n, cap, a);
+                                                 list_n, cap, flags, bw, a);
   k_integrate_exact<D><<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list,
                                                                      list_n, cap, a);
   KF_CHECK_LAUNCH("k_integrate");
