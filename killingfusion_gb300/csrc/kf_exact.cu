@@ -234,8 +234,8 @@ __device__ __forceinline__ FloatProjection project_float(const float4 *__restric
   return q;
 }
 
-// Whether no voxel of the kernel's tile (32 x blockDim.y voxels of plane z)
-// can integrate anything, decided by warp 0.  The camera depth is affine
+// Whether no voxel of the tile [x0, x0 + 32) x [y0, y0 + kTileY) of plane z
+// can integrate anything, decided by one warp.  The camera depth is affine
 // over the tile and positive at its four corners, so it is positive on the
 // whole tile, where u and v are linear-fractional and take their extremes
 // at the corners: each corner's float projection, widened by its error
@@ -243,13 +243,14 @@ __device__ __forceinline__ FloatProjection project_float(const float4 *__restric
 // off the image (every voxel's pixel is rejected by SDF.cpp:167-172), or
 // when every 16 x 16-pixel block its pixels can fall in holds no pixel that
 // passes the depth test (every voxel is rejected by SDF.cpp:176-179).
-__device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, int nx, int ny, int z,
+constexpr int kTileY = kBlock / 32;  // k_integrate's CTA: 32 x kTileY voxels
+
+__device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, int nx, int ny, int x0, int y0, int z,
                                                const uint8_t *__restrict__ flags, int bw,
                                                const IntegrateArgs &a) {
   const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x;  // warp 0: threadIdx.y == 0, blockDim.x == 32
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * blockDim.y;
-  const int x1 = min(x0 + 31, nx - 1), y1 = min(y0 + (int)blockDim.y - 1, ny - 1);
+  const int lane = threadIdx.x & 31;
+  const int x1 = min(x0 + 31, nx - 1), y1 = min(y0 + kTileY - 1, ny - 1);
   bool ok = true;
   float ulo = INFINITY, uhi = -INFINITY, vlo = INFINITY, vhi = -INFINITY;
   if (lane < 4) {
@@ -289,6 +290,20 @@ __device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, in
     if (__any_sync(full, v)) return false;
   }
   return true;
+}
+
+// One warp per tile of k_integrate (tiles x-fastest, then y, then z):
+// skip[t] = 1 when the tile can integrate nothing.
+__global__ void __launch_bounds__(kBlock) k_integrate_tiles(const float4 *__restrict__ tp, int nx, int ny, int nz,
+                                                            const uint8_t *__restrict__ flags, int bw,
+                                                            uint8_t *__restrict__ skip, IntegrateArgs a) {
+  const int tiles_x = (nx + 31) / 32, tiles_y = (ny + kTileY - 1) / kTileY;
+  const int64_t ntiles = (int64_t)tiles_x * tiles_y * nz;
+  const int64_t t = (int64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
+  if (t >= ntiles) return;  // (whole warps)
+  const int tx = (int)(t % tiles_x), ty = (int)((t / tiles_x) % tiles_y), z = (int)(t / ((int64_t)tiles_x * tiles_y));
+  const bool sk = tile_skippable(tp, nx, ny, tx * 32, ty * kTileY, z, flags, bw, a);
+  if ((threadIdx.x & 31) == 0) skip[t] = (uint8_t)sk;
 }
 
 // A fresh voxel (w == 0, phi finite) on float depth df, in float-float: the
@@ -358,20 +373,15 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
     k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
                 const D *__restrict__ depth, const double *__restrict__ tx, const double *__restrict__ ty,
                 const double *__restrict__ tz, const float4 *__restrict__ tp, int *__restrict__ list,
-                unsigned *__restrict__ list_n, unsigned list_cap, const uint8_t *__restrict__ flags, int bw,
+                unsigned *__restrict__ list_n, unsigned list_cap, const uint8_t *__restrict__ skip,
                 IntegrateArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  __shared__ int s_skip;
-  if (threadIdx.y == 0) {
-    const bool skip = tile_skippable(tp, nx, ny, z, flags, bw, a);
-    if (threadIdx.x == 0) s_skip = skip;
-  }
-  __syncthreads();
   if (x >= nx || y >= ny) return;
   const int64_t i = ((int64_t)z * ny + y) * nx + x;
-  if (s_skip) {  // nothing of the tile is integrated
+  if (__ldg(skip + ((int64_t)z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x)) {
+    // nothing of the tile is integrated (k_integrate_tiles)
     if (kFresh) {
       phi[i] = a.fresh_phi;
       w[i] = 0;
@@ -522,7 +532,9 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   const unsigned cap = (unsigned)std::min<int64_t>(std::max<int64_t>(g->count / 8, 65536), 0x7fffffff);
   const int bw = (width + kPixBlock - 1) / kPixBlock, bh = (height + kPixBlock - 1) / kPixBlock;
   const size_t tab_off = 256, flag_off = tab_off + (((size_t)(nx + ny + nz) * 24 + 255) & ~(size_t)255);
-  const size_t list_off = flag_off + (((size_t)bw * bh + 255) & ~(size_t)255);
+  const int64_t ntiles = (int64_t)((nx + 31) / 32) * ((ny + kTileY - 1) / kTileY) * nz;
+  const size_t skip_off = flag_off + (((size_t)bw * bh + 255) & ~(size_t)255);
+  const size_t list_off = skip_off + (((size_t)ntiles + 255) & ~(size_t)255);
   const size_t bytes = list_off + (size_t)cap * sizeof(int);
   if (g->integ_bytes < bytes) {
     cudaFree(g->integ);
@@ -540,19 +552,21 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   float4 *tp = (float4 *)(base + tab_off);
   double *tx = (double *)(tp + (nx + ny + nz)), *ty = tx + nx, *tz = ty + ny;
   uint8_t *flags = (uint8_t *)(base + flag_off);
+  uint8_t *skip = (uint8_t *)(base + skip_off);
   int *list = (int *)(base + list_off);
   KF_CHECK_CUDA(cudaMemsetAsync(list_n, 0, sizeof(unsigned), s));
   const unsigned tab_blocks = blocks_for(nx + ny + nz);
   k_integrate_prep<D><<<tab_blocks + (unsigned)(bw * bh), kBlock, 0, s>>>(tx, ty, tz, tp, nx, ny, nz, tab_blocks,
                                                                           depth_dev, flags, bw, a);
-  dim3 block(32, kBlock / 32);
-  dim3 grid((nx + 31) / 32, (ny + block.y - 1) / block.y, nz);
+  k_integrate_tiles<<<blocks_for(ntiles, kBlock / 32), kBlock, 0, s>>>(tp, nx, ny, nz, flags, bw, skip, a);
+  dim3 block(32, kTileY);
+  dim3 grid((nx + 31) / 32, (ny + kTileY - 1) / kTileY, nz);
   if (fresh_phi)
     k_integrate<D, true><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list, list_n,
-                                                cap, flags, bw, a);
+                                                cap, skip, a);
   else
     k_integrate<D, false><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list,
-                                                 list_n, cap, flags, bw, a);
+                                                 list_n, cap, skip, a);
   k_integrate_exact<D><<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list,
                                                                      list_n, cap, a);
   KF_CHECK_LAUNCH("k_integrate");
