@@ -248,32 +248,19 @@ constexpr int kTileY = kBlock / 32;  // k_integrate's CTA: 32 x kTileY voxels
 __device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, int nx, int ny, int x0, int y0, int z,
                                                const uint8_t *__restrict__ flags, int bw,
                                                const IntegrateArgs &a) {
-  const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
   const int x1 = min(x0 + 31, nx - 1), y1 = min(y0 + kTileY - 1, ny - 1);
-  bool ok = true;
   float ulo = INFINITY, uhi = -INFINITY, vlo = INFINITY, vhi = -INFINITY;
-  if (lane < 4) {
-    const FloatProjection q = project_float(tp, nx, ny, lane & 1 ? x1 : x0, lane & 2 ? y1 : y0, z, a);
-    ok = q.c2 > a.c2_min && isfinite(q.uf) && isfinite(q.vf) && fabsf(q.uf) < 1e7f && fabsf(q.vf) < 1e7f &&
-         isfinite(q.mu) && isfinite(q.mv) && q.mu < 1e6f && q.mv < 1e6f;
-    ulo = q.uf - q.mu;
-    uhi = q.uf + q.mu;
-    vlo = q.vf - q.mv;
-    vhi = q.vf + q.mv;
-  }
-  if (!__all_sync(full, ok)) return false;
 #pragma unroll
-  for (int o = 1; o < 4; o <<= 1) {
-    ulo = fminf(ulo, __shfl_xor_sync(full, ulo, o));
-    uhi = fmaxf(uhi, __shfl_xor_sync(full, uhi, o));
-    vlo = fminf(vlo, __shfl_xor_sync(full, vlo, o));
-    vhi = fmaxf(vhi, __shfl_xor_sync(full, vhi, o));
+  for (int c = 0; c < 4; ++c) {
+    const FloatProjection q = project_float(tp, nx, ny, c & 1 ? x1 : x0, c & 2 ? y1 : y0, z, a);
+    if (!(q.c2 > a.c2_min && isfinite(q.uf) && isfinite(q.vf) && fabsf(q.uf) < 1e7f && fabsf(q.vf) < 1e7f &&
+          q.mu < 1e6f && q.mv < 1e6f))
+      return false;  // (a NaN bound fails the comparisons too)
+    ulo = fminf(ulo, q.uf - q.mu);
+    uhi = fmaxf(uhi, q.uf + q.mu);
+    vlo = fminf(vlo, q.vf - q.mv);
+    vhi = fmaxf(vhi, q.vf + q.mv);
   }
-  ulo = __shfl_sync(full, ulo, 0);
-  uhi = __shfl_sync(full, uhi, 0);
-  vlo = __shfl_sync(full, vlo, 0);
-  vhi = __shfl_sync(full, vhi, 0);
   // col = roundf(u + 0.5) is below 0 for u < -1 and at least width for
   // u > width - 1 (the float rounding of u + 0.5 moves that by 2^-24 of it)
   if (uhi < -1.001f || ulo > (float)a.width - 0.999f || vhi < -1.001f || vlo > (float)a.height - 0.999f)
@@ -281,29 +268,23 @@ __device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, in
   // the pixels the tile's voxels can read, one more on every side
   const int c_lo = max(0, (int)floorf(ulo + 1.0f) - 1), c_hi = min(a.width - 1, (int)floorf(uhi + 1.0f) + 1);
   const int r_lo = max(0, (int)floorf(vlo + 1.0f) - 1), r_hi = min(a.height - 1, (int)floorf(vhi + 1.0f) + 1);
-  if (c_lo > c_hi || r_lo > r_hi) return true;
-  const int bx0 = c_lo / kPixBlock, nbx = c_hi / kPixBlock - bx0 + 1;
-  const int by0 = r_lo / kPixBlock, nb = nbx * (r_hi / kPixBlock - by0 + 1);
-  for (int k0 = 0; k0 < nb; k0 += 32) {
-    const int k = k0 + lane;
-    const bool v = k < nb && __ldg(flags + (by0 + k / nbx) * bw + bx0 + k % nbx) != 0;
-    if (__any_sync(full, v)) return false;
-  }
+  for (int by = r_lo / kPixBlock; by <= r_hi / kPixBlock; ++by)
+    for (int bx = c_lo / kPixBlock; bx <= c_hi / kPixBlock; ++bx)
+      if (__ldg(flags + by * bw + bx)) return false;
   return true;
 }
 
-// One warp per tile of k_integrate (tiles x-fastest, then y, then z):
+// One thread per tile of k_integrate (tiles x-fastest, then y, then z):
 // skip[t] = 1 when the tile can integrate nothing.
 __global__ void __launch_bounds__(kBlock) k_integrate_tiles(const float4 *__restrict__ tp, int nx, int ny, int nz,
                                                             const uint8_t *__restrict__ flags, int bw,
                                                             uint8_t *__restrict__ skip, IntegrateArgs a) {
   const int tiles_x = (nx + 31) / 32, tiles_y = (ny + kTileY - 1) / kTileY;
   const int64_t ntiles = (int64_t)tiles_x * tiles_y * nz;
-  const int64_t t = (int64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
-  if (t >= ntiles) return;  // (whole warps)
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
   const int tx = (int)(t % tiles_x), ty = (int)((t / tiles_x) % tiles_y), z = (int)(t / ((int64_t)tiles_x * tiles_y));
-  const bool sk = tile_skippable(tp, nx, ny, tx * 32, ty * kTileY, z, flags, bw, a);
-  if ((threadIdx.x & 31) == 0) skip[t] = (uint8_t)sk;
+  skip[t] = (uint8_t)tile_skippable(tp, nx, ny, tx * 32, ty * kTileY, z, flags, bw, a);
 }
 
 // A fresh voxel (w == 0, phi finite) on float depth df, in float-float: the
@@ -369,25 +350,12 @@ __device__ __forceinline__ int integrate_fresh_ff(float *__restrict__ phi, int32
 // read) and every voxel is written, the reset values where nothing is
 // integrated (KillingFusion::computeSDF: a new SDF, then the frame).
 template <typename D, bool kFresh>
-__global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a full SM
-    k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
-                const D *__restrict__ depth, const double *__restrict__ tx, const double *__restrict__ ty,
-                const double *__restrict__ tz, const float4 *__restrict__ tp, int *__restrict__ list,
-                unsigned *__restrict__ list_n, unsigned list_cap, const uint8_t *__restrict__ skip,
-                IntegrateArgs a) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
-  if (x >= nx || y >= ny) return;
-  const int64_t i = ((int64_t)z * ny + y) * nx + x;
-  if (__ldg(skip + ((int64_t)z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x)) {
-    // nothing of the tile is integrated (k_integrate_tiles)
-    if (kFresh) {
-      phi[i] = a.fresh_phi;
-      w[i] = 0;
-    }
-    return;
-  }
+__device__ __forceinline__ void integrate_voxel(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny,
+                                                int x, int y, int z, int64_t i, const D *__restrict__ depth,
+                                                const double *__restrict__ tx, const double *__restrict__ ty,
+                                                const double *__restrict__ tz, const float4 *__restrict__ tp,
+                                                int *__restrict__ list, unsigned *__restrict__ list_n,
+                                                unsigned list_cap, const IntegrateArgs &a) {
   // the voxel's weight and value, loaded first so that their latency runs
   // under the projection's arithmetic
   const int32_t wi = kFresh ? 0 : w[i];
@@ -446,6 +414,37 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
   double dd;
   const double zd = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
   if (!depth_at(depth, k, a, dd) || !integrate_update(phi, w, i, dd, zd, a, wi, ph)) leave();
+}
+
+// The tiles of 32 x kTileY voxels (tiles x-fastest, then y, then z), CTA c
+// taking the tiles c, c + G, c + 2G, ... (a resident grid of G CTAs: most
+// tiles only write a fresh grid's reset values, and a CTA per tile would be
+// bound by launching CTAs).  A tile k_integrate_tiles marked skips the
+// per-voxel work.
+template <typename D, bool kFresh>
+__global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a full SM
+    k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
+                const D *__restrict__ depth, const double *__restrict__ tx, const double *__restrict__ ty,
+                const double *__restrict__ tz, const float4 *__restrict__ tp, int *__restrict__ list,
+                unsigned *__restrict__ list_n, unsigned list_cap, const uint8_t *__restrict__ skip,
+                IntegrateArgs a) {
+  const int tiles_x = (nx + 31) / 32, tiles_y = (ny + kTileY - 1) / kTileY;
+  const int64_t ntiles = (int64_t)tiles_x * tiles_y * nz;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t txy = t % ((int64_t)tiles_x * tiles_y);
+    const int z = (int)(t / ((int64_t)tiles_x * tiles_y));
+    const int x = (int)(txy % tiles_x) * 32 + threadIdx.x, y = (int)(txy / tiles_x) * kTileY + threadIdx.y;
+    if (x >= nx || y >= ny) continue;
+    const int64_t i = ((int64_t)z * ny + y) * nx + x;
+    if (__ldg(skip + t)) {  // nothing of the tile is integrated
+      if (kFresh) {
+        phi[i] = a.fresh_phi;
+        w[i] = 0;
+      }
+      continue;
+    }
+    integrate_voxel<D, kFresh>(phi, w, nx, ny, x, y, z, i, depth, tx, ty, tz, tp, list, list_n, list_cap, a);
+  }
 }
 
 // The listed voxels of k_integrate, each on the float64 path.
@@ -558,9 +557,9 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   const unsigned tab_blocks = blocks_for(nx + ny + nz);
   k_integrate_prep<D><<<tab_blocks + (unsigned)(bw * bh), kBlock, 0, s>>>(tx, ty, tz, tp, nx, ny, nz, tab_blocks,
                                                                           depth_dev, flags, bw, a);
-  k_integrate_tiles<<<blocks_for(ntiles, kBlock / 32), kBlock, 0, s>>>(tp, nx, ny, nz, flags, bw, skip, a);
+  k_integrate_tiles<<<blocks_for(ntiles), kBlock, 0, s>>>(tp, nx, ny, nz, flags, bw, skip, a);
   dim3 block(32, kTileY);
-  dim3 grid((nx + 31) / 32, (ny + kTileY - 1) / kTileY, nz);
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)kf_num_sms() * (2048 / kBlock));
   if (fresh_phi)
     k_integrate<D, true><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list, list_n,
                                                 cap, skip, a);
