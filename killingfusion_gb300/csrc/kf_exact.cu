@@ -421,8 +421,10 @@ __device__ __forceinline__ void integrate_voxel(float *__restrict__ phi, int32_t
 // tiles only write a fresh grid's reset values, and a CTA per tile would be
 // bound by launching CTAs).  A tile k_integrate_tiles marked skips the
 // per-voxel work.
+constexpr int kIntegrateCtasPerSm = 6;  // 40 registers
+
 template <typename D, bool kFresh>
-__global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a full SM
+__global__ void __launch_bounds__(kBlock, kIntegrateCtasPerSm)
     k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
                 const D *__restrict__ depth, const double *__restrict__ tx, const double *__restrict__ ty,
                 const double *__restrict__ tz, const float4 *__restrict__ tp, int *__restrict__ list,
@@ -430,10 +432,26 @@ __global__ void __launch_bounds__(kBlock, 2048 / kBlock)  // 32 registers: a ful
                 IntegrateArgs a) {
   const int tiles_x = (nx + 31) / 32, tiles_y = (ny + kTileY - 1) / kTileY;
   const int64_t ntiles = (int64_t)tiles_x * tiles_y * nz;
+  // the tile's coordinates advance by the grid's stride with carries, not
+  // with a division per tile
+  const int64_t plane = (int64_t)tiles_x * tiles_y;
+  const int sx = (int)(gridDim.x % tiles_x), sy = (int)((gridDim.x / tiles_x) % tiles_y);
+  const int sz = (int)(gridDim.x / plane);
+  int cx = (int)(blockIdx.x % tiles_x), cy = (int)((blockIdx.x / tiles_x) % tiles_y), cz = (int)(blockIdx.x / plane);
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int64_t txy = t % ((int64_t)tiles_x * tiles_y);
-    const int z = (int)(t / ((int64_t)tiles_x * tiles_y));
-    const int x = (int)(txy % tiles_x) * 32 + threadIdx.x, y = (int)(txy / tiles_x) * kTileY + threadIdx.y;
+    const int z = cz;
+    const int x = cx * 32 + threadIdx.x, y = cy * kTileY + threadIdx.y;
+    cx += sx;
+    cy += sy;
+    cz += sz;
+    if (cx >= tiles_x) {
+      cx -= tiles_x;
+      ++cy;
+    }
+    if (cy >= tiles_y) {
+      cy -= tiles_y;
+      ++cz;
+    }
     if (x >= nx || y >= ny) continue;
     const int64_t i = ((int64_t)z * ny + y) * nx + x;
     if (__ldg(skip + t)) {  // nothing of the tile is integrated
@@ -559,7 +577,7 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
                                                                           depth_dev, flags, bw, a);
   k_integrate_tiles<<<blocks_for(ntiles), kBlock, 0, s>>>(tp, nx, ny, nz, flags, bw, skip, a);
   dim3 block(32, kTileY);
-  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)kf_num_sms() * (2048 / kBlock));
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)kf_num_sms() * kIntegrateCtasPerSm);
   if (fresh_phi)
     k_integrate<D, true><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list, list_n,
                                                 cap, skip, a);
