@@ -438,7 +438,16 @@ __global__ void __launch_bounds__(kBlock, kIntegrateCtasPerSm)
   const int sx = (int)(gridDim.x % tiles_x), sy = (int)((gridDim.x / tiles_x) % tiles_y);
   const int sz = (int)(gridDim.x / plane);
   int cx = (int)(blockIdx.x % tiles_x), cy = (int)((blockIdx.x / tiles_x) % tiles_y), cz = (int)(blockIdx.x / plane);
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  // lane l holds the flag of the CTA's tile 32 m + l of the current group of
+  // 32, loaded together, so that no tile waits for its own flag
+  int flag = 0;
+  int k = 0;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
+    if ((k & 31) == 0) {
+      const int64_t tt = t + (int64_t)threadIdx.x * gridDim.x;
+      flag = tt < ntiles ? (int)__ldg(skip + tt) : 1;
+    }
+    const int skip_tile = __shfl_sync(0xffffffffu, flag, k & 31);
     const int z = cz;
     const int x = cx * 32 + threadIdx.x, y = cy * kTileY + threadIdx.y;
     cx += sx;
@@ -454,7 +463,7 @@ __global__ void __launch_bounds__(kBlock, kIntegrateCtasPerSm)
     }
     if (x >= nx || y >= ny) continue;
     const int64_t i = ((int64_t)z * ny + y) * nx + x;
-    if (__ldg(skip + t)) {  // nothing of the tile is integrated
+    if (skip_tile) {  // nothing of the tile is integrated
       if (kFresh) {
         phi[i] = a.fresh_phi;
         w[i] = 0;
