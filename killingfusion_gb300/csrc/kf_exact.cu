@@ -136,7 +136,8 @@ __device__ __forceinline__ bool depth_at(const uint16_t *__restrict__ depth, int
 
 // The whole float64 path of one voxel (SDF.cpp:151-193).
 template <typename D>
-__device__ void integrate_exact_voxel(float *__restrict__ phi, int32_t *__restrict__ w, int x, int y, int z,
+__device__ __noinline__ void integrate_exact_voxel(float *__restrict__ phi, int32_t *__restrict__ w, int x, int y,
+                                                   int z,
                                       int64_t i, const D *__restrict__ depth, const IntegrateArgs &a) {
   double u, v, zc;
   project_exact(a, x, y, z, u, v, zc);
@@ -319,6 +320,26 @@ __device__ __forceinline__ int integrate_fresh_ff(float *__restrict__ phi, int32
   return kFfWritten;
 }
 
+// The voxel on the float64 path once its pixel k is known (the float-float
+// decision could not be made, or the voxel holds a weight already): the
+// reference's distance, clip test and running mean.  Out of line: it is
+// rare, and inline its float64 registers would crowd the common path.
+template <typename D, bool kFresh>
+__device__ __noinline__ void integrate_f64_tail(float *__restrict__ phi, int32_t *__restrict__ w, int64_t i, int x,
+                                                int y, int z, const D *__restrict__ depth, int64_t k,
+                                                const double *__restrict__ tx, const double *__restrict__ ty,
+                                                const double *__restrict__ tz, const IntegrateArgs &a, int32_t wi,
+                                                float ph) {
+  double dd;
+  const double zd = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
+  if (!depth_at(depth, k, a, dd) || !integrate_update(phi, w, i, dd, zd, a, wi, ph)) {
+    if (kFresh) {  // nothing integrated
+      phi[i] = a.fresh_phi;
+      w[i] = 0;
+    }
+  }
+}
+
 // SDF::integrateDepthFrame for one voxel per thread.  The pixel a voxel reads
 // flips only where u or v crosses an integer, so the projection runs in float
 // from the per-axis tables and is left to the float64 path when either
@@ -411,59 +432,38 @@ __device__ __forceinline__ void integrate_voxel(float *__restrict__ phi, int32_t
       if (r != kFfUndecided) return;
     }
   }
-  double dd;
-  const double zd = ((__ldg(tx + x) + __ldg(ty + y)) + __ldg(tz + z)) + a.W[11] * 1.0;
-  if (!depth_at(depth, k, a, dd) || !integrate_update(phi, w, i, dd, zd, a, wi, ph)) leave();
+  integrate_f64_tail<D, kFresh>(phi, w, i, x, y, z, depth, k, tx, ty, tz, a, wi, ph);
 }
 
-// The tiles of 32 x kTileY voxels (tiles x-fastest, then y, then z), CTA c
-// taking the tiles c, c + G, c + 2G, ... (a resident grid of G CTAs: most
-// tiles only write a fresh grid's reset values, and a CTA per tile would be
-// bound by launching CTAs).  A tile k_integrate_tiles marked skips the
-// per-voxel work.
-constexpr int kIntegrateCtasPerSm = 6;  // 40 registers
+// One CTA per column of kTileZ tiles of 32 x kTileY voxels (tiles are
+// numbered x-fastest, then y, then z): the column's tile flags are loaded
+// together, a tile k_integrate_tiles marked skips the per-voxel work (a
+// fresh grid only gets its reset values), and a CTA takes several tiles so
+// that the skipped ones are not bound by launching CTAs.
+constexpr int kTileZ = 4;
 
 template <typename D, bool kFresh>
-__global__ void __launch_bounds__(kBlock, kIntegrateCtasPerSm)
+__global__ void __launch_bounds__(kBlock, 6)  // 40 registers
     k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
                 const D *__restrict__ depth, const double *__restrict__ tx, const double *__restrict__ ty,
                 const double *__restrict__ tz, const float4 *__restrict__ tp, int *__restrict__ list,
                 unsigned *__restrict__ list_n, unsigned list_cap, const uint8_t *__restrict__ skip,
                 IntegrateArgs a) {
-  const int tiles_x = (nx + 31) / 32, tiles_y = (ny + kTileY - 1) / kTileY;
-  const int64_t ntiles = (int64_t)tiles_x * tiles_y * nz;
-  // the tile's coordinates advance by the grid's stride with carries, not
-  // with a division per tile
-  const int64_t plane = (int64_t)tiles_x * tiles_y;
-  const int sx = (int)(gridDim.x % tiles_x), sy = (int)((gridDim.x / tiles_x) % tiles_y);
-  const int sz = (int)(gridDim.x / plane);
-  int cx = (int)(blockIdx.x % tiles_x), cy = (int)((blockIdx.x / tiles_x) % tiles_y), cz = (int)(blockIdx.x / plane);
-  // lane l holds the flag of the CTA's tile 32 m + l of the current group of
-  // 32, loaded together, so that no tile waits for its own flag
-  int flag = 0;
-  int k = 0;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
-    if ((k & 31) == 0) {
-      const int64_t tt = t + (int64_t)threadIdx.x * gridDim.x;
-      flag = tt < ntiles ? (int)__ldg(skip + tt) : 1;
-    }
-    const int skip_tile = __shfl_sync(0xffffffffu, flag, k & 31);
-    const int z = cz;
-    const int x = cx * 32 + threadIdx.x, y = cy * kTileY + threadIdx.y;
-    cx += sx;
-    cy += sy;
-    cz += sz;
-    if (cx >= tiles_x) {
-      cx -= tiles_x;
-      ++cy;
-    }
-    if (cy >= tiles_y) {
-      cy -= tiles_y;
-      ++cz;
-    }
-    if (x >= nx || y >= ny) continue;
+  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * kTileY + threadIdx.y;
+  const int z0 = blockIdx.z * kTileZ;
+  const int64_t plane_tiles = (int64_t)gridDim.x * gridDim.y;
+  const int64_t t0 = (int64_t)z0 * plane_tiles + (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
+  unsigned flags = 0;  // bit j: tile j of the column is skipped
+#pragma unroll
+  for (int j = 0; j < kTileZ; ++j)
+    if (z0 + j >= nz || __ldg(skip + t0 + j * plane_tiles)) flags |= 1u << j;
+  if (x >= nx || y >= ny) return;
+#pragma unroll 1
+  for (int j = 0; j < kTileZ; ++j) {
+    const int z = z0 + j;
+    if (z >= nz) break;
     const int64_t i = ((int64_t)z * ny + y) * nx + x;
-    if (skip_tile) {  // nothing of the tile is integrated
+    if ((flags >> j) & 1u) {  // nothing of the tile is integrated
       if (kFresh) {
         phi[i] = a.fresh_phi;
         w[i] = 0;
@@ -586,7 +586,7 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
                                                                           depth_dev, flags, bw, a);
   k_integrate_tiles<<<blocks_for(ntiles), kBlock, 0, s>>>(tp, nx, ny, nz, flags, bw, skip, a);
   dim3 block(32, kTileY);
-  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)kf_num_sms() * kIntegrateCtasPerSm);
+  dim3 grid((nx + 31) / 32, (ny + kTileY - 1) / kTileY, (nz + kTileZ - 1) / kTileZ);
   if (fresh_phi)
     k_integrate<D, true><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list, list_n,
                                                 cap, skip, a);
