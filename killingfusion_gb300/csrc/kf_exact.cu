@@ -156,10 +156,13 @@ __device__ __noinline__ void integrate_exact_voxel(float *__restrict__ phi, int3
 // and the camera-depth product as a float pair, with the rows' constant
 // terms W[3], W[7] and W[11] added to the x entries.
 //
-// The CTAs from `tab_blocks` on mark the depth frame's 16 x 16-pixel blocks
-// that hold a pixel passing the reference's depth test (SDF.cpp:176-179; a
-// NaN passes it): flags[by * bw + bx] = 1.  k_integrate skips a tile of
-// voxels whose possible pixels lie in unmarked blocks only.
+// The next bw * bh CTAs mark the depth frame's 16 x 16-pixel blocks that
+// hold a pixel passing the reference's depth test (SDF.cpp:176-179; a NaN
+// passes it): flags[by * bw + bx] = 1.  k_integrate_tiles skips a tile of
+// voxels whose possible pixels lie in unmarked blocks only.  For a fresh
+// grid (fill != NULL) the remaining CTAs write every voxel's reset values
+// (phi = a.fresh_phi, w = 0; 16-byte stores), which only the listed tiles'
+// voxels then overwrite.
 constexpr int kPixBlock = 16;
 
 template <typename D>
@@ -167,8 +170,27 @@ __global__ void __launch_bounds__(kBlock) k_integrate_prep(double *__restrict__ 
                                                            double *__restrict__ tz, float4 *__restrict__ tp,
                                                            int nx, int ny, int nz, unsigned tab_blocks,
                                                            const D *__restrict__ depth,
-                                                           uint8_t *__restrict__ flags, int bw,
+                                                           uint8_t *__restrict__ flags, int bw, int bh,
+                                                           float *__restrict__ fill_phi,
+                                                           int32_t *__restrict__ fill_w, int64_t count,
                                                            IntegrateArgs a) {
+  const unsigned flag_end = tab_blocks + (unsigned)(bw * bh);
+  if (blockIdx.x >= flag_end) {
+    // phi, w come from cudaMalloc (256-byte aligned); the last count % 4 one by one
+    const unsigned nfill = gridDim.x - flag_end;
+    const int64_t n4 = count >> 2;
+    const float4 v4 = make_float4(a.fresh_phi, a.fresh_phi, a.fresh_phi, a.fresh_phi);
+    for (int64_t k = (int64_t)(blockIdx.x - flag_end) * blockDim.x + threadIdx.x; k < n4;
+         k += (int64_t)nfill * blockDim.x) {
+      reinterpret_cast<float4 *>(fill_phi)[k] = v4;
+      reinterpret_cast<int4 *>(fill_w)[k] = make_int4(0, 0, 0, 0);
+    }
+    if (blockIdx.x == flag_end && threadIdx.x < (count & 3)) {
+      fill_phi[4 * n4 + threadIdx.x] = a.fresh_phi;
+      fill_w[4 * n4 + threadIdx.x] = 0;
+    }
+    return;
+  }
   if (blockIdx.x >= tab_blocks) {
     const int b = (int)(blockIdx.x - tab_blocks), bx = b % bw, by = b / bw;
     const int col = bx * kPixBlock + (int)(threadIdx.x % kPixBlock);
@@ -245,6 +267,7 @@ __device__ __forceinline__ FloatProjection project_float(const float4 *__restric
 // when every 16 x 16-pixel block its pixels can fall in holds no pixel that
 // passes the depth test (every voxel is rejected by SDF.cpp:176-179).
 constexpr int kTileY = kBlock / 32;  // k_integrate's CTA: 32 x kTileY voxels
+constexpr int kIntegrateCtasPerSm = 6;  // resident CTAs of k_integrate (40 registers)
 
 __device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, int nx, int ny, int x0, int y0, int z,
                                                const uint8_t *__restrict__ flags, int bw,
@@ -275,17 +298,30 @@ __device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, in
   return true;
 }
 
-// One thread per tile of k_integrate (tiles x-fastest, then y, then z):
-// skip[t] = 1 when the tile can integrate nothing.
+// One thread per tile of 32 x kTileY voxels (tiles x-fastest, then y, then
+// z): the tiles that can integrate something are appended to `live` (one
+// atomic per warp; the order does not matter, every voxel is written by one
+// thread).
 __global__ void __launch_bounds__(kBlock) k_integrate_tiles(const float4 *__restrict__ tp, int nx, int ny, int nz,
                                                             const uint8_t *__restrict__ flags, int bw,
-                                                            uint8_t *__restrict__ skip, IntegrateArgs a) {
+                                                            int *__restrict__ live, unsigned *__restrict__ n_live,
+                                                            IntegrateArgs a) {
   const int tiles_x = (nx + 31) / 32, tiles_y = (ny + kTileY - 1) / kTileY;
   const int64_t ntiles = (int64_t)tiles_x * tiles_y * nz;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ntiles) return;
-  const int tx = (int)(t % tiles_x), ty = (int)((t / tiles_x) % tiles_y), z = (int)(t / ((int64_t)tiles_x * tiles_y));
-  skip[t] = (uint8_t)tile_skippable(tp, nx, ny, tx * 32, ty * kTileY, z, flags, bw, a);
+  bool keep = false;
+  if (t < ntiles) {
+    const int cx = (int)(t % tiles_x), cy = (int)((t / tiles_x) % tiles_y);
+    const int z = (int)(t / ((int64_t)tiles_x * tiles_y));
+    keep = !tile_skippable(tp, nx, ny, cx * 32, cy * kTileY, z, flags, bw, a);
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, keep);
+  if (!ball) return;
+  const int lane = threadIdx.x & 31;
+  unsigned base = 0;
+  if (lane == 0) base = atomicAdd(n_live, (unsigned)__popc(ball));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (keep) live[base + __popc(ball & ((1u << lane) - 1u))] = (int)t;
 }
 
 // A fresh voxel (w == 0, phi finite) on float depth df, in float-float: the
@@ -435,42 +471,27 @@ __device__ __forceinline__ void integrate_voxel(float *__restrict__ phi, int32_t
   integrate_f64_tail<D, kFresh>(phi, w, i, x, y, z, depth, k, tx, ty, tz, a, wi, ph);
 }
 
-// One CTA per column of kTileZ tiles of 32 x kTileY voxels (tiles are
-// numbered x-fastest, then y, then z): the column's tile flags are loaded
-// together, a tile k_integrate_tiles marked skips the per-voxel work (a
-// fresh grid only gets its reset values), and a CTA takes several tiles so
-// that the skipped ones are not bound by launching CTAs.
-constexpr int kTileZ = 4;
-
+// The live tiles (k_integrate_tiles), a resident grid of CTAs of 32 x
+// kTileY threads, CTA c taking the entries c, c + G, ... of the list.  The
+// other tiles hold nothing to integrate; a fresh grid has their reset
+// values from k_integrate_prep.
 template <typename D, bool kFresh>
-__global__ void __launch_bounds__(kBlock, 6)  // 40 registers
+__global__ void __launch_bounds__(kBlock, kIntegrateCtasPerSm)
     k_integrate(float *__restrict__ phi, int32_t *__restrict__ w, int nx, int ny, int nz,
                 const D *__restrict__ depth, const double *__restrict__ tx, const double *__restrict__ ty,
                 const double *__restrict__ tz, const float4 *__restrict__ tp, int *__restrict__ list,
-                unsigned *__restrict__ list_n, unsigned list_cap, const uint8_t *__restrict__ skip,
-                IntegrateArgs a) {
-  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * kTileY + threadIdx.y;
-  const int z0 = blockIdx.z * kTileZ;
-  const int64_t plane_tiles = (int64_t)gridDim.x * gridDim.y;
-  const int64_t t0 = (int64_t)z0 * plane_tiles + (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
-  unsigned flags = 0;  // bit j: tile j of the column is skipped
-#pragma unroll
-  for (int j = 0; j < kTileZ; ++j)
-    if (z0 + j >= nz || __ldg(skip + t0 + j * plane_tiles)) flags |= 1u << j;
-  if (x >= nx || y >= ny) return;
-#pragma unroll 1
-  for (int j = 0; j < kTileZ; ++j) {
-    const int z = z0 + j;
-    if (z >= nz) break;
-    const int64_t i = ((int64_t)z * ny + y) * nx + x;
-    if ((flags >> j) & 1u) {  // nothing of the tile is integrated
-      if (kFresh) {
-        phi[i] = a.fresh_phi;
-        w[i] = 0;
-      }
-      continue;
-    }
-    integrate_voxel<D, kFresh>(phi, w, nx, ny, x, y, z, i, depth, tx, ty, tz, tp, list, list_n, list_cap, a);
+                unsigned *__restrict__ list_n, unsigned list_cap, const int *__restrict__ live,
+                const unsigned *__restrict__ n_live, IntegrateArgs a) {
+  const unsigned tiles_x = (unsigned)(nx + 31) / 32u, tiles_y = (unsigned)(ny + kTileY - 1) / (unsigned)kTileY;
+  const unsigned n = *n_live;
+  for (unsigned e = blockIdx.x; e < n; e += gridDim.x) {
+    const unsigned t = (unsigned)__ldg(live + e);
+    const unsigned txy = t % (tiles_x * tiles_y);
+    const int z = (int)(t / (tiles_x * tiles_y));
+    const int x = (int)(txy % tiles_x) * 32 + threadIdx.x, y = (int)(txy / tiles_x) * kTileY + threadIdx.y;
+    if (x >= nx || y >= ny) continue;
+    integrate_voxel<D, kFresh>(phi, w, nx, ny, x, y, z, ((int64_t)z * ny + y) * nx + x, depth, tx, ty, tz, tp,
+                               list, list_n, list_cap, a);
   }
 }
 
@@ -559,8 +580,8 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   const int bw = (width + kPixBlock - 1) / kPixBlock, bh = (height + kPixBlock - 1) / kPixBlock;
   const size_t tab_off = 256, flag_off = tab_off + (((size_t)(nx + ny + nz) * 24 + 255) & ~(size_t)255);
   const int64_t ntiles = (int64_t)((nx + 31) / 32) * ((ny + kTileY - 1) / kTileY) * nz;
-  const size_t skip_off = flag_off + (((size_t)bw * bh + 255) & ~(size_t)255);
-  const size_t list_off = skip_off + (((size_t)ntiles + 255) & ~(size_t)255);
+  const size_t live_off = flag_off + (((size_t)bw * bh + 255) & ~(size_t)255);
+  const size_t list_off = live_off + (((size_t)ntiles * sizeof(int) + 255) & ~(size_t)255);
   const size_t bytes = list_off + (size_t)cap * sizeof(int);
   if (g->integ_bytes < bytes) {
     cudaFree(g->integ);
@@ -578,21 +599,23 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   float4 *tp = (float4 *)(base + tab_off);
   double *tx = (double *)(tp + (nx + ny + nz)), *ty = tx + nx, *tz = ty + ny;
   uint8_t *flags = (uint8_t *)(base + flag_off);
-  uint8_t *skip = (uint8_t *)(base + skip_off);
+  int *live = (int *)(base + live_off);
+  unsigned *n_live = list_n + 1;
   int *list = (int *)(base + list_off);
-  KF_CHECK_CUDA(cudaMemsetAsync(list_n, 0, sizeof(unsigned), s));
+  KF_CHECK_CUDA(cudaMemsetAsync(list_n, 0, 2 * sizeof(unsigned), s));
   const unsigned tab_blocks = blocks_for(nx + ny + nz);
-  k_integrate_prep<D><<<tab_blocks + (unsigned)(bw * bh), kBlock, 0, s>>>(tx, ty, tz, tp, nx, ny, nz, tab_blocks,
-                                                                          depth_dev, flags, bw, a);
-  k_integrate_tiles<<<blocks_for(ntiles), kBlock, 0, s>>>(tp, nx, ny, nz, flags, bw, skip, a);
+  const unsigned fill_blocks = fresh_phi ? (unsigned)kf_num_sms() * 4 : 0u;
+  k_integrate_prep<D><<<tab_blocks + (unsigned)(bw * bh) + fill_blocks, kBlock, 0, s>>>(
+      tx, ty, tz, tp, nx, ny, nz, tab_blocks, depth_dev, flags, bw, bh, g->phi, g->w, g->count, a);
+  k_integrate_tiles<<<blocks_for(ntiles), kBlock, 0, s>>>(tp, nx, ny, nz, flags, bw, live, n_live, a);
   dim3 block(32, kTileY);
-  dim3 grid((nx + 31) / 32, (ny + kTileY - 1) / kTileY, (nz + kTileZ - 1) / kTileZ);
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)kf_num_sms() * kIntegrateCtasPerSm);
   if (fresh_phi)
     k_integrate<D, true><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list, list_n,
-                                                cap, skip, a);
+                                                cap, live, n_live, a);
   else
     k_integrate<D, false><<<grid, block, 0, s>>>(g->phi, g->w, nx, ny, nz, depth_dev, tx, ty, tz, tp, list,
-                                                 list_n, cap, skip, a);
+                                                 list_n, cap, live, n_live, a);
   k_integrate_exact<D><<<(unsigned)kf_num_sms() * 4, kBlock, 0, s>>>(g->phi, g->w, nx, ny, depth_dev, list,
                                                                      list_n, cap, a);
   KF_CHECK_LAUNCH("k_integrate");
