@@ -294,7 +294,7 @@ __device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, in
   const int r_lo = max(0, (int)floorf(vlo + 1.0f) - 1), r_hi = min(a.height - 1, (int)floorf(vhi + 1.0f) + 1);
   for (int by = r_lo / kPixBlock; by <= r_hi / kPixBlock; ++by)
     for (int bx = c_lo / kPixBlock; bx <= c_hi / kPixBlock; ++bx)
-      if (flags[by * bw + bx]) return false;
+      if (__ldg(flags + by * bw + bx)) return false;
   return true;
 }
 
@@ -302,17 +302,10 @@ __device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, in
 // z): the tiles that can integrate something are appended to `live` (one
 // atomic per warp; the order does not matter, every voxel is written by one
 // thread).
-//
-// The pixel-block flags are staged in shared memory when they fit
-// (nflags_smem = bw * bh, else 0 and they are read from global memory).
 __global__ void __launch_bounds__(kBlock) k_integrate_tiles(const float4 *__restrict__ tp, int nx, int ny, int nz,
-                                                            const uint8_t *__restrict__ gflags, int bw,
-                                                            int nflags_smem, int *__restrict__ live,
-                                                            unsigned *__restrict__ n_live, IntegrateArgs a) {
-  extern __shared__ uint8_t s_flags[];
-  for (int k = threadIdx.x; k < nflags_smem; k += blockDim.x) s_flags[k] = __ldg(gflags + k);
-  __syncthreads();
-  const uint8_t *flags = nflags_smem ? s_flags : gflags;
+                                                            const uint8_t *__restrict__ flags, int bw,
+                                                            int *__restrict__ live, unsigned *__restrict__ n_live,
+                                                            IntegrateArgs a) {
   const int tiles_x = (nx + 31) / 32, tiles_y = (ny + kTileY - 1) / kTileY;
   const int64_t ntiles = (int64_t)tiles_x * tiles_y * nz;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -614,9 +607,7 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   const unsigned fill_blocks = fresh_phi ? (unsigned)kf_num_sms() * 16 : 0u;
   k_integrate_prep<D><<<tab_blocks + (unsigned)(bw * bh) + fill_blocks, kBlock, 0, s>>>(
       tx, ty, tz, tp, nx, ny, nz, tab_blocks, depth_dev, flags, bw, bh, g->phi, g->w, g->count, a);
-  const int nflags_smem = bw * bh <= 48 * 1024 ? bw * bh : 0;
-  k_integrate_tiles<<<blocks_for(ntiles), kBlock, (size_t)nflags_smem, s>>>(tp, nx, ny, nz, flags, bw, nflags_smem,
-                                                                           live, n_live, a);
+  k_integrate_tiles<<<blocks_for(ntiles), kBlock, 0, s>>>(tp, nx, ny, nz, flags, bw, live, n_live, a);
   dim3 block(32, kTileY);
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)kf_num_sms() * kIntegrateCtasPerSm);
   if (fresh_phi)
