@@ -378,9 +378,9 @@ __device__ __noinline__ void integrate_f64_tail(float *__restrict__ phi, int32_t
 
 // SDF::integrateDepthFrame for one voxel per thread.  The pixel a voxel reads
 // flips only where u or v crosses an integer, so the projection runs in float
-// from the per-axis tables and is left to the float64 path when either
-// coordinate lies within its error bound (below) of an integer, or is not
-// finite.  Those voxels are listed (warp-aggregated) for k_integrate_exact,
+// from the per-axis tables (project_float) and is left to the float64 path
+// when either coordinate lies within its error bound (derived below) of an
+// integer, or is not finite.  Those voxels are listed (warp-aggregated) for k_integrate_exact,
 // so the slow float64 projection runs on full warps instead of stalling the
 // warps they fall in; past the list's capacity a voxel takes the path in
 // place.
