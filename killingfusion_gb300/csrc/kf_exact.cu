@@ -302,10 +302,11 @@ __device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, in
 // z): the tiles that can integrate something are appended to `live` (one
 // atomic per warp; the order does not matter, every voxel is written by one
 // thread).
-__global__ void __launch_bounds__(kBlock) k_integrate_tiles(const float4 *__restrict__ tp, int nx, int ny, int nz,
-                                                            const uint8_t *__restrict__ flags, int bw,
-                                                            int *__restrict__ live, unsigned *__restrict__ n_live,
-                                                            IntegrateArgs a) {
+constexpr int kTileThreads = 64;  // small CTAs: the tile tests are latency chains, spread over every SM
+
+__global__ void __launch_bounds__(kTileThreads)
+    k_integrate_tiles(const float4 *__restrict__ tp, int nx, int ny, int nz, const uint8_t *__restrict__ flags,
+                      int bw, int *__restrict__ live, unsigned *__restrict__ n_live, IntegrateArgs a) {
   const int tiles_x = (nx + 31) / 32, tiles_y = (ny + kTileY - 1) / kTileY;
   const int64_t ntiles = (int64_t)tiles_x * tiles_y * nz;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -607,7 +608,8 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   const unsigned fill_blocks = fresh_phi ? (unsigned)kf_num_sms() * 16 : 0u;
   k_integrate_prep<D><<<tab_blocks + (unsigned)(bw * bh) + fill_blocks, kBlock, 0, s>>>(
       tx, ty, tz, tp, nx, ny, nz, tab_blocks, depth_dev, flags, bw, bh, g->phi, g->w, g->count, a);
-  k_integrate_tiles<<<blocks_for(ntiles), kBlock, 0, s>>>(tp, nx, ny, nz, flags, bw, live, n_live, a);
+  k_integrate_tiles<<<blocks_for(ntiles, kTileThreads), kTileThreads, 0, s>>>(tp, nx, ny, nz, flags, bw, live,
+                                                                               n_live, a);
   dim3 block(32, kTileY);
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)kf_num_sms() * kIntegrateCtasPerSm);
   if (fresh_phi)
