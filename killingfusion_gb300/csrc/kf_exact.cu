@@ -292,9 +292,13 @@ __device__ __forceinline__ bool tile_skippable(const float4 *__restrict__ tp, in
   // the pixels the tile's voxels can read, one more on every side
   const int c_lo = max(0, (int)floorf(ulo + 1.0f) - 1), c_hi = min(a.width - 1, (int)floorf(uhi + 1.0f) + 1);
   const int r_lo = max(0, (int)floorf(vlo + 1.0f) - 1), r_hi = min(a.height - 1, (int)floorf(vhi + 1.0f) + 1);
-  for (int by = r_lo / kPixBlock; by <= r_hi / kPixBlock; ++by)
-    for (int bx = c_lo / kPixBlock; bx <= c_hi / kPixBlock; ++bx)
-      if (__ldg(flags + by * bw + bx)) return false;
+  // a row of blocks at a time, its flags loaded back to back and or-ed
+  for (int by = r_lo / kPixBlock; by <= r_hi / kPixBlock; ++by) {
+    const uint8_t *row = flags + by * bw;
+    unsigned any = 0;
+    for (int bx = c_lo / kPixBlock; bx <= c_hi / kPixBlock; ++bx) any |= __ldg(row + bx);
+    if (any) return false;
+  }
   return true;
 }
 
