@@ -237,12 +237,14 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
 //   iterations, ordered by the barrier's fences), the SDFs through the
 //   read-only path.  A gated iteration (converged, diverged) ends the kernel
 //   in every block alike: each reads the same statistics after the barrier.
-// 128-thread blocks, 1 per SM: a 255-register budget (the band update does
-// not spill), four warps a block, half of each SM's registers left to the
+// 96-thread blocks, 1 per SM: a 255-register budget (the band update does
+// not spill), three warps a block, most of each SM's registers left to the
 // frame's other kernels, which run beside the solve.  The grid barrier's
 // cost grows with the number of blocks (alone, with no work between
-// barriers: 2.3 us for 608 blocks, 1.5 us for 304, 1.3 us for 152).
-constexpr int kPersistThreads = 128;
+// barriers: 2.3 us for 608 blocks, 1.5 us for 304, 1.3 us for 152); of
+// 64-256 threads a block, 96 gave the bench's band (about 95 voxels a block)
+// its shortest iterations.
+constexpr int kPersistThreads = 96;
 constexpr int kPersistWarps = kPersistThreads / 32;
 constexpr int kPersistBlocksPerSM = 1;
 
