@@ -236,7 +236,10 @@ __global__ void __launch_bounds__(kLaneThreads, kLaneBlocksPerSM) k_fused_band(F
 // - psi is read through L1 and L2 (kPsiL1: the blocks write it between
 //   iterations, ordered by the barrier's fences), the SDFs through the
 //   read-only path.  A gated iteration (converged, diverged) ends the kernel
-//   in every block alike: each reads the same statistics after the barrier.
+//   in every block alike: the barrier brings each block the same verdict
+//   (grid_sync_verdict), so no block reads the statistics after it, and a
+//   block's first round of voxels comes from shared memory: the psi loads
+//   of the next iteration start as soon as the barrier lets a block go.
 // 96-thread blocks, 1 per SM: a 255-register budget (the band update does
 // not spill), three warps a block, most of each SM's registers left to the
 // frame's other kernels, which run beside the solve.  The grid barrier's
@@ -250,9 +253,11 @@ constexpr int kPersistBlocksPerSM = 1;
 
 // Compacts the voxels `next` (>= 0 on the threads that carry one) of the
 // block into out[base...] (capacity entries), with no atomic; returns how
-// many there were.  Every thread of the block calls it.
+// many there were.  The first kPersistThreads entries of out (the next
+// iteration's first round) also go to first[].  Every thread of the block
+// calls it.
 __device__ __forceinline__ unsigned block_compact(int next, int *__restrict__ out, unsigned base,
-                                                  unsigned capacity) {
+                                                  unsigned capacity, int *first) {
   __shared__ unsigned s_w[kPersistWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool has = next >= 0;
@@ -269,27 +274,26 @@ __device__ __forceinline__ unsigned block_compact(int next, int *__restrict__ ou
   if (has) {
     const unsigned pos = base + before + (unsigned)__popc(ball & ((1u << lane) - 1u));
     if (KF_IN_BOUNDS(pos, capacity, KF_SITE_BAND_APPEND)) out[pos] = next;
+    if (pos < (unsigned)kPersistThreads) first[pos] = next;
   }
   __syncthreads();  // s_w is written again by the next call
   return total;
 }
 
 // Iteration `it` of the block's n voxels in[0..n) (carried ones to out,
-// n updated); false when the kernel must end (the iteration was gated, was
-// the last, or a barrier wait gave up).
+// n updated); false when the kernel must end (the iteration was the last,
+// a barrier wait gave up, or the next iteration is gated).  The entries
+// in[0..kPersistThreads) are read from first[] (from `in` at it == 0), so
+// that a thread's first voxel is known as soon as the barrier lets it go.
+// seen: grid_sync_verdict's record of this iteration's barrier word.
 __device__ __forceinline__ bool persistent_band_iteration(const FusedArgs &a, int it, bool last,
                                                           const int *__restrict__ in, int *__restrict__ out,
                                                           unsigned &n, unsigned capacity, GridSync *sync,
-                                                          unsigned long long limit_ns) {
+                                                          unsigned long long limit_ns, int *first,
+                                                          unsigned long long &seen) {
   const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned k0 = lane * kPersistWarps + warp;  // this thread's voxel of round 0
-  // its list entry is loaded before the gate reads the previous iteration's
-  // statistics, so that the two loads overlap
-  const int v0 = k0 < n ? __ldcg(in + k0) : -1;
-  if (iteration_gated(a.st, it, a.dp)) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.st[it].skipped = 1;
-    return false;
-  }
+  const int v0 = k0 < n ? (it == 0 ? __ldcg(in + k0) : first[k0]) : -1;
   const unsigned rounds = (n + kPersistThreads - 1) / kPersistThreads;
   float maxd = 0.f;
   double energy = 0.0;
@@ -302,13 +306,26 @@ __device__ __forceinline__ bool persistent_band_iteration(const FusedArgs &a, in
       const int v = r == 0 ? v0 : __ldcg(in + k);
       next = update_band_voxel<false, kPsiL1>(a, v, v, maxd, energy, active, diverged);
     }
-    carried += block_compact(next, out, carried, capacity);
+    carried += block_compact(next, out, carried, capacity, first);
   }
   n = carried;
-  reduce_iter_stats<kPersistThreads>(a.st + it, active, maxd, energy, diverged);
-  if (last) return false;
-  if (!grid_sync(sync, gridDim.x, limit_ns, it)) {
+  BlockStats b{};  // the block's totals, on thread 0
+  reduce_iter_stats<kPersistThreads>(a.st + it, active, maxd, energy, diverged, &b);
+  if (last) {
+    if (threadIdx.x == 0) commit_iter_stats(a.st + it, b);
+    return false;
+  }
+  // the gate of iteration it + 1 (iteration_gated): no block diverged, and
+  // with early_exit some block moved psi by more than the threshold; the
+  // statistics are committed while the barrier completes
+  bool any_open = false, any_fail = false;
+  if (!grid_sync_verdict(sync, gridDim.x, limit_ns, it, b.max_delta > (float)a.dp.threshold, b.diverged, seen,
+                         any_open, any_fail, [&] { commit_iter_stats(a.st + it, b); })) {
     if (threadIdx.x == 0) a.st[0].timeout = 1;
+    return false;
+  }
+  if (any_fail || (a.dp.early_exit && !any_open)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st[it + 1].skipped = 1;
     return false;
   }
   return true;
@@ -323,11 +340,14 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistBlocksPerSM)
   const unsigned per = (nq + gridDim.x - 1) / gridDim.x;  // this block's slice [k0, k0 + per)
   const unsigned k0 = min(blockIdx.x * per, nq);
   unsigned n = min(k0 + per, nq) - k0;
+  __shared__ int s_first[kPersistThreads];
+  unsigned long long seen_even = 0, seen_odd = 0;
   for (int it = 0; it < iterations; it += 2) {
-    if (!persistent_band_iteration(even, it, it + 1 == iterations, lst0 + k0, lst1 + k0, n, per, sync, limit_ns))
+    if (!persistent_band_iteration(even, it, it + 1 == iterations, lst0 + k0, lst1 + k0, n, per, sync, limit_ns,
+                                   s_first, seen_even))
       return;
     if (it + 1 < iterations && !persistent_band_iteration(odd, it + 1, it + 2 == iterations, lst1 + k0, lst0 + k0,
-                                                          n, per, sync, limit_ns))
+                                                          n, per, sync, limit_ns, s_first, seen_odd))
       return;
   }
 }

@@ -346,11 +346,31 @@ __device__ float monitor_energy(const P *px, const P *py, const P *pz, int nx, i
   return e;
 }
 
+// A block's totals of one iteration's statistics.
+struct BlockStats {
+  double energy;
+  unsigned active;
+  float max_delta;
+  bool diverged;
+};
+
+// Adds a block's totals into st (one atomic per quantity).
+__device__ __forceinline__ void commit_iter_stats(IterStats *st, const BlockStats &b) {
+  if (b.active || b.max_delta > 0.f || b.energy != 0.0) {
+    if (b.active) atomicAdd(&st->active, b.active);
+    atomicMax(&st->max_delta, __float_as_uint(b.max_delta));
+    atomicAdd(&st->energy, b.energy);
+  }
+  if (b.diverged) st->diverged = 1;
+}
+
 // Block-wide reduction of the per-iteration statistics into st (one atomic
-// per block and quantity).  Every thread of the block must call it.
+// per block and quantity).  Every thread of the block must call it.  With
+// `out`, thread 0 receives the block's totals there instead, and commits
+// them itself.
 template <int kThreads>
 __device__ void reduce_iter_stats(IterStats *st, unsigned active, float max_delta, double energy,
-                                  bool diverged) {
+                                  bool diverged, BlockStats *out = nullptr) {
   __shared__ double s_e[kThreads / 32];
   __shared__ float s_m[kThreads / 32];
   __shared__ unsigned s_a[kThreads / 32];
@@ -382,12 +402,13 @@ __device__ void reduce_iter_stats(IterStats *st, unsigned active, float max_delt
       max_delta = fmaxf(max_delta, __shfl_xor_sync(0xffffffffu, max_delta, o));
       active += __shfl_xor_sync(0xffffffffu, active, o);
     }
-    if (lane == 0 && (active || max_delta > 0.f || energy != 0.0)) {
-      if (active) atomicAdd(&st->active, active);
-      atomicMax(&st->max_delta, __float_as_uint(max_delta));
-      atomicAdd(&st->energy, energy);
+    if (lane == 0) {
+      const BlockStats b{energy, active, max_delta, s_d != 0};
+      if (out)
+        *out = b;
+      else
+        commit_iter_stats(st, b);
     }
-    if (lane == 0 && s_d) st->diverged = 1;
   }
 }
 

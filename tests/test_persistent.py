@@ -82,3 +82,50 @@ def test_wait_limit_gives_timeout_status(gpu):
     assert st["iterations_run"] == 20
     with pytest.raises(ValueError):
         capi.set_wait_limit(-1.0)
+
+
+@pytest.mark.parametrize("probe", [40, 41])
+def test_persistent_band_early_exit_either_parity(gpu, probe):
+    """The gate of the next iteration comes with the barrier, in one of two
+    words by the barrier's parity: a threshold at the last step of a solve
+    of `probe` iterations stops the loop after an even and an odd
+    iteration, where the dense solver stops."""
+    capi = gpu
+    P0 = capi.Params.reference(0.004, 5.0)
+    gl, gc, dims = grids(capi, P0, seed=61)
+    _, sp = solve(capi, gl, gc, dims, P0, probe, "band")
+    P = P0.with_(early_exit=True, threshold=float(sp["max_delta_last"]) * 1.0001)
+    a, sa = solve(capi, gl, gc, dims, P, 300, "band")
+    b, sb = solve(capi, gl, gc, dims, P, 300, "fused")
+    assert sa["converged"] == 1 and 1 < sa["iterations_run"] <= probe
+    for k in ("iterations_run", "active_first", "active_last", "max_delta_last", "converged", "diverged"):
+        assert sa[k] == sb[k], k
+    np.testing.assert_array_equal(a, b)
+
+
+def test_persistent_band_divergence_equals_dense(gpu):
+    """A non-finite psi inside the band: the band solver reports
+    KF_ERR_DIVERGED after the same iterations as the dense solver, with the
+    same psi and statistics."""
+    capi = gpu
+    L = capi.load()
+    P = capi.Params.paper(0.004)
+    gl, gc, dims = grids(capi, P, seed=63)
+    live, _ = gl.download()
+    z, y, x = np.argwhere((live > -0.004) & (live < 0.004))[0]
+    psi = np.zeros(live.shape + (3,), np.float32)
+    psi[z, y, x, 0] = np.nan
+    got = {}
+    for solver in ("band", "fused"):
+        f = capi.Field(dims, capi.KF_F32)
+        f.upload(psi)
+        st = capi.SolveStats()
+        rc = L.kf_psi_solve(gl.h, gc.h, f.h, capi.C.byref(P.c()), 20, capi.SOLVERS[solver], capi.C.byref(st), None)
+        assert rc == capi.KF_ERR_DIVERGED, (solver, rc)
+        got[solver] = (f.download(), st.as_dict())
+        f.close()
+    (a, sa), (b, sb) = got["band"], got["fused"]
+    assert sa["diverged"] == 1
+    for k in ("iterations_run", "active_first", "active_last", "converged", "diverged"):
+        assert sa[k] == sb[k], k
+    np.testing.assert_array_equal(a, b)
