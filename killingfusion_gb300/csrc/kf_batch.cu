@@ -303,6 +303,7 @@ static int batch_upload_table(kf_batch b, cudaStream_t s) {
   const int n = (int)b->items.size();
   for (int p = 0; p < n; ++p) {
     const kf_batch_item &it = b->items[p];
+    kf_field_written(it.psi);  // the batch's passes write both planes
     DevParams dp = kf_make_dev_params(it.live->n, &it.params);
     BatchEntry &e = b->tab_host[p];
     IterStats *st = b->stats + (int64_t)p * stats_stride(b);

@@ -442,8 +442,16 @@ int kf_field_ensure_pair(kf_field f) {
 
 extern "C" int kf_field_zero(kf_field f, void *stream) {
   KF_REQUIRE(f, "field is NULL");
-  for (int k = 0; k < 3; ++k)
-    KF_CHECK_CUDA(cudaMemsetAsync(f->p[k], 0, f->count * kf_prec_size(f->prec), kf_stream(stream)));
+  const bool q_was_zero = f->q_zero;
+  const bool q_too = f->q[0] && f->q_zero_wanted && !q_was_zero;
+  kf_field_written(f);  // (until every memset is queued)
+  const size_t bytes = f->count * kf_prec_size(f->prec);
+  for (int k = 0; k < 3; ++k) KF_CHECK_CUDA(cudaMemsetAsync(f->p[k], 0, bytes, kf_stream(stream)));
+  // the band-only solver's ping-pong buffer, once that solver has used the
+  // field: its first pass then reads phi_live alone (no copy of psi)
+  for (int k = 0; q_too && k < 3; ++k) KF_CHECK_CUDA(cudaMemsetAsync(f->q[k], 0, bytes, kf_stream(stream)));
+  f->p_zero = true;
+  f->q_zero = q_was_zero || q_too;
   return KF_OK;
 }
 
@@ -497,6 +505,7 @@ static int field_copy(kf_field f, void *xyz, bool upload, cudaStream_t s) {
 
 extern "C" int kf_field_upload(kf_field f, const void *xyz, void *stream) {
   KF_REQUIRE(f && xyz, "field or buffer is NULL");
+  kf_field_written(f);
   return field_copy(f, const_cast<void *>(xyz), true, kf_stream(stream));
 }
 
@@ -507,6 +516,7 @@ extern "C" int kf_field_download(kf_field f, void *xyz, void *stream) {
 
 extern "C" int kf_field_device(kf_field f, void **px, void **py, void **pz) {
   KF_REQUIRE(f, "field is NULL");
+  f->exposed = true;  // the caller may write the planes from now on
   if (px) *px = f->p[0];
   if (py) *py = f->p[1];
   if (pz) *pz = f->p[2];
@@ -763,10 +773,16 @@ static int solve_launch(kf_grid live, kf_grid canonical, kf_field psi, const kf_
   for (int k = 0; k < 3; ++k)
     if (!psi->ev[k]) KF_CHECK_CUDA(cudaEventCreate(&psi->ev[k]));
   KF_CHECK_CUDA(cudaEventRecord(psi->ev[0], s));
+  // every solver writes psi's planes; the band-only solver's first pass
+  // reads phi_live alone when both start at zero, and from now on
+  // kf_field_zero clears its ping-pong buffer too
+  const bool psi_zero = psi->p_zero && psi->q_zero && !psi->exposed;
+  kf_field_written(psi);
+  if (solver == KF_SOLVER_BAND) psi->q_zero_wanted = true;
   if (solver == KF_SOLVER_PERVOXEL)
     rc = kf_solve_pervoxel(live, canonical, psi, dp, iterations, st, s);
   else if (solver == KF_SOLVER_FUSED || solver == KF_SOLVER_BAND)
-    rc = kf_solve_fused(live, canonical, psi, dp, iterations, st, solver == KF_SOLVER_BAND, s);
+    rc = kf_solve_fused(live, canonical, psi, dp, iterations, st, solver == KF_SOLVER_BAND, psi_zero, s);
   else if (solver == KF_SOLVER_PLAIN)
     rc = kf_solve_plain(live, canonical, psi, dp, iterations, st, s);
   else

@@ -1005,6 +1005,7 @@ static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevPara
   // holds nothing between solves: values, weights and indices, N each
   int st = kf_field_ensure_pair(psi);
   if (st) return st;
+  kf_field_q_written(psi);
   float *side_phi = (float *)psi->q[0];
   int32_t *side_w = (int32_t *)psi->q[1];
   int32_t *side_i = (int32_t *)psi->q[2];
@@ -1341,6 +1342,7 @@ extern "C" int kf_field_add_voxels(kf_field f, const int32_t *xyz, int n, const 
                                    void *stream) {
   KF_REQUIRE(f && (xyz || n == 0) && (delta || n == 0), "NULL argument");
   KF_REQUIRE(n >= 0, "n must be >= 0");
+  kf_field_written(f);
   for (int i = 0; i < n; ++i) {
     int64_t j = (int64_t)xyz[3 * i + 2] * f->n[0] * f->n[1] + (int64_t)xyz[3 * i + 1] * f->n[0] + xyz[3 * i];
     KF_REQUIRE(j >= 0 && j < f->count, "voxel index outside the displacement field");
@@ -1369,6 +1371,7 @@ extern "C" int kf_field_add(kf_field f, kf_field other, void *stream) {
   KF_REQUIRE(f->count == other->count && f->n[0] == other->n[0] && f->n[1] == other->n[1],
              "field sizes differ");
   KF_REQUIRE(f->prec == other->prec, "field precisions differ");
+  kf_field_written(f);
   unsigned nb = blocks_for(f->count);
   cudaStream_t s = kf_stream(stream);
   if (f->prec == KF_F32)
@@ -1385,6 +1388,7 @@ extern "C" int kf_field_add(kf_field f, kf_field other, void *stream) {
 
 extern "C" int kf_field_fill(kf_field f, const double v[3], void *stream) {
   KF_REQUIRE(f && v, "NULL argument");
+  kf_field_written(f);
   unsigned nb = blocks_for(f->count);
   cudaStream_t s = kf_stream(stream);
   if (f->prec == KF_F32)

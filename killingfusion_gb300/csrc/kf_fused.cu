@@ -73,6 +73,15 @@ __global__ void __launch_bounds__(kThreads) k_fused_stream(FusedArgs a, int *__r
   stream_flat<kPassThrough>(a, blockIdx.x, list, &a.st[a.iter].list, runs ? runs + blockIdx.x : nullptr);
 }
 
+// The band-only solver's first band test when both psi buffers are zero at
+// every voxel: psi(i) = 0 samples voxel i's own cell with zero weights, so
+// the test reads phi_live alone (4 B a voxel, against 16 B read and 12 B
+// copied by k_fused_stream<true>), and the second buffer already holds
+// every voxel's psi.  The same list as k_fused_stream<true> gives.
+__global__ void __launch_bounds__(kThreads) k_band_first_zero(FusedArgs a, int *__restrict__ list) {
+  stream_flat<false, false, true>(a, blockIdx.x, list, &a.st[a.iter].list, nullptr);
+}
+
 // Split dense schedule (grids of at least kSplitMinRuns runs).  After the
 // first iteration's dense pass, k_split_runs sorts the runs into those that
 // listed band voxels ("hot") and the others ("cold"), each in run order.  A
@@ -636,11 +645,12 @@ static int persistent_blocks_per_sm() {
   return cached[dev];
 }
 
-// KF_SOLVER_BAND without the trust-region step: the dense first pass, then
-// every band pass in one cooperative launch (k_band_persistent).  Iteration
-// k reads buffer k % 2 and writes (k + 1) % 2, as the per-iteration form.
+// KF_SOLVER_BAND without the trust-region step: the dense first pass (on
+// phi_live alone when psi_zero: both buffers are zero), then every band pass
+// in one cooperative launch (k_band_persistent).  Iteration k reads buffer
+// k % 2 and writes (k + 1) % 2, as the per-iteration form.
 static int launch_band_persistent(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
-                                  int iterations, IterStats *st, cudaStream_t s) {
+                                  int iterations, IterStats *st, bool psi_zero, cudaStream_t s) {
   void *sync = nullptr;
   int rc = kf_field_sync(psi, &sync);
   if (rc) return rc;
@@ -662,7 +672,10 @@ static int launch_band_persistent(kf_grid live, kf_grid can, kf_field psi, const
   odd.oy = (float *)psi->p[1];
   odd.oz = (float *)psi->p[2];
   int *lst0 = psi->band, *lst1 = psi->band + dp.count;
-  k_fused_stream<true><<<(unsigned)num_runs(dp), kThreads, 0, s>>>(even, lst0, nullptr, nullptr);
+  if (psi_zero)
+    k_band_first_zero<<<(unsigned)num_runs(dp), kThreads, 0, s>>>(even, lst0);
+  else
+    k_fused_stream<true><<<(unsigned)num_runs(dp), kThreads, 0, s>>>(even, lst0, nullptr, nullptr);
   KF_CHECK_LAUNCH("dense first pass of the band-only solver");
   GridSync *gs = static_cast<GridSync *>(sync);
   unsigned long long limit = kf_wait_limit_ns();
@@ -675,7 +688,7 @@ static int launch_band_persistent(kf_grid live, kf_grid can, kf_field psi, const
 }
 
 int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp, int iterations,
-                   IterStats *st, bool band_only, cudaStream_t s) {
+                   IterStats *st, bool band_only, bool psi_zero, cudaStream_t s) {
   int rc = kf_field_ensure_pair(psi);
   if (rc) return rc;
   rc = kf_field_band_list(psi, &psi->band);
@@ -691,7 +704,7 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
     }
     psi->runs_cap = nruns;
   }
-  if (band_only && !dp.trust) return launch_band_persistent(live, can, psi, dp, iterations, st, s);
+  if (band_only && !dp.trust) return launch_band_persistent(live, can, psi, dp, iterations, st, psi_zero, s);
   int *rows = nullptr;
   if (dp.trust) {
     rc = kf_field_trust_rows(psi, &rows);

@@ -480,8 +480,9 @@ __device__ __forceinline__ void flat_test(const FusedArgs &a, int64_t i, float q
 
 // kCheck: the run is only tested, its band voxels are counted in *count and
 // not listed (the split schedule's runs without band voxels, where a band
-// voxel would break an invariant of the solver).
-template <bool kPassThrough, bool kCheck = false>
+// voxel would break an invariant of the solver).  kPsiZero: psi is zero at
+// every voxel (nothing of it is read), so the test reads phi_live alone.
+template <bool kPassThrough, bool kCheck = false, bool kPsiZero = false>
 __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int *__restrict__ list,
                                             unsigned *count, int2 *__restrict__ range = nullptr) {
   __shared__ int queue[kFlatVoxels + 4];
@@ -498,11 +499,11 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
 #pragma unroll
   for (int g = 0; g < kFlatGroups; ++g) {
     q[g] = run * (kThreads * kFlatGroups) + g * kThreads + tid;
-    const bool ok = q[g] < n4;
+    const bool ok = q[g] < n4, read_psi = ok && !kPsiZero;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    px[g] = ok ? __ldcs(ix + q[g]) : zero;
-    py[g] = ok ? __ldcs(iy + q[g]) : zero;
-    pz[g] = ok ? __ldcs(iz + q[g]) : zero;
+    px[g] = read_psi ? __ldcs(ix + q[g]) : zero;
+    py[g] = read_psi ? __ldcs(iy + q[g]) : zero;
+    pz[g] = read_psi ? __ldcs(iz + q[g]) : zero;
     ph[g] = ok ? __ldg(lv + q[g]) : zero;
   }
   unsigned moved = 0;  // bit 4g + e: element e of group g has moved
@@ -523,7 +524,7 @@ __device__ __forceinline__ void stream_flat(const FusedArgs &a, int64_t run, int
   // the ragged end of the grid, by run 0
   if (run == 0 && tid < (int)(dp.count & 3)) {
     const int64_t i = 4 * n4 + tid;
-    const float qx = a.ix[i], qy = a.iy[i], qz = a.iz[i];
+    const float qx = kPsiZero ? 0.f : a.ix[i], qy = kPsiZero ? 0.f : a.iy[i], qz = kPsiZero ? 0.f : a.iz[i];
     flat_test(a, i, qx, qy, qz, __ldg(a.live + i), queue, &qn, moved, 4 * kFlatGroups);
     if (kPassThrough) {
       a.ox[i] = qx;

@@ -60,7 +60,19 @@ struct kf_field_s {
   int last_iterations;
   kf_solver last_solver;
   int pending;
+  // What is known of the planes' contents once the work queued so far has
+  // run (the flags follow the order calls are made in, which is the order a
+  // caller must give the streams they use): p all zero (kf_field_zero),
+  // q all zero (kf_field_zero, once the band-only solver has used the field:
+  // q_zero_wanted).  Every other write clears them (kf_field_written), and
+  // nothing is known once kf_field_device has handed the planes out.  With
+  // both, the band-only solver's first pass reads phi_live alone.
+  bool p_zero, q_zero, q_zero_wanted, exposed;
 };
+
+// A call is about to write psi's planes (both, or q alone).
+inline void kf_field_written(kf_field f) { f->p_zero = f->q_zero = false; }
+inline void kf_field_q_written(kf_field f) { f->q_zero = false; }
 
 // ---------------------------------------------------------------------------
 // error state
@@ -149,13 +161,15 @@ int kf_bounds_tu_reset_mc(long long limit);
 
 // Limit of one device-side wait (kf_set_wait_limit), in nanoseconds.
 unsigned long long kf_wait_limit_ns();
-// Barrier state of the persistent kernels (GridSync, 16 bytes) of a field,
+// Barrier state of the persistent kernels (GridSync, 32 bytes) of a field,
 // lazily allocated.
 int kf_field_sync(kf_field f, void **out);
 
 // solver entry points implemented in the solver translation units
+// psi_zero: both of psi's planes are all zero when the solve starts
+// (kf_field_s::p_zero and q_zero).
 int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
-                   int iterations, IterStats *stats_dev, bool band_only, cudaStream_t s);
+                   int iterations, IterStats *stats_dev, bool band_only, bool psi_zero, cudaStream_t s);
 int kf_solve_plain(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
                    int iterations, IterStats *stats_dev, cudaStream_t s);
 int kf_solve_exact(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,

@@ -165,6 +165,7 @@ extern "C" int kf_state_load(const char *path, kf_grid canonical, kf_field psi, 
   }
   Pinned stage;
   KF_CHECK_CUDA(cudaMallocHost(&stage.p, kChunk));
+  if (psi) kf_field_written(psi);
   rc = read_device(f.f, canonical->phi, (size_t)h.count * sizeof(float), stage.p, s);
   if (!rc) rc = read_device(f.f, canonical->w, (size_t)h.count * sizeof(int32_t), stage.p, s);
   for (int k = 0; psi && !rc && k < 3; ++k)

@@ -129,3 +129,50 @@ def test_persistent_band_divergence_equals_dense(gpu):
     for k in ("iterations_run", "active_first", "active_last", "converged", "diverged"):
         assert sa[k] == sb[k], k
     np.testing.assert_array_equal(a, b)
+
+
+def test_band_first_pass_on_a_zero_field(gpu):
+    """Once the band-only solver has used a field, kf_field_zero clears both
+    of its buffers, and the next band-only solve's first pass reads phi_live
+    alone.  Whatever wrote psi before the zero (a warp, which borrows the
+    second buffer; an upload; a fill; a dense solve; a per-voxel update), a
+    band-only solve from zero gives the dense solver's psi and statistics;
+    and a write after the zero sends the solve back to the first pass that
+    reads psi, with the dense solver's result from the same psi."""
+    capi = gpu
+    P = capi.Params.reference(0.004, 5.0)
+    gl, gc, dims = grids(capi, P, seed=64)
+    expect, se = solve(capi, gl, gc, dims, P, 40, "fused")
+    scratch = capi.Grid(dims, P.voxel_size, (0, 0, 0), P.unknown_clip, P)
+    scratch.upload(*gl.download())
+    rng = np.random.default_rng(5)
+    nonzero = (rng.standard_normal(gl.shape + (3,)) * 0.2).astype(np.float32)
+    keys = ("iterations_run", "active_first", "active_last", "max_delta_last", "converged", "diverged")
+    f = capi.Field(dims, capi.KF_F32)
+    writes = [
+        lambda g: None,
+        lambda g: capi.warp(scratch, g, P),
+        lambda g: g.upload(nonzero),
+        lambda g: capi.field_fill(g, (0.05, -0.025, 0.0125)),
+        lambda g: capi.psi_solve(gl, gc, g, P, 3, "fused"),
+        lambda g: capi.field_add_voxels(g, [[20, 21, 19]], [[0.3, 0.0, -0.2]]),
+    ]
+    for k, write in enumerate(writes):
+        write(f)
+        f.zero()
+        st = capi.psi_solve(gl, gc, f, P, 40, "band")
+        np.testing.assert_array_equal(f.download(), expect, err_msg=str(k))
+        for key in keys:
+            assert st[key] == se[key], (k, key)
+    for k, write in enumerate(writes[2:]):
+        f.zero()
+        write(f)
+        st = capi.psi_solve(gl, gc, f, P, 40, "band")
+        g = capi.Field(dims, capi.KF_F32)
+        write(g)
+        sg = capi.psi_solve(gl, gc, g, P, 40, "fused")
+        np.testing.assert_array_equal(f.download(), g.download(), err_msg=str(k))
+        for key in keys:
+            assert st[key] == sg[key], (k, key)
+        g.close()
+    f.close()
