@@ -399,9 +399,25 @@ int kf_field_sync(kf_field f, void **out) {
   return KF_OK;
 }
 
+int kf_field_records(kf_field f, int **touched, unsigned **touched_n, unsigned **side_n) {
+  if (!f->touched && cudaMalloc(&f->touched, (f->count + 64) * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    f->touched = nullptr;
+    return kf_fail(KF_ERR_OOM, "cudaMalloc of the field's records failed");
+  }
+  *touched = f->touched;
+  *touched_n = reinterpret_cast<unsigned *>(f->touched + f->count);
+  *side_n = *touched_n + 1;
+  return KF_OK;
+}
+
 void kf_field_release_solver(kf_field f) {
   cudaFree(f->sync);
   f->sync = nullptr;
+  cudaFree(f->touched);
+  f->touched = nullptr;
+  f->p_state = f->p_state == kPsiRecorded ? kPsiUnknown : f->p_state;
+  f->q_state = f->q_state == kPsiRecorded ? kPsiUnknown : f->q_state;
   cudaFree(f->band);
   cudaFree(f->runs);
   f->runs = nullptr;
@@ -440,18 +456,49 @@ int kf_field_ensure_pair(kf_field f) {
   return KF_OK;
 }
 
+// kf_field_zero of float buffers that are zero outside the field's records:
+// every plane of p and/or q (NULL: left alone) at the voxels touched[0, n),
+// and q's planes at their entries [0, *side_n).
+__global__ void k_zero_records(float *p0, float *p1, float *p2, float *q0, float *q1, float *q2,
+                               const int *__restrict__ touched, const unsigned *touched_n,
+                               const unsigned *side_n, int64_t count) {
+  const int64_t n = *touched_n, m = q0 ? *side_n : 0u;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n + m; k += (int64_t)gridDim.x * blockDim.x) {
+    if (k < n) {
+      const int64_t v = touched[k];
+      if (v < 0 || v >= count) continue;
+      if (p0) p0[v] = p1[v] = p2[v] = 0.f;
+      if (q0) q0[v] = q1[v] = q2[v] = 0.f;
+    } else if (k - n < count) {
+      q0[k - n] = q1[k - n] = q2[k - n] = 0.f;
+    }
+  }
+}
+
 extern "C" int kf_field_zero(kf_field f, void *stream) {
   KF_REQUIRE(f, "field is NULL");
-  const bool q_was_zero = f->q_zero;
-  const bool q_too = f->q[0] && f->q_zero_wanted && !q_was_zero;
-  kf_field_written(f);  // (until every memset is queued)
+  cudaStream_t s = kf_stream(stream);
+  const int ps = f->exposed ? kPsiUnknown : f->p_state, qs = f->exposed ? kPsiUnknown : f->q_state;
+  // the band-only solver's ping-pong buffer too, once that solver has used
+  // the field: its first pass then reads phi_live alone (no copy of psi)
+  const bool q_too = f->q[0] && f->q_zero_wanted;
+  kf_field_written(f);  // (until every clear is queued)
+  if (ps == kPsiRecorded || (q_too && qs == kPsiRecorded)) {
+    int *touched;
+    unsigned *touched_n, *side_n;
+    int rc = kf_field_records(f, &touched, &touched_n, &side_n);
+    if (rc) return rc;
+    const bool zp = ps == kPsiRecorded, zq = q_too && qs == kPsiRecorded;
+    k_zero_records<<<(unsigned)kf_num_sms() * 4, 256, 0, s>>>(
+        zp ? (float *)f->p[0] : nullptr, (float *)f->p[1], (float *)f->p[2], zq ? (float *)f->q[0] : nullptr,
+        (float *)f->q[1], (float *)f->q[2], touched, touched_n, side_n, f->count);
+    KF_CHECK_LAUNCH("k_zero_records");
+  }
   const size_t bytes = f->count * kf_prec_size(f->prec);
-  for (int k = 0; k < 3; ++k) KF_CHECK_CUDA(cudaMemsetAsync(f->p[k], 0, bytes, kf_stream(stream)));
-  // the band-only solver's ping-pong buffer, once that solver has used the
-  // field: its first pass then reads phi_live alone (no copy of psi)
-  for (int k = 0; q_too && k < 3; ++k) KF_CHECK_CUDA(cudaMemsetAsync(f->q[k], 0, bytes, kf_stream(stream)));
-  f->p_zero = true;
-  f->q_zero = q_was_zero || q_too;
+  for (int k = 0; ps == kPsiUnknown && k < 3; ++k) KF_CHECK_CUDA(cudaMemsetAsync(f->p[k], 0, bytes, s));
+  for (int k = 0; q_too && qs == kPsiUnknown && k < 3; ++k) KF_CHECK_CUDA(cudaMemsetAsync(f->q[k], 0, bytes, s));
+  f->p_state = kPsiZero;
+  f->q_state = q_too ? kPsiZero : qs;
   return KF_OK;
 }
 
@@ -517,6 +564,7 @@ extern "C" int kf_field_download(kf_field f, void *xyz, void *stream) {
 extern "C" int kf_field_device(kf_field f, void **px, void **py, void **pz) {
   KF_REQUIRE(f, "field is NULL");
   f->exposed = true;  // the caller may write the planes from now on
+  kf_field_written(f);
   if (px) *px = f->p[0];
   if (py) *py = f->p[1];
   if (pz) *pz = f->p[2];
@@ -776,13 +824,14 @@ static int solve_launch(kf_grid live, kf_grid canonical, kf_field psi, const kf_
   // every solver writes psi's planes; the band-only solver's first pass
   // reads phi_live alone when both start at zero, and from now on
   // kf_field_zero clears its ping-pong buffer too
-  const bool psi_zero = psi->p_zero && psi->q_zero && !psi->exposed;
+  const bool p_zero = !psi->exposed && psi->p_state == kPsiZero;
+  const bool q_zero = !psi->exposed && psi->q_state == kPsiZero;
   kf_field_written(psi);
   if (solver == KF_SOLVER_BAND) psi->q_zero_wanted = true;
   if (solver == KF_SOLVER_PERVOXEL)
     rc = kf_solve_pervoxel(live, canonical, psi, dp, iterations, st, s);
   else if (solver == KF_SOLVER_FUSED || solver == KF_SOLVER_BAND)
-    rc = kf_solve_fused(live, canonical, psi, dp, iterations, st, solver == KF_SOLVER_BAND, psi_zero, s);
+    rc = kf_solve_fused(live, canonical, psi, dp, iterations, st, solver == KF_SOLVER_BAND, p_zero, q_zero, s);
   else if (solver == KF_SOLVER_PLAIN)
     rc = kf_solve_plain(live, canonical, psi, dp, iterations, st, s);
   else

@@ -1005,7 +1005,10 @@ static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevPara
   // holds nothing between solves: values, weights and indices, N each
   int st = kf_field_ensure_pair(psi);
   if (st) return st;
-  kf_field_q_written(psi);
+  // q zero outside the field's records stays so, with the list's entries
+  // [0, *live->ctr) recorded (once between two zeros of the field)
+  const bool record = psi->q_state == kPsiRecorded && !psi->side_recorded && !psi->exposed;
+  psi->q_state = kPsiUnknown;
   float *side_phi = (float *)psi->q[0];
   int32_t *side_w = (int32_t *)psi->q[1];
   int32_t *side_i = (int32_t *)psi->q[2];
@@ -1032,6 +1035,15 @@ static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevPara
                                                    side_w, side_i, live->ctr);
   k_warp_scatter<<<spread, kBlock, 0, s>>>(live->phi, live->w, side_phi, side_w, side_i, live->ctr, live->count);
   KF_CHECK_LAUNCH("k_warp_fuse");
+  if (record) {
+    int *touched;
+    unsigned *touched_n, *side_n;
+    st = kf_field_records(psi, &touched, &touched_n, &side_n);
+    if (st) return st;
+    KF_CHECK_CUDA(cudaMemcpyAsync(side_n, live->ctr, sizeof(unsigned), cudaMemcpyDeviceToDevice, s));
+    psi->q_state = kPsiRecorded;
+    psi->side_recorded = true;
+  }
   return KF_OK;
 }
 

@@ -341,14 +341,20 @@ __device__ __forceinline__ bool persistent_band_iteration(const FusedArgs &a, in
 }
 
 // even: psi in the primary planes, out to the second; odd: the reverse.
-// The band list of the dense first pass is lst0[0, st[0].list).
+// The band list of the dense first pass is lst0[0, st[0].list).  touched
+// (or NULL): a copy of that list and its length, the only voxels whose psi
+// the solve can change (the iterations overwrite lst0).
 __global__ void __launch_bounds__(kPersistThreads, kPersistBlocksPerSM)
     k_band_persistent(FusedArgs even, FusedArgs odd, int *lst0, int *lst1, int iterations, GridSync *sync,
-                      unsigned long long limit_ns) {
+                      unsigned long long limit_ns, int *touched, unsigned *touched_n) {
   const unsigned nq = __ldcg(&even.st[0].list);
   const unsigned per = (nq + gridDim.x - 1) / gridDim.x;  // this block's slice [k0, k0 + per)
   const unsigned k0 = min(blockIdx.x * per, nq);
   unsigned n = min(k0 + per, nq) - k0;
+  if (touched) {
+    for (unsigned j = threadIdx.x; j < n; j += kPersistThreads) touched[k0 + j] = __ldcg(lst0 + k0 + j);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *touched_n = nq;
+  }
   __shared__ int s_first[kPersistThreads];
   unsigned long long seen_even = 0, seen_odd = 0;
   for (int it = 0; it < iterations; it += 2) {
@@ -659,11 +665,14 @@ static int persistent_blocks_per_sm() {
 }
 
 // KF_SOLVER_BAND without the trust-region step: the dense first pass (on
-// phi_live alone when psi_zero: both buffers are zero), then every band pass
-// in one cooperative launch (k_band_persistent).  Iteration k reads buffer
-// k % 2 and writes (k + 1) % 2, as the per-iteration form.
+// phi_live alone when both buffers are zero), then every band pass in one
+// cooperative launch (k_band_persistent).  Iteration k reads buffer k % 2
+// and writes (k + 1) % 2, as the per-iteration form.  From a zero p the
+// first pass leaves both buffers zero outside its list (it copies p to q),
+// and the solve records the list: the field's buffers are then zero outside
+// its records (kf_field_zero clears just those).
 static int launch_band_persistent(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
-                                  int iterations, IterStats *st, bool psi_zero, cudaStream_t s) {
+                                  int iterations, IterStats *st, bool p_zero, bool q_zero, cudaStream_t s) {
   void *sync = nullptr;
   int rc = kf_field_sync(psi, &sync);
   if (rc) return rc;
@@ -685,7 +694,14 @@ static int launch_band_persistent(kf_grid live, kf_grid can, kf_field psi, const
   odd.oy = (float *)psi->p[1];
   odd.oz = (float *)psi->p[2];
   int *lst0 = psi->band, *lst1 = psi->band + dp.count;
-  if (psi_zero)
+  int *touched = nullptr;
+  unsigned *touched_n = nullptr, *side_n = nullptr;
+  if (p_zero) {
+    rc = kf_field_records(psi, &touched, &touched_n, &side_n);
+    if (rc) return rc;
+    KF_CHECK_CUDA(cudaMemsetAsync(side_n, 0, sizeof(unsigned), s));
+  }
+  if (p_zero && q_zero)
     k_band_first_zero<<<(unsigned)num_runs(dp), kThreads, 0, s>>>(even, lst0);
   else
     k_fused_stream<true><<<(unsigned)num_runs(dp), kThreads, 0, s>>>(even, lst0, nullptr, nullptr);
@@ -693,15 +709,19 @@ static int launch_band_persistent(kf_grid live, kf_grid can, kf_field psi, const
   GridSync *gs = static_cast<GridSync *>(sync);
   unsigned long long limit = kf_wait_limit_ns();
   int iters = iterations;
-  void *args[] = {&even, &odd, &lst0, &lst1, &iters, &gs, &limit};
+  void *args[] = {&even, &odd, &lst0, &lst1, &iters, &gs, &limit, &touched, &touched_n};
   KF_CHECK_CUDA(cudaLaunchCooperativeKernel((const void *)k_band_persistent,
                                             dim3((unsigned)(kf_num_sms() * bps)), dim3(kPersistThreads), args, 0,
                                             s));
+  if (p_zero) {
+    psi->p_state = psi->q_state = kPsiRecorded;
+    psi->side_recorded = false;
+  }
   return KF_OK;
 }
 
 int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp, int iterations,
-                   IterStats *st, bool band_only, bool psi_zero, cudaStream_t s) {
+                   IterStats *st, bool band_only, bool p_zero, bool q_zero, cudaStream_t s) {
   int rc = kf_field_ensure_pair(psi);
   if (rc) return rc;
   rc = kf_field_band_list(psi, &psi->band);
@@ -717,7 +737,7 @@ int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
     }
     psi->runs_cap = nruns;
   }
-  if (band_only && !dp.trust) return launch_band_persistent(live, can, psi, dp, iterations, st, psi_zero, s);
+  if (band_only && !dp.trust) return launch_band_persistent(live, can, psi, dp, iterations, st, p_zero, q_zero, s);
   int *rows = nullptr;
   if (dp.trust) {
     rc = kf_field_trust_rows(psi, &rows);

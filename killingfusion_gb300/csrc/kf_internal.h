@@ -60,19 +60,32 @@ struct kf_field_s {
   int last_iterations;
   kf_solver last_solver;
   int pending;
-  // What is known of the planes' contents once the work queued so far has
-  // run (the flags follow the order calls are made in, which is the order a
-  // caller must give the streams they use): p all zero (kf_field_zero),
-  // q all zero (kf_field_zero, once the band-only solver has used the field:
-  // q_zero_wanted).  Every other write clears them (kf_field_written), and
-  // nothing is known once kf_field_device has handed the planes out.  With
-  // both, the band-only solver's first pass reads phi_live alone.
-  bool p_zero, q_zero, q_zero_wanted, exposed;
+  // What is known of each buffer's contents once the work queued so far has
+  // run (the states follow the order calls are made in, which is the order
+  // a caller must give the streams they use; KfPsiState).  kf_field_zero
+  // makes p zero, and q too once the band-only solver has used the field
+  // (q_zero_wanted); a band-only solve that starts from a zero p changes
+  // psi only at the voxels of its first list, which it records in
+  // `touched`, and leaves both buffers zero elsewhere; warp + fuse then
+  // records how many entries of q its moved-voxel list takes
+  // (side_recorded).  Every other write makes a buffer unknown
+  // (kf_field_written), and nothing is known once kf_field_device has handed
+  // the planes out.  With both buffers zero, the band-only solver's first
+  // pass reads phi_live alone; zero outside the records, kf_field_zero
+  // clears the records alone.
+  int p_state, q_state;
+  bool q_zero_wanted, exposed, side_recorded;
+  int *touched;  // device: count voxel indices, then the counters touched_n
+                 // and side_n (kf_field_records)
 };
 
-// A call is about to write psi's planes (both, or q alone).
-inline void kf_field_written(kf_field f) { f->p_zero = f->q_zero = false; }
-inline void kf_field_q_written(kf_field f) { f->q_zero = false; }
+enum KfPsiState { kPsiUnknown = 0, kPsiZero = 1, kPsiRecorded = 2 };
+
+// A call is about to write psi's planes.
+inline void kf_field_written(kf_field f) { f->p_state = f->q_state = kPsiUnknown; }
+// The records of a field (lazily allocated): the voxel list and, after it,
+// its length and the entries of q that warp + fuse wrote.
+int kf_field_records(kf_field f, int **touched, unsigned **touched_n, unsigned **side_n);
 
 // ---------------------------------------------------------------------------
 // error state
@@ -166,10 +179,12 @@ unsigned long long kf_wait_limit_ns();
 int kf_field_sync(kf_field f, void **out);
 
 // solver entry points implemented in the solver translation units
-// psi_zero: both of psi's planes are all zero when the solve starts
-// (kf_field_s::p_zero and q_zero).
+// p_zero, q_zero: psi's buffers are all zero when the solve starts
+// (kf_field_s::p_state, q_state); the band-only solver then sets the
+// states it leaves.
 int kf_solve_fused(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
-                   int iterations, IterStats *stats_dev, bool band_only, bool psi_zero, cudaStream_t s);
+                   int iterations, IterStats *stats_dev, bool band_only, bool p_zero, bool q_zero,
+                   cudaStream_t s);
 int kf_solve_plain(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,
                    int iterations, IterStats *stats_dev, cudaStream_t s);
 int kf_solve_exact(kf_grid live, kf_grid can, kf_field psi, const DevParams &dp,

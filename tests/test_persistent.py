@@ -133,9 +133,10 @@ def test_persistent_band_divergence_equals_dense(gpu):
 
 def test_band_first_pass_on_a_zero_field(gpu):
     """Once the band-only solver has used a field, kf_field_zero clears both
-    of its buffers, and the next band-only solve's first pass reads phi_live
-    alone.  Whatever wrote psi before the zero (a warp, which borrows the
-    second buffer; an upload; a fill; a dense solve; a per-voxel update), a
+    of its buffers (all of them, or only the places the field has recorded),
+    and the next band-only solve's first pass reads phi_live alone.
+    Whatever wrote psi before the zero (a warp, which borrows the second
+    buffer; an upload; a fill; a dense solve; a per-voxel update), a
     band-only solve from zero gives the dense solver's psi and statistics;
     and a write after the zero sends the solve back to the first pass that
     reads psi, with the dense solver's result from the same psi."""
@@ -164,6 +165,15 @@ def test_band_first_pass_on_a_zero_field(gpu):
         np.testing.assert_array_equal(f.download(), expect, err_msg=str(k))
         for key in keys:
             assert st[key] == se[key], (k, key)
+    # the frame pipeline's cycle: a band-only solve from zero records the
+    # voxels it can change and warp + fuse the entries of the second buffer it
+    # borrows, and the next zero clears those alone
+    for _ in range(3):
+        f.zero()
+        assert not f.download().any()
+        st = capi.psi_solve(gl, gc, f, P, 40, "band")
+        np.testing.assert_array_equal(f.download(), expect)
+        capi.warp(scratch, f, P)
     for k, write in enumerate(writes[2:]):
         f.zero()
         write(f)
