@@ -68,6 +68,9 @@ def parse():
                          "paper: the values in the comment at config.cpp:32-41")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-band-frame", action="store_true", help="skip the band-only frame measurement")
+    ap.add_argument("--timeline", default=None, choices=["band", "fused"],
+                    help="instead of the bench line: per-frame, per-stream step times (CUDA events) of "
+                         "--steps frames of the per-frame workload in the two-frame pipeline with this solver")
     ap.add_argument("--log", default=None,
                     help="JSONL log: the configuration, each timed frame's solve time, the per-iteration "
                          "energy, max |dpsi| and band count of the parity frame's solve, the result line")
@@ -615,6 +618,10 @@ def main():
 
     if args.impl == "reference" and rank != 0:
         return
+    if args.timeline:
+        if rank == 0:
+            print(json.dumps(run_timeline(args, local)))
+        return
     if args.workload not in ("ellipsoid", "sphere"):
         if args.impl == "reference":
             if rank == 0:
@@ -626,6 +633,53 @@ def main():
             print(json.dumps(line))
         return
     run_main(args, rank, world, local)
+
+
+def run_timeline(args, local):
+    """Each frame's steps on the pipeline's streams (killingfusion_gb300.pipeline),
+    in microseconds from CUDA events: when the frame's solve started, how long
+    each step took, and the time between two frames' ends of warp + fuse."""
+    import torch
+
+    from killingfusion_gb300.pipeline import FramePipeline
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    seq, nseq, max_depth, name = workload_sequence(args)
+    grid = seq.grid
+    P = bench_params(args, grid.voxel)
+    nframes = 1 + args.warmup + args.steps
+    frames = [torch.from_numpy(seq.frame(0 if f == 0 else 1 + (f - 1) % (nseq - 1))).to(dev) for f in range(nframes)]
+    pipe = FramePipeline(grid.dims, grid.voxel, grid.origin, P, args.iters, args.timeline, max_depth=max_depth,
+                         mesh_capacity=MESH_CAP, device=local)
+    pipe.start(frames[0])
+    pipe.run([(f, frames[f]) for f in range(1, 1 + args.warmup)])
+    torch.cuda.synchronize(dev)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t0.record(pipe.s_main)
+    for s in (pipe.s_in, pipe.s_out):
+        s.wait_event(t0)
+    pipe.marks = []
+    pipe.run([(f, frames[f]) for f in range(1 + args.warmup, nframes)])
+    torch.cuda.synchronize(dev)
+    steps = [("integrate", "in_start", "integrated"), ("zero_psi", "integrated", "zeroed"),
+             ("live_mesh", "zeroed", "live_meshed"), ("solve", "solve_start", "solved"),
+             ("wait_before_fuse", "solved", "fuse_start"), ("warp_fuse", "fuse_start", "fused"),
+             ("registered_mesh", "out_start", "registered_meshed"),
+             ("canonical_mesh", "registered_meshed", "canonical_meshed")]
+    out, prev = [], None
+    for f, m in pipe.marks:
+        t = {k: t0.elapsed_time(e) * 1e3 for k, e in m.items()}
+        row = {"frame": f, "solve_start_us": round(t["solve_start"], 1)}
+        row.update({k + "_us": round(t[b] - t[a], 1) for k, a, b in steps})
+        if prev is not None:
+            row["frame_us"] = round(t["fused"] - prev, 1)
+        prev = t["fused"]
+        out.append(row)
+    pipe.close()
+    per = [r["frame_us"] for r in out if "frame_us" in r]
+    return {"timeline": args.timeline, "workload": name, "iterations_per_frame": args.iters,
+            "mean_frame_us": round(sum(per) / len(per), 1) if per else None, "frames": out}
 
 
 def max_over_ranks(values, device="cuda"):

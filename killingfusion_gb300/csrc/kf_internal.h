@@ -216,6 +216,21 @@ size_t kf_prec_size(kf_precision p);
 // Number of SMs of the current device (cached).
 int kf_num_sms();
 
+// Asks once per device (`done`: a flag per device) that `func` get
+// `percent` % of the largest shared-memory share
+// (cudaFuncAttributePreferredSharedMemoryCarveout); a preference only.
+inline void kf_prefer_carveout(const void *func, int percent, bool (&done)[64]) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return;
+  }
+  if (done[dev]) return;
+  if (cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout, percent) != cudaSuccess)
+    cudaGetLastError();
+  done[dev] = true;
+}
+
 // launches implemented in kf_exact.cu (float64 arithmetic without fused
 // multiply-add where the reference's rounding decides a discrete outcome)
 int kf_grid_ensure_alt(kf_grid g);

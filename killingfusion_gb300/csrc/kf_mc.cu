@@ -583,16 +583,7 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit_cells(McGrid g, McList L, 
 // it twice is harmless).
 void prefer_shared_for_count() {
   static bool done[64] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-    cudaGetLastError();
-    return;
-  }
-  if (done[dev]) return;
-  if (cudaFuncSetAttribute(k_mc_count_list, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
-    cudaGetLastError();  // a preference only
-  done[dev] = true;
+  kf_prefer_carveout((const void *)k_mc_count_list, (int)cudaSharedmemCarveoutMaxShared, done);
 }
 
 // Resident CTAs of the emit pass.

@@ -59,6 +59,9 @@ class FramePipeline:
         ev = lambda: [torch.cuda.Event(), torch.cuda.Event()]  # noqa: E731
         self.ev_integ, self.ev_fused, self.ev_meshed, self.ev_copied = ev(), ev(), ev(), ev()
         self.stats = capi.SolveStats()
+        # a list to record, per queued frame, timing events between its steps
+        # on each stream ((frame, {step: event}) pairs; see queue)
+        self.marks = None
 
     def _compute_sdf(self, grid, depth, stream):
         """KillingFusion::computeSDF: the grid reset and the frame integrated
@@ -82,13 +85,24 @@ class FramePipeline:
         lv, ps, ms = self.lives[k], self.psis[k], self.meshes[k]
         cptr = self.counts.data_ptr() + 24 * k
         s_in, s_main, s_out = self.s_in, self.s_main, self.s_out
+        marks = {}
+
+        def mark(name, stream):
+            if self.marks is not None:
+                marks[name] = torch.cuda.Event(enable_timing=True)
+                marks[name].record(stream)
+
         s_in.wait_event(self.ev_meshed[k])
+        mark("in_start", s_in)
         self._compute_sdf(lv, depth, s_in)
+        mark("integrated", s_in)
         ps.zero(stream=s_in)
+        mark("zeroed", s_in)
         s_in.wait_event(self.ev_copied[k])
         capi.check(L.kf_marching_cubes_async(lv.h, C.byref(Pc), ms[0].data_ptr(), self.cap, cptr,
                                              s_in.cuda_stream))
         self.ev_integ[k].record(s_in)
+        mark("live_meshed", s_in)
         s_main.wait_event(self.ev_integ[k])
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s_main)
@@ -96,15 +110,23 @@ class FramePipeline:
                                         s_main.cuda_stream))
         e1.record(s_main)
         s_main.wait_event(self.ev_meshed[1 - k])  # the canonical mesh of frame f - 1
+        mark("fuse_start", s_main)
         capi.check(L.kf_warp_fuse(self.can.h, lv.h, ps.h, C.byref(Pc), s_main.cuda_stream))
         self.ev_fused[k].record(s_main)
+        mark("fused", s_main)
         s_out.wait_event(self.ev_fused[k])
         s_out.wait_event(self.ev_copied[k])
+        mark("out_start", s_out)
         capi.check(L.kf_marching_cubes_async(lv.h, C.byref(Pc), ms[1].data_ptr(), self.cap, cptr + 8,
                                              s_out.cuda_stream))
+        mark("registered_meshed", s_out)
         capi.check(L.kf_marching_cubes_async(self.can.h, C.byref(Pc), ms[2].data_ptr(), self.cap, cptr + 16,
                                              s_out.cuda_stream))
         self.ev_meshed[k].record(s_out)
+        mark("canonical_meshed", s_out)
+        if self.marks is not None:
+            marks["solve_start"], marks["solved"] = e0, e1
+            self.marks.append((f, marks))
         return e0, e1
 
     def finish(self, f: int, copy: bool = False, wait_copy: bool = False):
