@@ -399,15 +399,21 @@ int kf_field_sync(kf_field f, void **out) {
   return KF_OK;
 }
 
-int kf_field_records(kf_field f, int **touched, unsigned **touched_n, unsigned **side_n) {
-  if (!f->touched && cudaMalloc(&f->touched, (f->count + 64) * sizeof(int)) != cudaSuccess) {
-    cudaGetLastError();
-    f->touched = nullptr;
-    return kf_fail(KF_ERR_OOM, "cudaMalloc of the field's records failed");
+int kf_field_records(kf_field f, cudaStream_t s, KfRecords *r) {
+  // touched[count], 64 words of counters, the bitmap
+  const size_t words = (size_t)(f->count + 31) / 32;
+  if (!f->touched) {
+    if (cudaMalloc(&f->touched, ((size_t)f->count + 64 + words) * sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      f->touched = nullptr;
+      return kf_fail(KF_ERR_OOM, "cudaMalloc of the field's records failed");
+    }
+    KF_CHECK_CUDA(cudaMemsetAsync(f->touched + f->count + 64, 0, words * sizeof(int), s));
   }
-  *touched = f->touched;
-  *touched_n = reinterpret_cast<unsigned *>(f->touched + f->count);
-  *side_n = *touched_n + 1;
+  r->touched = f->touched;
+  r->touched_n = reinterpret_cast<unsigned *>(f->touched + f->count);
+  r->side_n = r->touched_n + 1;
+  r->moved = reinterpret_cast<unsigned *>(f->touched + f->count + 64);
   return KF_OK;
 }
 
@@ -484,14 +490,13 @@ extern "C" int kf_field_zero(kf_field f, void *stream) {
   const bool q_too = f->q[0] && f->q_zero_wanted;
   kf_field_written(f);  // (until every clear is queued)
   if (ps == kPsiRecorded || (q_too && qs == kPsiRecorded)) {
-    int *touched;
-    unsigned *touched_n, *side_n;
-    int rc = kf_field_records(f, &touched, &touched_n, &side_n);
+    KfRecords r;
+    int rc = kf_field_records(f, s, &r);
     if (rc) return rc;
     const bool zp = ps == kPsiRecorded, zq = q_too && qs == kPsiRecorded;
     k_zero_records<<<(unsigned)kf_num_sms() * 4, 256, 0, s>>>(
         zp ? (float *)f->p[0] : nullptr, (float *)f->p[1], (float *)f->p[2], zq ? (float *)f->q[0] : nullptr,
-        (float *)f->q[1], (float *)f->q[2], touched, touched_n, side_n, f->count);
+        (float *)f->q[1], (float *)f->q[2], r.touched, r.touched_n, r.side_n, f->count);
     KF_CHECK_LAUNCH("k_zero_records");
   }
   const size_t bytes = f->count * kf_prec_size(f->prec);

@@ -713,8 +713,10 @@ __device__ __forceinline__ void fuse_voxel(float *__restrict__ cphi, int32_t *__
 // the surface, their float64 arithmetic was the kernel's tail), and
 // k_warp_scatter writes their values back once every moved voxel has read
 // its neighbours' old values.  Each thread takes four consecutive voxels
-// with 16-byte loads.  When `cphi` is null only the warp is done.
-template <typename P>
+// with 16-byte loads.  When `cphi` is null only the warp is done.  kMoved:
+// whether a voxel has moved comes from the bitmap `moved` (k_mark_moved)
+// instead of its psi (4 bits a thread, where psi is 12 bytes a voxel).
+template <typename P, bool kMoved = false>
 __global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ lphi,
                                                       const int32_t *__restrict__ lw,
                                                       float *__restrict__ cphi, int32_t *__restrict__ cw,
@@ -722,7 +724,8 @@ __global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ 
                                                       float *__restrict__ side_phi,
                                                       int32_t *__restrict__ side_w,
                                                       int32_t *__restrict__ side_i,
-                                                      unsigned *__restrict__ ctr) {
+                                                      unsigned *__restrict__ ctr,
+                                                      const unsigned *__restrict__ moved_bits = nullptr) {
   const int64_t N = (int64_t)nx * ny * nz;
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t i0 = 4 * q;
@@ -736,7 +739,9 @@ __global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ 
     const int4 b = __ldcs(reinterpret_cast<const int4 *>(lw) + q);
     ph[0] = a.x; ph[1] = a.y; ph[2] = a.z; ph[3] = a.w;
     wv[0] = b.x; wv[1] = b.y; wv[2] = b.z; wv[3] = b.w;
-    if (sizeof(P) == 4) {
+    if (kMoved) {
+      moved = (__ldg(moved_bits + (i0 >> 5)) >> (i0 & 31)) & 15u;  // (i0 is a multiple of 4)
+    } else if (sizeof(P) == 4) {
       const float4 x = __ldcs(reinterpret_cast<const float4 *>(f.x) + q);
       const float4 y = __ldcs(reinterpret_cast<const float4 *>(f.y) + q);
       const float4 z = __ldcs(reinterpret_cast<const float4 *>(f.z) + q);
@@ -754,7 +759,9 @@ __global__ void __launch_bounds__(kBlock) k_warp_fuse(const float *__restrict__ 
       if (e >= valid) break;
       ph[e] = lphi[i0 + e];
       wv[e] = lw[i0 + e];
-      if (f.x[i0 + e] != P(0) || f.y[i0 + e] != P(0) || f.z[i0 + e] != P(0)) moved |= 1u << e;
+      if (kMoved ? ((__ldg(moved_bits + ((i0 + e) >> 5)) >> ((i0 + e) & 31)) & 1u) != 0u
+                 : f.x[i0 + e] != P(0) || f.y[i0 + e] != P(0) || f.z[i0 + e] != P(0))
+        moved |= 1u << e;
     }
   }
   // one slot range per warp for its moved voxels
@@ -814,18 +821,34 @@ __global__ void __launch_bounds__(kBlock) k_warp_moved(const float *__restrict__
   }
 }
 
-// Writes the moved voxels' resampled values back (after k_warp_fuse).
+// Writes the moved voxels' resampled values back (after k_warp_fuse) and
+// clears their bits of `moved_bits` (when given), which leaves it clear.
 __global__ void __launch_bounds__(kBlock) k_warp_scatter(float *__restrict__ lphi, int32_t *__restrict__ lw,
                                                          const float *__restrict__ side_phi,
                                                          const int32_t *__restrict__ side_w,
                                                          const int32_t *__restrict__ side_i,
-                                                         const unsigned *__restrict__ ctr, int64_t count) {
+                                                         const unsigned *__restrict__ ctr, int64_t count,
+                                                         unsigned *__restrict__ moved_bits = nullptr) {
   const unsigned n = *ctr;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int32_t i = side_i[k];
     if (!KF_IN_BOUNDS(k, count, KF_SITE_SIDE_LIST) || !KF_IN_BOUNDS(i, count, KF_SITE_SIDE_LIST)) continue;
     lphi[i] = side_phi[k];
     lw[i] = side_w[k];
+    if (moved_bits) atomicAnd(moved_bits + (i >> 5), ~(1u << (i & 31)));
+  }
+}
+
+// The bits of `moved_bits` of the recorded voxels touched[0, *touched_n)
+// whose psi is not zero (psi is zero at every other voxel).
+__global__ void __launch_bounds__(kBlock) k_mark_moved(PsiPlanes<float> f, const int *__restrict__ touched,
+                                                       const unsigned *__restrict__ touched_n, int64_t count,
+                                                       unsigned *__restrict__ moved_bits) {
+  const unsigned n = *touched_n;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int i = touched[k];
+    if (!KF_IN_BOUNDS(i, count, KF_SITE_SIDE_LIST)) continue;
+    if (f.x[i] != 0.f || f.y[i] != 0.f || f.z[i] != 0.f) atomicOr(moved_bits + (i >> 5), 1u << (i & 31));
   }
 }
 
@@ -1008,7 +1031,15 @@ static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevPara
   // q zero outside the field's records stays so, with the list's entries
   // [0, *live->ctr) recorded (once between two zeros of the field)
   const bool record = psi->q_state == kPsiRecorded && !psi->side_recorded && !psi->exposed;
+  // p zero outside the recorded voxels: which voxels moved comes from a
+  // bitmap of those voxels instead of psi at every voxel
+  const bool by_bits = psi->p_state == kPsiRecorded && !psi->exposed && psi->prec == KF_F32;
   psi->q_state = kPsiUnknown;
+  KfRecords r{};
+  if (record || by_bits) {
+    st = kf_field_records(psi, s, &r);
+    if (st) return st;
+  }
   float *side_phi = (float *)psi->q[0];
   int32_t *side_w = (int32_t *)psi->q[1];
   int32_t *side_i = (int32_t *)psi->q[2];
@@ -1016,7 +1047,13 @@ static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevPara
   int32_t *cw = can ? can->w : nullptr;
   KF_CHECK_CUDA(cudaMemsetAsync(live->ctr, 0, sizeof(unsigned), s));
   const unsigned blocks = blocks_for((live->count + 3) / 4);
-  if (psi->prec == KF_F32)
+  const unsigned spread = (unsigned)kf_num_sms() * 4;
+  if (by_bits) {
+    k_mark_moved<<<spread, kBlock, 0, s>>>(planes<float>(psi), r.touched, r.touched_n, live->count, r.moved);
+    k_warp_fuse<float, true><<<blocks, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<float>(psi),
+                                                       live->n[0], live->n[1], live->n[2], dp.oob_phi, side_phi,
+                                                       side_w, side_i, live->ctr, r.moved);
+  } else if (psi->prec == KF_F32)
     k_warp_fuse<float><<<blocks, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<float>(psi), live->n[0],
                                                  live->n[1], live->n[2], dp.oob_phi, side_phi, side_w, side_i,
                                                  live->ctr);
@@ -1024,7 +1061,6 @@ static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevPara
     k_warp_fuse<double><<<blocks, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<double>(psi), live->n[0],
                                                   live->n[1], live->n[2], dp.oob_phi, side_phi, side_w, side_i,
                                                   live->ctr);
-  const unsigned spread = (unsigned)kf_num_sms() * 4;
   if (psi->prec == KF_F32)
     k_warp_moved<float><<<spread, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<float>(psi), live->n[0],
                                                   live->n[1], live->n[2], dp.oob_phi, side_phi, side_w, side_i,
@@ -1033,14 +1069,11 @@ static int warp_fuse_impl(kf_grid can, kf_grid live, kf_field psi, const DevPara
     k_warp_moved<double><<<spread, kBlock, 0, s>>>(live->phi, live->w, cphi, cw, planes<double>(psi),
                                                    live->n[0], live->n[1], live->n[2], dp.oob_phi, side_phi,
                                                    side_w, side_i, live->ctr);
-  k_warp_scatter<<<spread, kBlock, 0, s>>>(live->phi, live->w, side_phi, side_w, side_i, live->ctr, live->count);
+  k_warp_scatter<<<spread, kBlock, 0, s>>>(live->phi, live->w, side_phi, side_w, side_i, live->ctr, live->count,
+                                           by_bits ? r.moved : nullptr);
   KF_CHECK_LAUNCH("k_warp_fuse");
   if (record) {
-    int *touched;
-    unsigned *touched_n, *side_n;
-    st = kf_field_records(psi, &touched, &touched_n, &side_n);
-    if (st) return st;
-    KF_CHECK_CUDA(cudaMemcpyAsync(side_n, live->ctr, sizeof(unsigned), cudaMemcpyDeviceToDevice, s));
+    KF_CHECK_CUDA(cudaMemcpyAsync(r.side_n, live->ctr, sizeof(unsigned), cudaMemcpyDeviceToDevice, s));
     psi->q_state = kPsiRecorded;
     psi->side_recorded = true;
   }

@@ -696,11 +696,14 @@ static int launch_band_persistent(kf_grid live, kf_grid can, kf_field psi, const
   odd.oz = (float *)psi->p[2];
   int *lst0 = psi->band, *lst1 = psi->band + dp.count;
   int *touched = nullptr;
-  unsigned *touched_n = nullptr, *side_n = nullptr;
+  unsigned *touched_n = nullptr;
   if (p_zero) {
-    rc = kf_field_records(psi, &touched, &touched_n, &side_n);
+    KfRecords r;
+    rc = kf_field_records(psi, s, &r);
     if (rc) return rc;
-    KF_CHECK_CUDA(cudaMemsetAsync(side_n, 0, sizeof(unsigned), s));
+    KF_CHECK_CUDA(cudaMemsetAsync(r.side_n, 0, sizeof(unsigned), s));
+    touched = r.touched;
+    touched_n = r.touched_n;
   }
   if (p_zero && q_zero)
     k_band_first_zero<<<(unsigned)num_runs(dp), kThreads, 0, s>>>(even, lst0);

@@ -75,17 +75,23 @@ struct kf_field_s {
   // clears the records alone.
   int p_state, q_state;
   bool q_zero_wanted, exposed, side_recorded;
-  int *touched;  // device: count voxel indices, then the counters touched_n
-                 // and side_n (kf_field_records)
+  int *touched;  // device: the records (KfRecords, kf_field_records)
 };
 
 enum KfPsiState { kPsiUnknown = 0, kPsiZero = 1, kPsiRecorded = 2 };
 
 // A call is about to write psi's planes.
 inline void kf_field_written(kf_field f) { f->p_state = f->q_state = kPsiUnknown; }
-// The records of a field (lazily allocated): the voxel list and, after it,
-// its length and the entries of q that warp + fuse wrote.
-int kf_field_records(kf_field f, int **touched, unsigned **touched_n, unsigned **side_n);
+// The records of a field, in one allocation (made on first use; the bitmap
+// is cleared on stream s then).
+struct KfRecords {
+  int *touched;         // count entries: the voxels a band-only solve from zero listed
+  unsigned *touched_n;  // how many
+  unsigned *side_n;     // the entries of each q plane warp + fuse's moved-voxel list took
+  unsigned *moved;      // a bit per voxel (32 a word): warp + fuse's moved voxels,
+                        // all clear between its calls
+};
+int kf_field_records(kf_field f, cudaStream_t s, KfRecords *r);
 
 // ---------------------------------------------------------------------------
 // error state

@@ -166,14 +166,30 @@ def test_band_first_pass_on_a_zero_field(gpu):
         for key in keys:
             assert st[key] == se[key], (k, key)
     # the frame pipeline's cycle: a band-only solve from zero records the
-    # voxels it can change and warp + fuse the entries of the second buffer it
-    # borrows, and the next zero clears those alone
+    # voxels it can change; warp + fuse finds the moved ones among them
+    # (against warp + fuse reading psi at every voxel, from a field holding
+    # the same psi) and records the entries of the second buffer it borrows;
+    # the next zero clears those alone
+    def copy(g):
+        c = capi.Grid(dims, P.voxel_size, (0, 0, 0), P.unknown_clip, P)
+        c.upload(*g.download())
+        return c
+
     for _ in range(3):
         f.zero()
         assert not f.download().any()
         st = capi.psi_solve(gl, gc, f, P, 40, "band")
         np.testing.assert_array_equal(f.download(), expect)
-        capi.warp(scratch, f, P)
+        can1, live1, can2, live2 = copy(gc), copy(gl), copy(gc), copy(gl)
+        capi.warp_fuse(can1, live1, f, P)
+        g = capi.Field(dims, capi.KF_F32)
+        g.upload(f.download())
+        capi.warp_fuse(can2, live2, g, P)
+        for a, b in ((can1, can2), (live1, live2)):
+            for x, y in zip(a.download(), b.download()):
+                np.testing.assert_array_equal(x, y)
+        for h in (can1, live1, can2, live2, g):
+            h.close()
     for k, write in enumerate(writes[2:]):
         f.zero()
         write(f)
