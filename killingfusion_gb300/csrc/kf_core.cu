@@ -494,6 +494,8 @@ extern "C" int kf_field_zero(kf_field f, void *stream) {
     int rc = kf_field_records(f, s, &r);
     if (rc) return rc;
     const bool zp = ps == kPsiRecorded, zq = q_too && qs == kPsiRecorded;
+    static bool carveout[64] = {};
+    kf_prefer_carveout((const void *)k_zero_records, kBesideSolveCarveout, carveout);
     k_zero_records<<<(unsigned)kf_num_sms() * 4, 256, 0, s>>>(
         zp ? (float *)f->p[0] : nullptr, (float *)f->p[1], (float *)f->p[2], zq ? (float *)f->q[0] : nullptr,
         (float *)f->q[1], (float *)f->q[2], r.touched, r.touched_n, r.side_n, f->count);

@@ -608,6 +608,16 @@ static int launch_integrate(kf_grid g, const D *depth_dev, double depth_scale, i
   unsigned *n_live = list_n + 1;
   int *list = (int *)(base + list_off);
   KF_CHECK_CUDA(cudaMemsetAsync(list_n, 0, 2 * sizeof(unsigned), s));
+  {
+    // these passes run beside the band-only solver (kBesideSolveCarveout)
+    static bool done[5][64] = {};
+    const int c = kBesideSolveCarveout;
+    kf_prefer_carveout((const void *)k_integrate_prep<D>, c, done[0]);
+    kf_prefer_carveout((const void *)k_integrate_tiles, c, done[1]);
+    kf_prefer_carveout((const void *)k_integrate<D, true>, c, done[2]);
+    kf_prefer_carveout((const void *)k_integrate<D, false>, c, done[3]);
+    kf_prefer_carveout((const void *)k_integrate_exact<D>, c, done[4]);
+  }
   const unsigned tab_blocks = blocks_for(nx + ny + nz);
   const unsigned fill_blocks = fresh_phi ? (unsigned)kf_num_sms() * 16 : 0u;
   k_integrate_prep<D><<<tab_blocks + (unsigned)(bw * bh) + fill_blocks, kBlock, 0, s>>>(

@@ -637,22 +637,12 @@ static void launch_iterations(kf_grid live, kf_grid can, kf_field psi, const Dev
 
 // Resident blocks per SM of k_band_persistent on the current device (at most
 // kPersistBlocksPerSM): the cooperative launch must fit on the GPU at once.
-// The solve holds every SM for its whole length, and an SM keeps the split
-// of its on-chip memory between L1 and shared memory while any block is
-// resident.  With the default split for this kernel (which needs under 1 KB
-// of shared memory), a marching-cubes count pass launched beside the solve
-// (32 KB of cp.async rings a block) waited for the solve to end, and the
-// next frame's integration with it.  44 % of the largest share (100 KB)
-// holds two of its blocks, as many as fit beside this kernel's registers.
-// (Asking the same of the integration passes and the mesh emit pass, which
-// need little shared memory, made them wait for the solve instead: they
-// keep the default.)
-constexpr int kPersistCarveoutPercent = 44;
-
+// Its shared-memory carveout is kBesideSolveCarveout (kf_internal.h), the
+// one of the kernels that run beside it.
 static int persistent_blocks_per_sm() {
   static int cached[64] = {};
   static bool carveout[64] = {};
-  kf_prefer_carveout((const void *)k_band_persistent, kPersistCarveoutPercent, carveout);
+  kf_prefer_carveout((const void *)k_band_persistent, kBesideSolveCarveout, carveout);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
   if (!cached[dev]) {

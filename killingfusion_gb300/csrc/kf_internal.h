@@ -225,6 +225,16 @@ int kf_num_sms();
 // Asks once per device (`done`: a flag per device) that `func` get
 // `percent` % of the largest shared-memory share
 // (cudaFuncAttributePreferredSharedMemoryCarveout); a preference only.
+//
+// The kernels that run beside the band-only solver's persistent kernel (the
+// frame's integration and meshes, the zeroing of psi) and the solver itself
+// all ask for kBesideSolveCarveout, the largest shared share, which the
+// marching-cubes count pass wants for its cp.async rings.  The solve holds
+// every SM for its whole length, an SM keeps its L1 / shared split while any
+// block is resident, and a kernel that asked for another split than the
+// one an SM was in was seen to wait for the solve to end (one mesh or one
+// integration per frame took 1.2-1.3 ms instead of 60-90 us).
+constexpr int kBesideSolveCarveout = (int)cudaSharedmemCarveoutMaxShared;
 inline void kf_prefer_carveout(const void *func, int percent, bool (&done)[64]) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {

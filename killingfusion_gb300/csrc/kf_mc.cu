@@ -579,11 +579,12 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit_cells(McGrid g, McList L, 
 }
 
 // The count pass wants shared memory for kCountCtasPerSm rings of 32 KB per
-// SM: ask for the largest shared-memory carve-out, once per device (setting
-// it twice is harmless).
+// SM: the largest shared-memory carveout (kBesideSolveCarveout), as the
+// emit pass, which runs beside the band-only solver too.
 void prefer_shared_for_count() {
-  static bool done[64] = {};
-  kf_prefer_carveout((const void *)k_mc_count_list, (int)cudaSharedmemCarveoutMaxShared, done);
+  static bool done[2][64] = {};
+  kf_prefer_carveout((const void *)k_mc_count_list, kBesideSolveCarveout, done[0]);
+  kf_prefer_carveout((const void *)k_mc_emit_cells, kBesideSolveCarveout, done[1]);
 }
 
 // Resident CTAs of the emit pass.
