@@ -190,6 +190,11 @@ int kf_field_zero(kf_field f, void *stream);
  * float for KF_F32 fields and double for KF_F64 (host or device). */
 int kf_field_upload(kf_field f, const void *xyz, void *stream);
 int kf_field_download(kf_field f, void *xyz, void *stream);
+/* Raw device planes (valid until the next solve, which may exchange them
+ * with its second buffer).  From then on the library no longer relies on
+ * knowing where psi is zero (after kf_field_zero, the band-only solver
+ * otherwise tests the band on phi_live alone and zeroes only the voxels it
+ * changed). */
 int kf_field_device(kf_field f, void **px, void **py, void **pz);
 
 /* psi += other (DisplacementField::operator+, DisplacementField.cpp:73-80). */
